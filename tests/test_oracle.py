@@ -1,0 +1,265 @@
+"""Pins the CPU oracle before anything is checked against it.
+
+The reference ships no unit tests or golden vectors (its test/test_main.cpp
+only prints lattice indices).  The oracle is pinned by
+  * known answers written from the mathematics (U = 0 Green's function,
+    determinant ratios, Sherman-Morrison = fresh recomputation, UDV
+    reconstruction, checkerboard algebra, lattice tables),
+  * the exact uniform stream of libstdc++'s minstd_rand0 + bernoulli, and
+  * a statistical comparison with the reference's only shipped run
+    (example/log.out, fixture tests/golden/example_8x8.json).
+"""
+import multiprocessing as mp
+
+import numpy as np
+import pytest
+
+
+def _minstd_uniforms(seed, n):
+    m, a = 2147483647, 16807
+    x = seed % m or 1
+    R = 2147483646.0
+    out = []
+    for _ in range(n):
+        x = (a * x) % m
+        g1 = x
+        x = (a * x) % m
+        g2 = x
+        s = float(g1 - 1) + float(g2 - 1) * R
+        u = s / (R * R)
+        out.append(u if u < 1.0 else np.nextafter(1.0, 0.0))
+    return np.array(out)
+
+
+def test_uniform_stream_matches_libstdcxx(oracle_mod):
+    w = oracle_mod.Walker(L=2, Lt=4, pace=2)
+    for seed in (1, 12345, 2**31 - 1, 0):
+        w.seed(seed)
+        np.testing.assert_array_equal(w.uniforms(200), _minstd_uniforms(seed, 200))
+
+
+def _exact_G0(w, beta, K):
+    ev, V = np.linalg.eigh(K)
+    return V @ np.diag(1.0 / (1.0 + np.exp(-beta * ev))) @ V.T
+
+
+@pytest.mark.parametrize("model", [0, 1])
+@pytest.mark.parametrize("stack", [0, 1])
+def test_free_fermion_greens(oracle_mod, model, stack):
+    O = oracle_mod
+    w = O.Walker(model=model, L=4, U=0.0, mu=-0.3, beta=4.0, Lt=40, pace=10, stack=stack)
+    w.seed(7)
+    w.fields_random()
+    w.init()
+    K = -w.dense(2) + (-0.3) * np.eye(16)
+    g_exact = _exact_G0(w, 4.0, K)
+    for s in (0, 1):
+        assert abs(w.green(s) - g_exact).max() < 1e-12
+    w.sweep_0_to_beta()
+    w.sweep_beta_to_0()
+    for s in (0, 1):
+        assert abs(w.green(s) - g_exact).max() < 1e-12
+    assert w.wrap_error < 1e-12
+
+
+def test_checkerboard_algebra(oracle_mod):
+    O = oracle_mod
+    w = O.Walker(L=4, U=4.0, beta=1.0, Lt=20, pace=5, checkerboard=True)
+    I = np.eye(16)
+    E = w.mult_expK(0, I)
+    np.testing.assert_allclose(w.mult_expK(1, I), E, atol=1e-15)
+    np.testing.assert_allclose(w.mult_expK(4, I), E.T, atol=1e-15)
+    np.testing.assert_allclose(w.mult_expK(2, E), I, atol=1e-13)
+    np.testing.assert_allclose(w.mult_expK(3, E), I, atol=1e-13)
+    # the break-up approximates exp(dtau t H) to O(dtau^2) (mu = 0)
+    dense = O.Walker(L=4, U=4.0, beta=1.0, Lt=20, pace=5, checkerboard=False).dense(0)
+    err = abs(E - dense).max()
+    assert err < 0.05 ** 2 * 2
+    # plaquette in isolation: exp(dtau t h_plaq) for a 2x2 torus-free block
+    assert E.shape == (16, 16)
+
+
+def test_lattice_tables(oracle_mod):
+    w = oracle_mod.Walker(L=6, Lt=4, pace=2)
+    assert w.num_k_stars() == (3 + 1) * (3 + 2) // 2
+    m = w.m_point()
+    for d in range(36):
+        x, y = d % 6, d // 6
+        assert w.fourier(d, m) == pytest.approx((-1.0) ** (x + y), abs=1e-12)
+        assert w.fourier(d, 0) == pytest.approx(1.0)
+    H = w.dense(2)
+    assert (H == H.T).all() and H.sum() == 4 * 36
+
+
+def _chain_product(w, N, Lt, spin):
+    B = np.eye(N)
+    for t in range(1, Lt + 1):
+        B = w.mult_B(0, B, t, spin)  # B(t) . (B(t-1) ... B(1))
+    return B
+
+
+def _rest_product(w, N, Lt, spin):
+    """B(Lt) ... B(2)."""
+    rest = np.eye(N)
+    for t in range(2, Lt + 1):
+        rest = w.mult_B(0, rest, t, spin)
+    return rest
+
+
+def _greens_slice1(w, N, Lt):
+    """Equal-time G at slice 1: (1 + B(1) B(Lt)..B(2))^-1 for both spins."""
+    out = []
+    for spin in (+1, -1):
+        B1 = w.mult_B(0, np.eye(N), 1, spin)
+        out.append(np.linalg.inv(np.eye(N) + B1 @ _rest_product(w, N, Lt, spin)))
+    return out
+
+
+@pytest.mark.parametrize("model", [0, 1])
+def test_ratio_is_determinant_ratio(oracle_mod, model):
+    """get_update_ratio (repulsive_hubbard.cpp:112-124, attractive_hubbard.cpp:112-125)
+    equals the weight ratio: det ratio of (1 + B(1)..B(Lt)) over spins, times
+    exp(2 alpha s) for the attractive decoupling's bosonic factor."""
+    O = oracle_mod
+    N, Lt = 4, 8
+    w = O.Walker(model=model, L=2, U=3.0, mu=0.2, beta=1.0, Lt=Lt, pace=4)
+    w.seed(3)
+    w.fields_random()
+    i = 2
+    f = w.fields()
+    dets = []
+    for flip in (False, True):
+        ff = f.copy()
+        if flip:
+            ff[0, i] *= -1
+        w.set_fields(ff)
+        d = 1.0
+        for spin in (+1, -1):
+            B = w.mult_B(0, np.eye(N), 1, spin) @ _rest_product(w, N, Lt, spin)
+            d *= np.linalg.det(np.eye(N) + B)
+        dets.append(d)
+    w.set_fields(f)
+    g = _greens_slice1(w, N, Lt)
+    for s in (0, 1):
+        w.set_green(s, g[s])
+    expected = dets[1] / dets[0]
+    if model == O.ATTRACTIVE:
+        expected *= np.exp(2 * w.alpha * f[0, i])
+    assert w.ratio(0, i) == pytest.approx(expected, rel=1e-10)
+
+
+@pytest.mark.parametrize("model", [0, 1])
+def test_sherman_morrison_equals_fresh(oracle_mod, model):
+    """update_greens_function (repulsive_hubbard.cpp:127-155) vs recomputation."""
+    O = oracle_mod
+    N, Lt = 4, 6
+    w = O.Walker(model=model, L=2, U=4.0, beta=1.2, Lt=Lt, pace=3)
+    w.seed(11)
+    w.fields_random()
+    f = w.fields()
+    g_old = _greens_slice1(w, N, Lt)
+    for s in (0, 1):
+        w.set_green(s, g_old[s])
+    i = 1
+    w.update_greens(0, i)
+    f2 = f.copy()
+    f2[0, i] *= -1
+    w.set_fields(f2)
+    g_new = _greens_slice1(w, N, Lt)
+    for s in (0, 1):
+        np.testing.assert_allclose(w.green(s), g_new[s], atol=1e-11)
+
+
+def test_udv_factorisations(oracle_mod):
+    O = oracle_mod
+    rng = np.random.default_rng(5)
+    n = 12
+    scales = np.exp(np.linspace(-20, 20, n))
+    A = rng.standard_normal((n, n)) @ np.diag(scales) @ rng.standard_normal((n, n))
+    u, s, v = O.svd(A)
+    assert np.all(np.diff(s) <= 0)
+    np.testing.assert_allclose(u.T @ u, np.eye(n), atol=1e-13)
+    np.testing.assert_allclose(v.T @ v, np.eye(n), atol=1e-13)
+    np.testing.assert_allclose(u @ np.diag(s) @ v.T, A, rtol=0, atol=1e-12 * abs(A).max())
+    U, D, T = O.qrp_udt(A)
+    np.testing.assert_allclose(U.T @ U, np.eye(n), atol=1e-13)
+    np.testing.assert_allclose(U @ np.diag(D) @ T, A, rtol=0, atol=1e-12 * abs(A).max())
+    assert np.all(D > 0)
+    # (1 + U D T)^-1 from the stable assembly, on a spread where numpy's
+    # plain inverse is itself accurate
+    A2 = rng.standard_normal((n, n)) @ np.diag(np.exp(np.linspace(-4, 4, n))) @ rng.standard_normal((n, n))
+    U2, D2, T2 = O.qrp_udt(A2)
+    G = O.greens_from_udv(U2, D2, T2)
+    assert abs(G - np.linalg.inv(np.eye(n) + A2)).max() < 1e-11
+
+
+def test_svd_and_qrp_stacks_agree(oracle_mod):
+    """Reference SVD stack and the device QRP stack give the same walker."""
+    O = oracle_mod
+    ws = []
+    for stack in (O.STACK_SVD, O.STACK_QRP):
+        w = O.Walker(model=0, L=4, U=4.0, beta=4.0, Lt=80, pace=10, stack=stack)
+        w.seed(12345)
+        w.fields_random()
+        w.init()
+        w.trace(True)
+        for _ in range(2):
+            w.sweep_0_to_beta()
+            w.sweep_beta_to_0()
+        ws.append(w)
+    np.testing.assert_array_equal(ws[0].fields(), ws[1].fields())
+    ta, tb = ws[0].trace_get(), ws[1].trace_get()
+    assert ta.shape == tb.shape and ta.shape[0] == 2 * 2 * 8
+    assert abs(ta - tb).max() < 1e-10
+
+
+def _pin_chain(args):
+    import os
+    import sys
+
+    root = args[0]
+    sys.path.insert(0, os.path.join(root, "oracle"))
+    import oracle as O
+
+    O.use_scipy_lapack(True)
+    seed, fields, warm, nbins, binsize = args[1:]
+    w = O.Walker(model=O.ATTRACTIVE, L=8, U=4.0, beta=8.0, Lt=160, pace=10)
+    w.seed(seed)
+    w.set_fields(fields)
+    w.init()
+    for _ in range(warm):
+        w.sweep_0_to_beta()
+        w.sweep_beta_to_0()
+    bins = []
+    for _ in range(nbins):
+        for _ in range(binsize):
+            w.sweep_0_to_beta()
+            w.measure()
+            w.sweep_beta_to_0()
+            w.measure()
+        bins.append(w.write_bin())
+    return np.array(bins), w.wrap_error
+
+
+@pytest.mark.slow
+def test_statistical_pin_against_reference_example(oracle_mod, example_fixture):
+    """Oracle vs example/log.out:44-55 (attractive 8x8, beta=8, from fields.out)."""
+    import os
+
+    O = oracle_mod
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    jobs = [(root, 500 + k, example_fixture["fields"], 6, 3, 12) for k in range(8)]
+    with mp.get_context("spawn").Pool(8) as pool:
+        res = pool.map(_pin_chain, jobs)
+    bins = np.concatenate([r[0] for r in res])
+    mean, err = O.analyse(bins)
+    for k, name in enumerate(O.OBS_NAMES):
+        ref, ref_err = example_fixture["observables"][name]
+        sigma = np.hypot(err[k], ref_err)
+        if sigma == 0:
+            assert mean[k] == pytest.approx(ref)
+        else:
+            # bins of one chain are autocorrelated, so allow 4 combined sigma
+            assert abs(mean[k] - ref) < 4 * sigma, (name, mean[k], err[k], ref, ref_err)
+    wrap = max(r[1] for r in res)
+    assert 1e-11 < wrap < 1e-6  # published maximum wrap error 1.085e-8
