@@ -1,0 +1,342 @@
+#!/usr/bin/env python
+"""bench.py — HS-field updates/s of the DQMC sweep on GB300.
+
+Metric (the reference's sweep counting, src/dqmc.cpp:88-92): HS-field update
+attempts per second = walkers * N * Lt / half-sweep time.  One step = one
+half-sweep (alternating 0->beta and beta->0) of every walker, equal-time
+measurement fused.  Default workload: 256 independent FP64 walkers, repulsive
+Hubbard 8x8 (N=64), t=1, U=4, mu=0, beta=8, dtau=0.05 (Lt=160), checkerboard
+exp(-dtau K), stabilization every 10 slices, seeded +/-1 fields.
+
+Legs printed on one JSON line:
+  value        device-timed throughput (CUDA events on the library's stream,
+               inputs resident in HBM, Philox uniforms on the device)
+  e2e          the same metric through the C-ABI in reference-RNG mode: the
+               host draws each walker's minstd_rand0 uniforms, copies them in
+               (pinned -> HBM), runs the half-sweep and reads every walker's
+               observable accumulators back, all inside the timed region
+  roofline     the dominant kernel class, timed with CUDA events in the timed
+               region, against the FP64 FMA rate measured on this device
+  cpu_baseline the CPU oracle (reference algorithm restated, scipy LAPACK),
+               one walker per host core, on a bounded sample
+
+--impl reference times only the CPU restatement of the reference (all host
+cores), with the same metric and workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import multiprocessing as mp
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "dqmc-framework_gb300"))
+
+WORKLOADS = {
+    # batch of 256 FP64 walkers, checkerboard (the batched FP64 configuration)
+    "fp64_batch_8x8_checkerboard": dict(walkers=256, model=0, L=8, U=4.0, mu=0.0, beta=8.0, Lt=160, pace=10,
+                                         checkerboard=True),
+    # one FP64 walker, 4x4 dense (the reference's single-chain case)
+    "fp64_single_4x4_dense": dict(walkers=1, model=0, L=4, U=4.0, mu=0.0, beta=4.0, Lt=80, pace=10,
+                                  checkerboard=False),
+}
+DEFAULT_WORKLOAD = "fp64_batch_8x8_checkerboard"
+METRIC = "HS-field updates/s (walkers*N*Lt / half-sweep time)"
+
+
+def _descs(dq, wl, seed0=1000):
+    return [dq.WalkerDesc(model=wl["model"], L=wl["L"], U=wl["U"], mu=wl["mu"], beta=wl["beta"], Lt=wl["Lt"],
+                          pace=wl["pace"], checkerboard=wl["checkerboard"], seed=seed0 + w)
+            for w in range(wl["walkers"])]
+
+
+# ----------------------------------------------------------------------------
+# CPU leg (oracle).  Run in spawned processes: one walker per core.
+# ----------------------------------------------------------------------------
+def _cpu_walker(args):
+    wl, seed, budget_s = args
+    os.environ.setdefault("OPENBLAS_NUM_THREADS", "1")
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+
+    O.use_scipy_lapack(True)
+    w = O.Walker(model=wl["model"], L=wl["L"], U=wl["U"], mu=wl["mu"], beta=wl["beta"], Lt=wl["Lt"],
+                 pace=wl["pace"], checkerboard=wl["checkerboard"], stack=O.STACK_SVD, record=True)
+    w.seed(seed)
+    w.fields_random()
+    w.init()
+    w.sweep_0_to_beta()  # warm-up half-sweep
+    n, t0 = 0, time.perf_counter()
+    while True:
+        if n % 2 == 0:
+            w.sweep_beta_to_0()
+        else:
+            w.sweep_0_to_beta()
+        w.measure()
+        n += 1
+        el = time.perf_counter() - t0
+        if el >= budget_s or n >= 200:
+            break
+    return n, el
+
+
+def cpu_baseline(wl, budget_s=12.0):
+    cores = os.cpu_count() or 1
+    os.environ["OPENBLAS_NUM_THREADS"] = "1"
+    ctx = mp.get_context("spawn")
+    t0 = time.perf_counter()
+    with ctx.Pool(cores) as pool:
+        res = pool.map(_cpu_walker, [(wl, 5000 + c, budget_s) for c in range(cores)])
+    wall = time.perf_counter() - t0
+    upd = wl["L"] ** 2 * wl["Lt"]
+    per_core = [n * upd / el for n, el in res]
+    agg = sum(per_core)
+    sample = (f"{cores} independent oracle walkers (reference SVD-stack algorithm, scipy LAPACK, "
+              f"1 thread each), {min(n for n, _ in res)}-{max(n for n, _ in res)} measured half-sweeps "
+              f"each of {wl['L']}x{wl['L']}, Lt={wl['Lt']}, {budget_s:.0f} s budget; wall {wall:.1f} s")
+    return {"value": agg, "unit": "updates/s", "cores": cores, "kind": "port", "sample": sample,
+            "per_core": statistics.mean(per_core)}
+
+
+# ----------------------------------------------------------------------------
+# clocks during the timed region
+# ----------------------------------------------------------------------------
+class Clocks:
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.idx = gpu_index
+        self.p = None
+        self.path = None
+
+    def start(self):
+        try:
+            os.makedirs(os.path.join(ROOT, "gpurun_out"), exist_ok=True)
+            self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+            self.f = open(self.path, "w")
+            self.p = subprocess.Popen(["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.Q}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+
+    def stop(self):
+        if not self.p:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except Exception:
+            self.p.kill()
+        self.f.close()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ----------------------------------------------------------------------------
+# algorithmic work (per walker per half-sweep), the survey's figure F
+# ----------------------------------------------------------------------------
+def flops_model(wl, accepts_per_walker_per_half):
+    N, Lt, p = wl["L"] ** 2, wl["Lt"], wl["pace"]
+    S = 1 if wl["model"] == 1 else 2
+    ns = -(-Lt // p)
+    if wl["checkerboard"]:
+        W, C = 34 * N * N, 17 * N * N
+    else:
+        W, C = 4 * N ** 3 + 2 * N * N, 2 * N ** 3 + N * N
+    seg = S * Lt * (W + C) + S * accepts_per_walker_per_half * 2 * N * N
+    # stabilization counted as executed by this path (column-pivoted QR):
+    # push = QR 4/3 N^3 + forming Q 4/3 N^3 + triangular T F_prev N^3;
+    # greens = U_L^T U_R, F_L F_R^T (4 N^3) + LU 2/3 N^3 + solve 2 N^3 + final GEMM 2 N^3
+    push = S * ns * (8.0 / 3.0 + 1.0) * N ** 3
+    greens = S * ns * (4.0 + 2.0 / 3.0 + 2.0 + 2.0) * N ** 3
+    nominal = S * Lt * (W + C) + S * accepts_per_walker_per_half * 2 * N * N + S * ns * 33 * N ** 3
+    return {"segment": seg, "push": push, "greens": greens, "nominal_F": nominal}
+
+
+def run_gpu(args, wl, rank, world):
+    import torch
+
+    import dqmc_gb300 as dq
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=dev)
+    fp64_peak = dq.microbench_fp64()
+
+    descs = _descs(dq, wl, seed0=1000 + 100000 * rank)
+    batch = dq.Batch(descs, rng=dq.RNG_PHILOX)
+    # a dedicated stream: the library launches on it and the CUDA events below
+    # are recorded on it (torch's default stream would be handle 0)
+    stream = torch.cuda.Stream(device=dev)
+    torch.cuda.set_stream(stream)
+    batch.set_stream(stream.cuda_stream)
+    for w in range(len(descs)):
+        batch.fields_random(w)
+    batch.init_greens()
+    upd = batch.updates_per_half_sweep()
+
+    def step(k, b=batch):
+        if k % 2 == 0:
+            b.sweep_0_to_beta(measure=True)
+        else:
+            b.sweep_beta_to_0(measure=True)
+
+    for k in range(args.warmup):
+        step(k)
+    acc0 = sum(batch.accept_count(w) for w in range(len(descs)))
+    batch.profile_enable(True)
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+
+            dist.barrier()
+
+    clocks = Clocks(local)
+    barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for k in range(args.steps):
+        step(args.warmup + k)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1)
+    prof = batch.profile_read()
+    batch.profile_enable(False)
+    acc1 = sum(batch.accept_count(w) for w in range(len(descs)))
+    status = [batch.status(w) for w in range(len(descs))]
+    if world > 1:
+        import torch.distributed as dist
+
+        t = torch.tensor([ms], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * upd * args.steps / (ms * 1e-3)
+
+    # ---- roofline of the dominant kernel class
+    acc_per_walker_half = (acc1 - acc0) / len(descs) / args.steps
+    fm = flops_model(wl, acc_per_walker_half)
+    dom = max(["segment", "push", "greens"], key=lambda k: prof[k][0])
+    dom_ms, dom_n = prof[dom]
+    flops_per_launch = fm[dom] * len(descs) * args.steps / max(dom_n, 1)
+    avg_ms = dom_ms / max(dom_n, 1)
+    achieved = flops_per_launch / (avg_ms * 1e-3) / 1e12
+    roofline = {"bound": "fp64", "kernel": f"{dom}_kernel", "achieved": achieved, "peak": fp64_peak / 1e3,
+                "unit": "TFLOP/s", "frac": achieved / (fp64_peak / 1e3), "traffic": None,
+                "peak_source": "FP64 FMA probe measured in this run (dqmc_microbench_fp64); "
+                               "MEASURED_PEAKS.json holds no FP64 figure",
+                "avg_launch_ms": avg_ms,
+                "kernel_share": {k: prof[k][0] / ms for k in prof},
+                "sweep_nominal_F_tflops": fm["nominal_F"] * len(descs) * args.steps / (ms * 1e-3) / 1e12}
+    launches = sum(n for _, n in prof.values())
+
+    # ---- e2e: reference RNG on the host, copies in and out every step
+    e2e = None
+    if rank == 0 or world > 1:
+        eb = dq.Batch(descs, rng=dq.RNG_MINSTD)
+        eb.set_stream(stream.cuda_stream)
+        for w in range(len(descs)):
+            eb.fields_random(w)
+        eb.init_greens()
+        for k in range(max(1, min(args.warmup, 3))):
+            step(k, eb)
+        torch.cuda.synchronize()
+        barrier()
+        t0 = time.perf_counter()
+        ek = max(2, min(args.steps, 10))
+        for k in range(ek):
+            step(k, eb)
+            sums, counts = eb.observables_all()
+        el = time.perf_counter() - t0
+        barrier()
+        e2e = {"value": world * upd * ek / el, "unit": "updates/s",
+               "h2d_bytes_per_step": 8 * upd, "d2h_bytes_per_step": int(sums.nbytes + counts.nbytes),
+               "steps": ek, "rng": "host minstd_rand0 (reference stream)"}
+        eb.close()
+    return dict(value=value, ms=ms, roofline=roofline, e2e=e2e, clocks=clk, launches=launches, status=status,
+                accept_rate=acc_per_walker_half / (wl["L"] ** 2 * wl["Lt"]), fp64_peak=fp64_peak)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=4)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
+    ap.add_argument("--cpu-budget", type=float, default=12.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    wl = WORKLOADS[args.workload]
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    config = {"workload": args.workload, "walkers_per_gpu": wl["walkers"], "model": "repulsive" if wl["model"] == 0 else "attractive",
+              "L": wl["L"], "N": wl["L"] ** 2, "U": wl["U"], "mu": wl["mu"], "beta": wl["beta"], "Lt": wl["Lt"],
+              "pace": wl["pace"], "expK": "checkerboard" if wl["checkerboard"] else "dense",
+              "measure": "equal-time, fused", "parallelism": f"replicas x{args.gpus}",
+              "l2": "no flush: per-GPU working set (G, chains, UDT stacks) > 1 GB, larger than L2"}
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        cb = cpu_baseline(wl, budget_s=max(4.0, args.cpu_budget))
+        steps = args.steps
+        line = {"metric": METRIC, "value": cb["value"], "unit": "updates/s", "n_gpus": args.gpus, "steps": steps,
+                "warmup": args.warmup, "ms_per_step": wl["walkers"] * wl["L"] ** 2 * wl["Lt"] / cb["value"] * 1e3,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic (seeded +/-1 fields)", "config": config, "impl": "reference",
+                "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
+                "e2e": {"value": cb["value"], "unit": "updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        line["cpu_baseline"]["kind"] = "port"
+        print(json.dumps(line))
+        return
+
+    r = run_gpu(args, wl, rank, world)
+    if rank != 0:
+        return
+    cb = None
+    if world == 1 and not args.no_cpu:
+        cb = cpu_baseline(wl, budget_s=args.cpu_budget)
+        cb = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
+    line = {"metric": METRIC, "value": r["value"], "unit": "updates/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": r["ms"] / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded +/-1 fields)",
+            "config": config, "roofline": r["roofline"], "cpu_baseline": cb, "e2e": r["e2e"],
+            "gpu_launches": r["launches"], "clocks": r["clocks"], "accept_rate": r["accept_rate"],
+            "walker_status_nonzero": sum(1 for s in r["status"] if s)}
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,680 @@
+// batch.cu — C-ABI implementation: batch arena, per-walker constants,
+// parity-mode uniform streams and the half-sweep schedule.
+//
+// Schedule of one half-sweep (src/dqmc_walker.cpp:246-412), for step
+// j = 0 .. nstack-1 of every walker:
+//   segment kernel   slices of stabilization interval j (wrap, Metropolis,
+//                    measurement, B-chain started from the pushed stack's top)
+//   push kernel      stack push of the chain (QRP), right/left pop implicit
+//   greens kernel    fresh G from both stacks, wrap error, trace
+//   measure kernel   forward: the slice closing interval j;
+//                    backward: slot Lt-1 after the final stabilization
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <random>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "../../include/dqmc_gb300.h"
+#include "dqmc_device.cuh"
+
+namespace dqmc {
+cudaError_t configure_fp64_kernels(int maxN);
+void launch_segment(int mode, const WalkerDev* W, int nw, int j, int measure, int maxN, cudaStream_t st);
+void launch_push(int mode, const WalkerDev* W, int nw, int j, int maxN, cudaStream_t st);
+void launch_greens(int mode, const WalkerDev* W, int nw, int j, int check, int trace_slot, int maxN, cudaStream_t st);
+void launch_measure(int mode, const WalkerDev* W, int nw, int j, int maxN, cudaStream_t st);
+void launch_sign(const WalkerDev* W, int nw, int maxN, cudaStream_t st);
+double run_fp64_probe(cudaError_t* err);
+}  // namespace dqmc
+
+using namespace dqmc;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return code;
+}
+
+#define CUDA_TRY(expr)                                                                  \
+  do {                                                                                  \
+    cudaError_t e_ = (expr);                                                            \
+    if (e_ != cudaSuccess) return fail(DQMC_ERR_CUDA, "%s: %s", #expr, cudaGetErrorString(e_)); \
+  } while (0)
+
+// exp(x K) for symmetric K by cyclic Jacobi diagonalisation (host, once per batch).
+std::vector<double> sym_exp(int n, std::vector<double> a, double x) {
+  auto A = [&](int r, int c) -> double& { return a[(size_t)c * n + r]; };
+  std::vector<double> v((size_t)n * n, 0.0);
+  auto V = [&](int r, int c) -> double& { return v[(size_t)c * n + r]; };
+  for (int i = 0; i < n; ++i) V(i, i) = 1.0;
+  for (int sweep = 0; sweep < 100; ++sweep) {
+    double off = 0, dg = 0;
+    for (int c = 0; c < n; ++c)
+      for (int r = 0; r < n; ++r) (r == c ? dg : off) += A(r, c) * A(r, c);
+    if (off == 0.0 || off <= 1e-32 * (dg + off)) break;
+    for (int p = 0; p < n - 1; ++p)
+      for (int q = p + 1; q < n; ++q) {
+        const double apq = A(p, q);
+        if (apq == 0.0) continue;
+        const double th = (A(q, q) - A(p, p)) / (2 * apq);
+        const double t = (th >= 0 ? 1.0 : -1.0) / (std::fabs(th) + std::sqrt(th * th + 1));
+        const double c = 1 / std::sqrt(t * t + 1), s = t * c;
+        for (int k = 0; k < n; ++k) {
+          const double x1 = A(k, p), x2 = A(k, q);
+          A(k, p) = c * x1 - s * x2;
+          A(k, q) = s * x1 + c * x2;
+        }
+        for (int k = 0; k < n; ++k) {
+          const double x1 = A(p, k), x2 = A(q, k);
+          A(p, k) = c * x1 - s * x2;
+          A(q, k) = s * x1 + c * x2;
+        }
+        for (int k = 0; k < n; ++k) {
+          const double x1 = V(k, p), x2 = V(k, q);
+          V(k, p) = c * x1 - s * x2;
+          V(k, q) = s * x1 + c * x2;
+        }
+      }
+  }
+  std::vector<double> out((size_t)n * n, 0.0);
+  for (int m = 0; m < n; ++m) {
+    const double e = std::exp(x * A(m, m));
+    for (int c = 0; c < n; ++c) {
+      const double vc = V(c, m) * e;
+      for (int r = 0; r < n; ++r) out[(size_t)c * n + r] += V(r, m) * vc;
+    }
+  }
+  return out;
+}
+
+// K = -t H + mu I on the periodic square lattice (src/lattice/square.cpp:164-177,
+// with the hopping matrix zero-initialised).
+std::vector<double> kinetic_matrix(int L, double t, double mu) {
+  const int N = L * L;
+  std::vector<double> K((size_t)N * N, 0.0);
+  for (int i = 0; i < N; ++i) {
+    const int x = i % L, y = i / L;
+    const int jx = (x + 1) % L + L * y, jy = x + L * ((y + 1) % L);
+    for (int j : {jx, jy}) {
+      K[(size_t)j * N + i] += -t;
+      K[(size_t)i * N + j] += -t;
+    }
+  }
+  for (int i = 0; i < N; ++i) K[(size_t)i * N + i] += mu;
+  return K;
+}
+
+// Fourier factors cos(-r.k) per displacement index for k-star kidx
+// (src/lattice/square.cpp:42-66, 148-161).
+std::vector<double> fourier_table(int L, int kidx) {
+  std::vector<double> kx, ky;
+  for (int i = (L + 1) / 2; i <= L; ++i)
+    for (int j = (L + 1) / 2; j <= i; ++j) {
+      kx.push_back((double)i / L * 2 * M_PI - M_PI);
+      ky.push_back((double)j / L * 2 * M_PI - M_PI);
+    }
+  const int nk = (int)kx.size();
+  if (kidx < 0) kidx = nk - 1;  // M point
+  std::vector<double> f((size_t)L * L);
+  for (int d = 0; d < L * L; ++d) {
+    const int x = d % L, y = d / L;
+    f[d] = std::cos(-x * kx[kidx] - y * ky[kidx]);
+  }
+  return f;
+}
+
+size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+}  // namespace
+
+struct dqmc_batch {
+  int nw = 0, maxN = 0, maxNs = 0, maxLt = 0;
+  dqmc_batch_options opt{};
+  std::vector<dqmc_walker_desc> desc;
+  std::vector<WalkerDev> hw;        // host copies of the descriptors
+  WalkerDev* dW = nullptr;          // device descriptors
+  char* arena = nullptr;
+  size_t arena_bytes = 0;
+  cudaStream_t own = nullptr, stream = nullptr;
+  std::vector<std::minstd_rand0> eng;
+  double* h_uni = nullptr;          // pinned [nw][maxLt*maxN]
+  double* d_uni = nullptr;
+  size_t uni_stride = 0;
+  bool initialised = false;
+  unsigned long long sweep_id = 0;
+  int trace_count = 0, trace_cap = 0;
+  // per-walker device scalars
+  struct Scal {
+    double sign, sign_Lt;
+    unsigned long long wrap_bits;
+    long long accepts;
+    int status, pad;
+    double obs[kNumObs];
+    long long obs_cnt[kNumObs];
+  };
+  Scal* d_scal = nullptr;
+  // kernel-class profiling: event pairs recorded around launches
+  bool prof = false;
+  struct Mark { int cls; cudaEvent_t a, b; };
+  std::vector<Mark> marks;
+  std::vector<cudaEvent_t> pool;
+  double prof_ms[DQMC_NUM_KCLASS] = {0, 0, 0, 0};
+  int64_t prof_n[DQMC_NUM_KCLASS] = {0, 0, 0, 0};
+  cudaEvent_t ev() {
+    if (pool.empty()) {
+      cudaEvent_t e;
+      cudaEventCreate(&e);
+      return e;
+    }
+    cudaEvent_t e = pool.back();
+    pool.pop_back();
+    return e;
+  }
+  template <class F>
+  void timed(int cls, F launch) {
+    if (!prof) { launch(); return; }
+    Mark m{cls, ev(), ev()};
+    cudaEventRecord(m.a, stream);
+    launch();
+    cudaEventRecord(m.b, stream);
+    marks.push_back(m);
+  }
+  void collect() {
+    for (auto& m : marks) {
+      float ms = 0;
+      cudaEventSynchronize(m.b);
+      cudaEventElapsedTime(&ms, m.a, m.b);
+      prof_ms[m.cls] += ms;
+      prof_n[m.cls] += 1;
+      pool.push_back(m.a);
+      pool.push_back(m.b);
+    }
+    marks.clear();
+  }
+};
+
+extern "C" {
+
+const char* dqmc_last_error(void) { return g_err.c_str(); }
+int dqmc_abi_version(void) { return DQMC_ABI_VERSION; }
+
+int dqmc_batch_create(const dqmc_walker_desc* descs, int n, const dqmc_batch_options* opt, dqmc_batch** out) {
+  if (!descs || n <= 0 || !out) return fail(DQMC_ERR_ARG, "dqmc_batch_create: null argument or n_walkers <= 0");
+  *out = nullptr;
+  dqmc_batch_options o{};
+  if (opt) o = *opt;
+  if (o.rng != DQMC_RNG_MINSTD && o.rng != DQMC_RNG_PHILOX) return fail(DQMC_ERR_ARG, "unknown rng mode %d", o.rng);
+  if (o.precision != DQMC_FP64) return fail(DQMC_ERR_ARG, "unknown precision mode %d", o.precision);
+  for (int w = 0; w < n; ++w) {
+    const auto& d = descs[w];
+    if (d.model != DQMC_REPULSIVE_HUBBARD && d.model != DQMC_ATTRACTIVE_HUBBARD)
+      return fail(DQMC_ERR_ARG, "walker %d: unknown model %d", w, d.model);
+    if (d.L < 2) return fail(DQMC_ERR_ARG, "walker %d: lattice side %d < 2", w, d.L);
+    if (d.L * d.L > kMaxSmemN) return fail(DQMC_ERR_ARG, "walker %d: N = %d exceeds the supported %d", w, d.L * d.L, kMaxSmemN);
+    if (d.checkerboard && (d.L % 2)) return fail(DQMC_ERR_ARG, "walker %d: checkerboard needs an even side", w);
+    if (d.Lt < 1 || d.pace < 1) return fail(DQMC_ERR_ARG, "walker %d: Lt and pace must be >= 1", w);
+    if (!(d.beta > 0) || !(d.onsite_u >= 0) || !(d.hopping_t >= 0))
+      return fail(DQMC_ERR_ARG, "walker %d: need beta > 0, U >= 0, t >= 0", w);
+    const int nk = (d.L / 2 + 1) * (d.L / 2 + 2) / 2;
+    if (d.momentum_index >= nk) return fail(DQMC_ERR_ARG, "walker %d: momentum index out of range", w);
+  }
+  int dev_count = 0;
+  if (cudaGetDeviceCount(&dev_count) != cudaSuccess || dev_count == 0)
+    return fail(DQMC_ERR_CUDA, "no CUDA device available");
+
+  auto* b = new dqmc_batch();
+  b->nw = n;
+  b->opt = o;
+  b->desc.assign(descs, descs + n);
+  for (auto& d : b->desc) {
+    b->maxN = std::max(b->maxN, d.L * d.L);
+    const int ns = (d.Lt % d.pace == 0) ? d.Lt / d.pace : d.Lt / d.pace + 1;
+    b->maxNs = std::max(b->maxNs, ns);
+    b->maxLt = std::max(b->maxLt, d.Lt);
+  }
+  b->trace_cap = o.trace ? 4 * b->maxNs : 0;
+
+  // ---- arena layout ----
+  struct Off { size_t G, chain, stack, fields, ff, trace; int dense_id; };
+  std::vector<Off> off(n);
+  std::map<std::tuple<int, double, double, double>, int> dense_ids;  // (L, t, mu, dtau) -> id
+  std::vector<std::pair<std::vector<double>, std::vector<double>>> dense;
+  std::map<std::pair<int, int>, size_t> ff_off;
+  size_t cur = 0;
+  auto take = [&](size_t bytes) { size_t o2 = cur; cur = align256(cur + bytes); return o2; };
+  const size_t scal_off = take(sizeof(dqmc_batch::Scal) * n);
+  const size_t desc_off = take(sizeof(WalkerDev) * n);
+  for (int w = 0; w < n; ++w) {
+    const auto& d = b->desc[w];
+    const int N = d.L * d.L;
+    const int S = (d.model == DQMC_ATTRACTIVE_HUBBARD) ? 1 : 2;
+    const int ns = (d.Lt % d.pace == 0) ? d.Lt / d.pace : d.Lt / d.pace + 1;
+    const size_t lvl = (2 * (size_t)N * N + N + 31) & ~(size_t)31;
+    off[w].G = take(sizeof(double) * 2 * N * N);
+    off[w].chain = take(sizeof(double) * S * N * N);
+    off[w].stack = take(sizeof(double) * 2 * S * ns * lvl);
+    off[w].fields = take((size_t)d.Lt * N);
+    off[w].trace = b->trace_cap ? take(sizeof(double) * (size_t)b->trace_cap * 2 * N * N) : 0;
+    off[w].dense_id = -1;
+    if (!d.checkerboard) {
+      auto key = std::make_tuple(d.L, d.hopping_t, d.mu, d.beta / d.Lt);
+      auto it = dense_ids.find(key);
+      if (it == dense_ids.end()) {
+        const auto K = kinetic_matrix(d.L, d.hopping_t, d.mu);
+        const double dt = d.beta / d.Lt;
+        dense.push_back({sym_exp(N, K, -dt), sym_exp(N, K, +dt)});
+        it = dense_ids.emplace(key, (int)dense.size() - 1).first;
+      }
+      off[w].dense_id = it->second;
+    }
+    auto fk = std::make_pair(d.L, d.momentum_index < 0 ? -1 : d.momentum_index);
+    if (!ff_off.count(fk)) ff_off[fk] = take(sizeof(double) * N);
+    off[w].ff = ff_off[fk];
+  }
+  std::vector<size_t> dense_off(dense.size());
+  for (size_t i = 0; i < dense.size(); ++i) {
+    const size_t nn = dense[i].first.size();
+    dense_off[i] = take(sizeof(double) * 2 * nn);
+  }
+  b->uni_stride = (size_t)b->maxLt * b->maxN;
+  const size_t uni_off = (o.rng == DQMC_RNG_MINSTD) ? take(sizeof(double) * b->uni_stride * n) : 0;
+  b->arena_bytes = cur;
+
+  cudaError_t e = cudaMalloc(&b->arena, b->arena_bytes);
+  if (e != cudaSuccess) {
+    delete b;
+    return fail(DQMC_ERR_CUDA, "cudaMalloc(%zu bytes): %s", cur, cudaGetErrorString(e));
+  }
+  e = cudaStreamCreateWithFlags(&b->own, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = configure_fp64_kernels(kMaxSmemN);
+  if (e != cudaSuccess) {
+    cudaFree(b->arena);
+    delete b;
+    return fail(DQMC_ERR_CUDA, "stream/kernel set-up: %s", cudaGetErrorString(e));
+  }
+  b->stream = b->own;
+  cudaMemsetAsync(b->arena, 0, b->arena_bytes, b->stream);
+
+  char* base = b->arena;
+  b->d_scal = reinterpret_cast<dqmc_batch::Scal*>(base + scal_off);
+  b->dW = reinterpret_cast<WalkerDev*>(base + desc_off);
+  if (o.rng == DQMC_RNG_MINSTD) {
+    b->d_uni = reinterpret_cast<double*>(base + uni_off);
+    cudaMallocHost(&b->h_uni, sizeof(double) * b->uni_stride * n);
+  }
+  // upload dense matrices and Fourier tables
+  for (size_t i = 0; i < dense.size(); ++i) {
+    const size_t nn = dense[i].first.size();
+    cudaMemcpyAsync(base + dense_off[i], dense[i].first.data(), sizeof(double) * nn, cudaMemcpyHostToDevice, b->stream);
+    cudaMemcpyAsync(base + dense_off[i] + sizeof(double) * nn, dense[i].second.data(), sizeof(double) * nn,
+                    cudaMemcpyHostToDevice, b->stream);
+  }
+  std::vector<std::vector<double>> fftabs;
+  for (auto& kv : ff_off) {
+    fftabs.push_back(fourier_table(kv.first.first, kv.first.second));
+    cudaMemcpyAsync(base + kv.second, fftabs.back().data(), sizeof(double) * fftabs.back().size(),
+                    cudaMemcpyHostToDevice, b->stream);
+  }
+
+  b->hw.resize(n);
+  b->eng.resize(n);
+  std::vector<dqmc_batch::Scal> scal(n);
+  for (int w = 0; w < n; ++w) {
+    const auto& d = b->desc[w];
+    WalkerDev& h = b->hw[w];
+    std::memset(&h, 0, sizeof h);
+    const int N = d.L * d.L;
+    h.N = N;
+    h.L = d.L;
+    h.Lt = d.Lt;
+    h.pace = d.pace;
+    h.nstack = (d.Lt % d.pace == 0) ? d.Lt / d.pace : d.Lt / d.pace + 1;
+    h.S = (d.model == DQMC_ATTRACTIVE_HUBBARD) ? 1 : 2;
+    h.model = d.model;
+    h.cb = d.checkerboard;
+    h.rng = o.rng;
+    h.hop_t = d.hopping_t;
+    const double dtau = d.beta / d.Lt;
+    const double alpha = std::acosh(std::exp(0.5 * dtau * d.onsite_u));  // repulsive_hubbard.cpp:50
+    // exactly the exponentials the reference evaluates, s = +1 and s = -1
+    h.e_pa = std::exp(+1.0 * alpha * 1.0);
+    h.e_ma = std::exp(-1.0 * alpha * 1.0);
+    for (int si = 0; si < 2; ++si) {
+      const double s = si == 0 ? 1.0 : -1.0;
+      h.cm[si] = std::exp(-2 * alpha * s) - 1;
+      h.cp[si] = std::exp(+2 * alpha * s) - 1;
+      h.ex2[si] = std::exp(2 * alpha * s);
+    }
+    auto plaq = [](double* m, double ch, double sh, double f) {
+      const double v[16] = {ch * ch, ch * sh, ch * sh, sh * sh, ch * sh, ch * ch, sh * sh, ch * sh,
+                            ch * sh, sh * sh, ch * ch, ch * sh, sh * sh, ch * sh, ch * sh, ch * ch};
+      for (int k = 0; k < 16; ++k) m[k] = f * v[k];
+    };
+    // checkerboard/square.cpp:34-49 (note its exp(+0.5 dtau mu) sign)
+    plaq(h.cbP, std::cosh(dtau * d.hopping_t), std::sinh(dtau * d.hopping_t), std::exp(0.5 * dtau * d.mu));
+    plaq(h.cbI, std::cosh(-dtau * d.hopping_t), std::sinh(-dtau * d.hopping_t), std::exp(-0.5 * dtau * d.mu));
+    h.G = reinterpret_cast<double*>(base + off[w].G);
+    h.chain = reinterpret_cast<double*>(base + off[w].chain);
+    h.stack = reinterpret_cast<double*>(base + off[w].stack);
+    h.lvl_stride = (long long)((2 * (size_t)N * N + N + 31) & ~(size_t)31);
+    h.side_stride = (long long)h.S * h.nstack * h.lvl_stride;
+    h.fields = reinterpret_cast<int8_t*>(base + off[w].fields);
+    if (off[w].dense_id >= 0) {
+      h.expK = reinterpret_cast<const double*>(base + dense_off[off[w].dense_id]);
+      h.invK = h.expK + (size_t)N * N;
+    }
+    h.ff = reinterpret_cast<const double*>(base + off[w].ff);
+    dqmc_batch::Scal* sc = b->d_scal + w;
+    h.obs = sc->obs;
+    h.obs_cnt = sc->obs_cnt;
+    h.sign = &sc->sign;
+    h.sign_Lt = &sc->sign_Lt;
+    h.wrap_bits = &sc->wrap_bits;
+    h.accepts = &sc->accepts;
+    h.status = &sc->status;
+    h.uni = b->d_uni ? b->d_uni + b->uni_stride * w : nullptr;
+    h.seed = d.seed;
+    h.trace = b->trace_cap ? reinterpret_cast<double*>(base + off[w].trace) : nullptr;
+    h.trace_cap = b->trace_cap;
+    b->eng[w].seed((unsigned)d.seed);
+    std::memset(&scal[w], 0, sizeof scal[w]);
+    scal[w].sign = 1.0;
+    // fields default to +1 until set
+    std::vector<int8_t> ones((size_t)d.Lt * N, 1);
+    cudaMemcpyAsync(h.fields, ones.data(), ones.size(), cudaMemcpyHostToDevice, b->stream);
+    cudaStreamSynchronize(b->stream);
+  }
+  cudaMemcpyAsync(b->d_scal, scal.data(), sizeof(dqmc_batch::Scal) * n, cudaMemcpyHostToDevice, b->stream);
+  cudaMemcpyAsync(b->dW, b->hw.data(), sizeof(WalkerDev) * n, cudaMemcpyHostToDevice, b->stream);
+  e = cudaStreamSynchronize(b->stream);
+  if (e != cudaSuccess) {
+    dqmc_batch_destroy(b);
+    return fail(DQMC_ERR_CUDA, "batch upload: %s", cudaGetErrorString(e));
+  }
+  *out = b;
+  return DQMC_OK;
+}
+
+int dqmc_batch_destroy(dqmc_batch* b) {
+  if (!b) return DQMC_OK;
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  b->collect();
+  for (auto e : b->pool) cudaEventDestroy(e);
+  if (b->h_uni) cudaFreeHost(b->h_uni);
+  if (b->arena) cudaFree(b->arena);
+  if (b->own) cudaStreamDestroy(b->own);
+  delete b;
+  return DQMC_OK;
+}
+
+int dqmc_set_stream(dqmc_batch* b, void* s) {
+  if (!b) return fail(DQMC_ERR_ARG, "null batch");
+  CUDA_TRY(cudaStreamSynchronize(b->stream));
+  b->stream = s ? static_cast<cudaStream_t>(s) : b->own;
+  return DQMC_OK;
+}
+
+int dqmc_synchronize(dqmc_batch* b) {
+  if (!b) return fail(DQMC_ERR_ARG, "null batch");
+  CUDA_TRY(cudaStreamSynchronize(b->stream));
+  return DQMC_OK;
+}
+
+static int check_walker(dqmc_batch* b, int w) {
+  if (!b) return fail(DQMC_ERR_ARG, "null batch");
+  if (w < 0 || w >= b->nw) return fail(DQMC_ERR_ARG, "walker index %d out of range [0,%d)", w, b->nw);
+  return DQMC_OK;
+}
+
+int dqmc_fields_random(dqmc_batch* b, int w) {
+  if (int r = check_walker(b, w)) return r;
+  const auto& d = b->desc[w];
+  const int N = d.L * d.L;
+  std::vector<int8_t> f((size_t)d.Lt * N);
+  for (int t = 0; t < d.Lt; ++t)
+    for (int i = 0; i < N; ++i)  // bernoulli(0.5): u < 0.5 -> +1 (repulsive_hubbard.cpp:92-97)
+      f[(size_t)t * N + i] = (std::generate_canonical<double, 53>(b->eng[w]) < 0.5) ? 1 : -1;
+  CUDA_TRY(cudaMemcpyAsync(b->hw[w].fields, f.data(), f.size(), cudaMemcpyHostToDevice, b->stream));
+  CUDA_TRY(cudaStreamSynchronize(b->stream));
+  b->initialised = false;
+  return DQMC_OK;
+}
+
+int dqmc_set_fields(dqmc_batch* b, int w, const int8_t* f) {
+  if (int r = check_walker(b, w)) return r;
+  if (!f) return fail(DQMC_ERR_ARG, "null fields");
+  const auto& d = b->desc[w];
+  const size_t n = (size_t)d.Lt * d.L * d.L;
+  for (size_t k = 0; k < n; ++k)
+    if (f[k] != 1 && f[k] != -1) return fail(DQMC_ERR_ARG, "field value %d at %zu is not +/-1", (int)f[k], k);
+  CUDA_TRY(cudaMemcpyAsync(b->hw[w].fields, f, n, cudaMemcpyHostToDevice, b->stream));
+  CUDA_TRY(cudaStreamSynchronize(b->stream));
+  b->initialised = false;
+  return DQMC_OK;
+}
+
+int dqmc_get_fields(dqmc_batch* b, int w, int8_t* f) {
+  if (int r = check_walker(b, w)) return r;
+  if (!f) return fail(DQMC_ERR_ARG, "null output");
+  const auto& d = b->desc[w];
+  CUDA_TRY(cudaMemcpyAsync(f, b->hw[w].fields, (size_t)d.Lt * d.L * d.L, cudaMemcpyDeviceToHost, b->stream));
+  CUDA_TRY(cudaStreamSynchronize(b->stream));
+  return DQMC_OK;
+}
+
+static int launch_check(const char* what) {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return fail(DQMC_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+  return DQMC_OK;
+}
+
+int dqmc_init_greens(dqmc_batch* b) {
+  if (!b) return fail(DQMC_ERR_ARG, "null batch");
+  for (int j = 0; j < b->maxNs; ++j) {
+    launch_segment(MODE_INIT, b->dW, b->nw, j, 0, b->maxN, b->stream);
+    launch_push(MODE_INIT, b->dW, b->nw, j, b->maxN, b->stream);
+  }
+  launch_greens(MODE_INIT, b->dW, b->nw, 0, 0, -1, b->maxN, b->stream);
+  launch_sign(b->dW, b->nw, b->maxN, b->stream);
+  if (int r = launch_check("init kernels")) return r;
+  // wrap error and accumulators start from zero (DqmcWalker::initial, dqmc_walker.cpp:41-49)
+  for (int w = 0; w < b->nw; ++w) {
+    CUDA_TRY(cudaMemsetAsync(&b->d_scal[w].wrap_bits, 0, sizeof(unsigned long long), b->stream));
+  }
+  CUDA_TRY(cudaStreamSynchronize(b->stream));
+  b->initialised = true;
+  b->trace_count = 0;
+  return DQMC_OK;
+}
+
+static int half_sweep(dqmc_batch* b, int mode, int measure) {
+  if (!b) return fail(DQMC_ERR_ARG, "null batch");
+  if (!b->initialised) return fail(DQMC_ERR_STATE, "sweep before dqmc_init_greens");
+  if (b->opt.rng == DQMC_RNG_MINSTD) {
+    // one uniform per site attempt in sweep order, drawn as bernoulli_distribution does
+    for (int w = 0; w < b->nw; ++w) {
+      const auto& d = b->desc[w];
+      const size_t n = (size_t)d.Lt * d.L * d.L;
+      double* u = b->h_uni + b->uni_stride * w;
+      for (size_t k = 0; k < n; ++k) u[k] = std::generate_canonical<double, 53>(b->eng[w]);
+    }
+    CUDA_TRY(cudaMemcpyAsync(b->d_uni, b->h_uni, sizeof(double) * b->uni_stride * b->nw, cudaMemcpyHostToDevice,
+                             b->stream));
+  } else {
+    // Philox counter: the half-sweep index, carried in every descriptor
+    ++b->sweep_id;
+    for (int w = 0; w < b->nw; ++w) b->hw[w].sweep_id = b->sweep_id;
+    CUDA_TRY(cudaMemcpyAsync(b->dW, b->hw.data(), sizeof(WalkerDev) * b->nw, cudaMemcpyHostToDevice, b->stream));
+  }
+  for (int j = 0; j < b->maxNs; ++j) {
+    b->timed(DQMC_KCLASS_SEGMENT, [&] { launch_segment(mode, b->dW, b->nw, j, measure, b->maxN, b->stream); });
+    b->timed(DQMC_KCLASS_PUSH, [&] { launch_push(mode, b->dW, b->nw, j, b->maxN, b->stream); });
+    const int slot = (b->trace_cap && b->trace_count + j < b->trace_cap) ? b->trace_count + j : -1;
+    b->timed(DQMC_KCLASS_GREENS, [&] { launch_greens(mode, b->dW, b->nw, j, 1, slot, b->maxN, b->stream); });
+    if (measure) b->timed(DQMC_KCLASS_MEASURE, [&] { launch_measure(mode, b->dW, b->nw, j, b->maxN, b->stream); });
+  }
+  if (b->trace_cap) b->trace_count = std::min(b->trace_count + b->maxNs, b->trace_cap);
+  if (b->opt.rng == DQMC_RNG_MINSTD) {
+    // the pinned staging buffer is rewritten by the next half-sweep
+    CUDA_TRY(cudaStreamSynchronize(b->stream));
+  }
+  return launch_check("half-sweep kernels");
+}
+
+int dqmc_sweep_0_to_beta(dqmc_batch* b, int measure) { return half_sweep(b, MODE_FWD, measure); }
+int dqmc_sweep_beta_to_0(dqmc_batch* b, int measure) { return half_sweep(b, MODE_BWD, measure); }
+
+int dqmc_get_green(dqmc_batch* b, int w, int spin, double* out) {
+  if (int r = check_walker(b, w)) return r;
+  if (spin < 0 || spin > 1 || !out) return fail(DQMC_ERR_ARG, "bad spin or null output");
+  const int N = b->hw[w].N;
+  CUDA_TRY(cudaMemcpyAsync(out, b->hw[w].G + (size_t)spin * N * N, sizeof(double) * N * N, cudaMemcpyDeviceToHost,
+                           b->stream));
+  CUDA_TRY(cudaStreamSynchronize(b->stream));
+  return DQMC_OK;
+}
+
+static int read_scal_bytes(dqmc_batch* b, int w, const void* dptr, void* out, size_t bytes) {
+  if (int r = check_walker(b, w)) return r;
+  if (!out) return fail(DQMC_ERR_ARG, "null output");
+  CUDA_TRY(cudaMemcpyAsync(out, dptr, bytes, cudaMemcpyDeviceToHost, b->stream));
+  CUDA_TRY(cudaStreamSynchronize(b->stream));
+  return DQMC_OK;
+}
+#define read_scal(b, w, dptr, out) read_scal_bytes(b, w, dptr, out, sizeof(*(out)))
+
+int dqmc_get_config_sign(dqmc_batch* b, int w, double* out) {
+  if (int r = check_walker(b, w)) return r;
+  return read_scal(b, w, &b->d_scal[w].sign, out);
+}
+int dqmc_get_wrap_error(dqmc_batch* b, int w, double* out) {
+  if (int r = check_walker(b, w)) return r;
+  unsigned long long bits = 0;
+  if (int r = read_scal(b, w, &b->d_scal[w].wrap_bits, &bits)) return r;
+  std::memcpy(out, &bits, sizeof bits);
+  return DQMC_OK;
+}
+int dqmc_get_accept_count(dqmc_batch* b, int w, int64_t* out) {
+  if (int r = check_walker(b, w)) return r;
+  long long v = 0;
+  if (int r = read_scal(b, w, &b->d_scal[w].accepts, &v)) return r;
+  *out = v;
+  return DQMC_OK;
+}
+int dqmc_get_status(dqmc_batch* b, int w, int* out) {
+  if (int r = check_walker(b, w)) return r;
+  return read_scal(b, w, &b->d_scal[w].status, out);
+}
+
+int dqmc_get_observables(dqmc_batch* b, int w, double* sums, int64_t* counts) {
+  if (int r = check_walker(b, w)) return r;
+  if (!sums || !counts) return fail(DQMC_ERR_ARG, "null output");
+  dqmc_batch::Scal s;
+  CUDA_TRY(cudaMemcpyAsync(&s, &b->d_scal[w], sizeof s, cudaMemcpyDeviceToHost, b->stream));
+  CUDA_TRY(cudaStreamSynchronize(b->stream));
+  for (int k = 0; k < kNumObs; ++k) {
+    sums[k] = s.obs[k];
+    counts[k] = s.obs_cnt[k];
+  }
+  return DQMC_OK;
+}
+
+int dqmc_get_observables_all(dqmc_batch* b, double* sums, int64_t* counts) {
+  if (!b || !sums || !counts) return fail(DQMC_ERR_ARG, "null argument");
+  std::vector<dqmc_batch::Scal> s(b->nw);
+  CUDA_TRY(cudaMemcpyAsync(s.data(), b->d_scal, sizeof(dqmc_batch::Scal) * b->nw, cudaMemcpyDeviceToHost, b->stream));
+  CUDA_TRY(cudaStreamSynchronize(b->stream));
+  for (int w = 0; w < b->nw; ++w)
+    for (int k = 0; k < kNumObs; ++k) {
+      sums[(size_t)w * kNumObs + k] = s[w].obs[k];
+      counts[(size_t)w * kNumObs + k] = s[w].obs_cnt[k];
+    }
+  return DQMC_OK;
+}
+
+int dqmc_clear_observables(dqmc_batch* b) {
+  if (!b) return fail(DQMC_ERR_ARG, "null batch");
+  for (int w = 0; w < b->nw; ++w) {
+    CUDA_TRY(cudaMemsetAsync(b->d_scal[w].obs, 0, sizeof(double) * kNumObs, b->stream));
+    CUDA_TRY(cudaMemsetAsync(b->d_scal[w].obs_cnt, 0, sizeof(long long) * kNumObs, b->stream));
+  }
+  CUDA_TRY(cudaStreamSynchronize(b->stream));
+  return DQMC_OK;
+}
+
+int dqmc_trace_count(dqmc_batch* b, int* count) {
+  if (!b || !count) return fail(DQMC_ERR_ARG, "null argument");
+  *count = b->trace_count;
+  return DQMC_OK;
+}
+int dqmc_trace_get(dqmc_batch* b, int w, int k, int spin, double* out) {
+  if (int r = check_walker(b, w)) return r;
+  if (!b->trace_cap) return fail(DQMC_ERR_STATE, "batch created without trace");
+  if (k < 0 || k >= b->trace_count || spin < 0 || spin > 1 || !out) return fail(DQMC_ERR_ARG, "bad trace index");
+  const int N = b->hw[w].N;
+  CUDA_TRY(cudaMemcpyAsync(out, b->hw[w].trace + ((size_t)k * 2 + spin) * N * N, sizeof(double) * N * N,
+                           cudaMemcpyDeviceToHost, b->stream));
+  CUDA_TRY(cudaStreamSynchronize(b->stream));
+  return DQMC_OK;
+}
+int dqmc_trace_clear(dqmc_batch* b) {
+  if (!b) return fail(DQMC_ERR_ARG, "null batch");
+  b->trace_count = 0;
+  return DQMC_OK;
+}
+
+int dqmc_profile_enable(dqmc_batch* b, int on) {
+  if (!b) return fail(DQMC_ERR_ARG, "null batch");
+  b->collect();
+  b->prof = on != 0;
+  for (int k = 0; k < DQMC_NUM_KCLASS; ++k) { b->prof_ms[k] = 0; b->prof_n[k] = 0; }
+  return DQMC_OK;
+}
+
+int dqmc_profile_read(dqmc_batch* b, int cls, double* total_ms, int64_t* launches) {
+  if (!b) return fail(DQMC_ERR_ARG, "null batch");
+  if (cls < 0 || cls >= DQMC_NUM_KCLASS || !total_ms || !launches) return fail(DQMC_ERR_ARG, "bad kernel class");
+  b->collect();
+  *total_ms = b->prof_ms[cls];
+  *launches = b->prof_n[cls];
+  return DQMC_OK;
+}
+
+int dqmc_microbench_fp64(double* gflops) {
+  if (!gflops) return fail(DQMC_ERR_ARG, "null output");
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) return fail(DQMC_ERR_CUDA, "no CUDA device available");
+  cudaError_t e = cudaSuccess;
+  *gflops = run_fp64_probe(&e);
+  if (e != cudaSuccess) return fail(DQMC_ERR_CUDA, "fp64 probe: %s", cudaGetErrorString(e));
+  return DQMC_OK;
+}
+
+int dqmc_batch_info(dqmc_batch* b, int* nw, int64_t* upd) {
+  if (!b) return fail(DQMC_ERR_ARG, "null batch");
+  if (nw) *nw = b->nw;
+  if (upd) {
+    int64_t s = 0;
+    for (auto& d : b->desc) s += (int64_t)d.L * d.L * d.Lt;
+    *upd = s;
+  }
+  return DQMC_OK;
+}
+
+}  // extern "C"

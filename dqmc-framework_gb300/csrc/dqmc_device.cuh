@@ -1,0 +1,70 @@
+// dqmc_device.cuh — device data model of a walker batch (FP64 plain method).
+//
+// One WalkerDev per walker, in device memory.  Everything a CTA needs to run
+// one walker's segment or stabilization is reachable from it: the Green's
+// functions, the B-chain buffer, the UDT stacks, the Ising fields, the dense
+// exp(+/-dtau K) (shared by walkers with equal lattice parameters), the
+// Fourier table of the measured momentum and the per-walker accumulators.
+//
+// Layouts (all column-major, leading dimension N, 256-byte aligned bases):
+//   G      [2][N*N]      spin 0 = up, spin 1 = down (attractive: spin 1 aliases 0)
+//   chain  [S][N*N]      running B-chain product of the current segment
+//   stack  [side][S][level] { U (N*N) | F (N*N) | D (N) }, side 0 left, 1 right
+//   fields [Lt][N] int8  +/-1, slice-major (reference: Lt x N Eigen matrix of doubles)
+#pragma once
+#include <cstdint>
+
+namespace dqmc {
+
+constexpr int kThreads = 256;
+constexpr int kMaxSmemN = 64;    // N handled by the SMEM-resident kernels
+constexpr int kNumObs = 9;
+
+enum SweepMode { MODE_INIT = 0, MODE_FWD = 1, MODE_BWD = 2 };
+
+// status bits (per walker)
+enum : int {
+  ST_NONFINITE_G = 1,
+  ST_SINGULAR = 2,
+  ST_NONFINITE_RATIO = 4,
+};
+
+struct WalkerDev {
+  int N, L, Lt, pace, nstack, S, model, cb;  // model: 0 repulsive, 1 attractive
+  int rng;                                    // 0 host uniforms, 1 Philox
+  int pad0;
+  double hop_t;
+  // B-matrix diagonal factors exp(+alpha), exp(-alpha)
+  double e_pa, e_ma;
+  // ratio constants indexed by [s>0 ? 0 : 1]: exp(-2 alpha s) - 1, exp(+2 alpha s) - 1, exp(2 alpha s)
+  double cm[2], cp[2], ex2[2];
+  double cbP[16], cbI[16];   // checkerboard plaquettes exp(+dtau t h) e^{0.5 dtau mu}, inverse
+  double* G;                 // [2][N*N]
+  double* chain;             // [S][N*N]
+  double* stack;             // see header
+  long long lvl_stride;      // doubles per stack level (2 N^2 + N, padded)
+  long long side_stride;     // doubles per side (S * nstack * lvl_stride)
+  int8_t* fields;            // [Lt][N]
+  const double* expK;        // dense exp(-dtau K)  (N*N) or null
+  const double* invK;        // dense exp(+dtau K)
+  const double* ff;          // Fourier factor per displacement index, measured k
+  double* obs;               // [kNumObs] sums of sign * O
+  long long* obs_cnt;        // [kNumObs]
+  double* sign;              // current configuration sign
+  double* sign_Lt;           // sign recorded at t = Lt of the backward half-sweep
+  unsigned long long* wrap_bits;  // running max |G_fresh - G_wrapped| (bit pattern)
+  long long* accepts;
+  int* status;
+  const double* uni;         // parity uniforms of the current half-sweep [Lt*N]
+  unsigned long long seed;   // Philox key
+  unsigned long long sweep_id;  // Philox counter word (half-sweep index)
+  double* trace;             // [trace_cap][2][N*N] or null
+  int trace_cap;
+  int pad1;
+};
+
+__host__ __device__ inline double* stack_level(const WalkerDev& w, int side, int spin, int level) {
+  return w.stack + side * w.side_stride + ((long long)spin * w.nstack + level) * w.lvl_stride;
+}
+
+}  // namespace dqmc

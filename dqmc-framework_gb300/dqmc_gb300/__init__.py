@@ -1,0 +1,278 @@
+"""Python binding of the GB300 DQMC sweep library (ctypes over include/dqmc_gb300.h).
+
+The names follow the reference's operator interface (dqmc-framework:
+DqmcWalker, Model, MeasureHandler): a Batch is a set of independent walkers,
+each the equivalent of one reference MPI rank's DqmcWalker + Model + Lattice.
+The CUDA library is the only compute path: if libdqmc_gb300.so is missing or
+no GPU is present, calls raise instead of falling back to the CPU.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(os.path.dirname(_HERE), "lib", "libdqmc_gb300.so")
+
+REPULSIVE, ATTRACTIVE = 0, 1
+RNG_MINSTD, RNG_PHILOX = 0, 1
+FP64 = 0
+OBS_NAMES = [
+    "filling_number", "double_occupancy", "kinetic_energy", "momentum_distribution",
+    "local_spin_corr", "spin_density_structure_factor", "charge_density_structure_factor",
+    "s_wave_pairing_corr", "equaltime_sign",
+]
+NUM_OBS = len(OBS_NAMES)
+
+# every symbol include/dqmc_gb300.h declares
+EXPORTS = [
+    "dqmc_last_error", "dqmc_abi_version", "dqmc_batch_create", "dqmc_batch_destroy", "dqmc_set_stream",
+    "dqmc_synchronize", "dqmc_fields_random", "dqmc_set_fields", "dqmc_get_fields", "dqmc_init_greens",
+    "dqmc_sweep_0_to_beta", "dqmc_sweep_beta_to_0", "dqmc_get_green", "dqmc_get_config_sign",
+    "dqmc_get_wrap_error", "dqmc_get_accept_count", "dqmc_get_status", "dqmc_get_observables",
+    "dqmc_clear_observables", "dqmc_trace_count", "dqmc_trace_get", "dqmc_trace_clear", "dqmc_batch_info",
+    "dqmc_profile_enable", "dqmc_profile_read", "dqmc_microbench_fp64", "dqmc_get_observables_all",
+]
+KCLASSES = ["segment", "push", "greens", "measure"]
+
+
+class DqmcError(RuntimeError):
+    pass
+
+
+class _Desc(ctypes.Structure):
+    _fields_ = [
+        ("model", ctypes.c_int), ("L", ctypes.c_int), ("hopping_t", ctypes.c_double),
+        ("onsite_u", ctypes.c_double), ("mu", ctypes.c_double), ("beta", ctypes.c_double),
+        ("Lt", ctypes.c_int), ("pace", ctypes.c_int), ("checkerboard", ctypes.c_int),
+        ("momentum_index", ctypes.c_int), ("seed", ctypes.c_uint64),
+    ]
+
+
+class _Opts(ctypes.Structure):
+    _fields_ = [("rng", ctypes.c_int), ("precision", ctypes.c_int), ("trace", ctypes.c_int)]
+
+
+_lib = None
+
+
+def load() -> ctypes.CDLL:
+    """Load libdqmc_gb300.so (raises if it was not built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise DqmcError(f"{LIB_PATH} not built: run __graft_entry__.build()")
+    L = ctypes.CDLL(LIB_PATH)
+    vp, dp, i8p, i64p, ip = (ctypes.c_void_p, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int8),
+                             ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int))
+    c = ctypes.c_int
+    sig = {
+        "dqmc_last_error": (ctypes.c_char_p, []), "dqmc_abi_version": (c, []),
+        "dqmc_batch_create": (c, [ctypes.POINTER(_Desc), c, ctypes.POINTER(_Opts), ctypes.POINTER(vp)]),
+        "dqmc_batch_destroy": (c, [vp]), "dqmc_set_stream": (c, [vp, vp]), "dqmc_synchronize": (c, [vp]),
+        "dqmc_fields_random": (c, [vp, c]), "dqmc_set_fields": (c, [vp, c, i8p]),
+        "dqmc_get_fields": (c, [vp, c, i8p]), "dqmc_init_greens": (c, [vp]),
+        "dqmc_sweep_0_to_beta": (c, [vp, c]), "dqmc_sweep_beta_to_0": (c, [vp, c]),
+        "dqmc_get_green": (c, [vp, c, c, dp]), "dqmc_get_config_sign": (c, [vp, c, dp]),
+        "dqmc_get_wrap_error": (c, [vp, c, dp]), "dqmc_get_accept_count": (c, [vp, c, i64p]),
+        "dqmc_get_status": (c, [vp, c, ip]), "dqmc_get_observables": (c, [vp, c, dp, i64p]),
+        "dqmc_clear_observables": (c, [vp]), "dqmc_trace_count": (c, [vp, ip]),
+        "dqmc_trace_get": (c, [vp, c, c, c, dp]), "dqmc_trace_clear": (c, [vp]),
+        "dqmc_batch_info": (c, [vp, ip, i64p]),
+        "dqmc_profile_enable": (c, [vp, c]), "dqmc_profile_read": (c, [vp, c, dp, i64p]),
+        "dqmc_microbench_fp64": (c, [dp]), "dqmc_get_observables_all": (c, [vp, dp, i64p]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = L
+    return L
+
+
+def _check(rc: int):
+    if rc != 0:
+        raise DqmcError(f"status {rc}: {load().dqmc_last_error().decode()}")
+
+
+@dataclass
+class WalkerDesc:
+    """Parameters of one walker (Model::set_model_params + Lattice + DqmcWalker)."""
+    model: int = REPULSIVE
+    L: int = 4
+    t: float = 1.0
+    U: float = 4.0
+    mu: float = 0.0
+    beta: float = 4.0
+    Lt: int = 80
+    pace: int = 10
+    checkerboard: bool = False
+    momentum_index: int = -1
+    seed: int = 0
+
+    @property
+    def N(self) -> int:
+        return self.L * self.L
+
+    def _c(self) -> _Desc:
+        return _Desc(self.model, self.L, self.t, abs(self.U), self.mu, self.beta, self.Lt, self.pace,
+                     int(self.checkerboard), self.momentum_index, self.seed)
+
+
+class Batch:
+    """A batch of independent walkers on the current CUDA device."""
+
+    def __init__(self, walkers, rng=RNG_MINSTD, precision=FP64, trace=False):
+        L = load()
+        self.walkers = list(walkers)
+        arr = (_Desc * len(self.walkers))(*[w._c() for w in self.walkers])
+        opts = _Opts(rng, precision, int(trace))
+        h = ctypes.c_void_p()
+        _check(L.dqmc_batch_create(arr, len(self.walkers), ctypes.byref(opts), ctypes.byref(h)))
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            load().dqmc_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __len__(self):
+        return len(self.walkers)
+
+    # --- set-up ------------------------------------------------------------
+    def set_stream(self, stream_ptr: int):
+        _check(load().dqmc_set_stream(self.h, ctypes.c_void_p(stream_ptr)))
+
+    def synchronize(self):
+        _check(load().dqmc_synchronize(self.h))
+
+    def fields_random(self, w: int):
+        """Model::set_bosonic_fields_to_random with the walker's own engine."""
+        _check(load().dqmc_fields_random(self.h, w))
+
+    def set_fields(self, w: int, fields):
+        f = np.ascontiguousarray(fields, dtype=np.int8)
+        _check(load().dqmc_set_fields(self.h, w, f.ctypes.data_as(ctypes.POINTER(ctypes.c_int8))))
+
+    def fields(self, w: int) -> np.ndarray:
+        d = self.walkers[w]
+        f = np.zeros((d.Lt, d.N), dtype=np.int8)
+        _check(load().dqmc_get_fields(self.h, w, f.ctypes.data_as(ctypes.POINTER(ctypes.c_int8))))
+        return f
+
+    def init_greens(self):
+        """initial_svd_stacks + initial_greens_functions + initial_config_sign."""
+        _check(load().dqmc_init_greens(self.h))
+
+    # --- sweeps --------------------------------------------------------------
+    def sweep_0_to_beta(self, measure: bool = False):
+        _check(load().dqmc_sweep_0_to_beta(self.h, int(measure)))
+
+    def sweep_beta_to_0(self, measure: bool = False):
+        _check(load().dqmc_sweep_beta_to_0(self.h, int(measure)))
+
+    # --- accessors -------------------------------------------------------------
+    def green(self, w: int, spin: int) -> np.ndarray:
+        N = self.walkers[w].N
+        g = np.zeros((N, N), order="F")
+        _check(load().dqmc_get_green(self.h, w, spin, g.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
+        return g
+
+    def config_sign(self, w: int) -> float:
+        v = ctypes.c_double()
+        _check(load().dqmc_get_config_sign(self.h, w, ctypes.byref(v)))
+        return v.value
+
+    def wrap_error(self, w: int) -> float:
+        v = ctypes.c_double()
+        _check(load().dqmc_get_wrap_error(self.h, w, ctypes.byref(v)))
+        return v.value
+
+    def accept_count(self, w: int) -> int:
+        v = ctypes.c_int64()
+        _check(load().dqmc_get_accept_count(self.h, w, ctypes.byref(v)))
+        return v.value
+
+    def status(self, w: int) -> int:
+        v = ctypes.c_int()
+        _check(load().dqmc_get_status(self.h, w, ctypes.byref(v)))
+        return v.value
+
+    def observables(self, w: int):
+        s = np.zeros(NUM_OBS)
+        c = np.zeros(NUM_OBS, dtype=np.int64)
+        _check(load().dqmc_get_observables(self.h, w, s.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                           c.ctypes.data_as(ctypes.POINTER(ctypes.c_int64))))
+        return s, c
+
+    def observables_all(self):
+        n = len(self.walkers)
+        s = np.zeros((n, NUM_OBS))
+        c = np.zeros((n, NUM_OBS), dtype=np.int64)
+        _check(load().dqmc_get_observables_all(self.h, s.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                               c.ctypes.data_as(ctypes.POINTER(ctypes.c_int64))))
+        return s, c
+
+    def clear_observables(self):
+        _check(load().dqmc_clear_observables(self.h))
+
+    def trace(self, w: int) -> np.ndarray:
+        n = ctypes.c_int()
+        _check(load().dqmc_trace_count(self.h, ctypes.byref(n)))
+        N = self.walkers[w].N
+        out = np.zeros((n.value, 2, N, N))
+        for k in range(n.value):
+            for s in range(2):
+                g = np.zeros((N, N), order="F")
+                _check(load().dqmc_trace_get(self.h, w, k, s, g.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
+                out[k, s] = g
+        return out
+
+    def trace_clear(self):
+        _check(load().dqmc_trace_clear(self.h))
+
+    def profile_enable(self, on: bool = True):
+        _check(load().dqmc_profile_enable(self.h, int(on)))
+
+    def profile_read(self) -> dict:
+        out = {}
+        for k, name in enumerate(KCLASSES):
+            ms = ctypes.c_double()
+            n = ctypes.c_int64()
+            _check(load().dqmc_profile_read(self.h, k, ctypes.byref(ms), ctypes.byref(n)))
+            out[name] = (ms.value, n.value)
+        return out
+
+    def updates_per_half_sweep(self) -> int:
+        nw = ctypes.c_int()
+        u = ctypes.c_int64()
+        _check(load().dqmc_batch_info(self.h, ctypes.byref(nw), ctypes.byref(u)))
+        return u.value
+
+
+def microbench_fp64() -> float:
+    """Measured FP64 FMA throughput of the current device in GFLOP/s."""
+    v = ctypes.c_double()
+    _check(load().dqmc_microbench_fp64(ctypes.byref(v)))
+    return v.value
+
+
+def write_bin(sums, counts):
+    """MeasureHandler::normalize_stats for one bin (measure_handler.cpp:170-189):
+    observables divided by count and by the mean sign; the sign bin is |<sign>|."""
+    sums = np.asarray(sums, dtype=np.float64)
+    counts = np.asarray(counts, dtype=np.float64)
+    sign = sums[-1] / counts[-1]
+    out = sums / (counts * sign)
+    out[-1] = abs(sign)
+    return out

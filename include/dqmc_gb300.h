@@ -1,0 +1,172 @@
+/*
+ * dqmc_gb300.h — C-ABI of the GB300 (sm_103a) DQMC sweep library.
+ *
+ * The reference (dqmc-framework) has no FFI: its operator interface is the
+ * C++ virtual set ModelBase / CheckerBoardBase / DqmcWalker / MeasureHandler.
+ * Each entry point below replaces one call of that interface, for a batch of
+ * independent walkers (the reference runs one walker per MPI rank).  The
+ * reference interface each one stands in for is cited beside it.
+ *
+ * Conventions
+ *   - Every call returns a status (DQMC_OK = 0).  The library never exits.
+ *     dqmc_last_error() gives a one-line message for the last failure.
+ *   - Matrices crossing the ABI are column-major N x N doubles (Eigen's
+ *     layout in the reference); fields are int8 +/-1 laid out [t][i].
+ *   - A batch owns all its device memory and is bound to one CUDA stream.
+ *     Calls on one batch are not thread-safe; distinct batches are
+ *     independent.  Host buffers passed in are copied.
+ *   - The CUDA kernels are the only compute path; there is no CPU fallback.
+ */
+#ifndef DQMC_GB300_H
+#define DQMC_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DQMC_ABI_VERSION 1
+
+enum dqmc_status {
+  DQMC_OK = 0,
+  DQMC_ERR_ARG = 1,         /* invalid argument or unsupported size */
+  DQMC_ERR_CUDA = 2,        /* CUDA runtime error (no device, launch failure) */
+  DQMC_ERR_NUMERIC = 3,     /* non-finite Green's function / factorisation breakdown */
+  DQMC_ERR_TIMEOUT = 4,     /* a bounded device-side wait gave up */
+  DQMC_ERR_STATE = 5        /* call out of order (e.g. sweep before init) */
+};
+
+enum dqmc_model { DQMC_REPULSIVE_HUBBARD = 0, DQMC_ATTRACTIVE_HUBBARD = 1 };
+
+enum dqmc_rng {
+  DQMC_RNG_MINSTD = 0,  /* parity mode: per-walker std::minstd_rand0 on the host,
+                           consumed exactly as std::bernoulli_distribution does */
+  DQMC_RNG_PHILOX = 1   /* throughput mode: Philox4x32-10 on the device */
+};
+
+enum dqmc_precision {
+  DQMC_FP64 = 0  /* plain method: every product in FP64 */
+};
+
+/* Observable slots, the equal-time list of src/measure/observable_handler.cpp:11-20
+ * followed by the equal-time sign. */
+enum dqmc_observable {
+  DQMC_OBS_FILLING = 0,
+  DQMC_OBS_DOUBLE_OCCUPANCY = 1,
+  DQMC_OBS_KINETIC_ENERGY = 2,
+  DQMC_OBS_MOMENTUM_DISTRIBUTION = 3,
+  DQMC_OBS_LOCAL_SPIN_CORR = 4,
+  DQMC_OBS_SDW_STRUCTURE_FACTOR = 5,
+  DQMC_OBS_CDW_STRUCTURE_FACTOR = 6,
+  DQMC_OBS_S_WAVE_PAIRING = 7,
+  DQMC_OBS_SIGN = 8,
+  DQMC_NUM_OBS = 9
+};
+
+/* One walker: the parameters the reference spreads over
+ * Model::set_model_params (include/model/model_base.h:111-163),
+ * Lattice::Square::set_lattice_params (src/lattice/square.cpp:16-28),
+ * DqmcWalker::set_physical_params / set_stabilization_pace
+ * (src/dqmc_walker.cpp:25-38) and the checkerboard link
+ * (src/model/model_base.cpp:38-55). */
+typedef struct dqmc_walker_desc {
+  int model;           /* enum dqmc_model */
+  int L;               /* square lattice side, N = L*L sites */
+  double hopping_t;
+  double onsite_u;     /* |U|; the attractive model takes |U| (attractive_hubbard.cpp:37) */
+  double mu;
+  double beta;
+  int Lt;              /* imaginary-time slices, dtau = beta / Lt */
+  int pace;            /* stabilization pace */
+  int checkerboard;    /* 0: dense exp(-dtau K); 1: checkerboard break-up (even L) */
+  int momentum_index;  /* k-star index for SDW/CDW/n(k); -1 = M point (pi, pi) */
+  uint64_t seed;       /* minstd seed (parity) or Philox key (throughput) */
+} dqmc_walker_desc;
+
+typedef struct dqmc_batch_options {
+  int rng;             /* enum dqmc_rng */
+  int precision;       /* enum dqmc_precision */
+  int trace;           /* 1: keep G after every stabilization of the last half-sweep
+                          (parity tests; costs device memory) */
+} dqmc_batch_options;
+
+typedef struct dqmc_batch dqmc_batch;
+
+const char* dqmc_last_error(void);
+int dqmc_abi_version(void);
+
+/* Create / destroy a batch of walkers on the current CUDA device.
+ * Replaces DqmcInitializer::initial_modules (src/dqmc_initializer.cpp:341-392)
+ * for n_walkers independent chains. */
+int dqmc_batch_create(const dqmc_walker_desc* descs, int n_walkers,
+                      const dqmc_batch_options* opt, dqmc_batch** out);
+int dqmc_batch_destroy(dqmc_batch* b);
+
+/* Bind the batch to a caller-owned cudaStream_t (NULL = the batch's own stream). */
+int dqmc_set_stream(dqmc_batch* b, void* cuda_stream);
+int dqmc_synchronize(dqmc_batch* b);
+
+/* Fields.  dqmc_fields_random replaces Model::set_bosonic_fields_to_random
+ * (src/model/repulsive_hubbard.cpp:86-99) with the walker's own engine;
+ * set/get replace DqmcIO::read_bosonic_fields_from_file / output_bosonic_fields
+ * (include/dqmc_io.h:479-629) for in-memory arrays. */
+int dqmc_fields_random(dqmc_batch* b, int walker);
+int dqmc_set_fields(dqmc_batch* b, int walker, const int8_t* fields);
+int dqmc_get_fields(dqmc_batch* b, int walker, int8_t* fields);
+
+/* DqmcWalker::initial_svd_stacks + initial_greens_functions + initial_config_sign
+ * (src/dqmc_walker.cpp:109-163), for every walker. */
+int dqmc_init_greens(dqmc_batch* b);
+
+/* DqmcWalker::sweep_from_0_to_beta (src/dqmc_walker.cpp:246-325) and
+ * sweep_from_beta_to_0 (:334-412) for every walker.  measure != 0 fuses
+ * MeasureHandler::equaltime_measure (src/measure/measure_handler.cpp:136-150)
+ * over the half-sweep's Lt slices, exactly as the reference measures the
+ * recorded G(t,t) series after the half-sweep. */
+int dqmc_sweep_0_to_beta(dqmc_batch* b, int measure);
+int dqmc_sweep_beta_to_0(dqmc_batch* b, int measure);
+
+/* Accessors: DqmcWalker::GreenttUp/GreenttDn, ConfigSign, WrapError
+ * (include/dqmc_walker.h:150-184). spin 0 = up, 1 = down. */
+int dqmc_get_green(dqmc_batch* b, int walker, int spin, double* out);
+int dqmc_get_config_sign(dqmc_batch* b, int walker, double* out);
+int dqmc_get_wrap_error(dqmc_batch* b, int walker, double* out);
+int dqmc_get_accept_count(dqmc_batch* b, int walker, int64_t* out);
+int dqmc_get_status(dqmc_batch* b, int walker, int* out);
+
+/* Equal-time accumulators of a walker: sums[k] = sum over measured slices of
+ * sign * O_k (Observable::tmp_value) and counts[k] (Observable::counts),
+ * src/measure/measure_methods.cpp:22-255. */
+int dqmc_get_observables(dqmc_batch* b, int walker, double* sums, int64_t* counts);
+int dqmc_clear_observables(dqmc_batch* b);
+/* All walkers at once (one device-to-host copy): sums/counts [n_walkers][DQMC_NUM_OBS];
+ * the per-rank bin gather of include/utils/mpi.hpp:68-104 becomes this read. */
+int dqmc_get_observables_all(dqmc_batch* b, double* sums, int64_t* counts);
+
+/* Trace (options.trace = 1): G after the k-th stabilization of the most recent
+ * half-sweep(s) since the last clear; count is per walker. */
+int dqmc_trace_count(dqmc_batch* b, int* count);
+int dqmc_trace_get(dqmc_batch* b, int walker, int k, int spin, double* out);
+int dqmc_trace_clear(dqmc_batch* b);
+
+/* Statistics of the last half-sweep for throughput accounting. */
+int dqmc_batch_info(dqmc_batch* b, int* n_walkers, int64_t* updates_per_half_sweep);
+
+/* Kernel-class timing with CUDA events on the batch's stream (the reference
+ * has only a whole-run wall-clock timer, src/dqmc.cpp:37-41).  Classes:
+ * 0 segment, 1 push, 2 greens, 3 measure.  Enabling resets the totals. */
+enum { DQMC_KCLASS_SEGMENT = 0, DQMC_KCLASS_PUSH = 1, DQMC_KCLASS_GREENS = 2, DQMC_KCLASS_MEASURE = 3,
+       DQMC_NUM_KCLASS = 4 };
+int dqmc_profile_enable(dqmc_batch* b, int on);
+int dqmc_profile_read(dqmc_batch* b, int kclass, double* total_ms, int64_t* launches);
+
+/* FP64 FMA throughput of the current device (GFLOP/s), measured by a
+ * register-resident FMA loop over all SMs: the FP64 roofline denominator. */
+int dqmc_microbench_fp64(double* gflops);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

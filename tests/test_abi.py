@@ -1,0 +1,75 @@
+"""C-ABI checks that need no GPU: the library loads, exports every symbol the
+public header declares, and rejects bad arguments before touching a device."""
+import ctypes
+import os
+import re
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="module")
+def dq():
+    import __graft_entry__ as g
+
+    g.build_library()
+    import dqmc_gb300
+
+    dqmc_gb300.load()
+    return dqmc_gb300
+
+
+def _declared(header):
+    text = open(os.path.join(ROOT, "include", header)).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(dqmc_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_exports_every_declared_symbol(dq):
+    lib = ctypes.CDLL(dq.LIB_PATH)
+    declared = _declared("dqmc_gb300.h")
+    assert declared, "no declarations parsed"
+    missing = [s for s in declared if not hasattr(lib, s)]
+    assert not missing, missing
+    assert sorted(dq.EXPORTS) == sorted(declared)
+
+
+def test_abi_version(dq):
+    assert dq.load().dqmc_abi_version() == 1
+
+
+@pytest.mark.parametrize(
+    "kw, msg",
+    [
+        (dict(L=1), "side"),
+        (dict(L=9), "exceeds"),
+        (dict(L=3, checkerboard=True), "even"),
+        (dict(Lt=0), "Lt"),
+        (dict(pace=0), "pace"),
+        (dict(beta=-1.0), "beta"),
+        (dict(model=7), "model"),
+        (dict(L=4, momentum_index=99), "momentum"),
+    ],
+)
+def test_bad_arguments_rejected_before_device(dq, kw, msg):
+    with pytest.raises(dq.DqmcError) as e:
+        dq.Batch([dq.WalkerDesc(**kw)])
+    assert "status 1" in str(e.value) and msg in str(e.value)
+
+
+def test_null_batch_calls_fail_cleanly(dq):
+    L = dq.load()
+    assert L.dqmc_init_greens(None) == 1
+    assert L.dqmc_sweep_0_to_beta(None, 0) == 1
+    assert L.dqmc_batch_destroy(None) == 0
+
+
+def test_no_cpu_fallback_without_gpu(dq):
+    import torch
+
+    if torch.cuda.is_available():
+        pytest.skip("GPU present")
+    with pytest.raises(dq.DqmcError) as e:
+        dq.Batch([dq.WalkerDesc()])
+    assert "status 2" in str(e.value)

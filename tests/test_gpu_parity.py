@@ -1,0 +1,152 @@
+"""GPU parity: the CUDA path through the C-ABI against the CPU oracle.
+
+Bar (stated by the plain FP64 method): for the same seed, fields and
+uniforms, identical accept/reject decisions (hence identical Ising fields)
+and G / observables within 1e-10 relative.  G is compared at every
+stabilization point (fresh G) and at the end of each half-sweep.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+REL = 1e-10
+
+
+@pytest.fixture(scope="module")
+def dq():
+    import __graft_entry__ as g
+
+    g.build()
+    import dqmc_gb300
+
+    return dqmc_gb300
+
+
+def _oracle(O, d, stack):
+    w = O.Walker(model=d.model, L=d.L, t=d.t, U=d.U, mu=d.mu, beta=d.beta, Lt=d.Lt, pace=d.pace,
+                 checkerboard=d.checkerboard, stack=stack, momentum_index=d.momentum_index)
+    w.seed(d.seed)
+    return w
+
+
+def _close(a, b, rel=REL):
+    scale = max(1.0, abs(b).max())
+    return abs(a - b).max() <= rel * scale
+
+
+def _run_pair(dq, O, descs, sweeps=1, stack=None, fields=None, measure=True):
+    O.use_scipy_lapack(False)
+    stack = O.STACK_QRP if stack is None else stack
+    batch = dq.Batch(descs, rng=dq.RNG_MINSTD, trace=True)
+    refs = [_oracle(O, d, stack) for d in descs]
+    for k, (d, r) in enumerate(zip(descs, refs)):
+        if fields is None:
+            batch.fields_random(k)
+            r.fields_random()
+        else:
+            batch.set_fields(k, fields[k])
+            r.set_fields(fields[k])
+        r.init()
+        r.trace(True)
+    batch.init_greens()
+    for k, r in enumerate(refs):
+        for s in (0, 1):
+            assert _close(batch.green(k, s), r.green(s)), f"walker {k} initial G spin {s}"
+        assert batch.config_sign(k) == r.sign
+    for _ in range(sweeps):
+        batch.trace_clear()
+        for r in refs:
+            r.trace_clear()
+        batch.sweep_0_to_beta(measure=measure)
+        batch.sweep_beta_to_0(measure=measure)
+        for k, r in enumerate(refs):
+            r.sweep_0_to_beta()
+            if measure:
+                r.measure()
+            r.sweep_beta_to_0()
+            if measure:
+                r.measure()
+            np.testing.assert_array_equal(batch.fields(k), r.fields(), err_msg=f"walker {k}: decisions differ")
+            tg, tr = batch.trace(k), r.trace_get()
+            assert tg.shape == tr.shape
+            for i in range(tr.shape[0]):
+                for s in (0, 1):
+                    assert _close(tg[i, s], tr[i, s]), (k, i, s, abs(tg[i, s] - tr[i, s]).max())
+            for s in (0, 1):
+                assert _close(batch.green(k, s), r.green(s))
+            assert batch.config_sign(k) == r.sign
+            assert batch.accept_count(k) == r.accepts
+            assert batch.status(k) == 0
+    for k, r in enumerate(refs):
+        if measure:
+            sums, counts = batch.observables(k)
+            rs, rc = r.accumulators()
+            np.testing.assert_array_equal(counts, rc)
+            np.testing.assert_allclose(sums, rs, rtol=REL, atol=REL)
+        # the wrap error is rounding noise amplified by the B chain: same
+        # order of magnitude on both sides, not the same digits
+        we, wr = batch.wrap_error(k), r.wrap_error
+        assert we < 1e-6 and wr < 1e-6
+        assert we <= 10 * wr + 1e-13 and wr <= 10 * we + 1e-13, (we, wr)
+    return batch, refs
+
+
+def test_c1_single_walker_dense(dq, oracle_mod):
+    """4x4 repulsive, U=4, beta=4, Lt=80, dense, pace 10 (the plain single-walker case)."""
+    d = dq.WalkerDesc(model=0, L=4, U=4.0, beta=4.0, Lt=80, pace=10, seed=12345)
+    _run_pair(dq, oracle_mod, [d], sweeps=2)
+
+
+def test_c1_against_reference_svd_stack(dq, oracle_mod):
+    """Same walker against the reference algorithm itself (SVD stack, full-pivot QR)."""
+    d = dq.WalkerDesc(model=0, L=4, U=4.0, beta=4.0, Lt=80, pace=10, seed=777)
+    _run_pair(dq, oracle_mod, [d], sweeps=1, stack=oracle_mod.STACK_SVD)
+
+
+def test_checkerboard_batch(dq, oracle_mod):
+    """8x8 repulsive checkerboard walkers (the batched FP64 configuration's model)."""
+    descs = [dq.WalkerDesc(model=0, L=8, U=4.0, beta=8.0, Lt=160, pace=10, checkerboard=True, seed=1000 + w)
+             for w in range(3)]
+    _run_pair(dq, oracle_mod, descs, sweeps=1)
+
+
+def test_attractive_example_from_fixture(dq, oracle_mod, example_fixture):
+    """Attractive 8x8 dense, warm-started from the reference's example fields.out."""
+    d = dq.WalkerDesc(model=1, L=8, U=4.0, beta=8.0, Lt=160, pace=10, seed=42)
+    _run_pair(dq, oracle_mod, [d], sweeps=1, fields=[example_fixture["fields"]])
+
+
+def test_uneven_batch(dq, oracle_mod):
+    """Walkers of different sizes, beta, pace and models in one launch."""
+    descs = [
+        dq.WalkerDesc(model=0, L=2, U=2.0, beta=1.0, Lt=12, pace=5, seed=1),
+        dq.WalkerDesc(model=0, L=6, U=5.0, beta=2.0, Lt=40, pace=10, checkerboard=True, seed=2),
+        dq.WalkerDesc(model=1, L=4, U=3.0, mu=-0.5, beta=3.0, Lt=30, pace=8, seed=3),
+        dq.WalkerDesc(model=0, L=8, U=4.0, mu=0.3, beta=2.0, Lt=20, pace=6, momentum_index=3, seed=4),
+    ]
+    _run_pair(dq, oracle_mod, descs, sweeps=1)
+
+
+def test_philox_mode_consistent(dq, oracle_mod):
+    """Throughput RNG: the device G after a sweep pair equals the oracle's
+    G(0) recomputed from the device's final fields."""
+    O = oracle_mod
+    descs = [dq.WalkerDesc(model=0, L=8, U=4.0, beta=4.0, Lt=80, pace=10, checkerboard=True, seed=9 + w)
+             for w in range(4)]
+    batch = dq.Batch(descs, rng=dq.RNG_PHILOX)
+    for k in range(len(descs)):
+        batch.fields_random(k)
+    batch.init_greens()
+    f0 = batch.fields(0)
+    batch.sweep_0_to_beta()
+    batch.sweep_beta_to_0()
+    assert (batch.fields(0) != f0).any()
+    for k, d in enumerate(descs):
+        r = _oracle(O, d, O.STACK_QRP)
+        r.set_fields(batch.fields(k))
+        r.init()
+        for s in (0, 1):
+            assert _close(batch.green(k, s), r.green(s))
+        assert batch.status(k) == 0
+        assert batch.accept_count(k) > 0
