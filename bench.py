@@ -297,8 +297,11 @@ def main():
     ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
     ap.add_argument("--cpu-budget", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--walkers", type=int, default=0, help="override the walker count (profiling runs)")
     args = ap.parse_args()
-    wl = WORKLOADS[args.workload]
+    wl = dict(WORKLOADS[args.workload])
+    if args.walkers > 0:
+        wl["walkers"] = args.walkers
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     config = {"workload": args.workload, "walkers_per_gpu": wl["walkers"], "model": "repulsive" if wl["model"] == 0 else "attractive",

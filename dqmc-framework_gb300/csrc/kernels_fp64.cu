@@ -306,9 +306,12 @@ __device__ void measure_slice(const WalkerDev& w, const double* gu, const double
   const int N = w.N, L = w.L;
   double* du = scratch;
   double* dd = scratch + N;
+  __shared__ signed char s_x[kMaxSmemN], s_y[kMaxSmemN];
   for (int i = threadIdx.x; i < N; i += kThreads) {
     du[i] = 1.0 - at(gu, ld, i, i);
     dd[i] = 1.0 - at(gd, ld, i, i);
+    s_x[i] = (signed char)(i % L);
+    s_y[i] = (signed char)(i / L);
   }
   __syncthreads();
   // v: 0 trace, 1 double occ, 2 local spin, 3 kinetic, 4 n(k), 5 common, 6 cross, 7 s-wave
@@ -322,10 +325,13 @@ __device__ void measure_slice(const WalkerDev& w, const double* gu, const double
     const int jx = (x + 1) % L + L * y, jy = x + L * ((y + 1) % L);
     v[3] += at(gu, ld, i, jx) + at(gd, ld, i, jx) + at(gu, ld, i, jy) + at(gd, ld, i, jy);
   }
-  for (int e = threadIdx.x; e < N * N; e += kThreads) {
-    const int i = e % N, j = e / N;
-    const int xi = i % L, yi = i / L, xj = j % L, yj = j / L;
-    const double ff = w.ff[(xj - xi + L) % L + ((yj - yi + L) % L) * L];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for (int j = wid; j < N; j += kThreads / 32)
+  for (int i = lane; i < N; i += 32) {
+    int dx = s_x[j] - s_x[i], dy = s_y[j] - s_y[i];
+    dx += (dx < 0) ? L : 0;
+    dy += (dy < 0) ? L : 0;
+    const double ff = w.ff[dx + dy * L];
     const double gu_ij = at(gu, ld, i, j), gu_ji = at(gu, ld, j, i);
     const double gd_ij = at(gd, ld, i, j), gd_ji = at(gd, ld, j, i);
     const double dij = (i == j) ? 1.0 : 0.0;
@@ -375,30 +381,32 @@ __global__ void __launch_bounds__(kThreads) segment_kernel(const WalkerDev* __re
   double* dtab = vec + 4 * N;                   // [2 spins][2 (pos,neg)][N]
   double* red = dtab + 4 * N;                   // 64
   double* scratch = red + 64;                   // 2N
-  __shared__ int s_acc;
+  __shared__ int s_next;
   __shared__ double s_f[2];
   __shared__ int8_t s_field[kMaxSmemN];
+  __shared__ double diag_pre[2 * kMaxSmemN];
 
   const int k = (MODE == MODE_FWD) ? j : (w.nstack - 1 - j);
   const int t_lo = k * p + 1, t_hi = min((k + 1) * p, Lt);
   const int side = (MODE == MODE_FWD) ? 0 : 1;
 
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  constexpr int nwarp = kThreads / 32;
   // chain <- U_top diag(D_top)  or  I
   for (int sp = 0; sp < S; ++sp) {
     double* C = w.chain + (long long)sp * N * N;
-    if (j == 0) {
-      for (int e = threadIdx.x; e < N * N; e += kThreads) C[e] = ((e % N) == (e / N)) ? 1.0 : 0.0;
-    } else {
-      const double* lv = stack_level(w, side, sp, j - 1);
-      const double* U = lv;
-      const double* D = lv + 2LL * N * N;
-      for (int e = threadIdx.x; e < N * N; e += kThreads) C[e] = U[e] * D[e / N];
+    const double* lv = (j == 0) ? nullptr : stack_level(w, side, sp, j - 1);
+    for (int c = wid; c < N; c += nwarp) {
+      const double dc = lv ? lv[2LL * N * N + c] : 1.0;
+      for (int r = lane; r < N; r += 32)
+        C[(long long)c * N + r] = lv ? lv[(long long)c * N + r] * dc : ((r == c) ? 1.0 : 0.0);
     }
   }
   if (MODE != MODE_INIT) {
     for (int sp = 0; sp < S; ++sp) {
       const double* Gg = w.G + (long long)sp * N * N;
-      for (int e = threadIdx.x; e < N * N; e += kThreads) at(Gs[sp], ld, e % N, e / N) = Gg[e];
+      for (int c = wid; c < N; c += nwarp)
+        for (int r = lane; r < N; r += 32) at(Gs[sp], ld, r, c) = Gg[(long long)c * N + r];
     }
   }
   __syncthreads();
@@ -428,12 +436,25 @@ __global__ void __launch_bounds__(kThreads) segment_kernel(const WalkerDev* __re
       }
     }
 
-    if (MODE != MODE_INIT) {  // Metropolis over sites i = 0..N-1
-      for (int i = 0; i < N; ++i) {
-        if (threadIdx.x == 0) {
+    if (MODE != MODE_INIT) {
+      // Metropolis over sites i = 0..N-1 (dqmc_walker.cpp:173-197).
+      // Warp 0 decides; warps 1.. apply the rank-1 update of the last accepted
+      // site meanwhile.  Sites rejected in between leave G unchanged, so the
+      // decision thread scans ahead with the diagonal the pending update will
+      // produce, computed with the same fma the update uses (bit-identical).
+      auto decide_from = [&](int i0, bool pending) {
+        // returns the next accepted site (or N); thread 0 only
+        for (int i = i0; i < N; ++i) {
           const int s = s_field[i];
           const int si = s > 0 ? 0 : 1;
-          const double gu = at(Gs[0], ld, i, i), gd = at(Gs[1], ld, i, i);
+          double gu, gd;
+          if (pending) {
+            gu = fma(-vec[(2 + 0) * N + i], vec[0 * N + i], diag_pre[i]);
+            gd = (S == 2) ? fma(-vec[(2 + 1) * N + i], vec[1 * N + i], diag_pre[N + i]) : gu;
+          } else {
+            gu = at(Gs[0], ld, i, i);
+            gd = at(Gs[1], ld, i, i);
+          }
           const double cu = w.cm[si];
           const double cd = (w.model == 0) ? w.cp[si] : w.cm[si];
           // same operation order as the reference, no contraction
@@ -444,32 +465,52 @@ __global__ void __launch_bounds__(kThreads) segment_kernel(const WalkerDev* __re
           const double u = (w.rng == 0) ? w.uni[attempt]
                                         : philox_uniform(w.seed, blockIdx.x, w.sweep_id, (unsigned)(eff * N + i));
           const double prob = fmin(1.0, fabs(r));
-          const int acc = (u < prob) ? 1 : 0;
           if (!isfinite(r)) atomicOr(w.status, ST_NONFINITE_RATIO);
-          if (acc) {
+          if (u < prob) {
             s_f[0] = __ddiv_rn(cu, ru);
             s_f[1] = (w.model == 0) ? __ddiv_rn(cd, rd) : s_f[0];
             s_field[i] = (int8_t)(-s);
             sign = (r >= 0) ? sign : -sign;
             ++acc_count;
+            return i;
           }
-          s_acc = acc;
+        }
+        return N;
+      };
+      if (threadIdx.x == 0) s_next = decide_from(0, false);
+      __syncthreads();
+      while (s_next < N) {
+        const int i = s_next;
+        // vectors of site i from the fully updated G, and the diagonal before its update
+        if (threadIdx.x < N) {
+          const int r = threadIdx.x;
+          for (int sp = 0; sp < S; ++sp) {
+            const double* g = Gs[sp];
+            vec[sp * N + r] = s_f[sp] * at(g, ld, r, i);                       // f u
+            vec[(2 + sp) * N + r] = ((r == i) ? 1.0 : 0.0) - at(g, ld, i, r);  // e_i - G(i,:)
+            diag_pre[sp * N + r] = at(g, ld, r, r);
+          }
         }
         __syncthreads();
-        if (s_acc) {
-          for (int e = threadIdx.x; e < S * N; e += kThreads) {
-            const int sp = e / N, r = e % N;
-            vec[sp * N + r] = s_f[sp] * at(Gs[sp], ld, r, i);                         // f u
-            vec[(2 + sp) * N + r] = ((r == i) ? 1.0 : 0.0) - at(Gs[sp], ld, i, r);    // e_i - G(i,:)
+        if (threadIdx.x < 32) {
+          if (threadIdx.x == 0) s_next = decide_from(i + 1, true);
+        } else {
+          // warps 1..7: column c per warp, rows lane and lane+32 per lane
+          const int lane = threadIdx.x & 31, uw = (threadIdx.x >> 5) - 1;
+          const int r0 = lane, r1 = lane + 32;
+          for (int sp = 0; sp < S; ++sp) {
+            double* g = Gs[sp];
+            const double* wv = vec + (2 + sp) * N;
+            const double u0 = (r0 < N) ? vec[sp * N + r0] : 0.0;
+            const double u1 = (r1 < N) ? vec[sp * N + r1] : 0.0;
+            for (int c = uw; c < N; c += kThreads / 32 - 1) {
+              const double wc = -wv[c];
+              if (r0 < N) at(g, ld, r0, c) = fma(wc, u0, at(g, ld, r0, c));
+              if (r1 < N) at(g, ld, r1, c) = fma(wc, u1, at(g, ld, r1, c));
+            }
           }
-          __syncthreads();
-          for (int e = threadIdx.x; e < S * N * N; e += kThreads) {
-            const int sp = e / (N * N), rc = e % (N * N);
-            const int r = rc % N, c = rc / N;
-            at(Gs[sp], ld, r, c) = fma(-vec[(2 + sp) * N + c], vec[sp * N + r], at(Gs[sp], ld, r, c));
-          }
-          __syncthreads();
         }
+        __syncthreads();
       }
       // write back the flipped fields of this slice
       int8_t* frw = w.fields + (long long)eff * N;
@@ -512,7 +553,8 @@ __global__ void __launch_bounds__(kThreads) segment_kernel(const WalkerDev* __re
   if (MODE != MODE_INIT) {
     for (int sp = 0; sp < S; ++sp) {
       double* Gg = w.G + (long long)sp * N * N;
-      for (int e = threadIdx.x; e < N * N; e += kThreads) Gg[e] = at(Gs[sp], ld, e % N, e / N);
+      for (int c = wid; c < N; c += nwarp)
+        for (int r = lane; r < N; r += 32) Gg[(long long)c * N + r] = at(Gs[sp], ld, r, c);
     }
     if (threadIdx.x == 0) {
       *w.sign = sign;
@@ -525,10 +567,47 @@ __global__ void __launch_bounds__(kThreads) segment_kernel(const WalkerDev* __re
 // Stack push (svd_stack.cpp:34-61 with QRP for the SVD):
 //   X = chain (= B_p..B_1 U_top D_top), X P = Q R,
 //   U = Q, D = |diag R|, F_new = (D^-1 R P^T) F_prev.
-// One CTA per (walker, spin); X and Q in shared memory.
+// One CTA of kPushThreads per (walker, spin); thread j owns column j.  GB300
+// issues an FP64 warp instruction every ~64 cycles per SM sub-partition, so
+// the kernel avoids FP64 shuffle reductions in the O(N^3) parts: every dot
+// product runs down one thread's own column.  Q is formed in place from the
+// reflectors (LAPACK dorg2r order), so one N x N tile of SMEM suffices.
 // --------------------------------------------------------------------------
+constexpr int kPushThreads = 64;
+
+// argmax of non-negative key over threads (ties -> lowest index); all threads get it
+__device__ __forceinline__ int block64_argmax(double v, int idx, bool valid, int* s_i, long long* s_k) {
+  long long key = valid ? __double_as_longlong(v) : -1LL;  // non-negative doubles order as integers
+  int bi = idx;
+  for (int o = 16; o > 0; o >>= 1) {
+    const long long ok = __shfl_xor_sync(0xffffffffu, key, o);
+    const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+    if (ok > key || (ok == key && oi < bi)) { key = ok; bi = oi; }
+  }
+  const int wid = threadIdx.x >> 5;
+  if ((threadIdx.x & 31) == 0) { s_k[wid] = key; s_i[wid] = bi; }
+  __syncthreads();
+  int best = s_i[0];
+  long long bk = s_k[0];
+  for (int q = 1; q < kPushThreads / 32; ++q)
+    if (s_k[q] > bk || (s_k[q] == bk && s_i[q] < best)) { bk = s_k[q]; best = s_i[q]; }
+  __syncthreads();
+  return best;
+}
+
+__device__ __forceinline__ double block64_sum(double v, double* s_d) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  const int wid = threadIdx.x >> 5;
+  if ((threadIdx.x & 31) == 0) s_d[wid] = v;
+  __syncthreads();
+  double t = 0;
+  for (int q = 0; q < kPushThreads / 32; ++q) t += s_d[q];
+  __syncthreads();
+  return t;
+}
+
 template <int MODE>
-__global__ void __launch_bounds__(kThreads) push_kernel(const WalkerDev* __restrict__ W, int j) {
+__global__ void __launch_bounds__(kPushThreads) push_kernel(const WalkerDev* __restrict__ W, int j) {
   const int wi = blockIdx.x >> 1, sp = blockIdx.x & 1;
   const WalkerDev& w = W[wi];
   if (j >= w.nstack || sp >= w.S) return;
@@ -536,147 +615,173 @@ __global__ void __launch_bounds__(kThreads) push_kernel(const WalkerDev* __restr
   const int N = w.N, ld = N + 1;
   const int side = (MODE == MODE_FWD) ? 0 : 1;
   double* X = smem;
-  double* Q = X + (long long)N * ld;
-  double* vn1 = Q + (long long)N * ld;
+  double* vn1 = X + (long long)N * ld;
   double* vn2 = vn1 + N;
   double* tau = vn2 + N;
-  double* red = tau + N;          // 64
-  int* perm = (int*)(red + 64);   // N ints
-  __shared__ int s_piv;
-  __shared__ double s_tau;
+  double* invd = tau + N;
+  int* perm = (int*)(invd + N);
+  __shared__ int s_i[kPushThreads / 32];
+  __shared__ long long s_k[kPushThreads / 32];
+  __shared__ double s_d[kPushThreads / 32];
+  __shared__ double s_tau, s_scal, s_beta;
+  const int tj = threadIdx.x;  // column / row owned by this thread
+  const bool own = tj < N;
 
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = kThreads / 32;
   const double* C = w.chain + (long long)sp * N * N;
-  for (int e = threadIdx.x; e < N * N; e += kThreads) at(X, ld, e % N, e / N) = C[e];
-  for (int c = threadIdx.x; c < N; c += kThreads) perm[c] = c;
+  for (int c = 0; c < N; ++c)
+    if (own) at(X, ld, tj, c) = C[(long long)c * N + tj];
   __syncthreads();
-  for (int c = wid; c < N; c += nw) {  // column norms
-    double s = 0;
-    for (int r = lane; r < N; r += 32) s += at(X, ld, r, c) * at(X, ld, r, c);
-    s = warp_sum(s);
-    if (lane == 0) vn1[c] = vn2[c] = sqrt(s);
+  if (own) {
+    double s0 = 0, s1 = 0;
+    int r = 0;
+    for (; r + 1 < N; r += 2) {
+      const double a = at(X, ld, r, tj), b = at(X, ld, r + 1, tj);
+      s0 = fma(a, a, s0);
+      s1 = fma(b, b, s1);
+    }
+    if (r < N) s0 = fma(at(X, ld, r, tj), at(X, ld, r, tj), s0);
+    vn1[tj] = vn2[tj] = sqrt(s0 + s1);
+    perm[tj] = tj;
   }
   __syncthreads();
 
   const double tol3z = 1.4901161193847656e-08;  // sqrt(eps), LAPACK dlaqp2
   for (int k = 0; k < N; ++k) {
-    if (wid == 0) {  // pivot: largest remaining norm, lowest index on ties
-      double best = -1.0;
-      int bi = k;
-      for (int c = k + lane; c < N; c += 32)
-        if (vn1[c] > best) { best = vn1[c]; bi = c; }
-      for (int o = 16; o > 0; o >>= 1) {
-        const double ob = __shfl_xor_sync(0xffffffffu, best, o);
-        const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
-        if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
-      }
-      if (lane == 0) s_piv = bi;
-    }
-    __syncthreads();
-    const int pv = s_piv;
+    // ---- pivot: largest remaining column norm
+    const int pv = block64_argmax(own ? vn1[tj] : 0.0, tj, own && tj >= k, s_i, s_k);
     if (pv != k) {
-      for (int r = threadIdx.x; r < N; r += kThreads) {
-        const double tmp = at(X, ld, r, k);
-        at(X, ld, r, k) = at(X, ld, r, pv);
-        at(X, ld, r, pv) = tmp;
+      if (own) {
+        const double a = at(X, ld, tj, k);
+        at(X, ld, tj, k) = at(X, ld, tj, pv);
+        at(X, ld, tj, pv) = a;
       }
-      if (threadIdx.x == 0) {
+      if (tj == 0) {
         const int tp = perm[k]; perm[k] = perm[pv]; perm[pv] = tp;
         double tv = vn1[k]; vn1[k] = vn1[pv]; vn1[pv] = tv;
         tv = vn2[k]; vn2[k] = vn2[pv]; vn2[pv] = tv;
       }
+      __syncthreads();
     }
-    __syncthreads();
-    if (wid == 0) {  // Householder reflector of X[k:,k]
-      double s = 0;
-      for (int r = k + 1 + lane; r < N; r += 32) s += at(X, ld, r, k) * at(X, ld, r, k);
-      s = warp_sum(s);
+    // ---- Householder reflector of X[k:,k]: row r > k held by thread r
+    const double xr = (own && tj > k) ? at(X, ld, tj, k) : 0.0;
+    const double xnorm2 = block64_sum(xr * xr, s_d);
+    if (tj == 0) {
       const double alpha = at(X, ld, k, k);
       double t = 0.0, beta = alpha, scal = 1.0;
-      if (s != 0.0) {
-        const double nrm = sqrt(alpha * alpha + s);
+      if (xnorm2 != 0.0) {
+        const double nrm = sqrt(alpha * alpha + xnorm2);
         beta = alpha >= 0 ? -nrm : nrm;
         t = (beta - alpha) / beta;
         scal = 1.0 / (alpha - beta);
       }
-      for (int r = k + 1 + lane; r < N; r += 32) at(X, ld, r, k) *= scal;
-      __syncwarp();
-      if (lane == 0) { at(X, ld, k, k) = beta; tau[k] = t; s_tau = t; }
+      s_tau = t; s_scal = scal; s_beta = beta;
+      tau[k] = t;
     }
     __syncthreads();
+    if (own && tj > k) at(X, ld, tj, k) *= s_scal;
+    if (tj == 0) at(X, ld, k, k) = s_beta;
+    __syncthreads();
+    // ---- trailing update of column tj > k, then its norm downdate
     const double tk = s_tau;
-    for (int c = k + 1 + wid; c < N; c += nw) {  // trailing update, warp per column
-      double s = 0;
-      for (int r = k + 1 + lane; r < N; r += 32) s += at(X, ld, r, k) * at(X, ld, r, c);
-      s = warp_sum(s) + at(X, ld, k, c);
-      const double wv = s * tk;
-      for (int r = k + 1 + lane; r < N; r += 32) at(X, ld, r, c) -= wv * at(X, ld, r, k);
-      __syncwarp();
-      if (lane == 0) at(X, ld, k, c) -= wv;
-      __syncwarp();
-      // column-norm downdate with recomputation safeguard
-      double v1 = vn1[c];
+    if (own && tj > k && tk != 0.0) {
+      double a0 = at(X, ld, k, tj), a1 = 0.0;
+      int r = k + 1;
+      for (; r + 1 < N; r += 2) {
+        a0 = fma(at(X, ld, r, k), at(X, ld, r, tj), a0);
+        a1 = fma(at(X, ld, r + 1, k), at(X, ld, r + 1, tj), a1);
+      }
+      if (r < N) a0 = fma(at(X, ld, r, k), at(X, ld, r, tj), a0);
+      const double wv = (a0 + a1) * tk;
+      at(X, ld, k, tj) -= wv;
+      for (r = k + 1; r < N; ++r) at(X, ld, r, tj) = fma(-wv, at(X, ld, r, k), at(X, ld, r, tj));
+    }
+    if (own && tj > k) {
+      const double v1 = vn1[tj];
       if (v1 != 0.0) {
-        double tmp = fabs(at(X, ld, k, c)) / v1;
+        double tmp = fabs(at(X, ld, k, tj)) / v1;
         tmp = fmax(0.0, 1.0 - tmp * tmp);
-        const double r2 = v1 / vn2[c];
+        const double r2 = v1 / vn2[tj];
         if (tmp * r2 * r2 <= tol3z) {
-          double q = 0;
-          for (int r = k + 1 + lane; r < N; r += 32) q += at(X, ld, r, c) * at(X, ld, r, c);
-          q = sqrt(warp_sum(q));
-          if (lane == 0) { vn1[c] = q; vn2[c] = q; }
-        } else if (lane == 0) {
-          vn1[c] = v1 * sqrt(tmp);
+          double q0 = 0, q1 = 0;
+          int r = k + 1;
+          for (; r + 1 < N; r += 2) {
+            q0 = fma(at(X, ld, r, tj), at(X, ld, r, tj), q0);
+            q1 = fma(at(X, ld, r + 1, tj), at(X, ld, r + 1, tj), q1);
+          }
+          if (r < N) q0 = fma(at(X, ld, r, tj), at(X, ld, r, tj), q0);
+          vn1[tj] = vn2[tj] = sqrt(q0 + q1);
+        } else {
+          vn1[tj] = v1 * sqrt(tmp);
         }
       }
     }
     __syncthreads();
   }
 
-  // D and the new right factor F = (D^-1 R P^T) F_prev
+  // ---- D = |diag R| and the right factor F = (D^-1 R P^T) F_prev
   double* lv = stack_level(w, side, sp, j);
   double* Uo = lv;
   double* Fo = lv + (long long)N * N;
   double* Do = lv + 2LL * N * N;
-  for (int i = threadIdx.x; i < N; i += kThreads) {
-    const double d = fabs(at(X, ld, i, i));
-    Do[i] = d;
-    vn1[i] = (d != 0.0) ? 1.0 / d : 0.0;
+  if (own) {
+    const double d = fabs(at(X, ld, tj, tj));
+    Do[tj] = d;
+    invd[tj] = (d != 0.0) ? 1.0 / d : 0.0;
     if (d == 0.0 || !isfinite(d)) atomicOr(w.status, ST_SINGULAR);
   }
   __syncthreads();
   if (j == 0) {
-    for (int e = threadIdx.x; e < N * N; e += kThreads) {
-      const int i = e % N, c = e / N;  // T(i, perm[c]) = R(i,c)/D(i) for c >= i
-      Fo[(long long)perm[c] * N + i] = (c >= i) ? at(X, ld, i, c) * vn1[i] : 0.0;
+    // F = T: column perm[c] of T holds R(:,c)/D for rows i <= c
+    if (own) {
+      const int c = tj;
+      double* fc = Fo + (long long)perm[c] * N;
+      for (int i = 0; i < N; ++i) fc[i] = (i <= c) ? at(X, ld, i, c) * invd[i] : 0.0;
     }
-    __syncthreads();
-  } else {
-    const double* Fp = stack_level(w, side, sp, j - 1) + (long long)N * N;
-    block_gemm(N, [&](int r, int kk) { return (kk >= r) ? at(X, ld, r, kk) * vn1[r] : 0.0; },
-               [&](int kk, int c) { return __ldg(Fp + (long long)c * N + perm[kk]); },
-               [&](int r, int c, double v) { Fo[(long long)c * N + r] = v; });
-  }
-
-  // Q = H_0 H_1 .. H_{N-1} (backward accumulation into I)
-  for (int e = threadIdx.x; e < N * N; e += kThreads) at(Q, ld, e % N, e / N) = ((e % N) == (e / N)) ? 1.0 : 0.0;
-  __syncthreads();
-  for (int kk = N - 1; kk >= 0; --kk) {
-    const double tk = tau[kk];
-    if (tk != 0.0) {
-      for (int c = kk + wid; c < N; c += nw) {
-        double s = 0;
-        for (int r = kk + 1 + lane; r < N; r += 32) s += at(X, ld, r, kk) * at(Q, ld, r, c);
-        s = warp_sum(s) + at(Q, ld, kk, c);
-        const double wv = s * tk;
-        for (int r = kk + 1 + lane; r < N; r += 32) at(Q, ld, r, c) -= wv * at(X, ld, r, kk);
-        __syncwarp();
-        if (lane == 0) at(Q, ld, kk, c) -= wv;
+  } else if (own) {
+    // thread c: F_new(i,c) = sum_{k>=i} (R(i,k)/D(i)) F_prev(perm[k], c)
+    const int c = tj;
+    const double* fp = stack_level(w, side, sp, j - 1) + (long long)N * N + (long long)c * N;
+    double* fo = Fo + (long long)c * N;
+    for (int i = 0; i < N; ++i) {
+      double a0 = 0.0, a1 = 0.0;
+      int k = i;
+      for (; k + 1 < N; k += 2) {
+        a0 = fma(at(X, ld, i, k), __ldg(fp + perm[k]), a0);
+        a1 = fma(at(X, ld, i, k + 1), __ldg(fp + perm[k + 1]), a1);
       }
+      if (k < N) a0 = fma(at(X, ld, i, k), __ldg(fp + perm[k]), a0);
+      fo[i] = (a0 + a1) * invd[i];
+    }
+  }
+  __syncthreads();
+
+  // ---- Q = H_0 H_1 ... H_{N-1}, formed in place (dorg2r order)
+  for (int i = N - 1; i >= 0; --i) {
+    const double ti = tau[i];
+    if (i < N - 1 && own && tj > i) {
+      // apply H_i to column tj (rows i..N-1), v = [1; X(i+1:,i)]
+      double a0 = at(X, ld, i, tj), a1 = 0.0;
+      int r = i + 1;
+      for (; r + 1 < N; r += 2) {
+        a0 = fma(at(X, ld, r, i), at(X, ld, r, tj), a0);
+        a1 = fma(at(X, ld, r + 1, i), at(X, ld, r + 1, tj), a1);
+      }
+      if (r < N) a0 = fma(at(X, ld, r, i), at(X, ld, r, tj), a0);
+      const double wv = (a0 + a1) * ti;
+      at(X, ld, i, tj) -= wv;
+      for (r = i + 1; r < N; ++r) at(X, ld, r, tj) = fma(-wv, at(X, ld, r, i), at(X, ld, r, tj));
+    }
+    __syncthreads();
+    if (own) {  // column i of Q: thread tj handles row tj
+      const int r = tj;
+      if (r > i) at(X, ld, r, i) *= -ti;
+      else if (r == i) at(X, ld, r, i) = 1.0 - ti;
+      else at(X, ld, r, i) = 0.0;
     }
     __syncthreads();
   }
-  for (int e = threadIdx.x; e < N * N; e += kThreads) Uo[e] = at(Q, ld, e % N, e / N);
+  for (int c = 0; c < N; ++c)
+    if (own) Uo[(long long)c * N + tj] = at(X, ld, tj, c);
 }
 
 // --------------------------------------------------------------------------
@@ -1008,7 +1113,7 @@ double run_fp64_probe(cudaError_t* err) {
 // host-side launch helpers
 // --------------------------------------------------------------------------
 size_t segment_smem_bytes(int N, int S) { return sizeof(double) * ((size_t)S * N * (N + 1) + 8 * N + 64 + 2 * N); }
-size_t push_smem_bytes(int N) { return sizeof(double) * (2 * (size_t)N * (N + 1) + 3 * N + 64) + sizeof(int) * N; }
+size_t push_smem_bytes(int N) { return sizeof(double) * ((size_t)N * (N + 1) + 4 * N) + sizeof(int) * N; }
 size_t greens_smem_bytes(int N) { return sizeof(double) * (2 * (size_t)N * (N + 1) + 4 * N + 64); }
 size_t measure_smem_bytes(int N) { return sizeof(double) * (2 * (size_t)N * (N + 1) + 64 + 2 * N); }
 
@@ -1036,9 +1141,9 @@ void launch_segment(int mode, const WalkerDev* W, int nw, int j, int measure, in
 }
 void launch_push(int mode, const WalkerDev* W, int nw, int j, int maxN, cudaStream_t st) {
   const size_t sm = push_smem_bytes(maxN);
-  if (mode == MODE_INIT) push_kernel<MODE_INIT><<<2 * nw, kThreads, sm, st>>>(W, j);
-  else if (mode == MODE_FWD) push_kernel<MODE_FWD><<<2 * nw, kThreads, sm, st>>>(W, j);
-  else push_kernel<MODE_BWD><<<2 * nw, kThreads, sm, st>>>(W, j);
+  if (mode == MODE_INIT) push_kernel<MODE_INIT><<<2 * nw, kPushThreads, sm, st>>>(W, j);
+  else if (mode == MODE_FWD) push_kernel<MODE_FWD><<<2 * nw, kPushThreads, sm, st>>>(W, j);
+  else push_kernel<MODE_BWD><<<2 * nw, kPushThreads, sm, st>>>(W, j);
 }
 void launch_greens(int mode, const WalkerDev* W, int nw, int j, int check, int trace_slot, int maxN, cudaStream_t st) {
   greens_kernel<<<2 * nw, kThreads, greens_smem_bytes(maxN), st>>>(W, mode, j, check, trace_slot);

@@ -68,7 +68,11 @@ def _run_pair(dq, O, descs, sweeps=1, stack=None, fields=None, measure=True):
             if measure:
                 r.measure()
             np.testing.assert_array_equal(batch.fields(k), r.fields(), err_msg=f"walker {k}: decisions differ")
-            tg, tr = batch.trace(k), r.trace_get()
+            # the device keeps max-nstack slots per half-sweep for every walker
+            ns_max = max(-(-x.Lt // x.pace) for x in descs)
+            ns = -(-descs[k].Lt // descs[k].pace)
+            tg_all, tr = batch.trace(k), r.trace_get()
+            tg = np.concatenate([tg_all[h * ns_max:h * ns_max + ns] for h in range(2)])
             assert tg.shape == tr.shape
             for i in range(tr.shape[0]):
                 for s in (0, 1):
