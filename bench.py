@@ -41,6 +41,10 @@ WORKLOADS = {
     # batch of 256 FP64 walkers, checkerboard (the batched FP64 configuration)
     "fp64_batch_8x8_checkerboard": dict(walkers=256, model=0, L=8, U=4.0, mu=0.0, beta=8.0, Lt=160, pace=10,
                                          checkerboard=True),
+    # 128 FP64 walkers, attractive 16x16 dense, beta=10 (the plain-FP64 run of the
+    # mixed-precision configuration: same model, lattice, beta and pace)
+    "fp64_batch_16x16_attractive": dict(walkers=128, model=1, L=16, U=4.0, mu=-0.5, beta=10.0, Lt=100, pace=8,
+                                        checkerboard=False),
     # one FP64 walker, 4x4 dense (the reference's single-chain case)
     "fp64_single_4x4_dense": dict(walkers=1, model=0, L=4, U=4.0, mu=0.0, beta=4.0, Lt=80, pace=10,
                                   checkerboard=False),

@@ -33,6 +33,15 @@ void launch_greens(int mode, const WalkerDev* W, int nw, int j, int check, int t
 void launch_measure(int mode, const WalkerDev* W, int nw, int j, int maxN, cudaStream_t st);
 void launch_sign(const WalkerDev* W, int nw, int maxN, cudaStream_t st);
 double run_fp64_probe(cudaError_t* err);
+// general (N > 64) walkers, kernels_general.cu
+cudaError_t configure_general_kernels();
+void general_slice(int mode, const WalkerDev* W, int nw, int j, int q, int maxN, int measure, bool any_dense,
+                   bool any_cb, cudaStream_t st);
+void general_chain_init(int mode, const WalkerDev* W, int nw, int j, cudaStream_t st);
+void general_push(int mode, const WalkerDev* W, int nw, int j, int maxN, cudaStream_t st);
+void general_greens(int mode, const WalkerDev* W, int nw, int j, int trace_slot, int maxN, cudaStream_t st);
+void general_measure_after(int mode, const WalkerDev* W, int nw, int j, int maxN, cudaStream_t st);
+void general_sign(const WalkerDev* W, int nw, int maxN, cudaStream_t st);
 }  // namespace dqmc
 
 using namespace dqmc;
@@ -145,6 +154,9 @@ size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
 struct dqmc_batch {
   int nw = 0, maxN = 0, maxNs = 0, maxLt = 0;
+  // walkers split by kernel family: N <= 64 (SMEM-resident) and N > 64 (general)
+  int maxN_small = 0, maxN_general = 0, maxPace_general = 0;
+  bool any_small = false, any_general = false, any_general_dense = false, any_general_cb = false;
   dqmc_batch_options opt{};
   std::vector<dqmc_walker_desc> desc;
   std::vector<WalkerDev> hw;        // host copies of the descriptors
@@ -226,7 +238,7 @@ int dqmc_batch_create(const dqmc_walker_desc* descs, int n, const dqmc_batch_opt
     if (d.model != DQMC_REPULSIVE_HUBBARD && d.model != DQMC_ATTRACTIVE_HUBBARD)
       return fail(DQMC_ERR_ARG, "walker %d: unknown model %d", w, d.model);
     if (d.L < 2) return fail(DQMC_ERR_ARG, "walker %d: lattice side %d < 2", w, d.L);
-    if (d.L * d.L > kMaxSmemN) return fail(DQMC_ERR_ARG, "walker %d: N = %d exceeds the supported %d", w, d.L * d.L, kMaxSmemN);
+    if (d.L * d.L > kMaxN) return fail(DQMC_ERR_ARG, "walker %d: N = %d exceeds the supported %d", w, d.L * d.L, kMaxN);
     if (d.checkerboard && (d.L % 2)) return fail(DQMC_ERR_ARG, "walker %d: checkerboard needs an even side", w);
     if (d.Lt < 1 || d.pace < 1) return fail(DQMC_ERR_ARG, "walker %d: Lt and pace must be >= 1", w);
     if (!(d.beta > 0) || !(d.onsite_u >= 0) || !(d.hopping_t >= 0))
@@ -243,6 +255,16 @@ int dqmc_batch_create(const dqmc_walker_desc* descs, int n, const dqmc_batch_opt
   b->opt = o;
   b->desc.assign(descs, descs + n);
   for (auto& d : b->desc) {
+    const int N = d.L * d.L;
+    if (N > kMaxSmemN) {
+      b->any_general = true;
+      b->maxN_general = std::max(b->maxN_general, N);
+      b->maxPace_general = std::max(b->maxPace_general, d.pace);
+      if (d.checkerboard) b->any_general_cb = true; else b->any_general_dense = true;
+    } else {
+      b->any_small = true;
+      b->maxN_small = std::max(b->maxN_small, N);
+    }
     b->maxN = std::max(b->maxN, d.L * d.L);
     const int ns = (d.Lt % d.pace == 0) ? d.Lt / d.pace : d.Lt / d.pace + 1;
     b->maxNs = std::max(b->maxNs, ns);
@@ -251,7 +273,7 @@ int dqmc_batch_create(const dqmc_walker_desc* descs, int n, const dqmc_batch_opt
   b->trace_cap = o.trace ? 4 * b->maxNs : 0;
 
   // ---- arena layout ----
-  struct Off { size_t G, chain, stack, fields, ff, trace; int dense_id; };
+  struct Off { size_t G, chain, work, scr, stack, fields, ff, trace; int dense_id; };
   std::vector<Off> off(n);
   std::map<std::tuple<int, double, double, double>, int> dense_ids;  // (L, t, mu, dtau) -> id
   std::vector<std::pair<std::vector<double>, std::vector<double>>> dense;
@@ -266,8 +288,11 @@ int dqmc_batch_create(const dqmc_walker_desc* descs, int n, const dqmc_batch_opt
     const int S = (d.model == DQMC_ATTRACTIVE_HUBBARD) ? 1 : 2;
     const int ns = (d.Lt % d.pace == 0) ? d.Lt / d.pace : d.Lt / d.pace + 1;
     const size_t lvl = (2 * (size_t)N * N + N + 31) & ~(size_t)31;
+    const bool general = N > kMaxSmemN;
     off[w].G = take(sizeof(double) * 2 * N * N);
-    off[w].chain = take(sizeof(double) * S * N * N);
+    off[w].chain = take(sizeof(double) * (general ? 2 : 1) * S * N * N);
+    off[w].work = general ? take(sizeof(double) * S * N * N) : 0;
+    off[w].scr = general ? take(sizeof(double) * 2 * S * N * N) : 0;
     off[w].stack = take(sizeof(double) * 2 * S * ns * lvl);
     off[w].fields = take((size_t)d.Lt * N);
     off[w].trace = b->trace_cap ? take(sizeof(double) * (size_t)b->trace_cap * 2 * N * N) : 0;
@@ -303,6 +328,7 @@ int dqmc_batch_create(const dqmc_walker_desc* descs, int n, const dqmc_batch_opt
   }
   e = cudaStreamCreateWithFlags(&b->own, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = configure_fp64_kernels(kMaxSmemN);
+  if (e == cudaSuccess) e = configure_general_kernels();
   if (e != cudaSuccess) {
     cudaFree(b->arena);
     delete b;
@@ -371,6 +397,8 @@ int dqmc_batch_create(const dqmc_walker_desc* descs, int n, const dqmc_batch_opt
     plaq(h.cbI, std::cosh(-dtau * d.hopping_t), std::sinh(-dtau * d.hopping_t), std::exp(-0.5 * dtau * d.mu));
     h.G = reinterpret_cast<double*>(base + off[w].G);
     h.chain = reinterpret_cast<double*>(base + off[w].chain);
+    h.work = N > kMaxSmemN ? reinterpret_cast<double*>(base + off[w].work) : nullptr;
+    h.scr = N > kMaxSmemN ? reinterpret_cast<double*>(base + off[w].scr) : nullptr;
     h.stack = reinterpret_cast<double*>(base + off[w].stack);
     h.lvl_stride = (long long)((2 * (size_t)N * N + N + 31) & ~(size_t)31);
     h.side_stride = (long long)h.S * h.nstack * h.lvl_stride;
@@ -487,11 +515,26 @@ static int launch_check(const char* what) {
 int dqmc_init_greens(dqmc_batch* b) {
   if (!b) return fail(DQMC_ERR_ARG, "null batch");
   for (int j = 0; j < b->maxNs; ++j) {
-    launch_segment(MODE_INIT, b->dW, b->nw, j, 0, b->maxN, b->stream);
-    launch_push(MODE_INIT, b->dW, b->nw, j, b->maxN, b->stream);
+    if (b->any_small) {
+      launch_segment(MODE_INIT, b->dW, b->nw, j, 0, b->maxN_small, b->stream);
+      launch_push(MODE_INIT, b->dW, b->nw, j, b->maxN_small, b->stream);
+    }
+    if (b->any_general) {
+      general_chain_init(MODE_INIT, b->dW, b->nw, j, b->stream);
+      for (int q = 0; q < b->maxPace_general; ++q)
+        general_slice(MODE_INIT, b->dW, b->nw, j, q, b->maxN_general, 0, b->any_general_dense, b->any_general_cb,
+                      b->stream);
+      general_push(MODE_INIT, b->dW, b->nw, j, b->maxN_general, b->stream);
+    }
   }
-  launch_greens(MODE_INIT, b->dW, b->nw, 0, 0, -1, b->maxN, b->stream);
-  launch_sign(b->dW, b->nw, b->maxN, b->stream);
+  if (b->any_small) {
+    launch_greens(MODE_INIT, b->dW, b->nw, 0, 0, -1, b->maxN_small, b->stream);
+    launch_sign(b->dW, b->nw, b->maxN_small, b->stream);
+  }
+  if (b->any_general) {
+    general_greens(MODE_INIT, b->dW, b->nw, 0, -1, b->maxN_general, b->stream);
+    general_sign(b->dW, b->nw, b->maxN_general, b->stream);
+  }
   if (int r = launch_check("init kernels")) return r;
   // wrap error and accumulators start from zero (DqmcWalker::initial, dqmc_walker.cpp:41-49)
   for (int w = 0; w < b->nw; ++w) {
@@ -523,11 +566,30 @@ static int half_sweep(dqmc_batch* b, int mode, int measure) {
     CUDA_TRY(cudaMemcpyAsync(b->dW, b->hw.data(), sizeof(WalkerDev) * b->nw, cudaMemcpyHostToDevice, b->stream));
   }
   for (int j = 0; j < b->maxNs; ++j) {
-    b->timed(DQMC_KCLASS_SEGMENT, [&] { launch_segment(mode, b->dW, b->nw, j, measure, b->maxN, b->stream); });
-    b->timed(DQMC_KCLASS_PUSH, [&] { launch_push(mode, b->dW, b->nw, j, b->maxN, b->stream); });
     const int slot = (b->trace_cap && b->trace_count + j < b->trace_cap) ? b->trace_count + j : -1;
-    b->timed(DQMC_KCLASS_GREENS, [&] { launch_greens(mode, b->dW, b->nw, j, 1, slot, b->maxN, b->stream); });
-    if (measure) b->timed(DQMC_KCLASS_MEASURE, [&] { launch_measure(mode, b->dW, b->nw, j, b->maxN, b->stream); });
+    if (b->any_small) {
+      b->timed(DQMC_KCLASS_SEGMENT,
+               [&] { launch_segment(mode, b->dW, b->nw, j, measure, b->maxN_small, b->stream); });
+      b->timed(DQMC_KCLASS_PUSH, [&] { launch_push(mode, b->dW, b->nw, j, b->maxN_small, b->stream); });
+      b->timed(DQMC_KCLASS_GREENS,
+               [&] { launch_greens(mode, b->dW, b->nw, j, 1, slot, b->maxN_small, b->stream); });
+      if (measure)
+        b->timed(DQMC_KCLASS_MEASURE, [&] { launch_measure(mode, b->dW, b->nw, j, b->maxN_small, b->stream); });
+    }
+    if (b->any_general) {
+      b->timed(DQMC_KCLASS_SEGMENT, [&] {
+        general_chain_init(mode, b->dW, b->nw, j, b->stream);
+        for (int q = 0; q < b->maxPace_general; ++q)
+          general_slice(mode, b->dW, b->nw, j, q, b->maxN_general, measure, b->any_general_dense,
+                        b->any_general_cb, b->stream);
+      });
+      b->timed(DQMC_KCLASS_PUSH, [&] { general_push(mode, b->dW, b->nw, j, b->maxN_general, b->stream); });
+      b->timed(DQMC_KCLASS_GREENS,
+               [&] { general_greens(mode, b->dW, b->nw, j, slot, b->maxN_general, b->stream); });
+      if (measure)
+        b->timed(DQMC_KCLASS_MEASURE,
+                 [&] { general_measure_after(mode, b->dW, b->nw, j, b->maxN_general, b->stream); });
+    }
   }
   if (b->trace_cap) b->trace_count = std::min(b->trace_count + b->maxNs, b->trace_cap);
   if (b->opt.rng == DQMC_RNG_MINSTD) {

@@ -18,6 +18,7 @@ namespace dqmc {
 
 constexpr int kThreads = 256;
 constexpr int kMaxSmemN = 64;    // N handled by the SMEM-resident kernels
+constexpr int kMaxN = 1024;      // largest N of the general (HBM-resident) kernels
 constexpr int kNumObs = 9;
 
 enum SweepMode { MODE_INIT = 0, MODE_FWD = 1, MODE_BWD = 2 };
@@ -40,7 +41,9 @@ struct WalkerDev {
   double cm[2], cp[2], ex2[2];
   double cbP[16], cbI[16];   // checkerboard plaquettes exp(+dtau t h) e^{0.5 dtau mu}, inverse
   double* G;                 // [2][N*N]
-  double* chain;             // [S][N*N]
+  double* chain;             // [S][N*N] (general walkers: [2][S][N*N], ping-pong)
+  double* work;              // general walkers: GEMM temporary [S][N*N]
+  double* scr;               // general walkers: stabilization scratch [S][2][N*N]
   double* stack;             // see header
   long long lvl_stride;      // doubles per stack level (2 N^2 + N, padded)
   long long side_stride;     // doubles per side (S * nstack * lvl_stride)

@@ -1,0 +1,1024 @@
+// kernels_general.cu — FP64 plain-method kernels for walkers whose G does not
+// fit in shared memory (N > 64, up to 1024).
+//
+// G, the B-chain and the stacks stay in HBM/L2; a half-sweep runs slice by
+// slice as a short sequence of batched launches:
+//   wrap (two batched GEMMs with the diagonal exp(+/-alpha s) fused, or
+//   checkerboard passes) -> Metropolis (one CTA per walker, rank-1 updates,
+//   look-ahead decisions) -> measurement -> B-chain step (GEMM, ping-pong).
+// Stabilization: column-pivoted QR with one thread per column (row-major copy,
+// coalesced across threads), Green's assembly by batched GEMMs and an LU solve
+// with one thread per column of [M | Y].
+//
+// Reference behaviour is the same as kernels_fp64.cu (src/dqmc_walker.cpp,
+// src/model/*.cpp, src/svd_stack.cpp, include/utils/numerical_stable.hpp,
+// src/measure/measure_methods.cpp); only the data placement differs.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdint>
+
+#include "dqmc_device.cuh"
+
+namespace dqmc {
+
+__device__ double philox_uniform_g(unsigned long long seed, unsigned walker, unsigned long long sweep,
+                                   unsigned attempt);
+
+namespace {
+
+__device__ __forceinline__ double warp_sum_g(double v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+__device__ __forceinline__ bool is_general(const WalkerDev& w) { return w.N > kMaxSmemN; }
+
+// Slice t handled at step j, in-segment index q (false when q is past the segment).
+__device__ __forceinline__ bool slice_of(const WalkerDev& w, int mode, int j, int q, int& t, int& nsl, int& t_hi) {
+  if (j >= w.nstack) return false;
+  const int k = (mode == MODE_FWD) ? j : (w.nstack - 1 - j);
+  const int t_lo = k * w.pace + 1;
+  t_hi = min((k + 1) * w.pace, w.Lt);
+  nsl = t_hi - t_lo + 1;
+  if (q >= nsl) return false;
+  t = (mode == MODE_FWD) ? t_lo + q : t_hi - q;
+  return true;
+}
+
+// exp(sgn * spin_factor * alpha * s(t-1, i))
+__device__ __forceinline__ double bscale(const WalkerDev& w, int t, int spin, int sgn, int i) {
+  const int sf = (w.model == 0 && spin == 1) ? -1 : 1;
+  const int s = w.fields[(long long)(t - 1) * w.N + i];
+  return (sgn * sf * s > 0) ? w.e_pa : w.e_ma;
+}
+
+__device__ __forceinline__ double* chain_buf(const WalkerDev& w, int spin, int which) {
+  return w.chain + ((long long)which * w.S + spin) * w.N * w.N;
+}
+
+}  // namespace
+
+// --------------------------------------------------------------------------
+// Batched FP64 GEMM, 64x64 output tile per CTA, 16-deep K steps staged in
+// SMEM, 4x4 register tile per thread.  The operation (operands, transposes,
+// fused diagonal scalings, epilogue) is selected by OP; each CTA finds its
+// walker, spin and slice from the descriptors.
+// --------------------------------------------------------------------------
+enum GemmOp {
+  OP_WL_FWD = 0,   // work = diag(e^{+}) expK G          (mult_B_from_left)
+  OP_WR_FWD = 1,   // G    = work expK^-1 diag(e^{-})    (mult_invB_from_right)
+  OP_WR_BWD = 2,   // work = G diag(e^{+}) expK          (mult_B_from_right)
+  OP_WL_BWD = 3,   // G    = expK^-1 diag(e^{-}) work    (mult_invB_from_left)
+  OP_CH_FWD = 4,   // chain' = diag(e^{+}) expK chain    (B-chain, forward)
+  OP_CH_BWD = 5,   // chain' = expK^T diag(e^{+}) chain  (B-chain, backward / init)
+  OP_GA = 6,       // M  = Dlmax^-1 (U_L^T U_R) Drmax^-1
+  OP_GB = 7,       // M += Dlmin (F_L F_R^T) Drmin
+  OP_GG = 8,       // G  = (U_R Drmax^-1) X, wrap error, trace
+};
+
+constexpr int kTile = 64, kTk = 16;
+
+template <int OP>
+__global__ void __launch_bounds__(256) gemm_op_kernel(const WalkerDev* __restrict__ W, int mode, int j, int q,
+                                                      int trace_slot) {
+  const int wi = blockIdx.z >> 1, sp = blockIdx.z & 1;
+  const WalkerDev& w = W[wi];
+  if (!is_general(w) || sp >= w.S) return;
+  const int N = w.N;
+  const int r0 = blockIdx.y * kTile, c0 = blockIdx.x * kTile;
+  if (r0 >= N || c0 >= N) return;
+  int t = 0, nsl = 0, t_hi = 0;
+  const bool slice_op = OP <= OP_CH_BWD;
+  if (slice_op && w.cb) return;  // checkerboard walkers take cb_general_kernel (expK is null for them)
+  if (slice_op && !slice_of(w, mode, j, q, t, nsl, t_hi)) return;
+  if (!slice_op && j >= w.nstack) return;
+
+  const long long NN = (long long)N * N;
+  double* G = w.G + sp * NN;
+  double* work = w.work + sp * NN;
+  const double* A = nullptr;
+  const double* B = nullptr;
+  double* C = nullptr;
+  // stack tops for the Green's assembly (lengths after this step's push)
+  int nl = 0, nr = 0;
+  if (!slice_op) {
+    if (mode == MODE_FWD) { nl = j + 1; nr = w.nstack - 1 - j; }
+    else if (mode == MODE_BWD) { nl = w.nstack - 1 - j; nr = j + 1; }
+    else { nl = 0; nr = w.nstack; }
+  }
+  if (!slice_op && !(nl > 0 && nr > 0)) return;  // boundary steps: prep/out kernels
+  const double* UL = nl ? stack_level(w, 0, sp, nl - 1) : nullptr;
+  const double* UR = nr ? stack_level(w, 1, sp, nr - 1) : nullptr;
+  const double* DL = UL ? UL + 2 * NN : nullptr;
+  const double* DR = UR ? UR + 2 * NN : nullptr;
+  double* scr = w.scr + sp * 2 * NN;  // M (col-major), Y/X (row-major)
+  switch (OP) {
+    case OP_WL_FWD: A = w.expK; B = G; C = work; break;
+    case OP_WR_FWD: A = work; B = w.invK; C = G; break;
+    case OP_WR_BWD: A = G; B = w.expK; C = work; break;
+    case OP_WL_BWD: A = w.invK; B = work; C = G; break;
+    case OP_CH_FWD:
+    case OP_CH_BWD: A = w.expK; B = chain_buf(w, sp, q & 1); C = chain_buf(w, sp, (q + 1) & 1); break;
+    case OP_GA: A = UL; B = UR; C = scr; break;
+    case OP_GB: A = UL + NN; B = UR + NN; C = scr; break;      // F_L, F_R
+    case OP_GG: A = UR; B = scr + NN; C = G; break;           // U_R, X (row-major)
+  }
+
+  __shared__ double As[kTk][kTile + 1];
+  __shared__ double Bs[kTk][kTile + 1];
+  __shared__ double s_red[8];
+  __shared__ double s_inv[OP == OP_GG ? kMaxN : 1];  // 1 / max(D_R, 1) along k
+  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+  if (OP == OP_GG) {
+    for (int k = tid; k < N; k += 256) s_inv[k] = 1.0 / fmax(DR[k], 1.0);
+    __syncthreads();
+  }
+  double acc[4][4];
+#pragma unroll
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int b = 0; b < 4; ++b) acc[a][b] = 0.0;
+
+  for (int k0 = 0; k0 < N; k0 += kTk) {
+    // A tile: rows r0..r0+63, k k0..k0+15 -> As[kk][rr]
+#pragma unroll
+    for (int e = tid; e < kTile * kTk; e += 256) {
+      const int rr = e % kTile, kk = e / kTile;
+      const int r = r0 + rr, k = k0 + kk;
+      double v = 0.0;
+      if (r < N && k < N) {
+        switch (OP) {
+          case OP_WL_FWD: v = A[(long long)k * N + r] * bscale(w, t, sp, +1, r); break;
+          case OP_WR_FWD: v = A[(long long)k * N + r]; break;
+          case OP_WR_BWD: v = A[(long long)k * N + r] * bscale(w, t, sp, +1, k); break;
+          case OP_WL_BWD: v = A[(long long)k * N + r]; break;
+          case OP_CH_FWD: v = A[(long long)k * N + r] * bscale(w, t, sp, +1, r); break;
+          case OP_CH_BWD: v = A[(long long)r * N + k] * bscale(w, t, sp, +1, k); break;  // expK^T
+          case OP_GA: v = A[(long long)r * N + k]; break;  // U_L^T (r,k) = U_L(k,r)
+          case OP_GB: v = A[(long long)k * N + r]; break;
+          case OP_GG: v = A[(long long)k * N + r] * s_inv[k]; break;  // U_R(r,k) / drmax_k
+        }
+      }
+      As[kk][rr] = v;
+    }
+    // B tile: k k0..k0+15, cols c0..c0+63 -> Bs[kk][cc]
+#pragma unroll
+    for (int e = tid; e < kTile * kTk; e += 256) {
+      const int kk = e % kTk, cc = e / kTk;
+      const int k = k0 + kk, c = c0 + cc;
+      double v = 0.0;
+      if (k < N && c < N) {
+        switch (OP) {
+          case OP_WL_FWD: v = B[(long long)c * N + k]; break;
+          case OP_WR_FWD: v = B[(long long)c * N + k]; break;
+          case OP_WR_BWD: v = B[(long long)c * N + k]; break;
+          case OP_WL_BWD: v = B[(long long)c * N + k] * bscale(w, t, sp, -1, k); break;
+          case OP_CH_FWD: v = B[(long long)c * N + k]; break;
+          case OP_CH_BWD: v = B[(long long)c * N + k]; break;
+          case OP_GA: v = B[(long long)c * N + k]; break;
+          case OP_GB: v = B[(long long)k * N + c]; break;  // F_R^T(k,c) = F_R(c,k)
+          case OP_GG: v = B[(long long)k * N + c]; break;                     // X row-major
+        }
+      }
+      Bs[kk][cc] = v;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < kTk; ++kk) {
+      double av[4], bv[4];
+#pragma unroll
+      for (int a = 0; a < 4; ++a) av[a] = As[kk][ty + 16 * a];
+#pragma unroll
+      for (int b = 0; b < 4; ++b) bv[b] = Bs[kk][tx + 16 * b];
+#pragma unroll
+      for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) acc[a][b] = fma(av[a], bv[b], acc[a][b]);
+    }
+    __syncthreads();
+  }
+
+  // epilogue
+  double err = 0.0;
+  bool finite = true;
+  double* tr = (OP == OP_GG && w.trace && trace_slot >= 0 && trace_slot < w.trace_cap)
+                   ? w.trace + ((long long)trace_slot * 2 + sp) * NN : nullptr;
+  const bool check = (OP == OP_GG) && !(mode == MODE_INIT || (mode == MODE_BWD && j == w.nstack - 1));
+#pragma unroll
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+      const int r = r0 + ty + 16 * a, c = c0 + tx + 16 * b;
+      if (r >= N || c >= N) continue;
+      double v = acc[a][b];
+      const long long o = (long long)c * N + r;
+      switch (OP) {
+        case OP_WR_FWD: v *= bscale(w, t, sp, -1, c); break;
+        case OP_GA: v /= fmax(DL[r], 1.0) * fmax(DR[c], 1.0); break;
+        case OP_GB: v *= fmin(DL[r], 1.0) * fmin(DR[c], 1.0); break;
+        default: break;
+      }
+      if (OP == OP_GB) {
+        C[o] += v;
+      } else if (OP == OP_GG) {
+        if (check) err = fmax(err, fabs(v - C[o]));
+        if (!isfinite(v)) finite = false;
+        C[o] = v;
+        if (tr) tr[o] = v;
+        if (w.S == 1) {
+          C[NN + o] = v;
+          if (tr) tr[NN + o] = v;
+        }
+      } else {
+        C[o] = v;
+      }
+    }
+  if (OP == OP_GG) {
+    if (!finite) atomicOr(w.status, ST_NONFINITE_G);
+    if (check) {
+      for (int o = 16; o > 0; o >>= 1) err = fmax(err, __shfl_xor_sync(0xffffffffu, err, o));
+      if ((tid & 31) == 0) s_red[tid >> 5] = err;
+      __syncthreads();
+      if (tid == 0) {
+        double m = 0;
+        for (int k = 0; k < 8; ++k) m = fmax(m, s_red[k]);
+        atomicMax(w.wrap_bits, (unsigned long long)__double_as_longlong(m));
+      }
+    }
+  }
+}
+
+// --------------------------------------------------------------------------
+// Checkerboard on global matrices (general N): one CTA per (walker, spin).
+//   kind 0: wrap fwd  G <- P_A P_B G (scale rows e^+) ; G <- G P_B^-1 P_A^-1 (scale cols e^-)
+//   kind 1: wrap bwd  G <- G diag(e^+) P_A P_B ; G <- P_B^-1 P_A^-1 diag(e^-) G
+//   kind 2: chain fwd C <- diag(e^+) P_A P_B C
+//   kind 3: chain bwd C <- P_B P_A diag(e^+) C
+// --------------------------------------------------------------------------
+__device__ void cbg_pass(double* M, int N, int L, int parity, const double* P, bool left, const double* pre,
+                         const double* post) {
+  const int nq = (L >> 1) * (L >> 1), half = L >> 1;
+  for (int it = threadIdx.x; it < nq * N; it += blockDim.x) {
+    int q, x2;
+    if (left) { q = it % nq; x2 = it / nq; } else { x2 = it % N; q = it / N; }
+    const int x = 2 * (q % half) + parity, y = 2 * (q / half) + parity;
+    const int x1 = (x + 1) % L, y1 = (y + 1) % L;
+    const int idx[4] = {x + L * y, x1 + L * y, x + L * y1, x1 + L * y1};
+    double v[4];
+    for (int a = 0; a < 4; ++a) {
+      v[a] = left ? M[(long long)x2 * N + idx[a]] : M[(long long)idx[a] * N + x2];
+      if (pre) v[a] *= pre[idx[a]];
+    }
+    for (int a = 0; a < 4; ++a) {
+      double o = 0.0;
+      for (int b = 0; b < 4; ++b) o = left ? fma(P[a * 4 + b], v[b], o) : fma(v[b], P[b * 4 + a], o);
+      if (post) o *= post[idx[a]];
+      if (left) M[(long long)x2 * N + idx[a]] = o; else M[(long long)idx[a] * N + x2] = o;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(256) cb_general_kernel(const WalkerDev* __restrict__ W, int mode, int j, int q,
+                                                         int kind) {
+  const int wi = blockIdx.x >> 1, sp = blockIdx.x & 1;
+  const WalkerDev& w = W[wi];
+  if (!is_general(w) || !w.cb || sp >= w.S) return;
+  int t, nsl, t_hi;
+  if (!slice_of(w, mode, j, q, t, nsl, t_hi)) return;
+  extern __shared__ double sh[];
+  const int N = w.N, L = w.L;
+  double* dpos = sh;
+  double* dneg = sh + N;
+  for (int i = threadIdx.x; i < N; i += blockDim.x) {
+    dpos[i] = bscale(w, t, sp, +1, i);
+    dneg[i] = bscale(w, t, sp, -1, i);
+  }
+  __syncthreads();
+  double* G = w.G + (long long)sp * N * N;
+  double* C = chain_buf(w, sp, 0);
+  switch (kind) {
+    case 0:
+      cbg_pass(G, N, L, 1, w.cbP, true, nullptr, nullptr); __syncthreads();
+      cbg_pass(G, N, L, 0, w.cbP, true, nullptr, dpos); __syncthreads();
+      cbg_pass(G, N, L, 1, w.cbI, false, nullptr, nullptr); __syncthreads();
+      cbg_pass(G, N, L, 0, w.cbI, false, nullptr, dneg); __syncthreads();
+      break;
+    case 1:
+      cbg_pass(G, N, L, 0, w.cbP, false, dpos, nullptr); __syncthreads();
+      cbg_pass(G, N, L, 1, w.cbP, false, nullptr, nullptr); __syncthreads();
+      cbg_pass(G, N, L, 0, w.cbI, true, dneg, nullptr); __syncthreads();
+      cbg_pass(G, N, L, 1, w.cbI, true, nullptr, nullptr); __syncthreads();
+      break;
+    case 2:
+      cbg_pass(C, N, L, 1, w.cbP, true, nullptr, nullptr); __syncthreads();
+      cbg_pass(C, N, L, 0, w.cbP, true, nullptr, dpos); __syncthreads();
+      break;
+    case 3:
+      cbg_pass(C, N, L, 0, w.cbP, true, dpos, nullptr); __syncthreads();
+      cbg_pass(C, N, L, 1, w.cbP, true, nullptr, nullptr); __syncthreads();
+      break;
+  }
+}
+
+// --------------------------------------------------------------------------
+// Chain start of step j: chain <- U_top diag(D_top) or I (general walkers).
+// --------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) chain_init_general_kernel(const WalkerDev* __restrict__ W, int mode, int j) {
+  const int wi = blockIdx.y >> 1, sp = blockIdx.y & 1;
+  const WalkerDev& w = W[wi];
+  if (!is_general(w) || sp >= w.S || j >= w.nstack) return;
+  const int N = w.N;
+  const int side = (mode == MODE_FWD) ? 0 : 1;
+  const double* lv = j ? stack_level(w, side, sp, j - 1) : nullptr;
+  double* C = chain_buf(w, sp, 0);
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < (long long)N * N;
+       e += (long long)gridDim.x * blockDim.x) {
+    const int r = (int)(e % N), c = (int)(e / N);
+    C[e] = lv ? lv[e] * lv[2LL * N * N + c] : ((r == c) ? 1.0 : 0.0);
+  }
+}
+
+// --------------------------------------------------------------------------
+// Metropolis on global G (general N), one CTA of 512 threads per walker.
+// Warp 0 decides with look-ahead (as in the SMEM kernel), warps 1..15 apply
+// the rank-1 update of the previous accepted site.
+// --------------------------------------------------------------------------
+constexpr int kMetroThreads = 512;
+
+__global__ void __launch_bounds__(kMetroThreads) metropolis_general_kernel(const WalkerDev* __restrict__ W, int mode,
+                                                                          int j, int q) {
+  const WalkerDev& w = W[blockIdx.x];
+  if (!is_general(w)) return;
+  int t, nsl, t_hi;
+  if (!slice_of(w, mode, j, q, t, nsl, t_hi)) return;
+  extern __shared__ double sh[];
+  const int N = w.N, S = w.S, Lt = w.Lt;
+  double* vec = sh;             // [4][N]: f u (2 spins), e_i - G(i,:) (2 spins)
+  double* diag_pre = sh + 4 * N;  // [2][N]
+  int8_t* s_field = (int8_t*)(sh + 6 * N);
+  __shared__ int s_next;
+  __shared__ double s_f[2];
+  const long long NN = (long long)N * N;
+  double* Gs[2] = {w.G, (S == 2) ? w.G + NN : w.G};
+  const int eff = t - 1;
+  for (int i = threadIdx.x; i < N; i += blockDim.x) s_field[i] = w.fields[(long long)eff * N + i];
+  double sign = *w.sign;
+  long long acc_count = 0;
+  __syncthreads();
+
+  auto decide_from = [&](int i0, bool pending) {
+    for (int i = i0; i < N; ++i) {
+      const int s = s_field[i];
+      const int si = s > 0 ? 0 : 1;
+      double gu, gd;
+      if (pending) {
+        gu = fma(-vec[2 * N + i], vec[i], diag_pre[i]);
+        gd = (S == 2) ? fma(-vec[3 * N + i], vec[N + i], diag_pre[N + i]) : gu;
+      } else {
+        gu = Gs[0][(long long)i * N + i];
+        gd = Gs[1][(long long)i * N + i];
+      }
+      const double cu = w.cm[si];
+      const double cd = (w.model == 0) ? w.cp[si] : w.cm[si];
+      const double ru = __dadd_rn(1.0, __dmul_rn(__dsub_rn(1.0, gu), cu));
+      const double rd = __dadd_rn(1.0, __dmul_rn(__dsub_rn(1.0, gd), cd));
+      const double r = (w.model == 0) ? __dmul_rn(ru, rd) : __dmul_rn(__dmul_rn(w.ex2[si], ru), rd);
+      const int attempt = (mode == MODE_FWD) ? (eff * N + i) : ((Lt - t) * N + i);
+      const double u = (w.rng == 0) ? w.uni[attempt]
+                                    : philox_uniform_g(w.seed, blockIdx.x, w.sweep_id, (unsigned)(eff * N + i));
+      const double prob = fmin(1.0, fabs(r));
+      if (!isfinite(r)) atomicOr(w.status, ST_NONFINITE_RATIO);
+      if (u < prob) {
+        s_f[0] = __ddiv_rn(cu, ru);
+        s_f[1] = (w.model == 0) ? __ddiv_rn(cd, rd) : s_f[0];
+        s_field[i] = (int8_t)(-s);
+        sign = (r >= 0) ? sign : -sign;
+        ++acc_count;
+        return i;
+      }
+    }
+    return N;
+  };
+  if (threadIdx.x == 0) s_next = decide_from(0, false);
+  __syncthreads();
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+  while (s_next < N) {
+    const int i = s_next;
+    for (int r = threadIdx.x; r < N; r += blockDim.x) {
+      for (int sp = 0; sp < S; ++sp) {
+        const double* g = Gs[sp];
+        vec[sp * N + r] = s_f[sp] * g[(long long)i * N + r];
+        vec[(2 + sp) * N + r] = ((r == i) ? 1.0 : 0.0) - g[(long long)r * N + i];
+        diag_pre[sp * N + r] = g[(long long)r * N + r];
+      }
+    }
+    __syncthreads();
+    if (wid == 0) {
+      if (lane == 0) s_next = decide_from(i + 1, true);
+    } else {
+      for (int sp = 0; sp < S; ++sp) {
+        double* g = Gs[sp];
+        const double* wv = vec + (2 + sp) * N;
+        const double* uv = vec + sp * N;
+        for (int c = wid - 1; c < N; c += nwarp - 1) {
+          const double wc = -wv[c];
+          double* gc = g + (long long)c * N;
+          for (int r = lane; r < N; r += 32) gc[r] = fma(wc, uv[r], gc[r]);
+        }
+      }
+    }
+    __syncthreads();
+  }
+  int8_t* frw = w.fields + (long long)eff * N;
+  for (int i = threadIdx.x; i < N; i += blockDim.x) frw[i] = s_field[i];
+  if (threadIdx.x == 0) {
+    *w.sign = sign;
+    *w.accepts += acc_count;
+    if (mode == MODE_BWD && t == Lt) *w.sign_Lt = sign;
+  }
+}
+
+// --------------------------------------------------------------------------
+// Equal-time measurement on global G (general N); mode/j/q select the slot as
+// in the SMEM kernels.  after_stab = 1 measures the slot closing the step
+// with the fresh G (forward) or slot Lt-1 with the final G(0) (backward).
+// --------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) measure_general_kernel(const WalkerDev* __restrict__ W, int mode, int j, int q,
+                                                              int after_stab) {
+  const WalkerDev& w = W[blockIdx.x];
+  if (!is_general(w)) return;
+  double sg;
+  if (after_stab) {
+    if (j >= w.nstack) return;
+    if (mode == MODE_BWD && j != w.nstack - 1) return;
+    sg = (mode == MODE_BWD) ? *w.sign_Lt : *w.sign;
+  } else {
+    int t, nsl, t_hi;
+    if (!slice_of(w, mode, j, q, t, nsl, t_hi)) return;
+    const bool here = (mode == MODE_FWD) ? (t != t_hi) : (t != w.Lt);
+    if (!here) return;
+    sg = *w.sign;
+  }
+  const int N = w.N, L = w.L;
+  const long long NN = (long long)N * N;
+  const double* gu = w.G;
+  const double* gd = (w.S == 2) ? w.G + NN : w.G;
+  extern __shared__ double sh[];
+  double* du = sh;
+  double* dd = sh + N;
+  __shared__ double red[8 * 8];
+  for (int i = threadIdx.x; i < N; i += blockDim.x) {
+    du[i] = 1.0 - gu[(long long)i * N + i];
+    dd[i] = 1.0 - gd[(long long)i * N + i];
+  }
+  __syncthreads();
+  double v[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  for (int i = threadIdx.x; i < N; i += blockDim.x) {
+    const double a = 1.0 - du[i], b = 1.0 - dd[i];
+    v[0] += a + b;
+    v[1] += du[i] * dd[i];
+    v[2] += a + b - 2 * a * b;
+    const int x = i % L, y = i / L;
+    const int jx = (x + 1) % L + L * y, jy = x + L * ((y + 1) % L);
+    v[3] += gu[(long long)jx * N + i] + gd[(long long)jx * N + i] + gu[(long long)jy * N + i] + gd[(long long)jy * N + i];
+  }
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for (int jj = wid; jj < N; jj += blockDim.x >> 5) {
+    const int xj = jj % L, yj = jj / L;
+    for (int i = lane; i < N; i += 32) {
+      int dx = xj - i % L, dy = yj - i / L;
+      dx += (dx < 0) ? L : 0;
+      dy += (dy < 0) ? L : 0;
+      const double ff = w.ff[dx + dy * L];
+      const double gu_ij = gu[(long long)jj * N + i], gu_ji = gu[(long long)i * N + jj];
+      const double gd_ij = gd[(long long)jj * N + i], gd_ji = gd[(long long)i * N + jj];
+      const double dij = (i == jj) ? 1.0 : 0.0;
+      const double guc = dij - gu_ji, gdc = dij - gd_ji;
+      v[4] += (gu_ji + gd_ji) * ff;
+      v[5] += ff * (du[i] * du[jj] + guc * gu_ij + dd[i] * dd[jj] + gdc * gd_ij);
+      v[6] += ff * (dd[i] * du[jj] + du[i] * dd[jj]);
+      v[7] += guc * gdc;
+    }
+  }
+  for (int k = 0; k < 8; ++k) {
+    const double s = warp_sum_g(v[k]);
+    if (lane == 0) red[k * 8 + wid] = s;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double tot[8];
+    for (int k = 0; k < 8; ++k) {
+      tot[k] = 0;
+      for (int q2 = 0; q2 < (int)(blockDim.x >> 5); ++q2) tot[k] += red[k * 8 + q2];
+    }
+    const double n = (double)N;
+    double* o = w.obs;
+    o[0] += sg * (2.0 - tot[0] / n);
+    o[1] += sg * tot[1] / n;
+    o[2] += sg * (2.0 * w.hop_t) * tot[3] / n;
+    o[3] += sg * (1.0 - 0.5 * tot[4] / n);
+    o[4] += sg * tot[2] / n;
+    o[5] += sg * (tot[5] - tot[6]) / (n * n);
+    o[6] += sg * (tot[5] + tot[6]) / (n * n);
+    o[7] += sg * tot[7] / n;
+    o[8] += sg;
+    for (int k = 0; k < kNumObs; ++k) w.obs_cnt[k] += 1;
+  }
+}
+
+// --------------------------------------------------------------------------
+// Column-pivoted QR push, general N: one CTA per (walker, spin), thread per
+// column, matrix in a row-major HBM/L2 scratch (coalesced across threads).
+// --------------------------------------------------------------------------
+__global__ void __launch_bounds__(1024) push_general_kernel(const WalkerDev* __restrict__ W, int mode, int j) {
+  const int wi = blockIdx.x >> 1, sp = blockIdx.x & 1;
+  const WalkerDev& w = W[wi];
+  if (!is_general(w) || sp >= w.S || j >= w.nstack) return;
+  const int N = w.N;
+  const long long NN = (long long)N * N;
+  const int side = (mode == MODE_FWD) ? 0 : 1;
+  int nsl = 0;
+  {
+    const int k = (mode == MODE_FWD) ? j : (w.nstack - 1 - j);
+    nsl = min((k + 1) * w.pace, w.Lt) - k * w.pace;
+  }
+  const double* Cin = w.cb ? chain_buf(w, sp, 0) : chain_buf(w, sp, nsl & 1);
+  double* X = w.scr + sp * 2 * NN;  // row-major: X[r*N + c]
+  extern __shared__ double sh[];
+  double* v = sh;          // reflector / scratch column [N]
+  double* vn1 = sh + N;
+  double* vn2 = sh + 2 * N;
+  double* tau = sh + 3 * N;
+  double* invd = sh + 4 * N;
+  int* perm = (int*)(sh + 5 * N);
+  __shared__ int s_piv;
+  __shared__ double s_tau, s_scal;
+  __shared__ long long s_key[32];
+  __shared__ int s_idx[32];
+  const int tj = threadIdx.x;
+  const bool own = tj < N;
+  auto Xat = [&](int r, int c) -> double& { return X[(long long)r * N + c]; };
+
+  if (own) {
+    double s0 = 0, s1 = 0;
+    for (int r = 0; r < N; ++r) {
+      const double a = Cin[(long long)tj * N + r];
+      Xat(r, tj) = a;
+      if (r & 1) s1 = fma(a, a, s1); else s0 = fma(a, a, s0);
+    }
+    vn1[tj] = vn2[tj] = sqrt(s0 + s1);
+    perm[tj] = tj;
+  }
+  __syncthreads();
+  const double tol3z = 1.4901161193847656e-08;
+  const int nwarps = (blockDim.x + 31) >> 5;
+  for (int k = 0; k < N; ++k) {
+    // pivot
+    long long key = (own && tj >= k) ? __double_as_longlong(vn1[tj]) : -1LL;
+    int bi = tj;
+    for (int o = 16; o > 0; o >>= 1) {
+      const long long ok = __shfl_xor_sync(0xffffffffu, key, o);
+      const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+      if (ok > key || (ok == key && oi < bi)) { key = ok; bi = oi; }
+    }
+    if ((tj & 31) == 0) { s_key[tj >> 5] = key; s_idx[tj >> 5] = bi; }
+    __syncthreads();
+    if (tj == 0) {
+      long long bk = s_key[0];
+      int b = s_idx[0];
+      for (int q = 1; q < nwarps; ++q)
+        if (s_key[q] > bk || (s_key[q] == bk && s_idx[q] < b)) { bk = s_key[q]; b = s_idx[q]; }
+      s_piv = b;
+    }
+    __syncthreads();
+    const int pv = s_piv;
+    if (pv != k) {
+      if (own) {  // thread tj swaps row tj of columns k and pv
+        const double a = Xat(tj, k);
+        Xat(tj, k) = Xat(tj, pv);
+        Xat(tj, pv) = a;
+      }
+      if (tj == 0) {
+        const int tp = perm[k]; perm[k] = perm[pv]; perm[pv] = tp;
+        double tv = vn1[k]; vn1[k] = vn1[pv]; vn1[pv] = tv;
+        tv = vn2[k]; vn2[k] = vn2[pv]; vn2[pv] = tv;
+      }
+      __syncthreads();
+    }
+    // reflector: column k rows > k into v (SMEM), norm by block reduction
+    double xr = 0.0;
+    if (own && tj > k) { xr = Xat(tj, k); v[tj] = xr; }
+    double s = warp_sum_g(xr * xr);
+    if ((tj & 31) == 0) s_key[tj >> 5] = __double_as_longlong(s);
+    __syncthreads();
+    if (tj == 0) {
+      double xn2 = 0;
+      for (int q = 0; q < nwarps; ++q) xn2 += __longlong_as_double(s_key[q]);
+      const double alpha = Xat(k, k);
+      double t2 = 0.0, beta = alpha, scal = 1.0;
+      if (xn2 != 0.0) {
+        const double nrm = sqrt(alpha * alpha + xn2);
+        beta = alpha >= 0 ? -nrm : nrm;
+        t2 = (beta - alpha) / beta;
+        scal = 1.0 / (alpha - beta);
+      }
+      s_tau = t2; s_scal = scal;
+      tau[k] = t2;
+      Xat(k, k) = beta;
+    }
+    __syncthreads();
+    if (own && tj > k) {
+      const double vv = v[tj] * s_scal;
+      v[tj] = vv;
+      Xat(tj, k) = vv;
+    }
+    __syncthreads();
+    const double tk = s_tau;
+    if (own && tj > k) {
+      if (tk != 0.0) {
+        double a0 = Xat(k, tj), a1 = 0.0;
+        int r = k + 1;
+        for (; r + 1 < N; r += 2) {
+          a0 = fma(v[r], Xat(r, tj), a0);
+          a1 = fma(v[r + 1], Xat(r + 1, tj), a1);
+        }
+        if (r < N) a0 = fma(v[r], Xat(r, tj), a0);
+        const double wv = (a0 + a1) * tk;
+        Xat(k, tj) -= wv;
+        for (r = k + 1; r < N; ++r) Xat(r, tj) = fma(-wv, v[r], Xat(r, tj));
+      }
+      const double v1 = vn1[tj];
+      if (v1 != 0.0) {
+        double tmp = fabs(Xat(k, tj)) / v1;
+        tmp = fmax(0.0, 1.0 - tmp * tmp);
+        const double r2 = v1 / vn2[tj];
+        if (tmp * r2 * r2 <= tol3z) {
+          double q0 = 0, q1 = 0;
+          int r = k + 1;
+          for (; r + 1 < N; r += 2) {
+            q0 = fma(Xat(r, tj), Xat(r, tj), q0);
+            q1 = fma(Xat(r + 1, tj), Xat(r + 1, tj), q1);
+          }
+          if (r < N) q0 = fma(Xat(r, tj), Xat(r, tj), q0);
+          vn1[tj] = vn2[tj] = sqrt(q0 + q1);
+        } else {
+          vn1[tj] = v1 * sqrt(tmp);
+        }
+      }
+    }
+    __syncthreads();
+  }
+  // D and F = (D^-1 R P^T) F_prev
+  double* lv = stack_level(w, side, sp, j);
+  double* Uo = lv;
+  double* Fo = lv + NN;
+  double* Do = lv + 2 * NN;
+  if (own) {
+    const double d = fabs(Xat(tj, tj));
+    Do[tj] = d;
+    invd[tj] = (d != 0.0) ? 1.0 / d : 0.0;
+    if (d == 0.0 || !isfinite(d)) atomicOr(w.status, ST_SINGULAR);
+  }
+  __syncthreads();
+  if (own) {
+    const int c = tj;
+    if (j == 0) {
+      double* fc = Fo + (long long)perm[c] * N;
+      for (int i = 0; i < N; ++i) fc[i] = (i <= c) ? Xat(i, c) * invd[i] : 0.0;
+    } else {
+      const double* fp = stack_level(w, side, sp, j - 1) + NN + (long long)c * N;
+      double* fo = Fo + (long long)c * N;
+      for (int i = 0; i < N; ++i) {
+        double a0 = 0.0, a1 = 0.0;
+        int k = i;
+        for (; k + 1 < N; k += 2) {
+          a0 = fma(Xat(i, k), fp[perm[k]], a0);
+          a1 = fma(Xat(i, k + 1), fp[perm[k + 1]], a1);
+        }
+        if (k < N) a0 = fma(Xat(i, k), fp[perm[k]], a0);
+        fo[i] = (a0 + a1) * invd[i];
+      }
+    }
+  }
+  __syncthreads();
+  // Q in place (dorg2r order); reflector i staged into v
+  for (int i = N - 1; i >= 0; --i) {
+    const double ti = tau[i];
+    if (own && tj > i) v[tj] = Xat(tj, i);
+    __syncthreads();
+    if (i < N - 1 && own && tj > i && ti != 0.0) {
+      double a0 = Xat(i, tj), a1 = 0.0;
+      int r = i + 1;
+      for (; r + 1 < N; r += 2) {
+        a0 = fma(v[r], Xat(r, tj), a0);
+        a1 = fma(v[r + 1], Xat(r + 1, tj), a1);
+      }
+      if (r < N) a0 = fma(v[r], Xat(r, tj), a0);
+      const double wv = (a0 + a1) * ti;
+      Xat(i, tj) -= wv;
+      for (r = i + 1; r < N; ++r) Xat(r, tj) = fma(-wv, v[r], Xat(r, tj));
+    }
+    __syncthreads();
+    if (own) {
+      const int r = tj;
+      if (r > i) Xat(r, i) = v[r] * -ti;
+      else if (r == i) Xat(r, i) = 1.0 - ti;
+      else Xat(r, i) = 0.0;
+    }
+    __syncthreads();
+  }
+  if (own)
+    for (int r = 0; r < N; ++r) Uo[(long long)tj * N + r] = Xat(r, tj);
+}
+
+// --------------------------------------------------------------------------
+// Green's assembly support (general N).
+//   prep: boundary cases build M and Y; general case builds Y = Dlmax^-1 U_L^T
+//         (M comes from OP_GA/OP_GB).  M col-major in scr, Y row-major in scr+NN.
+//   lu:   solve M X = Y (partial pivoting), thread per column of [M | Y], X in Y.
+//   out:  boundary cases write G = X (or X^T) with wrap error and trace.
+// --------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) greens_prep_general_kernel(const WalkerDev* __restrict__ W, int mode, int j) {
+  const int wi = blockIdx.y >> 1, sp = blockIdx.y & 1;
+  const WalkerDev& w = W[wi];
+  if (!is_general(w) || sp >= w.S || j >= w.nstack) return;
+  const int N = w.N;
+  const long long NN = (long long)N * N;
+  int nl, nr;
+  if (mode == MODE_FWD) { nl = j + 1; nr = w.nstack - 1 - j; }
+  else if (mode == MODE_BWD) { nl = w.nstack - 1 - j; nr = j + 1; }
+  else { nl = 0; nr = w.nstack; }
+  double* M = w.scr + sp * 2 * NN;
+  double* Y = M + NN;
+  const bool both = nl > 0 && nr > 0;
+  const double* lv = (nl > 0) ? stack_level(w, 0, sp, nl - 1) : stack_level(w, 1, sp, nr - 1);
+  const double* U = lv;
+  const double* F = lv + NN;
+  const double* D = lv + 2 * NN;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < NN; e += (long long)gridDim.x * blockDim.x) {
+    const int r = (int)(e / N), c = (int)(e % N);   // Y row-major: Y[r*N + c]
+    const double y = U[(long long)r * N + c] / fmax(D[r], 1.0);  // (Dmax^-1 U^T)(r,c)
+    Y[e] = y;
+    if (!both) M[(long long)c * N + r] = y + fmin(D[r], 1.0) * F[(long long)c * N + r];
+  }
+}
+
+__global__ void __launch_bounds__(1024) lu_solve_general_kernel(const WalkerDev* __restrict__ W, int mode, int j) {
+  const int wi = blockIdx.x >> 1, sp = blockIdx.x & 1;
+  const WalkerDev& w = W[wi];
+  if (!is_general(w) || sp >= w.S || j >= w.nstack) return;
+  const int N = w.N;
+  const long long NN = (long long)N * N;
+  double* M = w.scr + sp * 2 * NN;  // col-major
+  double* Y = M + NN;               // row-major
+  extern __shared__ double sh[];
+  double* l = sh;  // multipliers of the current step
+  __shared__ int s_p;
+  __shared__ int s_bad;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  if (tid == 0) s_bad = 0;
+  for (int k = 0; k < N; ++k) {
+    if (tid < 32) {  // pivot: warp argmax of |M(r,k)|, r >= k, on the integer bit patterns
+      long long key = -1;
+      int bi = k;
+      for (int r = k + tid; r < N; r += 32) {
+        const long long a = __double_as_longlong(M[(long long)k * N + r]) & 0x7fffffffffffffffLL;
+        if (a > key) { key = a; bi = r; }
+      }
+      for (int o = 16; o > 0; o >>= 1) {
+        const long long ok = __shfl_xor_sync(0xffffffffu, key, o);
+        const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+        if (ok > key || (ok == key && oi < bi)) { key = ok; bi = oi; }
+      }
+      if (tid == 0) { s_p = bi; if (key == 0) s_bad = 1; }
+    }
+    __syncthreads();
+    const int p = s_p;
+    if (p != k) {  // swap rows k and p of M (all columns) and Y
+      for (int c = tid; c < N; c += nt) {
+        double* mc = M + (long long)c * N;
+        const double a = mc[k]; mc[k] = mc[p]; mc[p] = a;
+        const double b = Y[(long long)k * N + c]; Y[(long long)k * N + c] = Y[(long long)p * N + c];
+        Y[(long long)p * N + c] = b;
+      }
+      __syncthreads();
+    }
+    const double piv = M[(long long)k * N + k];
+    const double inv = (piv != 0.0) ? 1.0 / piv : 0.0;
+    for (int r = k + 1 + tid; r < N; r += nt) {
+      const double lr = M[(long long)k * N + r] * inv;
+      M[(long long)k * N + r] = lr;
+      l[r] = lr;
+    }
+    __syncthreads();
+    // columns of M right of k, then all columns of Y (row-major: thread per column c)
+    for (int c = k + 1 + tid; c < N; c += nt) {
+      double* mc = M + (long long)c * N;
+      const double mk = mc[k];
+      if (mk != 0.0)
+        for (int r = k + 1; r < N; ++r) mc[r] = fma(-l[r], mk, mc[r]);
+    }
+    for (int c = tid; c < N; c += nt) {
+      const double yk = Y[(long long)k * N + c];
+      if (yk != 0.0)
+        for (int r = k + 1; r < N; ++r) Y[(long long)r * N + c] = fma(-l[r], yk, Y[(long long)r * N + c]);
+    }
+    __syncthreads();
+  }
+  // back substitution, thread per column of Y (reciprocal diagonal staged in l)
+  for (int k = tid; k < N; k += nt) l[k] = 1.0 / M[(long long)k * N + k];
+  __syncthreads();
+  for (int c = tid; c < N; c += nt) {
+    for (int k = N - 1; k >= 0; --k) {
+      const double yk = Y[(long long)k * N + c] * l[k];
+      Y[(long long)k * N + c] = yk;
+      for (int r = 0; r < k; ++r) Y[(long long)r * N + c] = fma(-M[(long long)k * N + r], yk, Y[(long long)r * N + c]);
+    }
+  }
+  if (tid == 0 && s_bad) atomicOr(w.status, ST_SINGULAR);
+}
+
+__global__ void __launch_bounds__(256) greens_out_general_kernel(const WalkerDev* __restrict__ W, int mode, int j,
+                                                                 int trace_slot) {
+  const int wi = blockIdx.y >> 1, sp = blockIdx.y & 1;
+  const WalkerDev& w = W[wi];
+  if (!is_general(w) || sp >= w.S || j >= w.nstack) return;
+  int nl, nr;
+  if (mode == MODE_FWD) { nl = j + 1; nr = w.nstack - 1 - j; }
+  else if (mode == MODE_BWD) { nl = w.nstack - 1 - j; nr = j + 1; }
+  else { nl = 0; nr = w.nstack; }
+  if (nl > 0 && nr > 0) return;  // general case finished by OP_GG
+  const int N = w.N;
+  const long long NN = (long long)N * N;
+  const double* X = w.scr + sp * 2 * NN + NN;  // row-major
+  double* G = w.G + sp * NN;
+  double* tr = (w.trace && trace_slot >= 0 && trace_slot < w.trace_cap) ? w.trace + ((long long)trace_slot * 2 + sp) * NN
+                                                                       : nullptr;
+  const bool transpose_out = (nl == 0);
+  const bool check = !(mode == MODE_INIT || (mode == MODE_BWD && j == w.nstack - 1));
+  double err = 0.0;
+  bool finite = true;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < NN; e += (long long)gridDim.x * blockDim.x) {
+    const int r = (int)(e % N), c = (int)(e / N);  // G col-major (r, c)
+    const double v = transpose_out ? X[(long long)c * N + r] : X[(long long)r * N + c];
+    if (check) err = fmax(err, fabs(v - G[e]));
+    if (!isfinite(v)) finite = false;
+    G[e] = v;
+    if (tr) tr[e] = v;
+    if (w.S == 1) {
+      G[NN + e] = v;
+      if (tr) tr[NN + e] = v;
+    }
+  }
+  if (!finite) atomicOr(w.status, ST_NONFINITE_G);
+  if (check) {
+    for (int o = 16; o > 0; o >>= 1) err = fmax(err, __shfl_xor_sync(0xffffffffu, err, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(w.wrap_bits, (unsigned long long)__double_as_longlong(err));
+  }
+}
+
+// sign(det G_up det G_dn) for general walkers: LU of a copy in scr (col-major)
+__global__ void __launch_bounds__(1024) sign_general_kernel(const WalkerDev* __restrict__ W) {
+  const WalkerDev& w = W[blockIdx.x];
+  if (!is_general(w)) return;
+  const int N = w.N;
+  const long long NN = (long long)N * N;
+  __shared__ int s_p, s_neg;
+  extern __shared__ double sh[];
+  double* l = sh;
+  if (threadIdx.x == 0) s_neg = 0;
+  for (int sp = 0; sp < 2; ++sp) {
+    double* M = w.scr;  // spin 0 scratch reused sequentially
+    const double* Gg = w.G + sp * NN;
+    for (long long e = threadIdx.x; e < NN; e += blockDim.x) M[e] = Gg[e];
+    __syncthreads();
+    for (int k = 0; k < N; ++k) {
+      if (threadIdx.x == 0) {
+        int p = k;
+        double m = fabs(M[(long long)k * N + k]);
+        for (int r = k + 1; r < N; ++r) {
+          const double a = fabs(M[(long long)k * N + r]);
+          if (a > m) { m = a; p = r; }
+        }
+        s_p = p;
+        if (p != k) ++s_neg;
+        if (M[(long long)k * N + p] < 0) ++s_neg;
+      }
+      __syncthreads();
+      const int p = s_p;
+      if (p != k)
+        for (int c = threadIdx.x; c < N; c += blockDim.x) {
+          double* mc = M + (long long)c * N;
+          const double a = mc[k]; mc[k] = mc[p]; mc[p] = a;
+        }
+      __syncthreads();
+      const double inv = 1.0 / M[(long long)k * N + k];
+      for (int r = k + 1 + threadIdx.x; r < N; r += blockDim.x) l[r] = M[(long long)k * N + r] * inv;
+      __syncthreads();
+      for (int c = k + 1 + threadIdx.x; c < N; c += blockDim.x) {
+        double* mc = M + (long long)c * N;
+        const double mk = mc[k];
+        for (int r = k + 1; r < N; ++r) mc[r] = fma(-l[r], mk, mc[r]);
+      }
+      __syncthreads();
+    }
+  }
+  if (threadIdx.x == 0) *w.sign = (s_neg % 2 == 0) ? 1.0 : -1.0;
+}
+
+// Philox for the general Metropolis kernel (same generator as kernels_fp64.cu)
+__device__ double philox_uniform_g(unsigned long long seed, unsigned walker, unsigned long long sweep,
+                                   unsigned attempt) {
+  unsigned c0 = attempt, c1 = (unsigned)sweep, c2 = (unsigned)(sweep >> 32), c3 = walker;
+  unsigned k0 = (unsigned)seed, k1 = (unsigned)(seed >> 32);
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+    const unsigned hi0 = __umulhi(0xD2511F53u, c0), lo0 = 0xD2511F53u * c0;
+    const unsigned hi1 = __umulhi(0xCD9E8D57u, c2), lo1 = 0xCD9E8D57u * c2;
+    const unsigned n0 = hi1 ^ c1 ^ k0, n2 = hi0 ^ c3 ^ k1;
+    c0 = n0; c1 = lo1; c2 = n2; c3 = lo0;
+    k0 += 0x9E3779B9u;
+    k1 += 0xBB67AE85u;
+  }
+  const unsigned long long m = ((unsigned long long)(c0 >> 5) << 26) | (unsigned long long)(c1 >> 6);
+  return (double)m * (1.0 / 9007199254740992.0);
+}
+
+// --------------------------------------------------------------------------
+// host-side launchers for general walkers
+// --------------------------------------------------------------------------
+static dim3 gemm_grid(int maxN, int nw) {
+  const int t = (maxN + kTile - 1) / kTile;
+  return dim3(t, t, 2 * nw);
+}
+
+void general_slice(int mode, const WalkerDev* W, int nw, int j, int q, int maxN, int measure, bool any_dense,
+                   bool any_cb, cudaStream_t st) {
+  const dim3 g = gemm_grid(maxN, nw);
+  const size_t cb_sm = sizeof(double) * 2 * maxN;
+  const size_t met_sm = sizeof(double) * 6 * maxN + maxN + 16;
+  if (mode == MODE_FWD) {
+    if (any_dense) {
+      gemm_op_kernel<OP_WL_FWD><<<g, 256, 0, st>>>(W, mode, j, q, -1);
+      gemm_op_kernel<OP_WR_FWD><<<g, 256, 0, st>>>(W, mode, j, q, -1);
+    }
+    if (any_cb) cb_general_kernel<<<2 * nw, 256, cb_sm, st>>>(W, mode, j, q, 0);
+  }
+  if (mode != MODE_INIT) {
+    metropolis_general_kernel<<<nw, kMetroThreads, met_sm, st>>>(W, mode, j, q);
+    if (measure) measure_general_kernel<<<nw, 256, sizeof(double) * 2 * maxN, st>>>(W, mode, j, q, 0);
+  }
+  if (any_dense) {
+    if (mode == MODE_FWD) gemm_op_kernel<OP_CH_FWD><<<g, 256, 0, st>>>(W, mode, j, q, -1);
+    else gemm_op_kernel<OP_CH_BWD><<<g, 256, 0, st>>>(W, mode, j, q, -1);
+  }
+  if (any_cb) cb_general_kernel<<<2 * nw, 256, cb_sm, st>>>(W, mode, j, q, mode == MODE_FWD ? 2 : 3);
+  if (mode == MODE_BWD) {
+    if (any_dense) {
+      gemm_op_kernel<OP_WR_BWD><<<g, 256, 0, st>>>(W, mode, j, q, -1);
+      gemm_op_kernel<OP_WL_BWD><<<g, 256, 0, st>>>(W, mode, j, q, -1);
+    }
+    if (any_cb) cb_general_kernel<<<2 * nw, 256, cb_sm, st>>>(W, mode, j, q, 1);
+  }
+}
+
+cudaError_t configure_general_kernels() {
+  cudaError_t e;
+  const int met = (int)(sizeof(double) * 6 * kMaxN + kMaxN + 16);
+  if ((e = cudaFuncSetAttribute(metropolis_general_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, met))) return e;
+  return cudaSuccess;
+}
+
+void general_chain_init(int mode, const WalkerDev* W, int nw, int j, cudaStream_t st) {
+  chain_init_general_kernel<<<dim3(64, 2 * nw), 256, 0, st>>>(W, mode, j);
+}
+
+void general_push(int mode, const WalkerDev* W, int nw, int j, int maxN, cudaStream_t st) {
+  const int threads = ((maxN + 31) / 32) * 32;
+  push_general_kernel<<<2 * nw, threads, sizeof(double) * 5 * maxN + sizeof(int) * maxN, st>>>(W, mode, j);
+}
+
+void general_greens(int mode, const WalkerDev* W, int nw, int j, int trace_slot, int maxN, cudaStream_t st) {
+  const dim3 g = gemm_grid(maxN, nw);
+  // general case needs M from the two GEMMs; boundary cases skip them (kernels exit)
+  if (mode != MODE_INIT) {
+    gemm_op_kernel<OP_GA><<<g, 256, 0, st>>>(W, mode, j, 0, -1);
+    gemm_op_kernel<OP_GB><<<g, 256, 0, st>>>(W, mode, j, 0, -1);
+  }
+  greens_prep_general_kernel<<<dim3(64, 2 * nw), 256, 0, st>>>(W, mode, j);
+  const int threads = std::min(1024, ((maxN + 31) / 32) * 32);
+  lu_solve_general_kernel<<<2 * nw, threads, sizeof(double) * maxN, st>>>(W, mode, j);
+  if (mode != MODE_INIT) gemm_op_kernel<OP_GG><<<g, 256, 0, st>>>(W, mode, j, 0, trace_slot);
+  greens_out_general_kernel<<<dim3(64, 2 * nw), 256, 0, st>>>(W, mode, j, trace_slot);
+}
+
+void general_measure_after(int mode, const WalkerDev* W, int nw, int j, int maxN, cudaStream_t st) {
+  measure_general_kernel<<<nw, 256, sizeof(double) * 2 * maxN, st>>>(W, mode, j, 0, 1);
+}
+
+void general_sign(const WalkerDev* W, int nw, int maxN, cudaStream_t st) {
+  sign_general_kernel<<<nw, 1024, sizeof(double) * maxN, st>>>(W);
+}
+
+}  // namespace dqmc

@@ -43,7 +43,7 @@ def test_abi_version(dq):
     "kw, msg",
     [
         (dict(L=1), "side"),
-        (dict(L=9), "exceeds"),
+        (dict(L=33), "exceeds"),
         (dict(L=3, checkerboard=True), "even"),
         (dict(Lt=0), "Lt"),
         (dict(pace=0), "pace"),

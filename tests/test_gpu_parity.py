@@ -154,3 +154,36 @@ def test_philox_mode_consistent(dq, oracle_mod):
             assert _close(batch.green(k, s), r.green(s))
         assert batch.status(k) == 0
         assert batch.accept_count(k) > 0
+
+
+# ---- walkers whose G lives in HBM/L2 (N > 64): batched-GEMM wrap, global QRP/LU ----
+
+def test_general_dense_repulsive(dq, oracle_mod):
+    d = dq.WalkerDesc(model=0, L=10, U=4.0, beta=2.0, Lt=20, pace=5, seed=31)
+    _run_pair(dq, oracle_mod, [d], sweeps=1)
+
+
+def test_general_checkerboard(dq, oracle_mod):
+    d = dq.WalkerDesc(model=0, L=10, U=4.0, beta=2.0, Lt=20, pace=5, checkerboard=True, seed=32)
+    _run_pair(dq, oracle_mod, [d], sweeps=1)
+
+
+def test_general_attractive_odd_side(dq, oracle_mod):
+    d = dq.WalkerDesc(model=1, L=9, U=4.0, mu=-0.5, beta=2.0, Lt=20, pace=6, seed=33)
+    _run_pair(dq, oracle_mod, [d], sweeps=1)
+
+
+def test_mixed_small_and_general_batch(dq, oracle_mod):
+    descs = [
+        dq.WalkerDesc(model=0, L=6, U=3.0, beta=2.0, Lt=20, pace=5, seed=41),
+        dq.WalkerDesc(model=0, L=12, U=4.0, beta=1.5, Lt=15, pace=5, seed=42),
+        dq.WalkerDesc(model=1, L=8, U=4.0, mu=-0.5, beta=2.0, Lt=20, pace=10, checkerboard=True, seed=43),
+        dq.WalkerDesc(model=0, L=10, U=5.0, beta=2.0, Lt=24, pace=8, checkerboard=True, seed=44),
+    ]
+    _run_pair(dq, oracle_mod, descs, sweeps=1)
+
+
+def test_general_16x16_attractive(dq, oracle_mod):
+    """The 16x16 attractive model of the mixed-precision configuration (short beta)."""
+    d = dq.WalkerDesc(model=1, L=16, U=4.0, mu=-0.5, beta=1.6, Lt=16, pace=8, seed=51)
+    _run_pair(dq, oracle_mod, [d], sweeps=1)
