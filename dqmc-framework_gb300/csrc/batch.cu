@@ -36,12 +36,21 @@ double run_fp64_probe(cudaError_t* err);
 // general (N > 64) walkers, kernels_general.cu
 cudaError_t configure_general_kernels();
 void general_slice(int mode, const WalkerDev* W, int nw, int j, int q, int maxN, int measure, bool any_dense,
-                   bool any_cb, cudaStream_t st);
+                   bool any_cb, bool mixed, cudaStream_t st);
 void general_chain_init(int mode, const WalkerDev* W, int nw, int j, cudaStream_t st);
 void general_push(int mode, const WalkerDev* W, int nw, int j, int maxN, cudaStream_t st);
 void general_greens(int mode, const WalkerDev* W, int nw, int j, int trace_slot, int maxN, cudaStream_t st);
 void general_measure_after(int mode, const WalkerDev* W, int nw, int j, int maxN, cudaStream_t st);
 void general_sign(const WalkerDev* W, int nw, int maxN, cudaStream_t st);
+// mixed-precision products, kernels_ozaki.cu
+cudaError_t configure_ozaki_kernels();
+void mixed_wrap_fwd(const WalkerDev* W, int nw, int maxN, int j, int q, cudaStream_t st);
+void mixed_wrap_bwd(const WalkerDev* W, int nw, int maxN, int j, int q, cudaStream_t st);
+void mixed_chain(const WalkerDev* W, int nw, int maxN, int mode, int j, int q, cudaStream_t st);
+void oz_slice_const(const double* X, unsigned short* out, int* exps, int N, int ldk, int role, int bits, int slices,
+                    cudaStream_t st);
+void oz_selftest(const double* A, const double* B, double* C, unsigned short* sa, int* ea, unsigned short* sb, int* eb,
+                 int N, cudaStream_t st);
 }  // namespace dqmc
 
 using namespace dqmc;
@@ -157,6 +166,7 @@ struct dqmc_batch {
   // walkers split by kernel family: N <= 64 (SMEM-resident) and N > 64 (general)
   int maxN_small = 0, maxN_general = 0, maxPace_general = 0;
   bool any_small = false, any_general = false, any_general_dense = false, any_general_cb = false;
+  bool mixed = false;
   dqmc_batch_options opt{};
   std::vector<dqmc_walker_desc> desc;
   std::vector<WalkerDev> hw;        // host copies of the descriptors
@@ -232,7 +242,8 @@ int dqmc_batch_create(const dqmc_walker_desc* descs, int n, const dqmc_batch_opt
   dqmc_batch_options o{};
   if (opt) o = *opt;
   if (o.rng != DQMC_RNG_MINSTD && o.rng != DQMC_RNG_PHILOX) return fail(DQMC_ERR_ARG, "unknown rng mode %d", o.rng);
-  if (o.precision != DQMC_FP64) return fail(DQMC_ERR_ARG, "unknown precision mode %d", o.precision);
+  if (o.precision != DQMC_FP64 && o.precision != DQMC_MIXED)
+    return fail(DQMC_ERR_ARG, "unknown precision mode %d", o.precision);
   for (int w = 0; w < n; ++w) {
     const auto& d = descs[w];
     if (d.model != DQMC_REPULSIVE_HUBBARD && d.model != DQMC_ATTRACTIVE_HUBBARD)
@@ -256,7 +267,7 @@ int dqmc_batch_create(const dqmc_walker_desc* descs, int n, const dqmc_batch_opt
   b->desc.assign(descs, descs + n);
   for (auto& d : b->desc) {
     const int N = d.L * d.L;
-    if (N > kMaxSmemN) {
+    if (N > kMaxSmemN || o.precision == DQMC_MIXED) {
       b->any_general = true;
       b->maxN_general = std::max(b->maxN_general, N);
       b->maxPace_general = std::max(b->maxPace_general, d.pace);
@@ -271,9 +282,10 @@ int dqmc_batch_create(const dqmc_walker_desc* descs, int n, const dqmc_batch_opt
     b->maxLt = std::max(b->maxLt, d.Lt);
   }
   b->trace_cap = o.trace ? 4 * b->maxNs : 0;
+  b->mixed = (o.precision == DQMC_MIXED);
 
   // ---- arena layout ----
-  struct Off { size_t G, chain, work, scr, stack, fields, ff, trace; int dense_id; };
+  struct Off { size_t G, chain, work, scr, sl, sle, stack, fields, ff, trace; int dense_id; };
   std::vector<Off> off(n);
   std::map<std::tuple<int, double, double, double>, int> dense_ids;  // (L, t, mu, dtau) -> id
   std::vector<std::pair<std::vector<double>, std::vector<double>>> dense;
@@ -288,7 +300,10 @@ int dqmc_batch_create(const dqmc_walker_desc* descs, int n, const dqmc_batch_opt
     const int S = (d.model == DQMC_ATTRACTIVE_HUBBARD) ? 1 : 2;
     const int ns = (d.Lt % d.pace == 0) ? d.Lt / d.pace : d.Lt / d.pace + 1;
     const size_t lvl = (2 * (size_t)N * N + N + 31) & ~(size_t)31;
-    const bool general = N > kMaxSmemN;
+    const bool general = N > kMaxSmemN || o.precision == DQMC_MIXED;
+    const int ldk = (N + 15) / 16 * 16;
+    off[w].sl = (o.precision == DQMC_MIXED) ? take(sizeof(unsigned short) * S * 7 * (size_t)N * ldk) : 0;
+    off[w].sle = (o.precision == DQMC_MIXED) ? take(sizeof(int) * S * (size_t)N) : 0;
     off[w].G = take(sizeof(double) * 2 * N * N);
     off[w].chain = take(sizeof(double) * (general ? 2 : 1) * S * N * N);
     off[w].work = general ? take(sizeof(double) * S * N * N) : 0;
@@ -312,10 +327,17 @@ int dqmc_batch_create(const dqmc_walker_desc* descs, int n, const dqmc_batch_opt
     if (!ff_off.count(fk)) ff_off[fk] = take(sizeof(double) * N);
     off[w].ff = ff_off[fk];
   }
-  std::vector<size_t> dense_off(dense.size());
+  std::vector<size_t> dense_off(dense.size()), dense_sl(dense.size()), dense_sle(dense.size());
+  std::vector<int> dense_n(dense.size());
+  for (auto& kv : dense_ids) dense_n[kv.second] = std::get<0>(kv.first) * std::get<0>(kv.first);
   for (size_t i = 0; i < dense.size(); ++i) {
     const size_t nn = dense[i].first.size();
     dense_off[i] = take(sizeof(double) * 2 * nn);
+    if (o.precision == DQMC_MIXED) {  // 4 sliced copies: expK (A, B roles), invK (A, B roles)
+      const int N = dense_n[i], ldk = (N + 15) / 16 * 16;
+      dense_sl[i] = take(sizeof(unsigned short) * 4 * 7 * (size_t)N * ldk);
+      dense_sle[i] = take(sizeof(int) * 4 * (size_t)N);
+    }
   }
   b->uni_stride = (size_t)b->maxLt * b->maxN;
   const size_t uni_off = (o.rng == DQMC_RNG_MINSTD) ? take(sizeof(double) * b->uni_stride * n) : 0;
@@ -329,6 +351,7 @@ int dqmc_batch_create(const dqmc_walker_desc* descs, int n, const dqmc_batch_opt
   e = cudaStreamCreateWithFlags(&b->own, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = configure_fp64_kernels(kMaxSmemN);
   if (e == cudaSuccess) e = configure_general_kernels();
+  if (e == cudaSuccess) e = configure_ozaki_kernels();
   if (e != cudaSuccess) {
     cudaFree(b->arena);
     delete b;
@@ -350,6 +373,19 @@ int dqmc_batch_create(const dqmc_walker_desc* descs, int n, const dqmc_batch_opt
     cudaMemcpyAsync(base + dense_off[i], dense[i].first.data(), sizeof(double) * nn, cudaMemcpyHostToDevice, b->stream);
     cudaMemcpyAsync(base + dense_off[i] + sizeof(double) * nn, dense[i].second.data(), sizeof(double) * nn,
                     cudaMemcpyHostToDevice, b->stream);
+    if (o.precision == DQMC_MIXED) {
+      const int N = dense_n[i], ldk = (N + 15) / 16 * 16;
+      const auto cfg = N <= 256 ? std::make_pair(7, 6) : std::make_pair(6, 7);
+      const size_t one = 7 * (size_t)N * ldk;
+      auto* sl = reinterpret_cast<unsigned short*>(base + dense_sl[i]);
+      auto* se = reinterpret_cast<int*>(base + dense_sle[i]);
+      const double* ek = reinterpret_cast<const double*>(base + dense_off[i]);
+      const double* ik = ek + nn;
+      oz_slice_const(ek, sl + 0 * one, se + 0 * N, N, ldk, 0, cfg.first, cfg.second, b->stream);  // expK as A
+      oz_slice_const(ek, sl + 1 * one, se + 1 * N, N, ldk, 1, cfg.first, cfg.second, b->stream);  // expK as B
+      oz_slice_const(ik, sl + 2 * one, se + 2 * N, N, ldk, 0, cfg.first, cfg.second, b->stream);  // invK as A
+      oz_slice_const(ik, sl + 3 * one, se + 3 * N, N, ldk, 1, cfg.first, cfg.second, b->stream);  // invK as B
+    }
   }
   std::vector<std::vector<double>> fftabs;
   for (auto& kv : ff_off) {
@@ -397,8 +433,25 @@ int dqmc_batch_create(const dqmc_walker_desc* descs, int n, const dqmc_batch_opt
     plaq(h.cbI, std::cosh(-dtau * d.hopping_t), std::sinh(-dtau * d.hopping_t), std::exp(-0.5 * dtau * d.mu));
     h.G = reinterpret_cast<double*>(base + off[w].G);
     h.chain = reinterpret_cast<double*>(base + off[w].chain);
-    h.work = N > kMaxSmemN ? reinterpret_cast<double*>(base + off[w].work) : nullptr;
-    h.scr = N > kMaxSmemN ? reinterpret_cast<double*>(base + off[w].scr) : nullptr;
+    const bool gen = N > kMaxSmemN || o.precision == DQMC_MIXED;
+    h.path = (o.precision == DQMC_MIXED) ? 2 : (gen ? 1 : 0);
+    h.work = gen ? reinterpret_cast<double*>(base + off[w].work) : nullptr;
+    h.scr = gen ? reinterpret_cast<double*>(base + off[w].scr) : nullptr;
+    if (o.precision == DQMC_MIXED) {
+      h.ldk = (N + 15) / 16 * 16;
+      h.slice_bits = N <= 256 ? 7 : 6;
+      h.slices = N <= 256 ? 6 : 7;
+      h.sl = reinterpret_cast<unsigned short*>(base + off[w].sl);
+      h.sle = reinterpret_cast<int*>(base + off[w].sle);
+      if (off[w].dense_id >= 0) {
+        const int id = off[w].dense_id;
+        const size_t one = 7 * (size_t)N * h.ldk;
+        auto* sl = reinterpret_cast<const unsigned short*>(base + dense_sl[id]);
+        auto* se = reinterpret_cast<const int*>(base + dense_sle[id]);
+        h.kA = sl; h.kB = sl + one; h.iA = sl + 2 * one; h.iB = sl + 3 * one;
+        h.kAe = se; h.kBe = se + N; h.iAe = se + 2 * N; h.iBe = se + 3 * N;
+      }
+    }
     h.stack = reinterpret_cast<double*>(base + off[w].stack);
     h.lvl_stride = (long long)((2 * (size_t)N * N + N + 31) & ~(size_t)31);
     h.side_stride = (long long)h.S * h.nstack * h.lvl_stride;
@@ -523,7 +576,7 @@ int dqmc_init_greens(dqmc_batch* b) {
       general_chain_init(MODE_INIT, b->dW, b->nw, j, b->stream);
       for (int q = 0; q < b->maxPace_general; ++q)
         general_slice(MODE_INIT, b->dW, b->nw, j, q, b->maxN_general, 0, b->any_general_dense, b->any_general_cb,
-                      b->stream);
+                      b->mixed, b->stream);
       general_push(MODE_INIT, b->dW, b->nw, j, b->maxN_general, b->stream);
     }
   }
@@ -581,7 +634,7 @@ static int half_sweep(dqmc_batch* b, int mode, int measure) {
         general_chain_init(mode, b->dW, b->nw, j, b->stream);
         for (int q = 0; q < b->maxPace_general; ++q)
           general_slice(mode, b->dW, b->nw, j, q, b->maxN_general, measure, b->any_general_dense,
-                        b->any_general_cb, b->stream);
+                        b->any_general_cb, b->mixed, b->stream);
       });
       b->timed(DQMC_KCLASS_PUSH, [&] { general_push(mode, b->dW, b->nw, j, b->maxN_general, b->stream); });
       b->timed(DQMC_KCLASS_GREENS,
@@ -715,6 +768,39 @@ int dqmc_profile_read(dqmc_batch* b, int cls, double* total_ms, int64_t* launche
   b->collect();
   *total_ms = b->prof_ms[cls];
   *launches = b->prof_n[cls];
+  return DQMC_OK;
+}
+
+int dqmc_product_check(int n, const double* a, const double* b, double* c) {
+  if (n < 1 || n > kMaxN || !a || !b || !c) return fail(DQMC_ERR_ARG, "dqmc_product_check: bad arguments");
+  int nd = 0;
+  if (cudaGetDeviceCount(&nd) != cudaSuccess || nd == 0) return fail(DQMC_ERR_CUDA, "no CUDA device available");
+  const size_t nn = (size_t)n * n, ldk = (n + 15) / 16 * 16;
+  // every piece 256-byte aligned (the product kernel copies slices in 16-byte chunks)
+  const size_t o_b = align256(nn * sizeof(double)), o_c = o_b + align256(nn * sizeof(double));
+  const size_t o_sa = o_c + align256(nn * sizeof(double));
+  const size_t sl_bytes = align256(7 * (size_t)n * ldk * sizeof(unsigned short));
+  const size_t o_sb = o_sa + sl_bytes, o_ea = o_sb + sl_bytes, o_eb = o_ea + align256(n * sizeof(int));
+  const size_t bytes = o_eb + align256(n * sizeof(int));
+  char* buf = nullptr;
+  CUDA_TRY(cudaMalloc(&buf, bytes));
+  double* dA = reinterpret_cast<double*>(buf);
+  double* dB = reinterpret_cast<double*>(buf + o_b);
+  double* dC = reinterpret_cast<double*>(buf + o_c);
+  auto* sa = reinterpret_cast<unsigned short*>(buf + o_sa);
+  auto* sb = reinterpret_cast<unsigned short*>(buf + o_sb);
+  int* ea = reinterpret_cast<int*>(buf + o_ea);
+  int* eb = reinterpret_cast<int*>(buf + o_eb);
+  cudaError_t e = cudaMemcpy(dA, a, nn * sizeof(double), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(dB, b, nn * sizeof(double), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = configure_ozaki_kernels();
+  if (e == cudaSuccess) {
+    oz_selftest(dA, dB, dC, sa, ea, sb, eb, n, nullptr);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpy(c, dC, nn * sizeof(double), cudaMemcpyDeviceToHost);
+  cudaFree(buf);
+  if (e != cudaSuccess) return fail(DQMC_ERR_CUDA, "dqmc_product_check: %s", cudaGetErrorString(e));
   return DQMC_OK;
 }
 

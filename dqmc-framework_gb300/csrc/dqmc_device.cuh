@@ -33,7 +33,7 @@ enum : int {
 struct WalkerDev {
   int N, L, Lt, pace, nstack, S, model, cb;  // model: 0 repulsive, 1 attractive
   int rng;                                    // 0 host uniforms, 1 Philox
-  int pad0;
+  int path;                                   // 0 SMEM FP64, 1 HBM FP64, 2 HBM mixed (tensor-core products)
   double hop_t;
   // B-matrix diagonal factors exp(+alpha), exp(-alpha)
   double e_pa, e_ma;
@@ -44,6 +44,14 @@ struct WalkerDev {
   double* chain;             // [S][N*N] (general walkers: [2][S][N*N], ping-pong)
   double* work;              // general walkers: GEMM temporary [S][N*N]
   double* scr;               // general walkers: stabilization scratch [S][2][N*N]
+  // mixed walkers: BF16 slices of the operand being multiplied, [S][slices][N][ldk]
+  unsigned short* sl;
+  int* sle;                  // slice exponents [S][N]
+  int ldk;                   // padded slice row length (multiple of 16)
+  int slice_bits, slices;
+  // constant slices of exp(-dtau K) and exp(+dtau K) as left (A) and right (B) operands
+  const unsigned short* kA; const unsigned short* kB; const unsigned short* iA; const unsigned short* iB;
+  const int* kAe; const int* kBe; const int* iAe; const int* iBe;
   double* stack;             // see header
   long long lvl_stride;      // doubles per stack level (2 N^2 + N, padded)
   long long side_stride;     // doubles per side (S * nstack * lvl_stride)

@@ -371,7 +371,7 @@ __device__ void measure_slice(const WalkerDev& w, const double* gu, const double
 template <int MODE>
 __global__ void __launch_bounds__(kThreads) segment_kernel(const WalkerDev* __restrict__ W, int j, int measure) {
   const WalkerDev& w = W[blockIdx.x];
-  if (j >= w.nstack || w.N > kMaxSmemN) return;
+  if (j >= w.nstack || w.path != 0) return;
   extern __shared__ double smem[];
   const int N = w.N, ld = N + 1, S = w.S, Lt = w.Lt, p = w.pace;
   double* Gs[2];
@@ -610,7 +610,7 @@ template <int MODE>
 __global__ void __launch_bounds__(kPushThreads) push_kernel(const WalkerDev* __restrict__ W, int j) {
   const int wi = blockIdx.x >> 1, sp = blockIdx.x & 1;
   const WalkerDev& w = W[wi];
-  if (j >= w.nstack || sp >= w.S || w.N > kMaxSmemN) return;
+  if (j >= w.nstack || sp >= w.S || w.path != 0) return;
   extern __shared__ double smem[];
   const int N = w.N, ld = N + 1;
   const int side = (MODE == MODE_FWD) ? 0 : 1;
@@ -865,7 +865,7 @@ __global__ void __launch_bounds__(kThreads) greens_kernel(const WalkerDev* __res
                                                           int check_error, int trace_slot) {
   const int wi = blockIdx.x >> 1, sp = blockIdx.x & 1;
   const WalkerDev& w = W[wi];
-  if (j >= w.nstack || sp >= w.S || w.N > kMaxSmemN) return;
+  if (j >= w.nstack || sp >= w.S || w.path != 0) return;
   extern __shared__ double smem[];
   const int N = w.N, ld = N + 1, ns = w.nstack;
   double* Ms = smem;
@@ -984,7 +984,7 @@ __global__ void __launch_bounds__(kThreads) greens_kernel(const WalkerDev* __res
 // Measurement of a slot whose recorded G is the fresh one (after greens_kernel).
 __global__ void __launch_bounds__(kThreads) measure_kernel(const WalkerDev* __restrict__ W, int mode, int j) {
   const WalkerDev& w = W[blockIdx.x];
-  if (j >= w.nstack || w.N > kMaxSmemN) return;
+  if (j >= w.nstack || w.path != 0) return;
   if (mode == MODE_BWD && j != w.nstack - 1) return;
   extern __shared__ double smem[];
   const int N = w.N, ld = N + 1;
@@ -1005,7 +1005,7 @@ __global__ void __launch_bounds__(kThreads) measure_kernel(const WalkerDev* __re
 // sign(det G_up det G_dn) (dqmc_walker.cpp:150-163) via in-SMEM LU.
 __global__ void __launch_bounds__(kThreads) sign_kernel(const WalkerDev* __restrict__ W) {
   const WalkerDev& w = W[blockIdx.x];
-  if (w.N > kMaxSmemN) return;
+  if (w.path != 0) return;
   extern __shared__ double smem[];
   const int N = w.N, ld = N + 1;
   double* M = smem;

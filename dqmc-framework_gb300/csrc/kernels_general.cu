@@ -32,7 +32,7 @@ __device__ __forceinline__ double warp_sum_g(double v) {
   return v;
 }
 
-__device__ __forceinline__ bool is_general(const WalkerDev& w) { return w.N > kMaxSmemN; }
+__device__ __forceinline__ bool is_general(const WalkerDev& w) { return w.path != 0; }
 
 // Slice t handled at step j, in-segment index q (false when q is past the segment).
 __device__ __forceinline__ bool slice_of(const WalkerDev& w, int mode, int j, int q, int& t, int& nsl, int& t_hi) {
@@ -91,6 +91,7 @@ __global__ void __launch_bounds__(256) gemm_op_kernel(const WalkerDev* __restric
   int t = 0, nsl = 0, t_hi = 0;
   const bool slice_op = OP <= OP_CH_BWD;
   if (slice_op && w.cb) return;  // checkerboard walkers take cb_general_kernel (expK is null for them)
+  if (slice_op && w.path == 2) return;  // mixed walkers take the tensor-core products
   if (slice_op && !slice_of(w, mode, j, q, t, nsl, t_hi)) return;
   if (!slice_op && j >= w.nstack) return;
 
@@ -953,32 +954,42 @@ static dim3 gemm_grid(int maxN, int nw) {
   return dim3(t, t, 2 * nw);
 }
 
+void mixed_wrap_fwd(const WalkerDev* W, int nw, int maxN, int j, int q, cudaStream_t st);
+void mixed_wrap_bwd(const WalkerDev* W, int nw, int maxN, int j, int q, cudaStream_t st);
+void mixed_chain(const WalkerDev* W, int nw, int maxN, int mode, int j, int q, cudaStream_t st);
+
 void general_slice(int mode, const WalkerDev* W, int nw, int j, int q, int maxN, int measure, bool any_dense,
-                   bool any_cb, cudaStream_t st) {
+                   bool any_cb, bool mixed, cudaStream_t st) {
+  // in a mixed batch the dense products go through the tensor cores (kernels_ozaki.cu)
+  const bool fp64_dense = any_dense && !mixed;
+  const bool mixed_dense = any_dense && mixed;
   const dim3 g = gemm_grid(maxN, nw);
   const size_t cb_sm = sizeof(double) * 2 * maxN;
   const size_t met_sm = sizeof(double) * 6 * maxN + maxN + 16;
   if (mode == MODE_FWD) {
-    if (any_dense) {
+    if (fp64_dense) {
       gemm_op_kernel<OP_WL_FWD><<<g, 256, 0, st>>>(W, mode, j, q, -1);
       gemm_op_kernel<OP_WR_FWD><<<g, 256, 0, st>>>(W, mode, j, q, -1);
     }
+    if (mixed_dense) mixed_wrap_fwd(W, nw, maxN, j, q, st);
     if (any_cb) cb_general_kernel<<<2 * nw, 256, cb_sm, st>>>(W, mode, j, q, 0);
   }
   if (mode != MODE_INIT) {
     metropolis_general_kernel<<<nw, kMetroThreads, met_sm, st>>>(W, mode, j, q);
     if (measure) measure_general_kernel<<<nw, 256, sizeof(double) * 2 * maxN, st>>>(W, mode, j, q, 0);
   }
-  if (any_dense) {
+  if (fp64_dense) {
     if (mode == MODE_FWD) gemm_op_kernel<OP_CH_FWD><<<g, 256, 0, st>>>(W, mode, j, q, -1);
     else gemm_op_kernel<OP_CH_BWD><<<g, 256, 0, st>>>(W, mode, j, q, -1);
   }
+  if (mixed_dense) mixed_chain(W, nw, maxN, mode, j, q, st);
   if (any_cb) cb_general_kernel<<<2 * nw, 256, cb_sm, st>>>(W, mode, j, q, mode == MODE_FWD ? 2 : 3);
   if (mode == MODE_BWD) {
-    if (any_dense) {
+    if (fp64_dense) {
       gemm_op_kernel<OP_WR_BWD><<<g, 256, 0, st>>>(W, mode, j, q, -1);
       gemm_op_kernel<OP_WL_BWD><<<g, 256, 0, st>>>(W, mode, j, q, -1);
     }
+    if (mixed_dense) mixed_wrap_bwd(W, nw, maxN, j, q, st);
     if (any_cb) cb_general_kernel<<<2 * nw, 256, cb_sm, st>>>(W, mode, j, q, 1);
   }
 }

@@ -1,0 +1,67 @@
+// ozaki.cuh — FP64-accurate matrix products on the BF16 tensor cores.
+//
+// An FP64 operand is cut into S slices of B-bit signed integers that share one
+// power-of-two exponent per row (left operand) or per column (right operand):
+//     x(r,k) = 2^{e_r} * sum_i a_i(r,k) 2^{-B(i+1)} + (remainder < 2^{e_r - B S}),
+// computed from the IEEE bit pattern with integer operations only (no FP64 pipe).
+// Integers |a_i| < 2^B are exact in BF16, and a slice-pair product summed over
+// K terms stays below 2^24 when (2^B - 1)^2 K < 2^22, so the tensor core's FP32
+// accumulation of a group m = i + j (at most 4 pairs for m <= 3) is exact; the
+// groups m >= 4 carry weights 2^{-4B} and below, where FP32 rounding is far
+// under the kept precision.  The product is
+//     C(r,c) = 2^{e_r + f_c} sum_m 2^{-B(m+2)} S_m(r,c),   S_m = sum_{i+j=m} A_i B_j.
+// B = 7, S = 6 (42 bits, 21 slice products) for K <= 256; B = 6, S = 7
+// (42 bits, 28 products) for K <= 1024.  This is the splitting scheme of Ozaki,
+// Ogita, Oishi and Rump (Numer. Algorithms 2012) restated for BF16 inputs.
+#pragma once
+#include <cstdint>
+
+namespace dqmc {
+namespace ozaki {
+
+constexpr int kMaxSlices = 7;
+
+struct SliceCfg {
+  int bits, slices;
+};
+__host__ __device__ inline SliceCfg cfg_for_k(int K) { return K <= 256 ? SliceCfg{7, 6} : SliceCfg{6, 7}; }
+
+// exponent e with |x| < 2^e (0 for x == 0); integer only
+__device__ __forceinline__ int exp_bound(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const int ex = (int)((b >> 52) & 0x7ff);
+  return ex == 0 ? -1100 : ex - 1022;  // normal: |x| in [2^(ex-1023), 2^(ex-1022))
+}
+
+// 42-bit truncated fixed-point magnitude of |x| / 2^e (e >= exp_bound(x)), and sign
+__device__ __forceinline__ unsigned long long fixed42(double x, int e, bool& neg) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  neg = (b >> 63) != 0;
+  const int ex = (int)((b >> 52) & 0x7ff);
+  if (ex == 0) return 0ULL;  // zero (subnormals flushed: far below any kept bit here)
+  const unsigned long long m = (b & 0xFFFFFFFFFFFFFULL) | 0x10000000000000ULL;  // 53 bits
+  // |x| / 2^e = m * 2^{ex - 1075 - e};  want floor(that * 2^42) = m >> (1033 + e - ex)
+  const int sh = 1033 + e - ex;
+  if (sh >= 64) return 0ULL;
+  if (sh <= 0) return m << (-sh);  // cannot happen for e >= exp_bound(x)
+  return m >> sh;
+}
+
+// slice i of a 42-bit magnitude with B bits per slice, as a signed BF16 bit pattern
+__device__ __forceinline__ unsigned short slice_bf16(unsigned long long q, int i, int bits, bool neg) {
+  const int sh = 42 - bits * (i + 1);
+  const unsigned v = (unsigned)((sh >= 0 ? (q >> sh) : (q << (-sh))) & ((1u << bits) - 1));
+  const float f = neg ? -(float)v : (float)v;  // exact: v < 2^8
+  return (unsigned short)(__float_as_uint(f) >> 16);  // exact truncation: low 16 bits are zero
+}
+
+// x * 2^e by exponent arithmetic (two steps keep each factor a normal double)
+__device__ __forceinline__ double scale2(double x, int e) {
+  if (e > 1000) { x *= 0x1p1000; e -= 1000; }
+  if (e < -1000) { x *= 0x1p-1000; e += 1000; }
+  e = max(-1022, min(1023, e));
+  return x * __longlong_as_double((long long)(e + 1023) << 52);
+}
+
+}  // namespace ozaki
+}  // namespace dqmc

@@ -19,7 +19,7 @@ LIB_PATH = os.path.join(os.path.dirname(_HERE), "lib", "libdqmc_gb300.so")
 
 REPULSIVE, ATTRACTIVE = 0, 1
 RNG_MINSTD, RNG_PHILOX = 0, 1
-FP64 = 0
+FP64, MIXED = 0, 1
 OBS_NAMES = [
     "filling_number", "double_occupancy", "kinetic_energy", "momentum_distribution",
     "local_spin_corr", "spin_density_structure_factor", "charge_density_structure_factor",
@@ -35,6 +35,7 @@ EXPORTS = [
     "dqmc_get_wrap_error", "dqmc_get_accept_count", "dqmc_get_status", "dqmc_get_observables",
     "dqmc_clear_observables", "dqmc_trace_count", "dqmc_trace_get", "dqmc_trace_clear", "dqmc_batch_info",
     "dqmc_profile_enable", "dqmc_profile_read", "dqmc_microbench_fp64", "dqmc_get_observables_all",
+    "dqmc_product_check",
 ]
 KCLASSES = ["segment", "push", "greens", "measure"]
 
@@ -85,6 +86,7 @@ def load() -> ctypes.CDLL:
         "dqmc_batch_info": (c, [vp, ip, i64p]),
         "dqmc_profile_enable": (c, [vp, c]), "dqmc_profile_read": (c, [vp, c, dp, i64p]),
         "dqmc_microbench_fp64": (c, [dp]), "dqmc_get_observables_all": (c, [vp, dp, i64p]),
+        "dqmc_product_check": (c, [c, dp, dp, dp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -258,6 +260,17 @@ class Batch:
         u = ctypes.c_int64()
         _check(load().dqmc_batch_info(self.h, ctypes.byref(nw), ctypes.byref(u)))
         return u.value
+
+
+def product_check(a, b):
+    """C = A B through the mixed-precision product engine (column-major doubles)."""
+    a = np.asfortranarray(a, dtype=np.float64)
+    b = np.asfortranarray(b, dtype=np.float64)
+    n = a.shape[0]
+    c = np.zeros((n, n), order="F")
+    dp = ctypes.POINTER(ctypes.c_double)
+    _check(load().dqmc_product_check(n, a.ctypes.data_as(dp), b.ctypes.data_as(dp), c.ctypes.data_as(dp)))
+    return c
 
 
 def microbench_fp64() -> float:

@@ -47,7 +47,10 @@ enum dqmc_rng {
 };
 
 enum dqmc_precision {
-  DQMC_FP64 = 0  /* plain method: every product in FP64 */
+  DQMC_FP64 = 0,  /* plain method: every product in FP64 */
+  DQMC_MIXED = 1  /* wraps and B-chain products on the BF16 tensor cores, split into exact
+                     integer slices and recombined to 42 bits; Metropolis ratios, rank-1
+                     updates, UDT stabilization and Green's assembly stay FP64 */
 };
 
 /* Observable slots, the equal-time list of src/measure/observable_handler.cpp:11-20
@@ -161,6 +164,11 @@ enum { DQMC_KCLASS_SEGMENT = 0, DQMC_KCLASS_PUSH = 1, DQMC_KCLASS_GREENS = 2, DQ
        DQMC_NUM_KCLASS = 4 };
 int dqmc_profile_enable(dqmc_batch* b, int on);
 int dqmc_profile_read(dqmc_batch* b, int kclass, double* total_ms, int64_t* launches);
+
+/* The mixed-precision product engine on host matrices: C = A B for column-major
+ * N x N doubles, computed exactly as the DQMC_MIXED sweep computes its wraps
+ * (no reference counterpart: it exposes the engine for validation). */
+int dqmc_product_check(int n, const double* a, const double* b, double* c);
 
 /* FP64 FMA throughput of the current device (GFLOP/s), measured by a
  * register-resident FMA loop over all SMs: the FP64 roofline denominator. */

@@ -1,0 +1,72 @@
+"""Mixed-precision path (DQMC_MIXED): wraps and B-chain products on the BF16
+tensor cores through exact integer slices (42-bit), FP64 everywhere else.
+
+Bars: the product engine agrees with FP64 to 2^-38 of |A||B| (normwise) and is
+exact on integer inputs; the mixed sweep keeps max|dG| <= 1e-6 against the FP64
+path at every stabilization, on the same fields and uniforms.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def dq():
+    import __graft_entry__ as g
+
+    g.build()
+    import dqmc_gb300
+
+    return dqmc_gb300
+
+
+@pytest.mark.parametrize("n", [16, 37, 64, 100, 256, 300])
+def test_product_engine_accuracy(dq, n):
+    rng = np.random.default_rng(n)
+    # rows / columns graded over many decades, like U diag(D) operands of the chain
+    a = rng.standard_normal((n, n)) * np.exp(rng.uniform(-20, 20, n))[:, None]
+    b = rng.standard_normal((n, n)) * np.exp(rng.uniform(-30, 30, n))[None, :]
+    c = dq.product_check(a, b)
+    ref = a @ b
+    bound = np.abs(a).max(axis=1)[:, None] * np.abs(b).max(axis=0)[None, :] * n
+    assert (np.abs(c - ref) <= 2.0 ** -38 * bound).all()
+
+
+def test_product_engine_exact_on_integers(dq):
+    rng = np.random.default_rng(7)
+    n = 128
+    a = rng.integers(-1000, 1000, (n, n)).astype(np.float64)
+    b = rng.integers(-1000, 1000, (n, n)).astype(np.float64)
+    np.testing.assert_array_equal(dq.product_check(a, b), a @ b)
+
+
+def _run(dq, descs, precision, sweeps=1):
+    b = dq.Batch(descs, rng=dq.RNG_MINSTD, precision=precision, trace=True)
+    for w in range(len(descs)):
+        b.fields_random(w)
+    b.init_greens()
+    out = []
+    for _ in range(sweeps):
+        b.trace_clear()
+        b.sweep_0_to_beta(measure=True)
+        b.sweep_beta_to_0(measure=True)
+        out.append([(b.fields(w), b.trace(w)) for w in range(len(descs))])
+    return b, out
+
+
+@pytest.mark.parametrize("model,L,U,mu,beta,Lt,pace", [
+    (1, 8, 4.0, -0.5, 4.0, 40, 8),     # attractive, the mixed configuration's model on 8x8
+    (0, 6, 4.0, 0.0, 4.0, 80, 10),     # repulsive
+    (1, 16, 4.0, -0.5, 2.0, 20, 8),    # 16x16
+])
+def test_mixed_sweep_dG_against_fp64(dq, model, L, U, mu, beta, Lt, pace):
+    descs = [dq.WalkerDesc(model=model, L=L, U=U, mu=mu, beta=beta, Lt=Lt, pace=pace, seed=100 + w) for w in range(2)]
+    bm, om = _run(dq, descs, dq.MIXED)
+    bf, of = _run(dq, descs, dq.FP64)
+    worst = 0.0
+    for w in range(len(descs)):
+        np.testing.assert_array_equal(om[0][w][0], of[0][w][0])  # same decisions
+        worst = max(worst, float(np.abs(om[0][w][1] - of[0][w][1]).max()))
+        assert bm.status(w) == 0
+    assert worst <= 1e-6, worst
