@@ -45,6 +45,11 @@ WORKLOADS = {
     # mixed-precision configuration: same model, lattice, beta and pace)
     "fp64_batch_16x16_attractive": dict(walkers=128, model=1, L=16, U=4.0, mu=-0.5, beta=10.0, Lt=100, pace=8,
                                         checkerboard=False),
+    # the mixed-precision configuration: 128 walkers, attractive 16x16 (U=-4 as |U|=4
+    # on the attractive model), mu=-0.5, beta=10, dtau=0.1, wraps and B-chain on the
+    # tensor cores, FP64 stabilization every 8 slices
+    "mixed_batch_16x16_attractive": dict(walkers=128, model=1, L=16, U=4.0, mu=-0.5, beta=10.0, Lt=100, pace=8,
+                                         checkerboard=False, precision="mixed"),
     # one FP64 walker, 4x4 dense (the reference's single-chain case)
     "fp64_single_4x4_dense": dict(walkers=1, model=0, L=4, U=4.0, mu=0.0, beta=4.0, Lt=80, pace=10,
                                   checkerboard=False),
@@ -195,7 +200,8 @@ def run_gpu(args, wl, rank, world):
     fp64_peak = dq.microbench_fp64()
 
     descs = _descs(dq, wl, seed0=1000 + 100000 * rank)
-    batch = dq.Batch(descs, rng=dq.RNG_PHILOX)
+    prec = dq.MIXED if wl.get("precision") == "mixed" else dq.FP64
+    batch = dq.Batch(descs, rng=dq.RNG_PHILOX, precision=prec)
     # a dedicated stream: the library launches on it and the CUDA events below
     # are recorded on it (torch's default stream would be handle 0)
     stream = torch.cuda.Stream(device=dev)
@@ -268,7 +274,7 @@ def run_gpu(args, wl, rank, world):
     # ---- e2e: reference RNG on the host, copies in and out every step
     e2e = None
     if rank == 0 or world > 1:
-        eb = dq.Batch(descs, rng=dq.RNG_MINSTD)
+        eb = dq.Batch(descs, rng=dq.RNG_MINSTD, precision=prec)
         eb.set_stream(stream.cuda_stream)
         for w in range(len(descs)):
             eb.fields_random(w)
@@ -311,6 +317,7 @@ def main():
     config = {"workload": args.workload, "walkers_per_gpu": wl["walkers"], "model": "repulsive" if wl["model"] == 0 else "attractive",
               "L": wl["L"], "N": wl["L"] ** 2, "U": wl["U"], "mu": wl["mu"], "beta": wl["beta"], "Lt": wl["Lt"],
               "pace": wl["pace"], "expK": "checkerboard" if wl["checkerboard"] else "dense",
+              "precision": wl.get("precision", "fp64"),
               "measure": "equal-time, fused", "parallelism": f"replicas x{args.gpus}",
               "l2": "no flush: per-GPU working set (G, chains, UDT stacks) > 1 GB, larger than L2"}
 

@@ -161,6 +161,10 @@ size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
 }  // namespace
 
+namespace dqmc {
+int set_last_error(int code, const char* msg) { return fail(code, "%s", msg); }
+}  // namespace dqmc
+
 struct dqmc_batch {
   int nw = 0, maxN = 0, maxNs = 0, maxLt = 0;
   // walkers split by kernel family: N <= 64 (SMEM-resident) and N > 64 (general)

@@ -35,7 +35,7 @@ EXPORTS = [
     "dqmc_get_wrap_error", "dqmc_get_accept_count", "dqmc_get_status", "dqmc_get_observables",
     "dqmc_clear_observables", "dqmc_trace_count", "dqmc_trace_get", "dqmc_trace_clear", "dqmc_batch_info",
     "dqmc_profile_enable", "dqmc_profile_read", "dqmc_microbench_fp64", "dqmc_get_observables_all",
-    "dqmc_product_check",
+    "dqmc_product_check", "dqmc_product_device_noalloc",
 ]
 KCLASSES = ["segment", "push", "greens", "measure"]
 
@@ -87,6 +87,7 @@ def load() -> ctypes.CDLL:
         "dqmc_profile_enable": (c, [vp, c]), "dqmc_profile_read": (c, [vp, c, dp, i64p]),
         "dqmc_microbench_fp64": (c, [dp]), "dqmc_get_observables_all": (c, [vp, dp, i64p]),
         "dqmc_product_check": (c, [c, dp, dp, dp]),
+        "dqmc_product_device_noalloc": (c, [c, vp, vp, vp, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)

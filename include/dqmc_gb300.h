@@ -170,6 +170,17 @@ int dqmc_profile_read(dqmc_batch* b, int kclass, double* total_ms, int64_t* laun
  * (no reference counterpart: it exposes the engine for validation). */
 int dqmc_product_check(int n, const double* a, const double* b, double* c);
 
+/* The same product for callers that cannot allocate device memory (inside a
+ * CUDA-graph capture, or under a host framework that owns all device memory):
+ * a, b, c are the caller's device buffers (column-major n x n doubles) and the
+ * BF16 slice scratch is a fixed 1.5 MB array in the library's device image, so
+ * the call allocates nothing.  Limit: n <= 256 (larger n is rejected with
+ * DQMC_ERR_ARG).  All calls on a device share that scratch: calls that overlap
+ * on the GPU race, so the caller serialises them.  The first call on a device
+ * resolves the scratch address and must come before any stream capture.
+ * No counterpart in the reference (it has no device code). */
+int dqmc_product_device_noalloc(int n, const double* a, const double* b, double* c, void* cuda_stream);
+
 /* FP64 FMA throughput of the current device (GFLOP/s), measured by a
  * register-resident FMA loop over all SMs: the FP64 roofline denominator. */
 int dqmc_microbench_fp64(double* gflops);
