@@ -36,7 +36,9 @@ double run_fp64_probe(cudaError_t* err);
 // general (N > 64) walkers, kernels_general.cu
 cudaError_t configure_general_kernels();
 void general_slice(int mode, const WalkerDev* W, int nw, int j, int q, int maxN, int measure, bool any_dense,
-                   bool any_cb, bool mixed, cudaStream_t st);
+                   bool any_cb, bool mixed, int kd, int smax, cudaStream_t st);
+cudaError_t configure_delayed_kernels();
+int delayed_pick_kd(int N, int S);
 void general_chain_init(int mode, const WalkerDev* W, int nw, int j, cudaStream_t st);
 void general_push(int mode, const WalkerDev* W, int nw, int j, int maxN, cudaStream_t st);
 void general_greens(int mode, const WalkerDev* W, int nw, int j, int trace_slot, int maxN, cudaStream_t st);
@@ -171,6 +173,7 @@ struct dqmc_batch {
   int maxN_small = 0, maxN_general = 0, maxPace_general = 0;
   bool any_small = false, any_general = false, any_general_dense = false, any_general_cb = false;
   bool mixed = false;
+  int kd = 0, smax = 1;  // delayed-update block size of the general walkers (0: rank-1 kernel)
   dqmc_batch_options opt{};
   std::vector<dqmc_walker_desc> desc;
   std::vector<WalkerDev> hw;        // host copies of the descriptors
@@ -287,6 +290,9 @@ int dqmc_batch_create(const dqmc_walker_desc* descs, int n, const dqmc_batch_opt
   }
   b->trace_cap = o.trace ? 4 * b->maxNs : 0;
   b->mixed = (o.precision == DQMC_MIXED);
+  for (auto& d : b->desc)
+    if (d.model == DQMC_REPULSIVE_HUBBARD) b->smax = 2;
+  if (b->any_general) b->kd = delayed_pick_kd(b->maxN_general, b->smax);
 
   // ---- arena layout ----
   struct Off { size_t G, chain, work, scr, sl, sle, stack, fields, ff, trace; int dense_id; };
@@ -356,6 +362,7 @@ int dqmc_batch_create(const dqmc_walker_desc* descs, int n, const dqmc_batch_opt
   if (e == cudaSuccess) e = configure_fp64_kernels(kMaxSmemN);
   if (e == cudaSuccess) e = configure_general_kernels();
   if (e == cudaSuccess) e = configure_ozaki_kernels();
+  if (e == cudaSuccess) e = configure_delayed_kernels();
   if (e != cudaSuccess) {
     cudaFree(b->arena);
     delete b;
@@ -580,7 +587,7 @@ int dqmc_init_greens(dqmc_batch* b) {
       general_chain_init(MODE_INIT, b->dW, b->nw, j, b->stream);
       for (int q = 0; q < b->maxPace_general; ++q)
         general_slice(MODE_INIT, b->dW, b->nw, j, q, b->maxN_general, 0, b->any_general_dense, b->any_general_cb,
-                      b->mixed, b->stream);
+                      b->mixed, b->kd, b->smax, b->stream);
       general_push(MODE_INIT, b->dW, b->nw, j, b->maxN_general, b->stream);
     }
   }
@@ -638,7 +645,7 @@ static int half_sweep(dqmc_batch* b, int mode, int measure) {
         general_chain_init(mode, b->dW, b->nw, j, b->stream);
         for (int q = 0; q < b->maxPace_general; ++q)
           general_slice(mode, b->dW, b->nw, j, q, b->maxN_general, measure, b->any_general_dense,
-                        b->any_general_cb, b->mixed, b->stream);
+                        b->any_general_cb, b->mixed, b->kd, b->smax, b->stream);
       });
       b->timed(DQMC_KCLASS_PUSH, [&] { general_push(mode, b->dW, b->nw, j, b->maxN_general, b->stream); });
       b->timed(DQMC_KCLASS_GREENS,
@@ -795,16 +802,18 @@ int dqmc_product_check(int n, const double* a, const double* b, double* c) {
   auto* sb = reinterpret_cast<unsigned short*>(buf + o_sb);
   int* ea = reinterpret_cast<int*>(buf + o_ea);
   int* eb = reinterpret_cast<int*>(buf + o_eb);
+  const char* step = "upload";
   cudaError_t e = cudaMemcpy(dA, a, nn * sizeof(double), cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(dB, b, nn * sizeof(double), cudaMemcpyHostToDevice);
-  if (e == cudaSuccess) e = configure_ozaki_kernels();
+  if (e == cudaSuccess) { step = "kernel set-up"; e = configure_ozaki_kernels(); }
   if (e == cudaSuccess) {
+    step = "product launch";
     oz_selftest(dA, dB, dC, sa, ea, sb, eb, n, nullptr);
     e = cudaGetLastError();
   }
-  if (e == cudaSuccess) e = cudaMemcpy(c, dC, nn * sizeof(double), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) { step = "download"; e = cudaMemcpy(c, dC, nn * sizeof(double), cudaMemcpyDeviceToHost); }
   cudaFree(buf);
-  if (e != cudaSuccess) return fail(DQMC_ERR_CUDA, "dqmc_product_check: %s", cudaGetErrorString(e));
+  if (e != cudaSuccess) return fail(DQMC_ERR_CUDA, "dqmc_product_check (%s): %s", step, cudaGetErrorString(e));
   return DQMC_OK;
 }
 

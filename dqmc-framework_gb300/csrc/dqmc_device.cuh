@@ -74,6 +74,25 @@ struct WalkerDev {
   int pad1;
 };
 
+// Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11): uniform double in [0,1)
+// keyed by the walker's seed, counter (site attempt, half-sweep, walker).
+__device__ __forceinline__ double philox_uniform(unsigned long long seed, unsigned walker, unsigned long long sweep,
+                                                 unsigned attempt) {
+  unsigned c0 = attempt, c1 = (unsigned)sweep, c2 = (unsigned)(sweep >> 32), c3 = walker;
+  unsigned k0 = (unsigned)seed, k1 = (unsigned)(seed >> 32);
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+    const unsigned hi0 = __umulhi(0xD2511F53u, c0), lo0 = 0xD2511F53u * c0;
+    const unsigned hi1 = __umulhi(0xCD9E8D57u, c2), lo1 = 0xCD9E8D57u * c2;
+    const unsigned n0 = hi1 ^ c1 ^ k0, n2 = hi0 ^ c3 ^ k1;
+    c0 = n0; c1 = lo1; c2 = n2; c3 = lo0;
+    k0 += 0x9E3779B9u;
+    k1 += 0xBB67AE85u;
+  }
+  const unsigned long long m = ((unsigned long long)(c0 >> 5) << 26) | (unsigned long long)(c1 >> 6);
+  return (double)m * (1.0 / 9007199254740992.0);
+}
+
 __host__ __device__ inline double* stack_level(const WalkerDev& w, int side, int spin, int level) {
   return w.stack + side * w.side_stride + ((long long)spin * w.nstack + level) * w.lvl_stride;
 }

@@ -70,24 +70,6 @@ __device__ double block_max(double v, double* red) {
   return m;
 }
 
-// Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11), counter-based.
-__device__ __forceinline__ double philox_uniform(unsigned long long seed, unsigned walker,
-                                                 unsigned long long sweep, unsigned attempt) {
-  unsigned c0 = attempt, c1 = (unsigned)sweep, c2 = (unsigned)(sweep >> 32), c3 = walker;
-  unsigned k0 = (unsigned)seed, k1 = (unsigned)(seed >> 32);
-#pragma unroll
-  for (int r = 0; r < 10; ++r) {
-    const unsigned hi0 = __umulhi(0xD2511F53u, c0), lo0 = 0xD2511F53u * c0;
-    const unsigned hi1 = __umulhi(0xCD9E8D57u, c2), lo1 = 0xCD9E8D57u * c2;
-    const unsigned n0 = hi1 ^ c1 ^ k0, n2 = hi0 ^ c3 ^ k1;
-    c0 = n0; c1 = lo1; c2 = n2; c3 = lo0;
-    k0 += 0x9E3779B9u;
-    k1 += 0xBB67AE85u;
-  }
-  const unsigned long long m = ((unsigned long long)(c0 >> 5) << 26) | (unsigned long long)(c1 >> 6);
-  return (double)m * (1.0 / 9007199254740992.0);
-}
-
 // spin factor of the B matrices: repulsive couples spin down with -1, attractive +1
 __device__ __forceinline__ int spin_sign(const WalkerDev& w, int spin) {
   return (w.model == 0 && spin == 1) ? -1 : 1;

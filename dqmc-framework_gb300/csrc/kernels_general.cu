@@ -22,9 +22,6 @@
 
 namespace dqmc {
 
-__device__ double philox_uniform_g(unsigned long long seed, unsigned walker, unsigned long long sweep,
-                                   unsigned attempt);
-
 namespace {
 
 __device__ __forceinline__ double warp_sum_g(double v) {
@@ -387,7 +384,7 @@ __global__ void __launch_bounds__(kMetroThreads) metropolis_general_kernel(const
       const double r = (w.model == 0) ? __dmul_rn(ru, rd) : __dmul_rn(__dmul_rn(w.ex2[si], ru), rd);
       const int attempt = (mode == MODE_FWD) ? (eff * N + i) : ((Lt - t) * N + i);
       const double u = (w.rng == 0) ? w.uni[attempt]
-                                    : philox_uniform_g(w.seed, blockIdx.x, w.sweep_id, (unsigned)(eff * N + i));
+                                    : philox_uniform(w.seed, blockIdx.x, w.sweep_id, (unsigned)(eff * N + i));
       const double prob = fmin(1.0, fabs(r));
       if (!isfinite(r)) atomicOr(w.status, ST_NONFINITE_RATIO);
       if (u < prob) {
@@ -928,24 +925,6 @@ __global__ void __launch_bounds__(1024) sign_general_kernel(const WalkerDev* __r
   if (threadIdx.x == 0) *w.sign = (s_neg % 2 == 0) ? 1.0 : -1.0;
 }
 
-// Philox for the general Metropolis kernel (same generator as kernels_fp64.cu)
-__device__ double philox_uniform_g(unsigned long long seed, unsigned walker, unsigned long long sweep,
-                                   unsigned attempt) {
-  unsigned c0 = attempt, c1 = (unsigned)sweep, c2 = (unsigned)(sweep >> 32), c3 = walker;
-  unsigned k0 = (unsigned)seed, k1 = (unsigned)(seed >> 32);
-#pragma unroll
-  for (int r = 0; r < 10; ++r) {
-    const unsigned hi0 = __umulhi(0xD2511F53u, c0), lo0 = 0xD2511F53u * c0;
-    const unsigned hi1 = __umulhi(0xCD9E8D57u, c2), lo1 = 0xCD9E8D57u * c2;
-    const unsigned n0 = hi1 ^ c1 ^ k0, n2 = hi0 ^ c3 ^ k1;
-    c0 = n0; c1 = lo1; c2 = n2; c3 = lo0;
-    k0 += 0x9E3779B9u;
-    k1 += 0xBB67AE85u;
-  }
-  const unsigned long long m = ((unsigned long long)(c0 >> 5) << 26) | (unsigned long long)(c1 >> 6);
-  return (double)m * (1.0 / 9007199254740992.0);
-}
-
 // --------------------------------------------------------------------------
 // host-side launchers for general walkers
 // --------------------------------------------------------------------------
@@ -958,8 +937,11 @@ void mixed_wrap_fwd(const WalkerDev* W, int nw, int maxN, int j, int q, cudaStre
 void mixed_wrap_bwd(const WalkerDev* W, int nw, int maxN, int j, int q, cudaStream_t st);
 void mixed_chain(const WalkerDev* W, int nw, int maxN, int mode, int j, int q, cudaStream_t st);
 
+void launch_metropolis_delayed(bool mixed, const WalkerDev* W, int nw, int mode, int j, int q, int maxN, int S_max,
+                               int KD, cudaStream_t st);
+
 void general_slice(int mode, const WalkerDev* W, int nw, int j, int q, int maxN, int measure, bool any_dense,
-                   bool any_cb, bool mixed, cudaStream_t st) {
+                   bool any_cb, bool mixed, int kd, int smax, cudaStream_t st) {
   // in a mixed batch the dense products go through the tensor cores (kernels_ozaki.cu)
   const bool fp64_dense = any_dense && !mixed;
   const bool mixed_dense = any_dense && mixed;
@@ -975,7 +957,8 @@ void general_slice(int mode, const WalkerDev* W, int nw, int j, int q, int maxN,
     if (any_cb) cb_general_kernel<<<2 * nw, 256, cb_sm, st>>>(W, mode, j, q, 0);
   }
   if (mode != MODE_INIT) {
-    metropolis_general_kernel<<<nw, kMetroThreads, met_sm, st>>>(W, mode, j, q);
+    if (kd > 0) launch_metropolis_delayed(mixed, W, nw, mode, j, q, maxN, smax, kd, st);
+    else metropolis_general_kernel<<<nw, kMetroThreads, met_sm, st>>>(W, mode, j, q);
     if (measure) measure_general_kernel<<<nw, 256, sizeof(double) * 2 * maxN, st>>>(W, mode, j, q, 0);
   }
   if (fp64_dense) {

@@ -63,5 +63,15 @@ __device__ __forceinline__ double scale2(double x, int e) {
   return x * __longlong_as_double((long long)(e + 1023) << 52);
 }
 
+// one BF16 tensor-core MMA m16n8k16, FP32 accumulate in place
+__device__ __forceinline__ void mma16816(float (&c)[4], unsigned a0, unsigned a1, unsigned a2, unsigned a3,
+                                         unsigned b0, unsigned b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};\n"
+      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+      : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+}
+
 }  // namespace ozaki
 }  // namespace dqmc
