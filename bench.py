@@ -221,6 +221,8 @@ def run_gpu(args, wl, rank, world):
     for k in range(args.warmup):
         step(k)
     acc0 = sum(batch.accept_count(w) for w in range(len(descs)))
+    launches0 = batch.launch_count()
+    # per-kernel-class CUDA events as nodes of the replayed half-sweep graphs
     batch.profile_enable(True)
 
     def barrier():
@@ -269,7 +271,7 @@ def run_gpu(args, wl, rank, world):
                 "avg_launch_ms": avg_ms,
                 "kernel_share": {k: prof[k][0] / ms for k in prof},
                 "sweep_nominal_F_tflops": fm["nominal_F"] * len(descs) * args.steps / (ms * 1e-3) / 1e12}
-    launches = sum(n for _, n in prof.values())
+    launches = batch.launch_count() - launches0
 
     # ---- e2e: reference RNG on the host, copies in and out every step
     e2e = None

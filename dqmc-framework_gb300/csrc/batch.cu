@@ -33,6 +33,7 @@ void launch_greens(int mode, const WalkerDev* W, int nw, int j, int check, int t
 void launch_measure(int mode, const WalkerDev* W, int nw, int j, int maxN, cudaStream_t st);
 void launch_sign(const WalkerDev* W, int nw, int maxN, cudaStream_t st);
 double run_fp64_probe(cudaError_t* err);
+void launch_bump(unsigned long long* ctr, cudaStream_t st);
 // general (N > 64) walkers, kernels_general.cu
 cudaError_t configure_general_kernels();
 void general_slice(int mode, const WalkerDev* W, int nw, int j, int q, int maxN, int measure, bool any_dense,
@@ -186,7 +187,13 @@ struct dqmc_batch {
   double* d_uni = nullptr;
   size_t uni_stride = 0;
   bool initialised = false;
-  unsigned long long sweep_id = 0;
+  unsigned long long* d_sweep = nullptr;  // Philox half-sweep counter (device)
+  // one CUDA graph per (mode, measure) half-sweep; kernel-node counts for accounting
+  cudaGraphExec_t gexec[3][2] = {{nullptr, nullptr}, {nullptr, nullptr}, {nullptr, nullptr}};
+  // profiled graphs: the same half-sweep with CUDA-event nodes around each kernel class
+  cudaGraphExec_t pexec[3][2] = {{nullptr, nullptr}, {nullptr, nullptr}, {nullptr, nullptr}};
+  int64_t nodes[3][2] = {{-1, -1}, {-1, -1}, {-1, -1}};
+  int64_t launches = 0;
   int trace_count = 0, trace_cap = 0;
   // per-walker device scalars
   struct Scal {
@@ -202,6 +209,7 @@ struct dqmc_batch {
   bool prof = false;
   struct Mark { int cls; cudaEvent_t a, b; };
   std::vector<Mark> marks;
+  std::vector<Mark> pmarks[3][2];  // event nodes of the profiled graphs
   std::vector<cudaEvent_t> pool;
   double prof_ms[DQMC_NUM_KCLASS] = {0, 0, 0, 0};
   int64_t prof_n[DQMC_NUM_KCLASS] = {0, 0, 0, 0};
@@ -215,13 +223,15 @@ struct dqmc_batch {
     pool.pop_back();
     return e;
   }
+  bool capturing = false;  // inside a stream capture: events become graph event-record nodes
   template <class F>
   void timed(int cls, F launch) {
     if (!prof) { launch(); return; }
     Mark m{cls, ev(), ev()};
-    cudaEventRecord(m.a, stream);
+    const unsigned fl = capturing ? cudaEventRecordExternal : 0u;
+    cudaEventRecordWithFlags(m.a, stream, fl);
     launch();
-    cudaEventRecord(m.b, stream);
+    cudaEventRecordWithFlags(m.b, stream, fl);
     marks.push_back(m);
   }
   void collect() {
@@ -303,6 +313,7 @@ int dqmc_batch_create(const dqmc_walker_desc* descs, int n, const dqmc_batch_opt
   size_t cur = 0;
   auto take = [&](size_t bytes) { size_t o2 = cur; cur = align256(cur + bytes); return o2; };
   const size_t scal_off = take(sizeof(dqmc_batch::Scal) * n);
+  const size_t sweep_off = take(sizeof(unsigned long long));
   const size_t desc_off = take(sizeof(WalkerDev) * n);
   for (int w = 0; w < n; ++w) {
     const auto& d = b->desc[w];
@@ -373,6 +384,7 @@ int dqmc_batch_create(const dqmc_walker_desc* descs, int n, const dqmc_batch_opt
 
   char* base = b->arena;
   b->d_scal = reinterpret_cast<dqmc_batch::Scal*>(base + scal_off);
+  b->d_sweep = reinterpret_cast<unsigned long long*>(base + sweep_off);
   b->dW = reinterpret_cast<WalkerDev*>(base + desc_off);
   if (o.rng == DQMC_RNG_MINSTD) {
     b->d_uni = reinterpret_cast<double*>(base + uni_off);
@@ -482,6 +494,7 @@ int dqmc_batch_create(const dqmc_walker_desc* descs, int n, const dqmc_batch_opt
     h.status = &sc->status;
     h.uni = b->d_uni ? b->d_uni + b->uni_stride * w : nullptr;
     h.seed = d.seed;
+    h.sweep_ctr = b->d_sweep;
     h.trace = b->trace_cap ? reinterpret_cast<double*>(base + off[w].trace) : nullptr;
     h.trace_cap = b->trace_cap;
     b->eng[w].seed((unsigned)d.seed);
@@ -508,6 +521,15 @@ int dqmc_batch_destroy(dqmc_batch* b) {
   if (b->stream) cudaStreamSynchronize(b->stream);
   b->collect();
   for (auto e : b->pool) cudaEventDestroy(e);
+  for (auto& row : b->gexec)
+    for (auto& g : row)
+      if (g) cudaGraphExecDestroy(g);
+  for (auto& row : b->pexec)
+    for (auto& g : row)
+      if (g) cudaGraphExecDestroy(g);
+  for (auto& row : b->pmarks)
+    for (auto& v : row)
+      for (auto& m : v) { cudaEventDestroy(m.a); cudaEventDestroy(m.b); }
   if (b->h_uni) cudaFreeHost(b->h_uni);
   if (b->arena) cudaFree(b->arena);
   if (b->own) cudaStreamDestroy(b->own);
@@ -610,25 +632,12 @@ int dqmc_init_greens(dqmc_batch* b) {
   return DQMC_OK;
 }
 
-static int half_sweep(dqmc_batch* b, int mode, int measure) {
-  if (!b) return fail(DQMC_ERR_ARG, "null batch");
-  if (!b->initialised) return fail(DQMC_ERR_STATE, "sweep before dqmc_init_greens");
-  if (b->opt.rng == DQMC_RNG_MINSTD) {
-    // one uniform per site attempt in sweep order, drawn as bernoulli_distribution does
-    for (int w = 0; w < b->nw; ++w) {
-      const auto& d = b->desc[w];
-      const size_t n = (size_t)d.Lt * d.L * d.L;
-      double* u = b->h_uni + b->uni_stride * w;
-      for (size_t k = 0; k < n; ++k) u[k] = std::generate_canonical<double, 53>(b->eng[w]);
-    }
-    CUDA_TRY(cudaMemcpyAsync(b->d_uni, b->h_uni, sizeof(double) * b->uni_stride * b->nw, cudaMemcpyHostToDevice,
-                             b->stream));
-  } else {
-    // Philox counter: the half-sweep index, carried in every descriptor
-    ++b->sweep_id;
-    for (int w = 0; w < b->nw; ++w) b->hw[w].sweep_id = b->sweep_id;
-    CUDA_TRY(cudaMemcpyAsync(b->dW, b->hw.data(), sizeof(WalkerDev) * b->nw, cudaMemcpyHostToDevice, b->stream));
-  }
+// All device work of one half-sweep, in stream order (captured into a graph).
+static void issue_half_sweep(dqmc_batch* b, int mode, int measure) {
+  if (b->opt.rng == DQMC_RNG_MINSTD)
+    cudaMemcpyAsync(b->d_uni, b->h_uni, sizeof(double) * b->uni_stride * b->nw, cudaMemcpyHostToDevice, b->stream);
+  else
+    launch_bump(b->d_sweep, b->stream);  // Philox counter: the half-sweep index
   for (int j = 0; j < b->maxNs; ++j) {
     const int slot = (b->trace_cap && b->trace_count + j < b->trace_cap) ? b->trace_count + j : -1;
     if (b->any_small) {
@@ -655,12 +664,84 @@ static int half_sweep(dqmc_batch* b, int mode, int measure) {
                  [&] { general_measure_after(mode, b->dW, b->nw, j, b->maxN_general, b->stream); });
     }
   }
+}
+
+static int half_sweep(dqmc_batch* b, int mode, int measure) {
+  if (!b) return fail(DQMC_ERR_ARG, "null batch");
+  if (!b->initialised) return fail(DQMC_ERR_STATE, "sweep before dqmc_init_greens");
+  if (b->opt.rng == DQMC_RNG_MINSTD) {
+    // one uniform per site attempt in sweep order, drawn as bernoulli_distribution does
+    for (int w = 0; w < b->nw; ++w) {
+      const auto& d = b->desc[w];
+      const size_t n = (size_t)d.Lt * d.L * d.L;
+      double* u = b->h_uni + b->uni_stride * w;
+      for (size_t k = 0; k < n; ++k) u[k] = std::generate_canonical<double, 53>(b->eng[w]);
+    }
+  }
+  const int ms = measure ? 1 : 0;
+  const bool use_graph = b->opt.graphs && !b->trace_cap;
+  if (use_graph && b->prof) {
+    // profiled replay: event nodes around each kernel class, read after the replay
+    if (!b->pexec[mode][ms]) {
+      cudaGraph_t g = nullptr;
+      const size_t m0 = b->marks.size();
+      CUDA_TRY(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+      b->capturing = true;
+      issue_half_sweep(b, mode, measure);
+      b->capturing = false;
+      CUDA_TRY(cudaStreamEndCapture(b->stream, &g));
+      b->pmarks[mode][ms].assign(b->marks.begin() + m0, b->marks.end());
+      b->marks.resize(m0);
+      CUDA_TRY(cudaGraphInstantiate(&b->pexec[mode][ms], g, 0));
+      cudaGraphDestroy(g);
+    }
+    CUDA_TRY(cudaGraphLaunch(b->pexec[mode][ms], b->stream));
+    for (auto& m : b->pmarks[mode][ms]) {
+      float t = 0;
+      CUDA_TRY(cudaEventSynchronize(m.b));
+      CUDA_TRY(cudaEventElapsedTime(&t, m.a, m.b));
+      b->prof_ms[m.cls] += t;
+      b->prof_n[m.cls] += 1;
+    }
+  }
+  if (b->nodes[mode][ms] < 0 || (use_graph && !b->prof && !b->gexec[mode][ms])) {
+    // capture the half-sweep: its kernel nodes give the launch count; replayed when graphs are on
+    cudaGraph_t g = nullptr;
+    const bool prof = b->prof;
+    b->prof = false;
+    CUDA_TRY(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+    issue_half_sweep(b, mode, measure);
+    b->prof = prof;
+    CUDA_TRY(cudaStreamEndCapture(b->stream, &g));
+    size_t nn = 0;
+    CUDA_TRY(cudaGraphGetNodes(g, nullptr, &nn));
+    std::vector<cudaGraphNode_t> nodes(nn);
+    CUDA_TRY(cudaGraphGetNodes(g, nodes.data(), &nn));
+    int64_t k = 0;
+    for (auto nd : nodes) {
+      cudaGraphNodeType ty;
+      cudaGraphNodeGetType(nd, &ty);
+      if (ty == cudaGraphNodeTypeKernel) ++k;
+    }
+    b->nodes[mode][ms] = k;
+    if (use_graph && !b->prof) CUDA_TRY(cudaGraphInstantiate(&b->gexec[mode][ms], g, 0));
+    cudaGraphDestroy(g);
+  }
+  if (use_graph && !b->prof) CUDA_TRY(cudaGraphLaunch(b->gexec[mode][ms], b->stream));
+  else if (!use_graph) issue_half_sweep(b, mode, measure);
+  b->launches += b->nodes[mode][ms];
   if (b->trace_cap) b->trace_count = std::min(b->trace_count + b->maxNs, b->trace_cap);
   if (b->opt.rng == DQMC_RNG_MINSTD) {
     // the pinned staging buffer is rewritten by the next half-sweep
     CUDA_TRY(cudaStreamSynchronize(b->stream));
   }
   return launch_check("half-sweep kernels");
+}
+
+int dqmc_launch_count(dqmc_batch* b, int64_t* launches) {
+  if (!b || !launches) return fail(DQMC_ERR_ARG, "null argument");
+  *launches = b->launches;
+  return DQMC_OK;
 }
 
 int dqmc_sweep_0_to_beta(dqmc_batch* b, int measure) { return half_sweep(b, MODE_FWD, measure); }

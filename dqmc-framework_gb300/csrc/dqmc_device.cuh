@@ -68,7 +68,7 @@ struct WalkerDev {
   int* status;
   const double* uni;         // parity uniforms of the current half-sweep [Lt*N]
   unsigned long long seed;   // Philox key
-  unsigned long long sweep_id;  // Philox counter word (half-sweep index)
+  const unsigned long long* sweep_ctr;  // Philox counter word: the batch's half-sweep index (device)
   double* trace;             // [trace_cap][2][N*N] or null
   int trace_cap;
   int pad1;

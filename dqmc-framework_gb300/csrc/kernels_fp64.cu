@@ -395,6 +395,7 @@ __global__ void __launch_bounds__(kThreads) segment_kernel(const WalkerDev* __re
 
   double sign = *w.sign;
   long long acc_count = 0;
+  const unsigned long long sweep = (w.rng == 1) ? *w.sweep_ctr : 0ULL;
   const int nsl = t_hi - t_lo + 1;
   for (int q = 0; q < nsl; ++q) {
     const int t = (MODE == MODE_FWD) ? t_lo + q : t_hi - q;
@@ -445,7 +446,7 @@ __global__ void __launch_bounds__(kThreads) segment_kernel(const WalkerDev* __re
           const double r = (w.model == 0) ? __dmul_rn(ru, rd) : __dmul_rn(__dmul_rn(w.ex2[si], ru), rd);
           const int attempt = (MODE == MODE_FWD) ? (eff * N + i) : ((Lt - t) * N + i);
           const double u = (w.rng == 0) ? w.uni[attempt]
-                                        : philox_uniform(w.seed, blockIdx.x, w.sweep_id, (unsigned)(eff * N + i));
+                                        : philox_uniform(w.seed, blockIdx.x, sweep, (unsigned)(eff * N + i));
           const double prob = fmin(1.0, fabs(r));
           if (!isfinite(r)) atomicOr(w.status, ST_NONFINITE_RATIO);
           if (u < prob) {
@@ -1049,6 +1050,10 @@ __global__ void __launch_bounds__(kThreads) sign_kernel(const WalkerDev* __restr
   (void)red;
   if (threadIdx.x == 0) *w.sign = (total_neg % 2 == 0) ? 1.0 : -1.0;
 }
+
+// half-sweep counter of the Philox stream (a kernel, so a captured graph advances it)
+__global__ void bump_counter_kernel(unsigned long long* ctr) { *ctr += 1ULL; }
+void launch_bump(unsigned long long* ctr, cudaStream_t st) { bump_counter_kernel<<<1, 1, 0, st>>>(ctr); }
 
 // --------------------------------------------------------------------------
 // FP64 FMA throughput probe: 8 independent register FMA chains per thread.

@@ -363,6 +363,7 @@ __global__ void __launch_bounds__(kMetroThreads) metropolis_general_kernel(const
   for (int i = threadIdx.x; i < N; i += blockDim.x) s_field[i] = w.fields[(long long)eff * N + i];
   double sign = *w.sign;
   long long acc_count = 0;
+  const unsigned long long sweep = (w.rng == 1) ? *w.sweep_ctr : 0ULL;
   __syncthreads();
 
   auto decide_from = [&](int i0, bool pending) {
@@ -384,7 +385,7 @@ __global__ void __launch_bounds__(kMetroThreads) metropolis_general_kernel(const
       const double r = (w.model == 0) ? __dmul_rn(ru, rd) : __dmul_rn(__dmul_rn(w.ex2[si], ru), rd);
       const int attempt = (mode == MODE_FWD) ? (eff * N + i) : ((Lt - t) * N + i);
       const double u = (w.rng == 0) ? w.uni[attempt]
-                                    : philox_uniform(w.seed, blockIdx.x, w.sweep_id, (unsigned)(eff * N + i));
+                                    : philox_uniform(w.seed, blockIdx.x, sweep, (unsigned)(eff * N + i));
       const double prob = fmin(1.0, fabs(r));
       if (!isfinite(r)) atomicOr(w.status, ST_NONFINITE_RATIO);
       if (u < prob) {

@@ -35,7 +35,7 @@ EXPORTS = [
     "dqmc_get_wrap_error", "dqmc_get_accept_count", "dqmc_get_status", "dqmc_get_observables",
     "dqmc_clear_observables", "dqmc_trace_count", "dqmc_trace_get", "dqmc_trace_clear", "dqmc_batch_info",
     "dqmc_profile_enable", "dqmc_profile_read", "dqmc_microbench_fp64", "dqmc_get_observables_all",
-    "dqmc_product_check", "dqmc_product_device_noalloc",
+    "dqmc_product_check", "dqmc_product_device_noalloc", "dqmc_launch_count",
 ]
 KCLASSES = ["segment", "push", "greens", "measure"]
 
@@ -54,7 +54,8 @@ class _Desc(ctypes.Structure):
 
 
 class _Opts(ctypes.Structure):
-    _fields_ = [("rng", ctypes.c_int), ("precision", ctypes.c_int), ("trace", ctypes.c_int)]
+    _fields_ = [("rng", ctypes.c_int), ("precision", ctypes.c_int), ("trace", ctypes.c_int),
+                ("graphs", ctypes.c_int)]
 
 
 _lib = None
@@ -88,6 +89,7 @@ def load() -> ctypes.CDLL:
         "dqmc_microbench_fp64": (c, [dp]), "dqmc_get_observables_all": (c, [vp, dp, i64p]),
         "dqmc_product_check": (c, [c, dp, dp, dp]),
         "dqmc_product_device_noalloc": (c, [c, vp, vp, vp, vp]),
+        "dqmc_launch_count": (c, [vp, i64p]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -129,11 +131,11 @@ class WalkerDesc:
 class Batch:
     """A batch of independent walkers on the current CUDA device."""
 
-    def __init__(self, walkers, rng=RNG_MINSTD, precision=FP64, trace=False):
+    def __init__(self, walkers, rng=RNG_MINSTD, precision=FP64, trace=False, graphs=True):
         L = load()
         self.walkers = list(walkers)
         arr = (_Desc * len(self.walkers))(*[w._c() for w in self.walkers])
-        opts = _Opts(rng, precision, int(trace))
+        opts = _Opts(rng, precision, int(trace), int(graphs))
         h = ctypes.c_void_p()
         _check(L.dqmc_batch_create(arr, len(self.walkers), ctypes.byref(opts), ctypes.byref(h)))
         self.h = h
@@ -255,6 +257,11 @@ class Batch:
             _check(load().dqmc_profile_read(self.h, k, ctypes.byref(ms), ctypes.byref(n)))
             out[name] = (ms.value, n.value)
         return out
+
+    def launch_count(self) -> int:
+        v = ctypes.c_int64()
+        _check(load().dqmc_launch_count(self.h, ctypes.byref(v)))
+        return v.value
 
     def updates_per_half_sweep(self) -> int:
         nw = ctypes.c_int()

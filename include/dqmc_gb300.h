@@ -93,6 +93,8 @@ typedef struct dqmc_batch_options {
   int precision;       /* enum dqmc_precision */
   int trace;           /* 1: keep G after every stabilization of the last half-sweep
                           (parity tests; costs device memory) */
+  int graphs;          /* 1: capture each kind of half-sweep once into a CUDA graph and replay
+                          it (ignored while tracing or profiling) */
 } dqmc_batch_options;
 
 typedef struct dqmc_batch dqmc_batch;
@@ -156,6 +158,10 @@ int dqmc_trace_clear(dqmc_batch* b);
 
 /* Statistics of the last half-sweep for throughput accounting. */
 int dqmc_batch_info(dqmc_batch* b, int* n_walkers, int64_t* updates_per_half_sweep);
+
+/* Kernels launched by this batch since creation (graph replays count every
+ * kernel node of the replayed graph). */
+int dqmc_launch_count(dqmc_batch* b, int64_t* launches);
 
 /* Kernel-class timing with CUDA events on the batch's stream (the reference
  * has only a whole-run wall-clock timer, src/dqmc.cpp:37-41).  Classes:
