@@ -211,6 +211,7 @@ def run_gpu(args, wl, rank, world):
         batch.fields_random(w)
     batch.init_greens()
     upd = batch.updates_per_half_sweep()
+    tuning = batch.tuning()
 
     def step(k, b=batch):
         if k % 2 == 0:
@@ -297,6 +298,7 @@ def run_gpu(args, wl, rank, world):
                "steps": ek, "rng": "host minstd_rand0 (reference stream)"}
         eb.close()
     return dict(value=value, ms=ms, roofline=roofline, e2e=e2e, clocks=clk, launches=launches, status=status,
+                tuning=tuning,
                 accept_rate=acc_per_walker_half / (wl["L"] ** 2 * wl["Lt"]), fp64_peak=fp64_peak)
 
 
@@ -351,6 +353,8 @@ def main():
             "config": config, "roofline": r["roofline"], "cpu_baseline": cb, "e2e": r["e2e"],
             "gpu_launches": r["launches"], "clocks": r["clocks"], "accept_rate": r["accept_rate"],
             "walker_status_nonzero": sum(1 for s in r["status"] if s)}
+    if r["tuning"]["candidates"]:
+        line["autotune"] = r["tuning"]
     print(json.dumps(line))
 
 

@@ -37,7 +37,10 @@ void launch_bump(unsigned long long* ctr, cudaStream_t st);
 // general (N > 64) walkers, kernels_general.cu
 cudaError_t configure_general_kernels();
 void general_slice(int mode, const WalkerDev* W, int nw, int j, int q, int maxN, int measure, bool any_dense,
-                   bool any_cb, bool mixed, int kd, int smax, cudaStream_t st);
+                   bool any_cb, bool mixed, int kd, int smax, int tc_flush, cudaStream_t st);
+void launch_metropolis_delayed(bool mixed, const WalkerDev* W, int nw, int mode, int j, int q, int maxN, int S_max,
+                               int KD, int tc_flush, cudaStream_t st);
+size_t delayed_smem_bytes_host(int N, int S, int KD);
 cudaError_t configure_delayed_kernels();
 int delayed_pick_kd(int N, int S);
 void general_chain_init(int mode, const WalkerDev* W, int nw, int j, cudaStream_t st);
@@ -175,6 +178,9 @@ struct dqmc_batch {
   bool any_small = false, any_general = false, any_general_dense = false, any_general_cb = false;
   bool mixed = false;
   int kd = 0, smax = 1;  // delayed-update block size of the general walkers (0: rank-1 kernel)
+  int tc_flush = 1;      // mixed walkers: flush the delayed block on the tensor cores
+  bool tuned = false;
+  std::vector<std::pair<std::pair<int, int>, float>> tune_log;  // ((kd, tc), ms) per candidate
   dqmc_batch_options opt{};
   std::vector<dqmc_walker_desc> desc;
   std::vector<WalkerDev> hw;        // host copies of the descriptors
@@ -598,6 +604,68 @@ static int launch_check(const char* what) {
   return DQMC_OK;
 }
 
+// Autotuner of the delayed-update Metropolis: times one slice of every walker
+// for each candidate (block size k, flush kind) on the batch's own state,
+// restoring G, the fields and the walker scalars after each trial, and keeps
+// the fastest.  Candidates: k in {32, 16, 8} that fit shared memory; on the
+// mixed path each k with the tensor-core flush and with the FP64 flush.
+static int autotune_delayed(dqmc_batch* b) {
+  std::vector<std::pair<int, int>> cand;
+  const int kmax = b->kd;
+  for (int kd : {32, 16, 8}) {
+    if (kd > kmax) continue;
+    if (b->mixed && kd >= 16) cand.push_back({kd, 1});
+    cand.push_back({kd, 0});
+  }
+  // back up what one Metropolis slice changes: G (spins < S) into work, fields into scr
+  std::vector<dqmc_batch::Scal> scal(b->nw);
+  CUDA_TRY(cudaMemcpyAsync(scal.data(), b->d_scal, sizeof(dqmc_batch::Scal) * b->nw, cudaMemcpyDeviceToHost,
+                           b->stream));
+  for (int w = 0; w < b->nw; ++w) {
+    const WalkerDev& h = b->hw[w];
+    if (h.path == 0) continue;
+    CUDA_TRY(cudaMemcpyAsync(h.work, h.G, sizeof(double) * h.S * h.N * h.N, cudaMemcpyDeviceToDevice, b->stream));
+    CUDA_TRY(cudaMemcpyAsync(h.scr, h.fields, (size_t)h.Lt * h.N, cudaMemcpyDeviceToDevice, b->stream));
+  }
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  float best = 1e30f;
+  std::pair<int, int> pick = cand.empty() ? std::make_pair(b->kd, 1) : cand[0];
+  b->tune_log.clear();
+  for (auto c : cand) {
+    for (int rep = 0; rep < 2; ++rep) {  // first run warms caches and code
+      cudaEventRecord(e0, b->stream);
+      launch_metropolis_delayed(b->mixed, b->dW, b->nw, MODE_FWD, 0, 0, b->maxN_general, b->smax, c.first, c.second,
+                                b->stream);
+      cudaEventRecord(e1, b->stream);
+      CUDA_TRY(cudaEventSynchronize(e1));
+      float ms = 0;
+      cudaEventElapsedTime(&ms, e0, e1);
+      for (int w = 0; w < b->nw; ++w) {  // restore
+        const WalkerDev& h = b->hw[w];
+        if (h.path == 0) continue;
+        CUDA_TRY(cudaMemcpyAsync(h.G, h.work, sizeof(double) * h.S * h.N * h.N, cudaMemcpyDeviceToDevice, b->stream));
+        CUDA_TRY(cudaMemcpyAsync(h.fields, h.scr, (size_t)h.Lt * h.N, cudaMemcpyDeviceToDevice, b->stream));
+      }
+      if (rep == 1) {
+        b->tune_log.push_back({c, ms});
+        if (ms < best) { best = ms; pick = c; }
+      }
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  CUDA_TRY(cudaMemcpyAsync(b->d_scal, scal.data(), sizeof(dqmc_batch::Scal) * b->nw, cudaMemcpyHostToDevice,
+                           b->stream));
+  CUDA_TRY(cudaStreamSynchronize(b->stream));
+  if (int r = launch_check("autotune")) return r;
+  b->kd = pick.first;
+  b->tc_flush = pick.second;
+  b->tuned = true;
+  return DQMC_OK;
+}
+
 int dqmc_init_greens(dqmc_batch* b) {
   if (!b) return fail(DQMC_ERR_ARG, "null batch");
   for (int j = 0; j < b->maxNs; ++j) {
@@ -609,7 +677,7 @@ int dqmc_init_greens(dqmc_batch* b) {
       general_chain_init(MODE_INIT, b->dW, b->nw, j, b->stream);
       for (int q = 0; q < b->maxPace_general; ++q)
         general_slice(MODE_INIT, b->dW, b->nw, j, q, b->maxN_general, 0, b->any_general_dense, b->any_general_cb,
-                      b->mixed, b->kd, b->smax, b->stream);
+                      b->mixed, b->kd, b->smax, b->tc_flush, b->stream);
       general_push(MODE_INIT, b->dW, b->nw, j, b->maxN_general, b->stream);
     }
   }
@@ -629,6 +697,9 @@ int dqmc_init_greens(dqmc_batch* b) {
   CUDA_TRY(cudaStreamSynchronize(b->stream));
   b->initialised = true;
   b->trace_count = 0;
+  if (b->any_general && b->kd > 0 && !b->tuned) {
+    if (int r = autotune_delayed(b)) return r;
+  }
   return DQMC_OK;
 }
 
@@ -654,7 +725,7 @@ static void issue_half_sweep(dqmc_batch* b, int mode, int measure) {
         general_chain_init(mode, b->dW, b->nw, j, b->stream);
         for (int q = 0; q < b->maxPace_general; ++q)
           general_slice(mode, b->dW, b->nw, j, q, b->maxN_general, measure, b->any_general_dense,
-                        b->any_general_cb, b->mixed, b->kd, b->smax, b->stream);
+                        b->any_general_cb, b->mixed, b->kd, b->smax, b->tc_flush, b->stream);
       });
       b->timed(DQMC_KCLASS_PUSH, [&] { general_push(mode, b->dW, b->nw, j, b->maxN_general, b->stream); });
       b->timed(DQMC_KCLASS_GREENS,
@@ -736,6 +807,20 @@ static int half_sweep(dqmc_batch* b, int mode, int measure) {
     CUDA_TRY(cudaStreamSynchronize(b->stream));
   }
   return launch_check("half-sweep kernels");
+}
+
+int dqmc_tuning(dqmc_batch* b, int* kd, int* tc_flush, int* n_candidates, int* cand_kd, int* cand_tc,
+                float* cand_ms) {
+  if (!b) return fail(DQMC_ERR_ARG, "null batch");
+  if (kd) *kd = b->kd;
+  if (tc_flush) *tc_flush = b->tc_flush;
+  if (n_candidates) *n_candidates = (int)b->tune_log.size();
+  for (size_t k = 0; k < b->tune_log.size(); ++k) {
+    if (cand_kd) cand_kd[k] = b->tune_log[k].first.first;
+    if (cand_tc) cand_tc[k] = b->tune_log[k].first.second;
+    if (cand_ms) cand_ms[k] = b->tune_log[k].second;
+  }
+  return DQMC_OK;
 }
 
 int dqmc_launch_count(dqmc_batch* b, int64_t* launches) {

@@ -168,7 +168,7 @@ __device__ void flush_ozaki(double* G0, int N, const double* U, const double* V,
 // --------------------------------------------------------------------------
 template <bool MIXED>
 __global__ void __launch_bounds__(kDelThreads) metropolis_delayed_kernel(const WalkerDev* __restrict__ W, int mode,
-                                                                        int j, int q, int KD) {
+                                                                        int j, int q, int KD, int tc_flush) {
   const WalkerDev& w = W[blockIdx.x];
   if (w.path == 0 || (MIXED != (w.path == 2))) return;
   int t;
@@ -199,7 +199,7 @@ __global__ void __launch_bounds__(kDelThreads) metropolis_delayed_kernel(const W
   int M = 0;  // pending columns of U, V
   auto flush = [&]() {
     if (M == 0) return;
-    if (MIXED && KD >= 16) {
+    if (MIXED && tc_flush && KD >= 16) {
       // zero the stale columns m >= M so the K = KD product sees only the pending block
       for (int sp = 0; sp < S; ++sp)
         for (int e = threadIdx.x; e < N * (KD - M); e += kDelThreads) {
@@ -312,10 +312,10 @@ cudaError_t configure_delayed_kernels() {
 }
 
 void launch_metropolis_delayed(bool mixed, const WalkerDev* W, int nw, int mode, int j, int q, int maxN, int S_max,
-                               int KD, cudaStream_t st) {
+                               int KD, int tc_flush, cudaStream_t st) {
   const size_t sm = delayed_smem_bytes(maxN, S_max, KD);
-  if (mixed) metropolis_delayed_kernel<true><<<nw, kDelThreads, sm, st>>>(W, mode, j, q, KD);
-  else metropolis_delayed_kernel<false><<<nw, kDelThreads, sm, st>>>(W, mode, j, q, KD);
+  if (mixed) metropolis_delayed_kernel<true><<<nw, kDelThreads, sm, st>>>(W, mode, j, q, KD, tc_flush);
+  else metropolis_delayed_kernel<false><<<nw, kDelThreads, sm, st>>>(W, mode, j, q, KD, 0);
 }
 
 }  // namespace dqmc

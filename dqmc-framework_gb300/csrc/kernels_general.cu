@@ -939,10 +939,10 @@ void mixed_wrap_bwd(const WalkerDev* W, int nw, int maxN, int j, int q, cudaStre
 void mixed_chain(const WalkerDev* W, int nw, int maxN, int mode, int j, int q, cudaStream_t st);
 
 void launch_metropolis_delayed(bool mixed, const WalkerDev* W, int nw, int mode, int j, int q, int maxN, int S_max,
-                               int KD, cudaStream_t st);
+                               int KD, int tc_flush, cudaStream_t st);
 
 void general_slice(int mode, const WalkerDev* W, int nw, int j, int q, int maxN, int measure, bool any_dense,
-                   bool any_cb, bool mixed, int kd, int smax, cudaStream_t st) {
+                   bool any_cb, bool mixed, int kd, int smax, int tc_flush, cudaStream_t st) {
   // in a mixed batch the dense products go through the tensor cores (kernels_ozaki.cu)
   const bool fp64_dense = any_dense && !mixed;
   const bool mixed_dense = any_dense && mixed;
@@ -958,7 +958,7 @@ void general_slice(int mode, const WalkerDev* W, int nw, int j, int q, int maxN,
     if (any_cb) cb_general_kernel<<<2 * nw, 256, cb_sm, st>>>(W, mode, j, q, 0);
   }
   if (mode != MODE_INIT) {
-    if (kd > 0) launch_metropolis_delayed(mixed, W, nw, mode, j, q, maxN, smax, kd, st);
+    if (kd > 0) launch_metropolis_delayed(mixed, W, nw, mode, j, q, maxN, smax, kd, tc_flush, st);
     else metropolis_general_kernel<<<nw, kMetroThreads, met_sm, st>>>(W, mode, j, q);
     if (measure) measure_general_kernel<<<nw, 256, sizeof(double) * 2 * maxN, st>>>(W, mode, j, q, 0);
   }

@@ -35,7 +35,7 @@ EXPORTS = [
     "dqmc_get_wrap_error", "dqmc_get_accept_count", "dqmc_get_status", "dqmc_get_observables",
     "dqmc_clear_observables", "dqmc_trace_count", "dqmc_trace_get", "dqmc_trace_clear", "dqmc_batch_info",
     "dqmc_profile_enable", "dqmc_profile_read", "dqmc_microbench_fp64", "dqmc_get_observables_all",
-    "dqmc_product_check", "dqmc_product_device_noalloc", "dqmc_launch_count",
+    "dqmc_product_check", "dqmc_product_device_noalloc", "dqmc_launch_count", "dqmc_tuning",
 ]
 KCLASSES = ["segment", "push", "greens", "measure"]
 
@@ -90,6 +90,7 @@ def load() -> ctypes.CDLL:
         "dqmc_product_check": (c, [c, dp, dp, dp]),
         "dqmc_product_device_noalloc": (c, [c, vp, vp, vp, vp]),
         "dqmc_launch_count": (c, [vp, i64p]),
+        "dqmc_tuning": (c, [vp, ip, ip, ip, ip, ip, ctypes.POINTER(ctypes.c_float)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -257,6 +258,16 @@ class Batch:
             _check(load().dqmc_profile_read(self.h, k, ctypes.byref(ms), ctypes.byref(n)))
             out[name] = (ms.value, n.value)
         return out
+
+    def tuning(self) -> dict:
+        """The autotuner's pick (delayed block k, tensor-core flush) and every candidate's time."""
+        kd, tc, n = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        ck = (ctypes.c_int * 8)()
+        ct = (ctypes.c_int * 8)()
+        cm = (ctypes.c_float * 8)()
+        _check(load().dqmc_tuning(self.h, ctypes.byref(kd), ctypes.byref(tc), ctypes.byref(n), ck, ct, cm))
+        return {"kd": kd.value, "tc_flush": tc.value,
+                "candidates": [{"kd": ck[i], "tc_flush": ct[i], "ms_per_slice": cm[i]} for i in range(n.value)]}
 
     def launch_count(self) -> int:
         v = ctypes.c_int64()

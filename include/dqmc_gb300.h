@@ -159,6 +159,13 @@ int dqmc_trace_clear(dqmc_batch* b);
 /* Statistics of the last half-sweep for throughput accounting. */
 int dqmc_batch_info(dqmc_batch* b, int* n_walkers, int64_t* updates_per_half_sweep);
 
+/* The autotuner's choice for walkers whose G lives in HBM (N > 64 or the mixed
+ * path): delayed-update block size k and whether its flush runs on the tensor
+ * cores, with every candidate's time for one slice of the whole batch (arrays
+ * sized 8).  dqmc_init_greens runs the tuner on the batch's own state. */
+int dqmc_tuning(dqmc_batch* b, int* kd, int* tc_flush, int* n_candidates, int* cand_kd, int* cand_tc,
+                float* cand_ms);
+
 /* Kernels launched by this batch since creation (graph replays count every
  * kernel node of the replayed graph). */
 int dqmc_launch_count(dqmc_batch* b, int64_t* launches);

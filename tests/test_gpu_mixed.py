@@ -70,3 +70,22 @@ def test_mixed_sweep_dG_against_fp64(dq, model, L, U, mu, beta, Lt, pace):
         worst = max(worst, float(np.abs(om[0][w][1] - of[0][w][1]).max()))
         assert bm.status(w) == 0
     assert worst <= 1e-6, worst
+
+
+def test_autotuner_picks_a_timed_candidate(dq):
+    """dqmc_init_greens times every (k, flush) candidate on the batch's own
+    state and restores it: the pick is the fastest candidate, and the sweep that
+    follows still matches the FP64 path (same decisions)."""
+    descs = [dq.WalkerDesc(model=1, L=12, U=4.0, mu=-0.5, beta=2.0, Lt=20, pace=10, seed=300 + w) for w in range(3)]
+    bm, om = _run(dq, descs, dq.MIXED)
+    t = bm.tuning()
+    cands = t["candidates"]
+    assert {(c["kd"], c["tc_flush"]) for c in cands} >= {(32, 1), (32, 0), (16, 1), (16, 0), (8, 0)}
+    best = min(cands, key=lambda c: c["ms_per_slice"])
+    assert (t["kd"], t["tc_flush"]) == (best["kd"], best["tc_flush"])
+    assert all(c["ms_per_slice"] > 0 for c in cands)
+    bf, of = _run(dq, descs, dq.FP64)
+    assert {c["tc_flush"] for c in bf.tuning()["candidates"]} == {0}
+    for w in range(len(descs)):
+        np.testing.assert_array_equal(om[0][w][0], of[0][w][0])
+        assert float(np.abs(om[0][w][1] - of[0][w][1]).max()) <= 1e-6
