@@ -42,9 +42,15 @@ void launch_metropolis_delayed(bool mixed, const WalkerDev* W, int nw, int mode,
                                int KD, int tc_flush, cudaStream_t st);
 size_t delayed_smem_bytes_host(int N, int S, int KD);
 cudaError_t configure_delayed_kernels();
+cudaError_t configure_submatrix_kernel();
+size_t submatrix_scratch_bytes(int N);
+void launch_metropolis_sub(const WalkerDev* W, int nw, int mode, int j, int q, int maxN, int S_max, cudaStream_t st);
 int delayed_pick_kd(int N, int S);
 void general_chain_init(int mode, const WalkerDev* W, int nw, int j, cudaStream_t st);
 void general_push(int mode, const WalkerDev* W, int nw, int j, int maxN, cudaStream_t st);
+void oz_push(int mode, const WalkerDev* W, int nw, int j, int maxN, cudaStream_t st);
+void oz_greens(int mode, const WalkerDev* W, int nw, int j, int trace_slot, int maxN, cudaStream_t st);
+cudaError_t configure_stab_oz_kernels(int maxN);
 void general_greens(int mode, const WalkerDev* W, int nw, int j, int trace_slot, int maxN, cudaStream_t st);
 void general_measure_after(int mode, const WalkerDev* W, int nw, int j, int maxN, cudaStream_t st);
 void general_sign(const WalkerDev* W, int nw, int maxN, cudaStream_t st);
@@ -62,6 +68,11 @@ void oz_selftest(const double* A, const double* B, double* C, unsigned short* sa
 using namespace dqmc;
 
 namespace {
+
+// walkers of the tensor-core path with 128 <= N <= 768 are stabilized by the
+// blocked QR of kernels_stab_oz.cu (its FP64 panel of 32 columns fits shared memory)
+constexpr int kMaxOzN = 768;
+bool uses_ozstab(int N, int precision) { return precision == DQMC_MIXED && N >= 128 && N <= kMaxOzN; }
 
 thread_local std::string g_err;
 
@@ -176,9 +187,13 @@ struct dqmc_batch {
   // walkers split by kernel family: N <= 64 (SMEM-resident) and N > 64 (general)
   int maxN_small = 0, maxN_general = 0, maxPace_general = 0;
   bool any_small = false, any_general = false, any_general_dense = false, any_general_cb = false;
+  bool any_ozstab = false;  // walkers stabilized by the tensor-core blocked QR
+  int maxN_oz = 0;
   bool mixed = false;
   int kd = 0, smax = 1;  // delayed-update block size of the general walkers (0: rank-1 kernel)
-  int tc_flush = 1;      // mixed walkers: flush the delayed block on the tensor cores
+  // Metropolis of HBM walkers: 0 delayed with FP64 flush, 1 delayed with tensor-core
+  // flush, 2 submatrix updates with tensor-core flush (mixed walkers)
+  int tc_flush = 1;
   bool tuned = false;
   std::vector<std::pair<std::pair<int, int>, float>> tune_log;  // ((kd, tc), ms) per candidate
   dqmc_batch_options opt{};
@@ -295,6 +310,10 @@ int dqmc_batch_create(const dqmc_walker_desc* descs, int n, const dqmc_batch_opt
       b->maxN_general = std::max(b->maxN_general, N);
       b->maxPace_general = std::max(b->maxPace_general, d.pace);
       if (d.checkerboard) b->any_general_cb = true; else b->any_general_dense = true;
+      if (uses_ozstab(N, o.precision)) {
+        b->any_ozstab = true;
+        b->maxN_oz = std::max(b->maxN_oz, N);
+      }
     } else {
       b->any_small = true;
       b->maxN_small = std::max(b->maxN_small, N);
@@ -309,9 +328,10 @@ int dqmc_batch_create(const dqmc_walker_desc* descs, int n, const dqmc_batch_opt
   for (auto& d : b->desc)
     if (d.model == DQMC_REPULSIVE_HUBBARD) b->smax = 2;
   if (b->any_general) b->kd = delayed_pick_kd(b->maxN_general, b->smax);
+  if (b->mixed) b->tc_flush = 2;  // submatrix updates until the tuner has timed the candidates
 
   // ---- arena layout ----
-  struct Off { size_t G, chain, work, scr, sl, sle, stack, fields, ff, trace; int dense_id; };
+  struct Off { size_t G, chain, work, scr, sl, sle, stack, fields, ff, trace, msub; int dense_id; };
   std::vector<Off> off(n);
   std::map<std::tuple<int, double, double, double>, int> dense_ids;  // (L, t, mu, dtau) -> id
   std::vector<std::pair<std::vector<double>, std::vector<double>>> dense;
@@ -338,6 +358,7 @@ int dqmc_batch_create(const dqmc_walker_desc* descs, int n, const dqmc_batch_opt
     off[w].stack = take(sizeof(double) * 2 * S * ns * lvl);
     off[w].fields = take((size_t)d.Lt * N);
     off[w].trace = b->trace_cap ? take(sizeof(double) * (size_t)b->trace_cap * 2 * N * N) : 0;
+    off[w].msub = (o.precision == DQMC_MIXED) ? take((size_t)S * submatrix_scratch_bytes(N)) : 0;
     off[w].dense_id = -1;
     if (!d.checkerboard) {
       auto key = std::make_tuple(d.L, d.hopping_t, d.mu, d.beta / d.Lt);
@@ -380,6 +401,8 @@ int dqmc_batch_create(const dqmc_walker_desc* descs, int n, const dqmc_batch_opt
   if (e == cudaSuccess) e = configure_general_kernels();
   if (e == cudaSuccess) e = configure_ozaki_kernels();
   if (e == cudaSuccess) e = configure_delayed_kernels();
+  if (e == cudaSuccess) e = configure_submatrix_kernel();
+  if (e == cudaSuccess) e = configure_stab_oz_kernels(kMaxOzN);
   if (e != cudaSuccess) {
     cudaFree(b->arena);
     delete b;
@@ -466,6 +489,8 @@ int dqmc_batch_create(const dqmc_walker_desc* descs, int n, const dqmc_batch_opt
     h.path = (o.precision == DQMC_MIXED) ? 2 : (gen ? 1 : 0);
     h.work = gen ? reinterpret_cast<double*>(base + off[w].work) : nullptr;
     h.scr = gen ? reinterpret_cast<double*>(base + off[w].scr) : nullptr;
+    h.msub = (o.precision == DQMC_MIXED) ? reinterpret_cast<unsigned char*>(base + off[w].msub) : nullptr;
+    h.ozstab = uses_ozstab(N, o.precision) ? 1 : 0;
     if (o.precision == DQMC_MIXED) {
       h.ldk = (N + 15) / 16 * 16;
       h.slice_bits = N <= 256 ? 7 : 6;
@@ -604,14 +629,16 @@ static int launch_check(const char* what) {
   return DQMC_OK;
 }
 
-// Autotuner of the delayed-update Metropolis: times one slice of every walker
-// for each candidate (block size k, flush kind) on the batch's own state,
+// Autotuner of the Metropolis of HBM walkers: times one slice of every walker
+// for each candidate (block size k, update kind) on the batch's own state,
 // restoring G, the fields and the walker scalars after each trial, and keeps
-// the fastest.  Candidates: k in {32, 16, 8} that fit shared memory; on the
-// mixed path each k with the tensor-core flush and with the FP64 flush.
+// the fastest.  Candidates: delayed updates with k in {32, 16, 8} that fit
+// shared memory; on the mixed path, submatrix updates (k = 32) and each
+// delayed k with the tensor-core flush and with the FP64 flush.
 static int autotune_delayed(dqmc_batch* b) {
   std::vector<std::pair<int, int>> cand;
   const int kmax = b->kd;
+  if (b->mixed) cand.push_back({32, 2});
   for (int kd : {32, 16, 8}) {
     if (kd > kmax) continue;
     if (b->mixed && kd >= 16) cand.push_back({kd, 1});
@@ -636,8 +663,11 @@ static int autotune_delayed(dqmc_batch* b) {
   for (auto c : cand) {
     for (int rep = 0; rep < 2; ++rep) {  // first run warms caches and code
       cudaEventRecord(e0, b->stream);
-      launch_metropolis_delayed(b->mixed, b->dW, b->nw, MODE_FWD, 0, 0, b->maxN_general, b->smax, c.first, c.second,
-                                b->stream);
+      if (c.second == 2)
+        launch_metropolis_sub(b->dW, b->nw, MODE_FWD, 0, 0, b->maxN_general, b->smax, b->stream);
+      else
+        launch_metropolis_delayed(b->mixed, b->dW, b->nw, MODE_FWD, 0, 0, b->maxN_general, b->smax, c.first,
+                                  c.second, b->stream);
       cudaEventRecord(e1, b->stream);
       CUDA_TRY(cudaEventSynchronize(e1));
       float ms = 0;
@@ -679,6 +709,7 @@ int dqmc_init_greens(dqmc_batch* b) {
         general_slice(MODE_INIT, b->dW, b->nw, j, q, b->maxN_general, 0, b->any_general_dense, b->any_general_cb,
                       b->mixed, b->kd, b->smax, b->tc_flush, b->stream);
       general_push(MODE_INIT, b->dW, b->nw, j, b->maxN_general, b->stream);
+      if (b->any_ozstab) oz_push(MODE_INIT, b->dW, b->nw, j, b->maxN_oz, b->stream);
     }
   }
   if (b->any_small) {
@@ -687,6 +718,7 @@ int dqmc_init_greens(dqmc_batch* b) {
   }
   if (b->any_general) {
     general_greens(MODE_INIT, b->dW, b->nw, 0, -1, b->maxN_general, b->stream);
+    if (b->any_ozstab) oz_greens(MODE_INIT, b->dW, b->nw, 0, -1, b->maxN_oz, b->stream);
     general_sign(b->dW, b->nw, b->maxN_general, b->stream);
   }
   if (int r = launch_check("init kernels")) return r;
@@ -697,7 +729,7 @@ int dqmc_init_greens(dqmc_batch* b) {
   CUDA_TRY(cudaStreamSynchronize(b->stream));
   b->initialised = true;
   b->trace_count = 0;
-  if (b->any_general && b->kd > 0 && !b->tuned) {
+  if (b->any_general && (b->kd > 0 || b->mixed) && !b->tuned) {
     if (int r = autotune_delayed(b)) return r;
   }
   return DQMC_OK;
@@ -727,9 +759,15 @@ static void issue_half_sweep(dqmc_batch* b, int mode, int measure) {
           general_slice(mode, b->dW, b->nw, j, q, b->maxN_general, measure, b->any_general_dense,
                         b->any_general_cb, b->mixed, b->kd, b->smax, b->tc_flush, b->stream);
       });
-      b->timed(DQMC_KCLASS_PUSH, [&] { general_push(mode, b->dW, b->nw, j, b->maxN_general, b->stream); });
+      b->timed(DQMC_KCLASS_PUSH, [&] {
+        general_push(mode, b->dW, b->nw, j, b->maxN_general, b->stream);
+        if (b->any_ozstab) oz_push(mode, b->dW, b->nw, j, b->maxN_oz, b->stream);
+      });
       b->timed(DQMC_KCLASS_GREENS,
-               [&] { general_greens(mode, b->dW, b->nw, j, slot, b->maxN_general, b->stream); });
+               [&] {
+                 general_greens(mode, b->dW, b->nw, j, slot, b->maxN_general, b->stream);
+                 if (b->any_ozstab) oz_greens(mode, b->dW, b->nw, j, slot, b->maxN_oz, b->stream);
+               });
       if (measure)
         b->timed(DQMC_KCLASS_MEASURE,
                  [&] { general_measure_after(mode, b->dW, b->nw, j, b->maxN_general, b->stream); });

@@ -44,6 +44,9 @@ struct WalkerDev {
   double* chain;             // [S][N*N] (general walkers: [2][S][N*N], ping-pong)
   double* work;              // general walkers: GEMM temporary [S][N*N]
   double* scr;               // general walkers: stabilization scratch [S][2][N*N]
+  // mixed walkers, submatrix Metropolis: per spin T [N][32] FP64, then the BF16
+  // slices of T and of G0(:, accepted sites) [2][6][N][40] and their exponents [2][N]
+  unsigned char* msub;
   // mixed walkers: BF16 slices of the operand being multiplied, [S][slices][N][ldk]
   unsigned short* sl;
   int* sle;                  // slice exponents [S][N]
@@ -71,7 +74,7 @@ struct WalkerDev {
   const unsigned long long* sweep_ctr;  // Philox counter word: the batch's half-sweep index (device)
   double* trace;             // [trace_cap][2][N*N] or null
   int trace_cap;
-  int pad1;
+  int ozstab;                // 1: stabilization by the tensor-core blocked QR (kernels_stab_oz.cu)
 };
 
 // Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11): uniform double in [0,1)

@@ -144,7 +144,6 @@ __device__ void flush_ozaki(double* G0, int N, const double* U, const double* V,
           }
         }
       }
-      const double x = 1.0 / (double)(1 << B);
 #pragma unroll
       for (int mt = 0; mt < 2; ++mt)
 #pragma unroll
@@ -154,10 +153,10 @@ __device__ void flush_ozaki(double* G0, int N, const double* U, const double* V,
             const int rl = wm * 32 + mt * 16 + g + ((v >> 1) << 3), cl = wn * 16 + nt * 8 + 2 * t4 + (v & 1);
             const int r = r0 + rl, c = c0 + cl;
             if (r >= N || c >= N) continue;
-            double s = (double)acc[S - 1][mt][nt][v];
+            long long s = 0;
 #pragma unroll
-            for (int m = S - 2; m >= 0; --m) s = fma(s, x, (double)acc[m][mt][nt][v]);
-            if (s != 0.0) G0[(long long)c * N + r] -= ozaki::scale2(s, eA[rl] + eB[cl] - 2 * B);
+            for (int m = 0; m < S; ++m) s = (s << B) + (long long)ozaki::f2i_small(acc[m][mt][nt][v]);
+            if (s != 0) G0[(long long)c * N + r] -= ozaki::ldexp_i64(s, eA[rl] + eB[cl] - B * (S + 1));
           }
       __syncthreads();
     }

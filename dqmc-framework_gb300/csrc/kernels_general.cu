@@ -91,6 +91,7 @@ __global__ void __launch_bounds__(256) gemm_op_kernel(const WalkerDev* __restric
   if (slice_op && w.path == 2) return;  // mixed walkers take the tensor-core products
   if (slice_op && !slice_of(w, mode, j, q, t, nsl, t_hi)) return;
   if (!slice_op && j >= w.nstack) return;
+  if (!slice_op && w.ozstab) return;  // stabilized by kernels_stab_oz.cu
 
   const long long NN = (long long)N * N;
   double* G = w.G + sp * NN;
@@ -533,7 +534,7 @@ __global__ void __launch_bounds__(256) measure_general_kernel(const WalkerDev* _
 __global__ void __launch_bounds__(1024) push_general_kernel(const WalkerDev* __restrict__ W, int mode, int j) {
   const int wi = blockIdx.x >> 1, sp = blockIdx.x & 1;
   const WalkerDev& w = W[wi];
-  if (!is_general(w) || sp >= w.S || j >= w.nstack) return;
+  if (!is_general(w) || w.ozstab || sp >= w.S || j >= w.nstack) return;
   const int N = w.N;
   const long long NN = (long long)N * N;
   const int side = (mode == MODE_FWD) ? 0 : 1;
@@ -741,7 +742,7 @@ __global__ void __launch_bounds__(1024) push_general_kernel(const WalkerDev* __r
 __global__ void __launch_bounds__(256) greens_prep_general_kernel(const WalkerDev* __restrict__ W, int mode, int j) {
   const int wi = blockIdx.y >> 1, sp = blockIdx.y & 1;
   const WalkerDev& w = W[wi];
-  if (!is_general(w) || sp >= w.S || j >= w.nstack) return;
+  if (!is_general(w) || w.ozstab || sp >= w.S || j >= w.nstack) return;
   const int N = w.N;
   const long long NN = (long long)N * N;
   int nl, nr;
@@ -766,7 +767,7 @@ __global__ void __launch_bounds__(256) greens_prep_general_kernel(const WalkerDe
 __global__ void __launch_bounds__(1024) lu_solve_general_kernel(const WalkerDev* __restrict__ W, int mode, int j) {
   const int wi = blockIdx.x >> 1, sp = blockIdx.x & 1;
   const WalkerDev& w = W[wi];
-  if (!is_general(w) || sp >= w.S || j >= w.nstack) return;
+  if (!is_general(w) || w.ozstab || sp >= w.S || j >= w.nstack) return;
   const int N = w.N;
   const long long NN = (long long)N * N;
   double* M = w.scr + sp * 2 * NN;  // col-major
@@ -842,7 +843,7 @@ __global__ void __launch_bounds__(256) greens_out_general_kernel(const WalkerDev
                                                                  int trace_slot) {
   const int wi = blockIdx.y >> 1, sp = blockIdx.y & 1;
   const WalkerDev& w = W[wi];
-  if (!is_general(w) || sp >= w.S || j >= w.nstack) return;
+  if (!is_general(w) || w.ozstab || sp >= w.S || j >= w.nstack) return;
   int nl, nr;
   if (mode == MODE_FWD) { nl = j + 1; nr = w.nstack - 1 - j; }
   else if (mode == MODE_BWD) { nl = w.nstack - 1 - j; nr = j + 1; }
@@ -940,6 +941,7 @@ void mixed_chain(const WalkerDev* W, int nw, int maxN, int mode, int j, int q, c
 
 void launch_metropolis_delayed(bool mixed, const WalkerDev* W, int nw, int mode, int j, int q, int maxN, int S_max,
                                int KD, int tc_flush, cudaStream_t st);
+void launch_metropolis_sub(const WalkerDev* W, int nw, int mode, int j, int q, int maxN, int S_max, cudaStream_t st);
 
 void general_slice(int mode, const WalkerDev* W, int nw, int j, int q, int maxN, int measure, bool any_dense,
                    bool any_cb, bool mixed, int kd, int smax, int tc_flush, cudaStream_t st) {
@@ -958,7 +960,8 @@ void general_slice(int mode, const WalkerDev* W, int nw, int j, int q, int maxN,
     if (any_cb) cb_general_kernel<<<2 * nw, 256, cb_sm, st>>>(W, mode, j, q, 0);
   }
   if (mode != MODE_INIT) {
-    if (kd > 0) launch_metropolis_delayed(mixed, W, nw, mode, j, q, maxN, smax, kd, tc_flush, st);
+    if (mixed && tc_flush == 2) launch_metropolis_sub(W, nw, mode, j, q, maxN, smax, st);
+    else if (kd > 0) launch_metropolis_delayed(mixed, W, nw, mode, j, q, maxN, smax, kd, tc_flush, st);
     else metropolis_general_kernel<<<nw, kMetroThreads, met_sm, st>>>(W, mode, j, q);
     if (measure) measure_general_kernel<<<nw, 256, sizeof(double) * 2 * maxN, st>>>(W, mode, j, q, 0);
   }

@@ -200,13 +200,11 @@ __device__ void ozaki_product_tile(const ProdJob& job, int N, int ldk, int bits,
         const int r = r0 + wm * 32 + mt * 16 + g + ((v >> 1) << 3);
         const int c = c0 + wn * 16 + nt * 8 + 2 * t4 + (v & 1);
         if (r >= N || c >= N) continue;
-        // Horner in x = 2^-bits: s = sum_m S_m x^m, then value = s 2^{ea+eb-2 bits}
-        const double x = 1.0 / (double)(1 << bits);
-        double s = (double)acc[S - 1][mt][nt][v];
+        // integer Horner: v = sum_m S_m 2^{bits (S-1-m)}, value = v 2^{ea+eb-bits (S+1)}
+        long long s = 0;
 #pragma unroll
-        for (int m = S - 2; m >= 0; --m) s = fma(s, x, (double)acc[m][mt][nt][v]);
-        const int e = job.ea[r] + job.eb[c] - bits * 2;
-        epi(r, c, (s == 0.0) ? 0.0 : ozaki::scale2(s, e));
+        for (int m = 0; m < S; ++m) s = (s << bits) + (long long)__float2int_rn(acc[m][mt][nt][v]);
+        epi(r, c, ozaki::ldexp_i64(s, job.ea[r] + job.eb[c] - bits * (S + 1)));
       }
 }
 

@@ -1,0 +1,779 @@
+// kernels_stab_oz.cu — stabilization of tensor-core-path walkers (N >= 128):
+// the UDT push and the Green's assembly as blocked Householder factorizations
+// whose matrix products run on the BF16 tensor cores at FP64 accuracy.
+//
+// Reference: SvdStack::push (src/svd_stack.cpp:34-87) factors the B-chain with
+// MKL dgesvd and compute_equaltime_greens (include/utils/numerical_stable.hpp:
+// 186-239) assembles G through an LU inverse.  The plain path restates them
+// with column-pivoted QR (kernels_general.cu), a latency-bound FP64 loop.  Here
+//   push:   the columns of the chain are ordered once by norm (pre-pivoting,
+//           Bai, Lee, Li and Xu, Linear Algebra Appl. 435 (2011) 659) and
+//           factored by blocked Householder QR with 32-column panels.  Each
+//           panel is factored in FP64 in shared memory (LAPACK dgeqr2 and
+//           dlarft order); the trailing update A -= V T^T (V^T A), the formation
+//           of Q and F = D^-1 R P^T F_prev are products.
+//   greens: M = Dlmax^-1 U_L^T U_R Drmax^-1 + Dlmin F_L F_R^T Drmin and
+//           Y = Dlmax^-1 U_L^T; M = QR by the same blocked Householder; X =
+//           R^-1 Q^T Y by blocked reflector application and blocked back
+//           substitution (FP64 diagonal blocks); G = U_R Drmax^-1 X.  Boundary
+//           steps (one stack empty) form M = Y + Dmin F and G = X or X^T.
+// Every product slices its FP64 operands in the kernel into 8 integer slices
+// of 7 bits (56 significant bits, K <= 256) or 9 of 6 (54 bits, K <= 1024) and
+// multiplies them on the BF16 tensor cores with FP32 accumulation (exact for
+// the leading weight groups): an FP64-class GEMM.  Panels, diagonal solves,
+// reflectors and reductions are native FP64.  G equals the pivoted-QR path's
+// mathematically; the UDT factors differ only in the column order of the QR.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "dqmc_device.cuh"
+#include "ozaki.cuh"
+
+namespace dqmc {
+
+namespace {
+
+constexpr int TB = 32;           // Householder panel width
+constexpr int ZT = 64;           // product tile edge
+constexpr int ZK = 32;           // k chunk sliced at a time
+constexpr int ZKP = ZK + 8;      // padded BF16 row (80 bytes)
+
+__device__ __forceinline__ double zwarp_sum(double v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+__device__ __forceinline__ void zstack_tops(const WalkerDev& w, int mode, int j, int& nl, int& nr) {
+  if (mode == MODE_FWD) { nl = j + 1; nr = w.nstack - 1 - j; }
+  else if (mode == MODE_BWD) { nl = w.nstack - 1 - j; nr = j + 1; }
+  else { nl = 0; nr = w.nstack; }
+}
+
+// per-spin scratch: scr = X (matrix being factored) | Y (right-hand sides);
+// work = Wb [TB N] | W2 [TB N] | T factors [ceil(N/TB) TB TB] | invd | four
+// diagonal scale vectors | perm: 2 TB N + TB (N + TB) + 5.5 N <= N^2 for N >= 110
+struct ZScr {
+  double *X, *Y, *Wb, *W2, *Tb, *invd, *dlmaxi, *drmaxi, *dlmin, *drmin;
+  int* perm;
+};
+__device__ __forceinline__ ZScr zscr(const WalkerDev& w, int sp) {
+  const long long NN = (long long)w.N * w.N;
+  const long long TN = (long long)TB * w.N;
+  const long long TT = (long long)TB * TB * ((w.N + TB - 1) / TB);
+  ZScr z;
+  z.X = w.scr + sp * 2 * NN;
+  z.Y = z.X + NN;
+  double* wk = w.work + sp * NN;
+  z.Wb = wk;
+  z.W2 = wk + TN;
+  z.Tb = wk + 2 * TN;
+  z.invd = wk + 2 * TN + TT;
+  z.dlmaxi = z.invd + w.N;
+  z.drmaxi = z.dlmaxi + w.N;
+  z.dlmin = z.drmaxi + w.N;
+  z.drmin = z.dlmin + w.N;
+  z.perm = reinterpret_cast<int*>(z.drmin + w.N);
+  return z;
+}
+
+// An operand of C = op(A) op(B).  Element (row, col) of the stored block sits at
+// p[col * ld + row'] with row' = rowmap ? rowmap[row] : row.  For A the logical
+// element (i, k) is stored (i, k), or (k, i) when tr; for B the logical (k, i)
+// is stored (k, i), or (i, k) when tr (i: output row of A / column of B).
+struct ZOpnd {
+  const double* p;
+  long long ld;
+  int tr;
+  int kind;            // 0 full, 1 unit lower (Householder vectors), 2 upper with diagonal
+  const int* rowmap;
+  const double* ks;    // multiplier along k, or null
+};
+struct ZJob {
+  ZOpnd a, b;
+  double* c;
+  long long ldc;
+  int M, N, K;
+  int beta;            // 1: C += alpha AB
+  double alpha;
+  const double* rs;    // row multiplier of the product, or null
+  const double* cs;    // column multiplier, or null
+  int out;             // 1: Green's function output (wrap error, trace, spin copy)
+};
+
+__device__ __forceinline__ double zel(const ZOpnd& o, int i, int k, bool isB) {
+  const int row = (o.tr != (int)isB) ? k : i;
+  const int col = (o.tr != (int)isB) ? i : k;
+  double v;
+  if (o.kind == 1 && row <= col) v = (row == col) ? 1.0 : 0.0;
+  else if (o.kind == 2 && row > col) v = 0.0;
+  else v = o.p[(long long)col * o.ld + (o.rowmap ? o.rowmap[row] : row)];
+  if (o.ks) v *= o.ks[k];
+  return v;
+}
+
+enum ZOp {
+  Z_QR_W = 0,    // Wb = V_p^T X(j0:, j0+pb:)
+  Z_QR_W2,       // W2 = T_p^T Wb
+  Z_QR_UPD,      // X(j0:, j0+pb:) -= V_p W2
+  Z_Q_W,         // Wb = V_p^T U(j0:, j0:)        (forming Q, backward)
+  Z_Q_W2,        // W2 = T_p Wb
+  Z_Q_UPD,       // U(j0:, j0:) -= V_p W2
+  Z_F,           // F = D^-1 R P^T F_prev
+  Z_GA,          // M = Dlmax^-1 U_L^T U_R Drmax^-1
+  Z_GB,          // M += Dlmin F_L F_R^T Drmin
+  Z_AQ_W,        // Wb = V_p^T Y(j0:, :)
+  Z_AQ_W2,       // W2 = T_p^T Wb
+  Z_AQ_UPD,      // Y(j0:, :) -= V_p W2
+  Z_TR_UPD,      // Y(j0:j0+pb, :) -= R(j0:j0+pb, j0+pb:) Y(j0+pb:, :)
+  Z_GG,          // G = U_R Drmax^-1 X
+};
+
+__device__ bool zjob(const WalkerDev& w, int op, int mode, int j, int p, int sp, ZJob& jb) {
+  if (j >= w.nstack) return false;
+  const int N = w.N;
+  const long long NN = (long long)N * N;
+  const ZScr z = zscr(w, sp);
+  const int j0 = p * TB;
+  const int m = N - j0, pb = min(TB, m);
+  jb = ZJob{};
+  jb.alpha = 1.0;
+  const bool panel_op = op != Z_F && op != Z_GA && op != Z_GB && op != Z_GG;
+  if (panel_op && j0 >= N) return false;
+  const ZOpnd Vp{z.X + (long long)j0 * N + j0, N, 0, 1, nullptr, nullptr};
+  ZOpnd VpT = Vp;
+  VpT.tr = 1;
+  const ZOpnd Tp{z.Tb + (long long)p * TB * TB, TB, 0, 2, nullptr, nullptr};
+  ZOpnd TpT = Tp;
+  TpT.tr = 1;
+  int nl = 0, nr = 0;
+  zstack_tops(w, mode, j, nl, nr);
+  const int side = (mode == MODE_FWD) ? 0 : 1;
+  switch (op) {
+    case Z_QR_W:
+    case Z_QR_W2:
+    case Z_QR_UPD: {
+      const int nt = m - pb;
+      if (nt <= 0) return false;
+      if (op == Z_QR_W) {
+        jb.a = VpT;
+        jb.b = ZOpnd{z.X + (long long)(j0 + pb) * N + j0, N, 0, 0, nullptr, nullptr};
+        jb.c = z.Wb; jb.ldc = TB; jb.M = pb; jb.N = nt; jb.K = m;
+      } else if (op == Z_QR_W2) {
+        jb.a = TpT;
+        jb.b = ZOpnd{z.Wb, TB, 0, 0, nullptr, nullptr};
+        jb.c = z.W2; jb.ldc = TB; jb.M = pb; jb.N = nt; jb.K = pb;
+      } else {
+        jb.a = Vp;
+        jb.b = ZOpnd{z.W2, TB, 0, 0, nullptr, nullptr};
+        jb.c = z.X + (long long)(j0 + pb) * N + j0; jb.ldc = N; jb.M = m; jb.N = nt; jb.K = pb;
+        jb.beta = 1; jb.alpha = -1.0;
+      }
+      return true;
+    }
+    case Z_Q_W:
+    case Z_Q_W2:
+    case Z_Q_UPD: {
+      double* Uo = stack_level(w, side, sp, j);
+      if (op == Z_Q_W) {
+        jb.a = VpT;
+        jb.b = ZOpnd{Uo + (long long)j0 * N + j0, N, 0, 0, nullptr, nullptr};
+        jb.c = z.Wb; jb.ldc = TB; jb.M = pb; jb.N = m; jb.K = m;
+      } else if (op == Z_Q_W2) {
+        jb.a = Tp;
+        jb.b = ZOpnd{z.Wb, TB, 0, 0, nullptr, nullptr};
+        jb.c = z.W2; jb.ldc = TB; jb.M = pb; jb.N = m; jb.K = pb;
+      } else {
+        jb.a = Vp;
+        jb.b = ZOpnd{z.W2, TB, 0, 0, nullptr, nullptr};
+        jb.c = Uo + (long long)j0 * N + j0; jb.ldc = N; jb.M = m; jb.N = m; jb.K = pb;
+        jb.beta = 1; jb.alpha = -1.0;
+      }
+      return true;
+    }
+    case Z_F: {
+      if (j == 0) return false;
+      double* lv = stack_level(w, side, sp, j);
+      const double* fp = stack_level(w, side, sp, j - 1) + NN;
+      jb.a = ZOpnd{z.X, N, 0, 2, nullptr, nullptr};
+      jb.b = ZOpnd{fp, N, 0, 0, z.perm, nullptr};
+      jb.rs = z.invd;
+      jb.c = lv + NN; jb.ldc = N; jb.M = N; jb.N = N; jb.K = N;
+      return true;
+    }
+    case Z_GA:
+    case Z_GB:
+    case Z_GG: {
+      if (!(nl > 0 && nr > 0)) return false;
+      const double* UL = stack_level(w, 0, sp, nl - 1);
+      const double* UR = stack_level(w, 1, sp, nr - 1);
+      if (op == Z_GA) {
+        jb.a = ZOpnd{UL, N, 1, 0, nullptr, nullptr};
+        jb.b = ZOpnd{UR, N, 0, 0, nullptr, nullptr};
+        jb.rs = z.dlmaxi; jb.cs = z.drmaxi;
+        jb.c = z.X; jb.ldc = N; jb.M = N; jb.N = N; jb.K = N;
+      } else if (op == Z_GB) {
+        jb.a = ZOpnd{UL + NN, N, 0, 0, nullptr, nullptr};
+        jb.b = ZOpnd{UR + NN, N, 1, 0, nullptr, nullptr};
+        jb.rs = z.dlmin; jb.cs = z.drmin;
+        jb.c = z.X; jb.ldc = N; jb.M = N; jb.N = N; jb.K = N; jb.beta = 1;
+      } else {
+        jb.a = ZOpnd{UR, N, 0, 0, nullptr, z.drmaxi};
+        jb.b = ZOpnd{z.Y, N, 0, 0, nullptr, nullptr};
+        jb.c = w.G + sp * NN; jb.ldc = N; jb.M = N; jb.N = N; jb.K = N; jb.out = 1;
+      }
+      return true;
+    }
+    case Z_AQ_W:
+    case Z_AQ_W2:
+    case Z_AQ_UPD: {
+      if (op == Z_AQ_W) {
+        jb.a = VpT;
+        jb.b = ZOpnd{z.Y + j0, N, 0, 0, nullptr, nullptr};
+        jb.c = z.Wb; jb.ldc = TB; jb.M = pb; jb.N = N; jb.K = m;
+      } else if (op == Z_AQ_W2) {
+        jb.a = TpT;
+        jb.b = ZOpnd{z.Wb, TB, 0, 0, nullptr, nullptr};
+        jb.c = z.W2; jb.ldc = TB; jb.M = pb; jb.N = N; jb.K = pb;
+      } else {
+        jb.a = Vp;
+        jb.b = ZOpnd{z.W2, TB, 0, 0, nullptr, nullptr};
+        jb.c = z.Y + j0; jb.ldc = N; jb.M = m; jb.N = N; jb.K = pb;
+        jb.beta = 1; jb.alpha = -1.0;
+      }
+      return true;
+    }
+    case Z_TR_UPD: {
+      if (j0 + pb >= N) return false;
+      jb.a = ZOpnd{z.X + (long long)(j0 + pb) * N + j0, N, 0, 0, nullptr, nullptr};
+      jb.b = ZOpnd{z.Y + j0 + pb, N, 0, 0, nullptr, nullptr};
+      jb.c = z.Y + j0; jb.ldc = N; jb.M = pb; jb.N = N; jb.K = N - j0 - pb;
+      jb.beta = 1; jb.alpha = -1.0;
+      return true;
+    }
+  }
+  return false;
+}
+
+// fixed-point magnitude |x| / 2^e with Q fraction bits (e >= exp_bound(x), Q <= 62)
+__device__ __forceinline__ unsigned long long zfixed(double x, int e, int Q, bool& neg) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  neg = (b >> 63) != 0;
+  const int ex = (int)((b >> 52) & 0x7ff);
+  if (ex == 0) return 0ULL;
+  const unsigned long long mant = (b & 0xFFFFFFFFFFFFFULL) | 0x10000000000000ULL;
+  const int s = ex - 1075 - e + Q;  // |x| 2^{Q-e} = mant 2^s
+  if (s >= 0) return mant << s;     // s <= Q - 53 here
+  if (s <= -64) return 0ULL;
+  return mant >> (-s);
+}
+__device__ __forceinline__ unsigned zslice2(unsigned long long q0, bool n0, unsigned long long q1, bool n1, int i,
+                                            int Bb, int Q) {
+  const int sh = Q - Bb * (i + 1);
+  const unsigned m = (1u << Bb) - 1;
+  const unsigned v0 = (unsigned)((q0 >> sh) & m), v1 = (unsigned)((q1 >> sh) & m);
+  const float f0 = n0 ? -(float)v0 : (float)v0, f1 = n1 ? -(float)v1 : (float)v1;
+  return (__float_as_uint(f0) >> 16) | (__float_as_uint(f1) & 0xFFFF0000u);
+}
+
+}  // namespace
+
+// --------------------------------------------------------------------------
+// Batched product C (op)= alpha rs (A B) cs, 64 x 64 tile per CTA, operands
+// sliced in the kernel (S slices of B bits, fraction Q = S B), BF16 MMA.
+// --------------------------------------------------------------------------
+template <int S, int B>
+__global__ void __launch_bounds__(256) zgemm_kernel(const WalkerDev* __restrict__ W, int op, int mode, int j, int p,
+                                                    int trace_slot) {
+  const int wi = blockIdx.z >> 1, sp = blockIdx.z & 1;
+  const WalkerDev& w = W[wi];
+  if (!w.ozstab || sp >= w.S) return;
+  ZJob jb;
+  if (!zjob(w, op, mode, j, p, sp, jb)) return;
+  if ((jb.K <= 256) != (B == 7)) return;
+  const int r0 = blockIdx.y * ZT, c0 = blockIdx.x * ZT;
+  if (r0 >= jb.M || c0 >= jb.N) return;
+  constexpr int Q = S * B;
+  extern __shared__ __align__(16) unsigned short zsm[];
+  unsigned short* sa = zsm;                 // [S][64][ZKP]
+  unsigned short* sb = zsm + S * ZT * ZKP;  // [S][64][ZKP]
+  __shared__ int eA[ZT], eB[ZT];
+  __shared__ int etmp[2][4][ZT];
+  const int tid = threadIdx.x, ll = tid & 63, part = tid >> 6;
+  const int lane = tid & 31, wid = tid >> 5;
+  const int wm = wid >> 2, wn = wid & 3, g = lane >> 2, t4 = lane & 3;
+  {
+    int ea = -1100, eb = -1100;
+    const int r = r0 + ll, c = c0 + ll;
+    for (int k = part; k < jb.K; k += 4) {
+      if (r < jb.M) ea = max(ea, ozaki::exp_bound(zel(jb.a, r, k, false)));
+      if (c < jb.N) eb = max(eb, ozaki::exp_bound(zel(jb.b, c, k, true)));
+    }
+    etmp[0][part][ll] = ea;
+    etmp[1][part][ll] = eb;
+  }
+  __syncthreads();
+  if (tid < 128) {
+    const int o = tid >> 6, l = tid & 63;
+    const int e = max(max(etmp[o][0][l], etmp[o][1][l]), max(etmp[o][2][l], etmp[o][3][l]));
+    (o ? eB : eA)[l] = e;
+  }
+  __syncthreads();
+
+  float acc[S][2][2][4];
+#pragma unroll
+  for (int m = 0; m < S; ++m)
+#pragma unroll
+    for (int a = 0; a < 2; ++a)
+#pragma unroll
+      for (int b = 0; b < 2; ++b)
+#pragma unroll
+        for (int v = 0; v < 4; ++v) acc[m][a][b][v] = 0.f;
+
+  for (int k0 = 0; k0 < jb.K; k0 += ZK) {
+#pragma unroll
+    for (int opd = 0; opd < 2; ++opd) {
+      const int line = (opd ? c0 : r0) + ll;
+      const bool ok = line < (opd ? jb.N : jb.M);
+      const int e = (opd ? eB : eA)[ll];
+      unsigned pk[S][4];
+#pragma unroll
+      for (int u = 0; u < 8; u += 2) {
+        const int k = k0 + part * 8 + u;
+        const double x0 = (ok && k < jb.K) ? zel(opd ? jb.b : jb.a, line, k, opd == 1) : 0.0;
+        const double x1 = (ok && k + 1 < jb.K) ? zel(opd ? jb.b : jb.a, line, k + 1, opd == 1) : 0.0;
+        bool n0, n1;
+        const unsigned long long q0 = zfixed(x0, e, Q, n0), q1 = zfixed(x1, e, Q, n1);
+#pragma unroll
+        for (int s = 0; s < S; ++s) pk[s][u >> 1] = zslice2(q0, n0, q1, n1, s, B, Q);
+      }
+      unsigned short* dst = opd ? sb : sa;
+#pragma unroll
+      for (int s = 0; s < S; ++s)
+        *reinterpret_cast<uint4*>(dst + (s * ZT + ll) * ZKP + part * 8) =
+            make_uint4(pk[s][0], pk[s][1], pk[s][2], pk[s][3]);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < ZK; kk += 16) {
+#pragma unroll
+      for (int i = 0; i < S; ++i) {
+        unsigned a[2][4];
+#pragma unroll
+        for (int mt = 0; mt < 2; ++mt) {
+          const unsigned short* pa = sa + (i * ZT + wm * 32 + mt * 16 + g) * ZKP + kk + 2 * t4;
+          a[mt][0] = *(const unsigned*)(pa);
+          a[mt][1] = *(const unsigned*)(pa + 8 * ZKP);
+          a[mt][2] = *(const unsigned*)(pa + 8);
+          a[mt][3] = *(const unsigned*)(pa + 8 * ZKP + 8);
+        }
+#pragma unroll
+        for (int jj = 0; jj < S - i; ++jj) {
+          unsigned bf[2][2];
+#pragma unroll
+          for (int nt = 0; nt < 2; ++nt) {
+            const unsigned short* pb2 = sb + (jj * ZT + wn * 16 + nt * 8 + g) * ZKP + kk + 2 * t4;
+            bf[nt][0] = *(const unsigned*)(pb2);
+            bf[nt][1] = *(const unsigned*)(pb2 + 8);
+          }
+#pragma unroll
+          for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+            for (int nt = 0; nt < 2; ++nt)
+              ozaki::mma16816(acc[i + jj][mt][nt], a[mt][0], a[mt][1], a[mt][2], a[mt][3], bf[nt][0], bf[nt][1]);
+        }
+      }
+    }
+    __syncthreads();
+  }
+
+  // epilogue: C = 2^{ea+eb} sum_m 2^{-B(m+2)} S_m, the groups summed exactly in two 64-bit halves
+  const long long NN = (long long)w.N * w.N;
+  double err = 0.0;
+  bool finite = true;
+  double* tr = (jb.out && w.trace && trace_slot >= 0 && trace_slot < w.trace_cap)
+                   ? w.trace + ((long long)trace_slot * 2 + sp) * NN : nullptr;
+  const bool check = jb.out && !(mode == MODE_INIT || (mode == MODE_BWD && j == w.nstack - 1));
+#pragma unroll
+  for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+    for (int nt = 0; nt < 2; ++nt)
+#pragma unroll
+      for (int v = 0; v < 4; ++v) {
+        const int rl = wm * 32 + mt * 16 + g + ((v >> 1) << 3), cl = wn * 16 + nt * 8 + 2 * t4 + (v & 1);
+        const int r = r0 + rl, c = c0 + cl;
+        if (r >= jb.M || c >= jb.N) continue;
+        long long hi = 0, lo = 0;
+#pragma unroll
+        for (int m = 0; m < 4; ++m) hi = (hi << B) + (long long)__float2int_rn(acc[m][mt][nt][v]);
+#pragma unroll
+        for (int m = 4; m < S; ++m) lo = (lo << B) + (long long)__float2int_rn(acc[m][mt][nt][v]);
+        const int e = eA[rl] + eB[cl];
+        double val = ozaki::ldexp_i64(hi, e - 5 * B) + ozaki::ldexp_i64(lo, e - B * (S + 1));
+        if (jb.rs) val *= jb.rs[r];
+        if (jb.cs) val *= jb.cs[c];
+        const long long o = (long long)c * jb.ldc + r;
+        if (!jb.out) {
+          val *= jb.alpha;
+          jb.c[o] = jb.beta ? jb.c[o] + val : val;
+        } else {
+          if (check) err = fmax(err, fabs(val - jb.c[o]));
+          if (!isfinite(val)) finite = false;
+          jb.c[o] = val;
+          if (tr) tr[o] = val;
+          if (w.S == 1) {
+            jb.c[NN + o] = val;
+            if (tr) tr[NN + o] = val;
+          }
+        }
+      }
+  if (jb.out) {
+    if (!finite) atomicOr(w.status, ST_NONFINITE_G);
+    if (check) {
+      for (int o = 16; o > 0; o >>= 1) err = fmax(err, __shfl_xor_sync(0xffffffffu, err, o));
+      if (lane == 0) atomicMax(w.wrap_bits, (unsigned long long)__double_as_longlong(err));
+    }
+  }
+}
+
+// --------------------------------------------------------------------------
+// Push preparation: column norms of the chain, order by decreasing norm
+// (ties by index), X = chain(:, perm).  One CTA per (walker, spin).
+// --------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) zpush_prep_kernel(const WalkerDev* __restrict__ W, int mode, int j) {
+  const int wi = blockIdx.x >> 1, sp = blockIdx.x & 1;
+  const WalkerDev& w = W[wi];
+  if (!w.ozstab || sp >= w.S || j >= w.nstack) return;
+  const int N = w.N;
+  int nsl;
+  {
+    const int k = (mode == MODE_FWD) ? j : (w.nstack - 1 - j);
+    nsl = min((k + 1) * w.pace, w.Lt) - k * w.pace;
+  }
+  const long long NN = (long long)N * N;
+  const double* Cin = w.chain + (long long)((w.cb ? 0 : (nsl & 1)) * w.S + sp) * NN;
+  const ZScr z = zscr(w, sp);
+  extern __shared__ long long zkey[];  // [N] norm bit patterns
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for (int c = wid; c < N; c += 8) {
+    double s = 0.0;
+    for (int r = lane; r < N; r += 32) {
+      const double a = Cin[(long long)c * N + r];
+      s = fma(a, a, s);
+    }
+    s = zwarp_sum(s);
+    if (lane == 0) zkey[c] = __double_as_longlong(sqrt(s));  // >= 0 (or NaN): bit order = value order
+  }
+  for (int k = threadIdx.x; k < N; k += 256) z.perm[k] = k;
+  __syncthreads();
+  for (int c = threadIdx.x; c < N; c += 256) {
+    const long long kc = zkey[c];
+    int rank = 0;
+    for (int c2 = 0; c2 < N; ++c2) {
+      const long long k2 = zkey[c2];
+      rank += (k2 > kc || (k2 == kc && c2 < c)) ? 1 : 0;
+    }
+    z.perm[rank] = c;
+  }
+  __syncthreads();
+  for (int k = wid; k < N; k += 8) {
+    const int c = z.perm[k];
+    for (int r = lane; r < N; r += 32) z.X[(long long)k * N + r] = Cin[(long long)c * N + r];
+  }
+}
+
+// --------------------------------------------------------------------------
+// Householder panel p of X (rows j0:N, columns j0:j0+pb) in shared memory:
+// reflectors into X below the diagonal, R on and above, T_p (dlarft) into the
+// scratch; for the push also D = |diag R| into the stack level and 1/D.
+// --------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) zqr_panel_kernel(const WalkerDev* __restrict__ W, int mode, int j, int p,
+                                                        int push) {
+  const int wi = blockIdx.x >> 1, sp = blockIdx.x & 1;
+  const WalkerDev& w = W[wi];
+  if (!w.ozstab || sp >= w.S || j >= w.nstack) return;
+  const int N = w.N, j0 = p * TB;
+  if (j0 >= N) return;
+  const int m = N - j0, pb = min(TB, m);
+  const ZScr z = zscr(w, sp);
+  extern __shared__ double psm[];
+  double* P = psm;                // [TB][m], P[c * m + r]
+  double* T = P + TB * m;         // [TB][TB], T[c * TB + r]
+  double* Z = T + TB * TB;        // [TB][TB] Gram V^T V
+  __shared__ double s_red[8];
+  __shared__ double s_tau, s_scal;
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  for (int c = 0; c < pb; ++c)
+    for (int r = tid; r < m; r += 256) P[c * m + r] = z.X[(long long)(j0 + c) * N + j0 + r];
+  __syncthreads();
+  for (int c = 0; c < pb; ++c) {
+    double s = 0.0;
+    for (int r = c + 1 + tid; r < m; r += 256) s = fma(P[c * m + r], P[c * m + r], s);
+    s = zwarp_sum(s);
+    if (lane == 0) s_red[wid] = s;
+    __syncthreads();
+    if (tid == 0) {
+      double xn2 = 0.0;
+      for (int q = 0; q < 8; ++q) xn2 += s_red[q];
+      const double alpha = P[c * m + c];
+      double tau = 0.0, beta = alpha, scal = 1.0;
+      if (xn2 != 0.0) {
+        const double nrm = sqrt(alpha * alpha + xn2);
+        beta = alpha >= 0 ? -nrm : nrm;
+        tau = (beta - alpha) / beta;
+        scal = 1.0 / (alpha - beta);
+      }
+      s_tau = tau;
+      s_scal = scal;
+      P[c * m + c] = beta;
+      T[c * TB + c] = tau;
+    }
+    __syncthreads();
+    const double scal = s_scal, tau = s_tau;
+    for (int r = c + 1 + tid; r < m; r += 256) P[c * m + r] *= scal;
+    __syncthreads();
+    if (tau != 0.0)
+      for (int cc = c + 1 + wid; cc < pb; cc += 8) {
+        double d = 0.0;
+        for (int r = c + 1 + lane; r < m; r += 32) d = fma(P[c * m + r], P[cc * m + r], d);
+        d = zwarp_sum(d) + P[cc * m + c];
+        const double wv = tau * d;
+        if (lane == 0) P[cc * m + c] -= wv;
+        for (int r = c + 1 + lane; r < m; r += 32) P[cc * m + r] = fma(-wv, P[c * m + r], P[cc * m + r]);
+      }
+    __syncthreads();
+  }
+  // Gram Z(i, c) = v_i^T v_c for i < c (unit diagonal, zeros above)
+  for (int pr = wid; pr < pb * pb; pr += 8) {
+    const int i = pr / pb, c = pr % pb;
+    if (i >= c) continue;
+    double d = 0.0;
+    for (int r = c + 1 + lane; r < m; r += 32) d = fma(P[i * m + r], P[c * m + r], d);
+    d = zwarp_sum(d);
+    if (lane == 0) Z[c * TB + i] = d + P[i * m + c];
+  }
+  __syncthreads();
+  // T(0:c, c) = -tau_c T(0:c, 0:c) Z(0:c, c)
+  for (int c = 1; c < pb; ++c) {
+    if (tid < c) {
+      double s = 0.0;
+      for (int k = tid; k < c; ++k) s = fma(T[k * TB + tid], Z[c * TB + k], s);
+      T[c * TB + tid] = -T[c * TB + c] * s;
+    }
+    __syncthreads();
+  }
+  for (int c = 0; c < pb; ++c)
+    for (int r = tid; r < m; r += 256) z.X[(long long)(j0 + c) * N + j0 + r] = P[c * m + r];
+  double* Tg = z.Tb + (long long)p * TB * TB;
+  for (int e = tid; e < TB * TB; e += 256) {
+    const int r = e % TB, c = e / TB;
+    Tg[e] = (r <= c && c < pb) ? T[c * TB + r] : 0.0;
+  }
+  if (push && tid < pb) {
+    const int side = (mode == MODE_FWD) ? 0 : 1;
+    double* Do = stack_level(w, side, sp, j) + 2 * (long long)N * N;
+    const double d = fabs(P[tid * m + tid]);
+    Do[j0 + tid] = d;
+    z.invd[j0 + tid] = (d != 0.0) ? 1.0 / d : 0.0;
+    if (d == 0.0 || !isfinite(d)) atomicOr(w.status, ST_SINGULAR);
+  }
+}
+
+// U = I before forming Q; at the first level F = D^-1 R P^T directly
+__global__ void __launch_bounds__(256) zpush_fin_kernel(const WalkerDev* __restrict__ W, int mode, int j) {
+  const int wi = blockIdx.y >> 1, sp = blockIdx.y & 1;
+  const WalkerDev& w = W[wi];
+  if (!w.ozstab || sp >= w.S || j >= w.nstack) return;
+  const int N = w.N;
+  const long long NN = (long long)N * N;
+  const int side = (mode == MODE_FWD) ? 0 : 1;
+  double* Uo = stack_level(w, side, sp, j);
+  double* Fo = Uo + NN;
+  const ZScr z = zscr(w, sp);
+  for (long long e = blockIdx.x * 256LL + threadIdx.x; e < NN; e += (long long)gridDim.x * 256) {
+    const int r = (int)(e % N), c = (int)(e / N);
+    Uo[e] = (r == c) ? 1.0 : 0.0;
+    if (j == 0) Fo[(long long)z.perm[c] * N + r] = (r <= c) ? z.X[e] * z.invd[r] : 0.0;
+  }
+}
+
+// --------------------------------------------------------------------------
+// Green's preparation: scale vectors; Y = Dmax^-1 U^T (col-major); boundary
+// steps also M = Y + Dmin F.  Grid over the N^2 elements.
+// --------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) zgreens_prep_kernel(const WalkerDev* __restrict__ W, int mode, int j) {
+  const int wi = blockIdx.y >> 1, sp = blockIdx.y & 1;
+  const WalkerDev& w = W[wi];
+  if (!w.ozstab || sp >= w.S || j >= w.nstack) return;
+  const int N = w.N;
+  const long long NN = (long long)N * N;
+  int nl, nr;
+  zstack_tops(w, mode, j, nl, nr);
+  const ZScr z = zscr(w, sp);
+  const bool both = nl > 0 && nr > 0;
+  const double* lv = (nl > 0) ? stack_level(w, 0, sp, nl - 1) : stack_level(w, 1, sp, nr - 1);
+  const double* U = lv;
+  const double* F = lv + NN;
+  const double* D = lv + 2 * NN;
+  if (blockIdx.x == 0 && both) {
+    const double* DR = stack_level(w, 1, sp, nr - 1) + 2 * NN;
+    for (int k = threadIdx.x; k < N; k += 256) {
+      z.dlmaxi[k] = 1.0 / fmax(D[k], 1.0);
+      z.dlmin[k] = fmin(D[k], 1.0);
+      z.drmaxi[k] = 1.0 / fmax(DR[k], 1.0);
+      z.drmin[k] = fmin(DR[k], 1.0);
+    }
+  }
+  for (long long e = blockIdx.x * 256LL + threadIdx.x; e < NN; e += (long long)gridDim.x * 256) {
+    const int r = (int)(e % N), c = (int)(e / N);
+    const double dr = D[r];
+    const double y = U[(long long)r * N + c] / fmax(dr, 1.0);  // (Dmax^-1 U^T)(r, c)
+    z.Y[e] = y;
+    if (!both) z.X[e] = y + fmin(dr, 1.0) * F[e];
+  }
+}
+
+// back substitution of the diagonal block p: R_pp X(j0:j0+pb, c) = Y(j0:j0+pb, c), thread per column
+__global__ void __launch_bounds__(128) ztrsm_diag_kernel(const WalkerDev* __restrict__ W, int mode, int j, int p) {
+  const int wi = blockIdx.y >> 1, sp = blockIdx.y & 1;
+  const WalkerDev& w = W[wi];
+  if (!w.ozstab || sp >= w.S || j >= w.nstack) return;
+  const int N = w.N, j0 = p * TB;
+  if (j0 >= N) return;
+  const int pb = min(TB, N - j0);
+  const ZScr z = zscr(w, sp);
+  __shared__ double R[TB][TB + 1];
+  __shared__ double rinv[TB];
+  for (int e = threadIdx.x; e < TB * TB; e += 128) {
+    const int i = e % TB, k = e / TB;
+    R[i][k] = (i < pb && k < pb && i <= k) ? z.X[(long long)(j0 + k) * N + j0 + i] : 0.0;
+  }
+  __syncthreads();
+  if (threadIdx.x < TB) {  // rows past a partial panel: 0 (their x stays 0)
+    const double d = R[threadIdx.x][threadIdx.x];
+    rinv[threadIdx.x] = (d != 0.0) ? 1.0 / d : 0.0;
+    if (d == 0.0 && threadIdx.x < pb && blockIdx.x == 0) atomicOr(w.status, ST_SINGULAR);
+  }
+  __syncthreads();
+  const int c = blockIdx.x * 128 + threadIdx.x;
+  if (c >= N) return;
+  double* y = z.Y + (long long)c * N + j0;
+  double x[TB];
+#pragma unroll
+  for (int i = 0; i < TB; ++i) x[i] = (i < pb) ? y[i] : 0.0;
+#pragma unroll
+  for (int i = TB - 1; i >= 0; --i) {
+    double s = x[i];
+#pragma unroll
+    for (int k = i + 1; k < TB; ++k) s = fma(-R[i][k], x[k], s);
+    x[i] = s * rinv[i];
+  }
+#pragma unroll
+  for (int i = 0; i < TB; ++i)
+    if (i < pb) y[i] = x[i];
+}
+
+// boundary steps: G = X (left stack present) or X^T (right only), wrap error, trace
+__global__ void __launch_bounds__(256) zgreens_out_kernel(const WalkerDev* __restrict__ W, int mode, int j,
+                                                          int trace_slot) {
+  const int wi = blockIdx.y >> 1, sp = blockIdx.y & 1;
+  const WalkerDev& w = W[wi];
+  if (!w.ozstab || sp >= w.S || j >= w.nstack) return;
+  int nl, nr;
+  zstack_tops(w, mode, j, nl, nr);
+  if (nl > 0 && nr > 0) return;
+  const int N = w.N;
+  const long long NN = (long long)N * N;
+  const ZScr z = zscr(w, sp);
+  double* G = w.G + sp * NN;
+  double* tr = (w.trace && trace_slot >= 0 && trace_slot < w.trace_cap) ? w.trace + ((long long)trace_slot * 2 + sp) * NN
+                                                                       : nullptr;
+  const bool transpose_out = (nl == 0);
+  const bool check = !(mode == MODE_INIT || (mode == MODE_BWD && j == w.nstack - 1));
+  double err = 0.0;
+  bool finite = true;
+  for (long long e = blockIdx.x * 256LL + threadIdx.x; e < NN; e += (long long)gridDim.x * 256) {
+    const int r = (int)(e % N), c = (int)(e / N);
+    const double v = transpose_out ? z.Y[(long long)r * N + c] : z.Y[e];
+    if (check) err = fmax(err, fabs(v - G[e]));
+    if (!isfinite(v)) finite = false;
+    G[e] = v;
+    if (tr) tr[e] = v;
+    if (w.S == 1) {
+      G[NN + e] = v;
+      if (tr) tr[NN + e] = v;
+    }
+  }
+  if (!finite) atomicOr(w.status, ST_NONFINITE_G);
+  if (check) {
+    for (int o = 16; o > 0; o >>= 1) err = fmax(err, __shfl_xor_sync(0xffffffffu, err, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(w.wrap_bits, (unsigned long long)__double_as_longlong(err));
+  }
+}
+
+// --------------------------------------------------------------------------
+// host side
+// --------------------------------------------------------------------------
+static size_t zgemm_smem(int S) { return 2ull * S * ZT * ZKP * sizeof(unsigned short); }
+static size_t zpanel_smem(int maxN) { return sizeof(double) * ((size_t)TB * maxN + 2 * TB * TB); }
+
+cudaError_t configure_stab_oz_kernels(int maxN) {
+  cudaError_t e;
+  if ((e = cudaFuncSetAttribute(zgemm_kernel<8, 7>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)zgemm_smem(8))))
+    return e;
+  if ((e = cudaFuncSetAttribute(zgemm_kernel<9, 6>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)zgemm_smem(9))))
+    return e;
+  if ((e = cudaFuncSetAttribute(zqr_panel_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)zpanel_smem(maxN > 0 ? maxN : 1))))
+    return e;
+  return cudaSuccess;
+}
+
+static void zgemm(const WalkerDev* W, int nw, int maxN, int op, int mode, int j, int p, int rows_max, int cols_max,
+                  int trace_slot, cudaStream_t st) {
+  const dim3 g((cols_max + ZT - 1) / ZT, (rows_max + ZT - 1) / ZT, 2 * nw);
+  zgemm_kernel<8, 7><<<g, 256, zgemm_smem(8), st>>>(W, op, mode, j, p, trace_slot);
+  if (maxN > 256) zgemm_kernel<9, 6><<<g, 256, zgemm_smem(9), st>>>(W, op, mode, j, p, trace_slot);
+}
+
+void oz_push(int mode, const WalkerDev* W, int nw, int j, int maxN, cudaStream_t st) {
+  const int np = (maxN + TB - 1) / TB;
+  zpush_prep_kernel<<<2 * nw, 256, sizeof(long long) * maxN, st>>>(W, mode, j);
+  for (int p = 0; p < np; ++p) {
+    zqr_panel_kernel<<<2 * nw, 256, zpanel_smem(maxN), st>>>(W, mode, j, p, 1);
+    zgemm(W, nw, maxN, Z_QR_W, mode, j, p, TB, maxN, -1, st);
+    zgemm(W, nw, maxN, Z_QR_W2, mode, j, p, TB, maxN, -1, st);
+    zgemm(W, nw, maxN, Z_QR_UPD, mode, j, p, maxN, maxN, -1, st);
+  }
+  zpush_fin_kernel<<<dim3(64, 2 * nw), 256, 0, st>>>(W, mode, j);
+  zgemm(W, nw, maxN, Z_F, mode, j, 0, maxN, maxN, -1, st);
+  for (int p = np - 1; p >= 0; --p) {
+    zgemm(W, nw, maxN, Z_Q_W, mode, j, p, TB, maxN, -1, st);
+    zgemm(W, nw, maxN, Z_Q_W2, mode, j, p, TB, maxN, -1, st);
+    zgemm(W, nw, maxN, Z_Q_UPD, mode, j, p, maxN, maxN, -1, st);
+  }
+}
+
+void oz_greens(int mode, const WalkerDev* W, int nw, int j, int trace_slot, int maxN, cudaStream_t st) {
+  const int np = (maxN + TB - 1) / TB;
+  zgreens_prep_kernel<<<dim3(64, 2 * nw), 256, 0, st>>>(W, mode, j);
+  zgemm(W, nw, maxN, Z_GA, mode, j, 0, maxN, maxN, -1, st);
+  zgemm(W, nw, maxN, Z_GB, mode, j, 0, maxN, maxN, -1, st);
+  for (int p = 0; p < np; ++p) {
+    zqr_panel_kernel<<<2 * nw, 256, zpanel_smem(maxN), st>>>(W, mode, j, p, 0);
+    zgemm(W, nw, maxN, Z_QR_W, mode, j, p, TB, maxN, -1, st);
+    zgemm(W, nw, maxN, Z_QR_W2, mode, j, p, TB, maxN, -1, st);
+    zgemm(W, nw, maxN, Z_QR_UPD, mode, j, p, maxN, maxN, -1, st);
+    zgemm(W, nw, maxN, Z_AQ_W, mode, j, p, TB, maxN, -1, st);
+    zgemm(W, nw, maxN, Z_AQ_W2, mode, j, p, TB, maxN, -1, st);
+    zgemm(W, nw, maxN, Z_AQ_UPD, mode, j, p, maxN, maxN, -1, st);
+  }
+  for (int p = np - 1; p >= 0; --p) {
+    zgemm(W, nw, maxN, Z_TR_UPD, mode, j, p, TB, maxN, -1, st);
+    ztrsm_diag_kernel<<<dim3((maxN + 127) / 128, 2 * nw), 128, 0, st>>>(W, mode, j, p);
+  }
+  zgemm(W, nw, maxN, Z_GG, mode, j, 0, maxN, maxN, trace_slot, st);
+  zgreens_out_kernel<<<dim3(64, 2 * nw), 256, 0, st>>>(W, mode, j, trace_slot);
+}
+
+}  // namespace dqmc

@@ -63,6 +63,29 @@ __device__ __forceinline__ double scale2(double x, int e) {
   return x * __longlong_as_double((long long)(e + 1023) << 52);
 }
 
+// ---- epilogue: recombining the S weight groups with integer operations -----
+// GB300 issues FP64 at 1/64 of its FP32 rate, so the epilogue avoids FP64
+// arithmetic: each group sum is an integer-valued FP32 number, the groups are
+// added as one 64-bit integer v = sum_m S_m 2^{B(S-1-m)} (|v| < 2^61 for the
+// configurations above), and v 2^e is assembled as IEEE-754 bits (truncated
+// to 53 bits, below the kept precision).
+
+// exact value of an integer-valued float with |x| < 2^22 (FP32 add + integer subtract)
+__device__ __forceinline__ int f2i_small(float x) { return __float_as_int(x + 12582912.0f) - 0x4B400000; }
+
+// v * 2^e as a double, built from the bits (0 below the normal range)
+__device__ __forceinline__ double ldexp_i64(long long v, int e) {
+  if (v == 0) return 0.0;
+  const unsigned long long sgn = (unsigned long long)v & 0x8000000000000000ULL;
+  unsigned long long a = sgn ? (0ULL - (unsigned long long)v) : (unsigned long long)v;
+  const int p = 63 - __clzll((long long)a);  // index of the leading one
+  a = (p >= 52) ? (a >> (p - 52)) : (a << (52 - p));
+  const int ex = p + e + 1023;
+  if (ex <= 0) return 0.0;
+  if (ex >= 2047) return __longlong_as_double((long long)(sgn | 0x7FF0000000000000ULL));
+  return __longlong_as_double((long long)(sgn | ((unsigned long long)ex << 52) | (a & 0xFFFFFFFFFFFFFULL)));
+}
+
 // one BF16 tensor-core MMA m16n8k16, FP32 accumulate in place
 __device__ __forceinline__ void mma16816(float (&c)[4], unsigned a0, unsigned a1, unsigned a2, unsigned a3,
                                          unsigned b0, unsigned b1) {

@@ -59,6 +59,8 @@ def _run(dq, descs, precision, sweeps=1):
     (1, 8, 4.0, -0.5, 4.0, 40, 8),     # attractive, the mixed configuration's model on 8x8
     (0, 6, 4.0, 0.0, 4.0, 80, 10),     # repulsive
     (1, 16, 4.0, -0.5, 2.0, 20, 8),    # 16x16
+    (0, 12, 4.0, 0.0, 2.0, 20, 5),     # repulsive N = 144: tensor-core QR, two spins, partial panel
+    (1, 12, 3.0, -0.3, 2.0, 20, 10),   # attractive N = 144
 ])
 def test_mixed_sweep_dG_against_fp64(dq, model, L, U, mu, beta, Lt, pace):
     descs = [dq.WalkerDesc(model=model, L=L, U=U, mu=mu, beta=beta, Lt=Lt, pace=pace, seed=100 + w) for w in range(2)]
