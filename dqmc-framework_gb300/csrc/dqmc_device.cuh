@@ -28,6 +28,7 @@ enum : int {
   ST_NONFINITE_G = 1,
   ST_SINGULAR = 2,
   ST_NONFINITE_RATIO = 4,
+  ST_TIMEOUT = 8,  // a bounded device-side wait gave up (the kernel skipped its output)
 };
 
 struct WalkerDev {

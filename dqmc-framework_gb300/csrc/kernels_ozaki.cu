@@ -2,9 +2,10 @@
 // (42-bit) matrix products on the BF16 tensor cores (see ozaki.cuh).
 //
 // Slicing is integer work on the FP64 bit patterns; the product runs the
-// S(S+1)/2 slice pairs on mma.sync BF16 with FP32 accumulation (exact by
-// construction), one accumulator per weight group, and recombines the groups
-// in the epilogue.  Used for the wraps and the B-chain (the reference's
+// S(S+1)/2 slice pairs on the BF16 tensor cores (tcgen05, TMEM accumulators;
+// the stand-alone product of the test hook uses mma.sync) with FP32
+// accumulation, exact by construction, one accumulator per weight group, and
+// recombines the groups in the epilogue.  Used for the wraps and the B-chain (the reference's
 // mult_B_from_left/right, mult_invB_*, mult_transB_from_left,
 // src/model/repulsive_hubbard.cpp:158-243, src/model/model_base.cpp:7-35).
 #include <cuda_bf16.h>
@@ -15,6 +16,7 @@
 
 #include "dqmc_device.cuh"
 #include "ozaki.cuh"
+#include "tcgen05.cuh"
 
 namespace dqmc {
 
@@ -268,20 +270,28 @@ __global__ void __launch_bounds__(256) oz_slice_kernel(const WalkerDev* __restri
   slice_lines(job, N, w.ldk, role, w.slice_bits, w.slices, blockIdx.x * 32);
 }
 
-// product of op OP: grid (ceil(N/64), ceil(N/64), 2*nw), 256 threads
+// Product of op OP on the 5th-generation tensor cores: a 128 x 64 output
+// tile per CTA with the S weight groups accumulated in TMEM (S x 64 columns).
+// The pre-sliced operands stream 32 k at a time through two shared stages
+// (cp.async, 16-byte pieces placed as K-major core matrices); one thread
+// issues the S (S+1) / 2 x 2 MMAs of a chunk and commits them to the stage's
+// mbarrier, so the copies of chunk c+1 overlap the MMAs of chunk c.
 template <int OP, int S>
-__global__ void __launch_bounds__(256) oz_prod_kernel(const WalkerDev* __restrict__ W, int mode, int j, int q) {
+__global__ void __launch_bounds__(256, 1) oz_prod_tc_kernel(const WalkerDev* __restrict__ W, int mode, int j,
+                                                            int q) {
+  constexpr int MT = 128, NT = 64, KC = 32, CM = 128, RG = (KC / 8) * CM;
+  constexpr int A_SL = MT * KC * 2, B_SL = NT * KC * 2, STAGE = S * (A_SL + B_SL);
+  constexpr unsigned TCOLS = (S * NT <= 256) ? 256u : 512u;
   const int wi = blockIdx.z >> 1, sp = blockIdx.z & 1;
   const WalkerDev& w = W[wi];
   if (w.path != 2 || w.cb || sp >= w.S || w.slices != S) return;
   int t;
   if (!oz_slice_of(w, mode, j, q, t)) return;
-  const int N = w.N;
-  const int r0 = blockIdx.y * 64, c0 = blockIdx.x * 64;
+  const int N = w.N, ldk = w.ldk;
+  const int r0 = blockIdx.y * MT, c0 = blockIdx.x * NT;
   if (r0 >= N || c0 >= N) return;
   const long long NN = (long long)N * N;
-  extern __shared__ unsigned short ozsm[];
-  const unsigned short* ws = w.sl + (long long)sp * w.slices * N * w.ldk;
+  const unsigned short* ws = w.sl + (long long)sp * w.slices * N * ldk;
   const int* we = w.sle + (long long)sp * N;
   ProdJob job{};
   double* out = nullptr;
@@ -293,11 +303,107 @@ __global__ void __launch_bounds__(256) oz_prod_kernel(const WalkerDev* __restric
     case OZ_WR_BWD: job = ProdJob{ws, w.kB, we, w.kBe}; out = w.work + sp * NN; break;
     case OZ_WL_BWD: job = ProdJob{w.iA, ws, w.iAe, we}; out = w.G + sp * NN; break;
   }
-  ozaki_product_tile<S>(job, N, w.ldk, w.slice_bits, r0, c0, ozsm, [&](int r, int c, double v) {
-    if (OP == OZ_WL_FWD || OP == OZ_CH_FWD) v *= oz_bscale(w, t, sp, +1, r);
-    if (OP == OZ_WR_FWD) v *= oz_bscale(w, t, sp, -1, c);
-    out[(long long)c * N + r] = v;
-  });
+  extern __shared__ __align__(1024) unsigned char tsm[];
+  __shared__ int eA[MT], eB[NT];
+  __shared__ __align__(8) unsigned long long mbar[2];
+  __shared__ unsigned tbase;
+  __shared__ int s_fail;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  if (tid < MT) eA[tid] = (r0 + tid < N) ? job.ea[r0 + tid] : -1100;
+  if (tid < NT) eB[tid] = (c0 + tid < N) ? job.eb[c0 + tid] : -1100;
+  if (tid == 0) {
+    s_fail = 0;
+    tc::mbar_init(&mbar[0]);
+    tc::mbar_init(&mbar[1]);
+    tc::mbar_fence_init();
+  }
+  if (warp == 0) tc::alloc(&tbase, TCOLS);
+  tc::fence_before();
+  __syncthreads();
+  tc::fence_after();
+  const unsigned taddr = tbase;
+  constexpr uint32_t idesc = tc::idesc_bf16(MT, NT);
+  const int nch = (ldk + KC - 1) / KC;
+  auto load = [&](int c, int st) {
+    unsigned char* sA = tsm + st * STAGE;
+    unsigned char* sB = sA + S * A_SL;
+    const int k0 = c * KC;
+    for (int gi = tid; gi < S * (MT + NT) * (KC / 8); gi += 256) {
+      const bool isA = gi < S * MT * (KC / 8);
+      const int g2 = isA ? gi : gi - S * MT * (KC / 8);
+      const int nl = isA ? MT : NT;
+      const int line = g2 % nl, rest = g2 / nl, kq = rest % (KC / 8), s = rest / (KC / 8);
+      const int gl = (isA ? r0 : c0) + line, k = k0 + kq * 8;
+      const unsigned short* src = (isA ? job.A : job.B) + ((long long)s * N + min(gl, N - 1)) * ldk + min(k, ldk - 8);
+      unsigned char* dst = (isA ? sA + s * A_SL : sB + s * B_SL) + (line & 7) * 16 + kq * CM + (line >> 3) * RG;
+      cp_async16(dst, src, gl < N && k < ldk);
+    }
+    cp_async_commit();
+  };
+  load(0, 0);
+  for (int c = 0; c < nch; ++c) {
+    const int st = c & 1;
+    if (c + 1 < nch) {
+      if (c >= 1 && !tc::mbar_wait(&mbar[(c + 1) & 1], ((c - 1) >> 1) & 1)) s_fail = 1;
+      load(c + 1, (c + 1) & 1);
+      asm volatile("cp.async.wait_group 1;\n" ::: "memory");
+    } else {
+      asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+    }
+    tc::fence_proxy_async();
+    __syncthreads();
+    if (tid == 0) {
+      tc::fence_after();
+      const unsigned char* sA = tsm + st * STAGE;
+      const unsigned char* sB = sA + S * A_SL;
+#pragma unroll
+      for (int kk = 0; kk < KC / 16; ++kk) {
+#pragma unroll
+        for (int i = 0; i < S; ++i) {
+          const uint64_t ad = tc::desc(tc::su32(sA + i * A_SL) + kk * 2 * CM, CM, RG);
+#pragma unroll
+          for (int jj = 0; jj < S - i; ++jj) {
+            const uint64_t bd = tc::desc(tc::su32(sB + jj * B_SL) + kk * 2 * CM, CM, RG);
+            tc::mma(taddr + (unsigned)((i + jj) * NT), ad, bd, idesc, c > 0 || kk > 0 || i > 0);
+          }
+        }
+      }
+      tc::commit(&mbar[st]);
+    }
+  }
+  if (!tc::mbar_wait(&mbar[(nch - 1) & 1], ((nch - 1) >> 1) & 1)) s_fail = 1;
+  tc::fence_after();
+  __syncthreads();
+  const int bits = w.slice_bits;
+  const int q4 = warp & 3, half = warp >> 2;
+  const int rl = q4 * 32 + lane, r = r0 + rl;
+  if (!s_fail) {
+    for (int cc = half * (NT / 2); cc < (half + 1) * (NT / 2); cc += 16) {
+      uint32_t v[S][16];
+#pragma unroll
+      for (int m = 0; m < S; ++m) tc::ld16(v[m], taddr + ((unsigned)(q4 * 32) << 16) + (unsigned)(m * NT + cc));
+      tc::wait_ld();
+      if (r < N) {
+#pragma unroll
+        for (int u = 0; u < 16; ++u) {
+          const int cl = cc + u, col = c0 + cl;
+          if (col >= N) continue;
+          long long sv = 0;
+#pragma unroll
+          for (int m = 0; m < S; ++m) sv = (sv << bits) + (long long)__float2int_rn(__uint_as_float(v[m][u]));
+          double val = ozaki::ldexp_i64(sv, eA[rl] + eB[cl] - bits * (S + 1));
+          if (OP == OZ_WL_FWD || OP == OZ_CH_FWD) val *= oz_bscale(w, t, sp, +1, r);
+          if (OP == OZ_WR_FWD) val *= oz_bscale(w, t, sp, -1, col);
+          out[(long long)col * N + r] = val;
+        }
+      }
+    }
+  } else if (tid == 0) {
+    atomicOr(w.status, ST_TIMEOUT);
+  }
+  tc::fence_before();
+  __syncthreads();
+  if (warp == 0) tc::dealloc(taddr, TCOLS);
 }
 
 // constant operands (exp(-dtau K), exp(+dtau K)), sliced once per batch
@@ -319,27 +425,29 @@ __global__ void __launch_bounds__(256) oz_selftest_prod_kernel(const unsigned sh
   else ozaki_product_tile<7>(job, N, ldk, bits, r0, c0, ozsm, epi);
 }
 
+static size_t oz_tc_smem(int S) { return 2ull * S * (128 + 64) * 32 * 2; }
 size_t oz_prod_smem(int S) { return sizeof(unsigned short) * 2 * 2 * S * 64 * kOzRow; }
 
 cudaError_t configure_ozaki_kernels() {
   cudaError_t e;
-#define OZCFG(...) if ((e = cudaFuncSetAttribute(__VA_ARGS__, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)oz_prod_smem(7)))) return e
-  OZCFG(oz_prod_kernel<OZ_WL_FWD, 6>); OZCFG(oz_prod_kernel<OZ_WR_FWD, 6>); OZCFG(oz_prod_kernel<OZ_CH_FWD, 6>);
-  OZCFG(oz_prod_kernel<OZ_CH_BWD, 6>); OZCFG(oz_prod_kernel<OZ_WR_BWD, 6>); OZCFG(oz_prod_kernel<OZ_WL_BWD, 6>);
-  OZCFG(oz_prod_kernel<OZ_WL_FWD, 7>); OZCFG(oz_prod_kernel<OZ_WR_FWD, 7>); OZCFG(oz_prod_kernel<OZ_CH_FWD, 7>);
-  OZCFG(oz_prod_kernel<OZ_CH_BWD, 7>); OZCFG(oz_prod_kernel<OZ_WR_BWD, 7>); OZCFG(oz_prod_kernel<OZ_WL_BWD, 7>);
-  OZCFG(oz_selftest_prod_kernel);
+#define OZCFG(...) if ((e = cudaFuncSetAttribute(__VA_ARGS__, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)oz_tc_smem(7)))) return e
+  OZCFG(oz_prod_tc_kernel<OZ_WL_FWD, 6>); OZCFG(oz_prod_tc_kernel<OZ_WR_FWD, 6>); OZCFG(oz_prod_tc_kernel<OZ_CH_FWD, 6>);
+  OZCFG(oz_prod_tc_kernel<OZ_CH_BWD, 6>); OZCFG(oz_prod_tc_kernel<OZ_WR_BWD, 6>); OZCFG(oz_prod_tc_kernel<OZ_WL_BWD, 6>);
+  OZCFG(oz_prod_tc_kernel<OZ_WL_FWD, 7>); OZCFG(oz_prod_tc_kernel<OZ_WR_FWD, 7>); OZCFG(oz_prod_tc_kernel<OZ_CH_FWD, 7>);
+  OZCFG(oz_prod_tc_kernel<OZ_CH_BWD, 7>); OZCFG(oz_prod_tc_kernel<OZ_WR_BWD, 7>); OZCFG(oz_prod_tc_kernel<OZ_WL_BWD, 7>);
 #undef OZCFG
+  if ((e = cudaFuncSetAttribute(oz_selftest_prod_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)oz_prod_smem(7))))
+    return e;
   return cudaSuccess;
 }
 
 template <int OP>
 static void oz_op(const WalkerDev* W, int nw, int maxN, int mode, int j, int q, cudaStream_t st) {
   oz_slice_kernel<OP><<<dim3((maxN + 31) / 32, 2 * nw), 256, 0, st>>>(W, mode, j, q);
-  const int t = (maxN + 63) / 64;
-  const dim3 g(t, t, 2 * nw);
-  oz_prod_kernel<OP, 6><<<g, 256, oz_prod_smem(6), st>>>(W, mode, j, q);
-  if (maxN > 256) oz_prod_kernel<OP, 7><<<g, 256, oz_prod_smem(7), st>>>(W, mode, j, q);
+  const dim3 g((maxN + 63) / 64, (maxN + 127) / 128, 2 * nw);
+  oz_prod_tc_kernel<OP, 6><<<g, 256, oz_tc_smem(6), st>>>(W, mode, j, q);
+  if (maxN > 256) oz_prod_tc_kernel<OP, 7><<<g, 256, oz_tc_smem(7), st>>>(W, mode, j, q);
 }
 
 // the slice work of mixed walkers (wraps and chain through the tensor cores)

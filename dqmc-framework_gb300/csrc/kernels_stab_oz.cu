@@ -25,10 +25,12 @@
 // mathematically; the UDT factors differ only in the column order of the QR.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdint>
 
 #include "dqmc_device.cuh"
 #include "ozaki.cuh"
+#include "tcgen05.cuh"
 
 namespace dqmc {
 
@@ -52,10 +54,11 @@ __device__ __forceinline__ void zstack_tops(const WalkerDev& w, int mode, int j,
 
 // per-spin scratch: scr = X (matrix being factored) | Y (right-hand sides);
 // work = Wb [TB N] | W2 [TB N] | T factors [ceil(N/TB) TB TB] | invd | four
-// diagonal scale vectors | perm: 2 TB N + TB (N + TB) + 5.5 N <= N^2 for N >= 110
+// diagonal scale vectors | perm | line exponents of the two operands of the
+// current product: 2 TB N + TB (N + TB) + 6.5 N <= N^2 for N >= 110
 struct ZScr {
   double *X, *Y, *Wb, *W2, *Tb, *invd, *dlmaxi, *drmaxi, *dlmin, *drmin;
-  int* perm;
+  int *perm, *expA, *expB;
 };
 __device__ __forceinline__ ZScr zscr(const WalkerDev& w, int sp) {
   const long long NN = (long long)w.N * w.N;
@@ -74,6 +77,8 @@ __device__ __forceinline__ ZScr zscr(const WalkerDev& w, int sp) {
   z.dlmin = z.drmaxi + w.N;
   z.drmin = z.dlmin + w.N;
   z.perm = reinterpret_cast<int*>(z.drmin + w.N);
+  z.expA = z.perm + w.N;
+  z.expB = z.expA + w.N;
   return z;
 }
 
@@ -305,9 +310,20 @@ __global__ void __launch_bounds__(256) zgemm_kernel(const WalkerDev* __restrict_
   {
     int ea = -1100, eb = -1100;
     const int r = r0 + ll, c = c0 + ll;
-    for (int k = part; k < jb.K; k += 4) {
-      if (r < jb.M) ea = max(ea, ozaki::exp_bound(zel(jb.a, r, k, false)));
-      if (c < jb.N) eb = max(eb, ozaki::exp_bound(zel(jb.b, c, k, true)));
+    // 8 independent loads per operand in flight per step
+    for (int k0 = part * 8; k0 < jb.K; k0 += 32) {
+      double xa[8], xb[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int k = k0 + u;
+        xa[u] = (r < jb.M && k < jb.K) ? zel(jb.a, r, k, false) : 0.0;
+        xb[u] = (c < jb.N && k < jb.K) ? zel(jb.b, c, k, true) : 0.0;
+      }
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        ea = max(ea, ozaki::exp_bound(xa[u]));
+        eb = max(eb, ozaki::exp_bound(xb[u]));
+      }
     }
     etmp[0][part][ll] = ea;
     etmp[1][part][ll] = eb;
@@ -434,6 +450,217 @@ __global__ void __launch_bounds__(256) zgemm_kernel(const WalkerDev* __restrict_
       if (lane == 0) atomicMax(w.wrap_bits, (unsigned long long)__double_as_longlong(err));
     }
   }
+}
+
+
+// --------------------------------------------------------------------------
+// Line exponents of both operands of a product (one pass over the operands,
+// shared by all output tiles): blockIdx.y = 0 rows of op(A), 1 columns of
+// op(B); 32 lines x 8 k groups per CTA.
+// --------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) zexp_kernel(const WalkerDev* __restrict__ W, int op, int mode, int j, int p) {
+  const int wi = blockIdx.z >> 1, sp = blockIdx.z & 1;
+  const WalkerDev& w = W[wi];
+  if (!w.ozstab || sp >= w.S) return;
+  ZJob jb;
+  if (!zjob(w, op, mode, j, p, sp, jb)) return;
+  const bool isB = blockIdx.y == 1;
+  const ZOpnd& o = isB ? jb.b : jb.a;
+  const int nlines = isB ? jb.N : jb.M;
+  const int l0 = blockIdx.x * 32;
+  if (l0 >= nlines) return;
+  // lines contiguous in memory when the stored row index runs along the line
+  const bool line_fast = (o.tr != (int)isB) ? false : true;
+  const int ll = line_fast ? (threadIdx.x & 31) : (threadIdx.x >> 3);
+  const int kg = line_fast ? (threadIdx.x >> 5) : (threadIdx.x & 7);
+  const int line = l0 + ll;
+  int e = -1100;
+  if (line < nlines)
+    for (int k0 = kg; k0 < jb.K; k0 += 64) {
+      double x[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int k = k0 + 8 * u;
+        x[u] = (k < jb.K) ? zel(o, line, k, isB) : 0.0;
+      }
+#pragma unroll
+      for (int u = 0; u < 8; ++u) e = max(e, ozaki::exp_bound(x[u]));
+    }
+  __shared__ int s_e[8][32];
+  s_e[kg][ll] = e;
+  __syncthreads();
+  if (threadIdx.x < 32 && l0 + threadIdx.x < nlines) {
+    int m = s_e[0][threadIdx.x];
+#pragma unroll
+    for (int q = 1; q < 8; ++q) m = max(m, s_e[q][threadIdx.x]);
+    const ZScr z = zscr(w, sp);
+    (isB ? z.expB : z.expA)[l0 + threadIdx.x] = m;
+  }
+}
+
+// --------------------------------------------------------------------------
+// The same product on the 5th-generation tensor cores (tcgen05): a 128 x NT
+// output tile per CTA, the S weight groups accumulated in TMEM (S NT columns).
+// Per 32-deep k chunk, all 256 threads slice both operands into one shared
+// stage (K-major, 8-row x 16-byte core matrices, no swizzle) while the MMAs
+// of the previous chunk run from the other stage; one thread issues the
+// S (S+1) / 2 x 2 MMAs of a chunk and commits them to the stage's mbarrier.
+// --------------------------------------------------------------------------
+template <int S, int B, int NT>
+__global__ void __launch_bounds__(256, 1) zgemm_tc_kernel(const WalkerDev* __restrict__ W, int op, int mode, int j,
+                                                          int p, int trace_slot) {
+  constexpr int MT = 128, KC = 32;
+  constexpr int Q = S * B;
+  constexpr int CM = 128;                 // bytes of one core matrix (8 rows x 16 bytes)
+  constexpr int RG = (KC / 8) * CM;       // bytes between 8-row groups
+  constexpr int A_SL = MT * KC * 2, B_SL = NT * KC * 2;
+  constexpr int STAGE = S * (A_SL + B_SL);
+  constexpr unsigned TCOLS = (S * NT <= 256) ? 256u : 512u;
+  const int wi = blockIdx.z >> 1, sp = blockIdx.z & 1;
+  const WalkerDev& w = W[wi];
+  if (!w.ozstab || sp >= w.S) return;
+  ZJob jb;
+  if (!zjob(w, op, mode, j, p, sp, jb)) return;
+  if ((jb.K <= 256) != (B == 7)) return;
+  const int r0 = blockIdx.y * MT, c0 = blockIdx.x * NT;
+  if (r0 >= jb.M || c0 >= jb.N) return;
+  extern __shared__ __align__(1024) unsigned char tsm[];
+  __shared__ int eA[MT], eB[NT];
+  __shared__ __align__(8) unsigned long long mbar[2];
+  __shared__ unsigned tbase;
+  __shared__ int s_fail;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const ZScr z = zscr(w, sp);
+  if (tid < MT) eA[tid] = (r0 + tid < jb.M) ? z.expA[r0 + tid] : -1100;
+  if (tid < NT) eB[tid] = (c0 + tid < jb.N) ? z.expB[c0 + tid] : -1100;
+  if (tid == 0) {
+    s_fail = 0;
+    tc::mbar_init(&mbar[0]);
+    tc::mbar_init(&mbar[1]);
+    tc::mbar_fence_init();
+  }
+  if (warp == 0) tc::alloc(&tbase, TCOLS);
+  tc::fence_before();
+  __syncthreads();
+  tc::fence_after();
+  const unsigned taddr = tbase;
+  constexpr uint32_t idesc = tc::idesc_bf16(MT, NT);
+  const int nch = (jb.K + KC - 1) / KC;
+
+  for (int c = 0; c < nch; ++c) {
+    const int st = c & 1;
+    unsigned char* sA = tsm + st * STAGE;
+    unsigned char* sB = sA + S * A_SL;
+    if (c >= 2 && !tc::mbar_wait(&mbar[st], ((c - 2) >> 1) & 1)) s_fail = 1;
+    const int k0 = c * KC;
+    // each thread slices groups of 8 consecutive k of one line (lines fastest: coalesced)
+#pragma unroll
+    for (int opd = 0; opd < 2; ++opd) {
+      const int nl = opd ? NT : MT;
+      unsigned char* base = opd ? sB : sA;
+      for (int gi = tid; gi < nl * (KC / 8); gi += 256) {
+        const int line = gi % nl, kl = (gi / nl) * 8;
+        const int gline = (opd ? c0 : r0) + line;
+        const bool ok = gline < (opd ? jb.N : jb.M);
+        const int e = (opd ? eB : eA)[line];
+        unsigned pk[S][4];
+#pragma unroll
+        for (int u = 0; u < 8; u += 2) {
+          const int k = k0 + kl + u;
+          const double x0 = (ok && k < jb.K) ? zel(opd ? jb.b : jb.a, gline, k, opd == 1) : 0.0;
+          const double x1 = (ok && k + 1 < jb.K) ? zel(opd ? jb.b : jb.a, gline, k + 1, opd == 1) : 0.0;
+          bool n0, n1;
+          const unsigned long long q0 = zfixed(x0, e, Q, n0), q1 = zfixed(x1, e, Q, n1);
+#pragma unroll
+          for (int s2 = 0; s2 < S; ++s2) pk[s2][u >> 1] = zslice2(q0, n0, q1, n1, s2, B, Q);
+        }
+        const int off = (line & 7) * 16 + (kl >> 3) * CM + (line >> 3) * RG;
+#pragma unroll
+        for (int s2 = 0; s2 < S; ++s2)
+          *reinterpret_cast<uint4*>(base + s2 * (opd ? B_SL : A_SL) + off) =
+              make_uint4(pk[s2][0], pk[s2][1], pk[s2][2], pk[s2][3]);
+      }
+    }
+    tc::fence_proxy_async();
+    __syncthreads();
+    if (tid == 0) {
+      tc::fence_after();
+#pragma unroll
+      for (int kk = 0; kk < KC / 16; ++kk) {
+#pragma unroll
+        for (int i = 0; i < S; ++i) {
+          const uint64_t ad = tc::desc(tc::su32(sA + i * A_SL) + kk * 2 * CM, CM, RG);
+#pragma unroll
+          for (int jj = 0; jj < S - i; ++jj) {
+            const uint64_t bd = tc::desc(tc::su32(sB + jj * B_SL) + kk * 2 * CM, CM, RG);
+            tc::mma(taddr + (unsigned)((i + jj) * NT), ad, bd, idesc, c > 0 || kk > 0 || i > 0);
+          }
+        }
+      }
+      tc::commit(&mbar[st]);
+    }
+  }
+  if (!tc::mbar_wait(&mbar[(nch - 1) & 1], ((nch - 1) >> 1) & 1)) s_fail = 1;
+  tc::fence_after();
+  __syncthreads();
+
+  // epilogue: warp w reads TMEM lanes 32 (w & 3) .. + 31 (rows), column half (w >> 2)
+  const long long NN = (long long)w.N * w.N;
+  double err = 0.0;
+  bool finite = true;
+  double* tr = (jb.out && w.trace && trace_slot >= 0 && trace_slot < w.trace_cap)
+                   ? w.trace + ((long long)trace_slot * 2 + sp) * NN : nullptr;
+  const bool check = jb.out && !(mode == MODE_INIT || (mode == MODE_BWD && j == w.nstack - 1));
+  const int q4 = warp & 3, half = warp >> 2;
+  const int rl = q4 * 32 + lane, r = r0 + rl;
+  if (!s_fail) {
+    for (int cc = half * (NT / 2); cc < (half + 1) * (NT / 2); cc += 16) {
+      uint32_t v[S][16];
+#pragma unroll
+      for (int m = 0; m < S; ++m) tc::ld16(v[m], taddr + ((unsigned)(q4 * 32) << 16) + (unsigned)(m * NT + cc));
+      tc::wait_ld();
+#pragma unroll
+      for (int u = 0; u < 16; ++u) {
+        const int cl = cc + u, col = c0 + cl;
+        if (r >= jb.M || col >= jb.N) continue;
+        long long hi = 0, lo = 0;
+#pragma unroll
+        for (int m = 0; m < 4; ++m) hi = (hi << B) + (long long)__float2int_rn(__uint_as_float(v[m][u]));
+#pragma unroll
+        for (int m = 4; m < S; ++m) lo = (lo << B) + (long long)__float2int_rn(__uint_as_float(v[m][u]));
+        const int e = eA[rl] + eB[cl];
+        double val = ozaki::ldexp_i64(hi, e - 5 * B) + ozaki::ldexp_i64(lo, e - B * (S + 1));
+        if (jb.rs) val *= jb.rs[r];
+        if (jb.cs) val *= jb.cs[col];
+        const long long o = (long long)col * jb.ldc + r;
+        if (!jb.out) {
+          val *= jb.alpha;
+          jb.c[o] = jb.beta ? jb.c[o] + val : val;
+        } else {
+          if (check) err = fmax(err, fabs(val - jb.c[o]));
+          if (!isfinite(val)) finite = false;
+          jb.c[o] = val;
+          if (tr) tr[o] = val;
+          if (w.S == 1) {
+            jb.c[NN + o] = val;
+            if (tr) tr[NN + o] = val;
+          }
+        }
+      }
+    }
+  } else if (tid == 0) {
+    atomicOr(w.status, ST_TIMEOUT);
+  }
+  if (jb.out) {
+    if (!finite) atomicOr(w.status, ST_NONFINITE_G);
+    if (check) {
+      for (int o = 16; o > 0; o >>= 1) err = fmax(err, __shfl_xor_sync(0xffffffffu, err, o));
+      if (lane == 0) atomicMax(w.wrap_bits, (unsigned long long)__double_as_longlong(err));
+    }
+  }
+  tc::fence_before();
+  __syncthreads();
+  if (warp == 0) tc::dealloc(taddr, TCOLS);
 }
 
 // --------------------------------------------------------------------------
@@ -715,10 +942,17 @@ __global__ void __launch_bounds__(256) zgreens_out_kernel(const WalkerDev* __res
 // host side
 // --------------------------------------------------------------------------
 static size_t zgemm_smem(int S) { return 2ull * S * ZT * ZKP * sizeof(unsigned short); }
+static size_t ztc_smem(int S, int NT) { return 2ull * S * (128 + NT) * 32 * 2; }
 static size_t zpanel_smem(int maxN) { return sizeof(double) * ((size_t)TB * maxN + 2 * TB * TB); }
 
 cudaError_t configure_stab_oz_kernels(int maxN) {
   cudaError_t e;
+  if ((e = cudaFuncSetAttribute(zgemm_tc_kernel<8, 7, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)ztc_smem(8, 64))))
+    return e;
+  if ((e = cudaFuncSetAttribute(zgemm_tc_kernel<9, 6, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)ztc_smem(9, 32))))
+    return e;
   if ((e = cudaFuncSetAttribute(zgemm_kernel<8, 7>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)zgemm_smem(8))))
     return e;
   if ((e = cudaFuncSetAttribute(zgemm_kernel<9, 6>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)zgemm_smem(9))))
@@ -731,9 +965,13 @@ cudaError_t configure_stab_oz_kernels(int maxN) {
 
 static void zgemm(const WalkerDev* W, int nw, int maxN, int op, int mode, int j, int p, int rows_max, int cols_max,
                   int trace_slot, cudaStream_t st) {
-  const dim3 g((cols_max + ZT - 1) / ZT, (rows_max + ZT - 1) / ZT, 2 * nw);
-  zgemm_kernel<8, 7><<<g, 256, zgemm_smem(8), st>>>(W, op, mode, j, p, trace_slot);
-  if (maxN > 256) zgemm_kernel<9, 6><<<g, 256, zgemm_smem(9), st>>>(W, op, mode, j, p, trace_slot);
+  zexp_kernel<<<dim3((std::max(rows_max, cols_max) + 31) / 32, 2, 2 * nw), 256, 0, st>>>(W, op, mode, j, p);
+  const dim3 g8((cols_max + 63) / 64, (rows_max + 127) / 128, 2 * nw);
+  zgemm_tc_kernel<8, 7, 64><<<g8, 256, ztc_smem(8, 64), st>>>(W, op, mode, j, p, trace_slot);
+  if (maxN > 256) {
+    const dim3 g9((cols_max + 31) / 32, (rows_max + 127) / 128, 2 * nw);
+    zgemm_tc_kernel<9, 6, 32><<<g9, 256, ztc_smem(9, 32), st>>>(W, op, mode, j, p, trace_slot);
+  }
 }
 
 void oz_push(int mode, const WalkerDev* W, int nw, int j, int maxN, cudaStream_t st) {

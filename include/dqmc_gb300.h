@@ -139,6 +139,9 @@ int dqmc_get_green(dqmc_batch* b, int walker, int spin, double* out);
 int dqmc_get_config_sign(dqmc_batch* b, int walker, double* out);
 int dqmc_get_wrap_error(dqmc_batch* b, int walker, double* out);
 int dqmc_get_accept_count(dqmc_batch* b, int walker, int64_t* out);
+/* Per-walker status word, 0 when healthy; bits: 1 non-finite G, 2 zero pivot
+ * in a factorization, 4 non-finite Metropolis ratio, 8 a bounded device-side
+ * wait gave up (that kernel skipped its output). */
 int dqmc_get_status(dqmc_batch* b, int walker, int* out);
 
 /* Equal-time accumulators of a walker: sums[k] = sum over measured slices of
