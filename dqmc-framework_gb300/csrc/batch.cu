@@ -48,6 +48,10 @@ void launch_metropolis_sub(const WalkerDev* W, int nw, int mode, int j, int q, i
 int delayed_pick_kd(int N, int S);
 void general_chain_init(int mode, const WalkerDev* W, int nw, int j, cudaStream_t st);
 void general_push(int mode, const WalkerDev* W, int nw, int j, int maxN, cudaStream_t st);
+void general_dynamic_slice(const WalkerDev* W, int nw, int j, int q, int maxN, bool mixed, cudaStream_t st);
+void general_dynamic_stab(const WalkerDev* W, int nw, int j, int maxN, cudaStream_t st);
+void general_dynamic_begin(const WalkerDev* W, int nw, cudaStream_t st);
+void general_dynamic_end(const WalkerDev* W, int nw, cudaStream_t st);
 void oz_push(int mode, const WalkerDev* W, int nw, int j, int maxN, cudaStream_t st);
 void oz_greens(int mode, const WalkerDev* W, int nw, int j, int trace_slot, int maxN, cudaStream_t st);
 cudaError_t configure_stab_oz_kernels(int maxN);
@@ -199,6 +203,11 @@ struct dqmc_batch {
   dqmc_batch_options opt{};
   std::vector<dqmc_walker_desc> desc;
   std::vector<WalkerDev> hw;        // host copies of the descriptors
+  // dynamic half-sweep: buffers allocated on first use, the listed tau, stack position
+  char* dyn_arena = nullptr;
+  int* d_taus = nullptr;
+  std::vector<int> taus;
+  bool at_zero = false;  // stacks of t = 0 (after set-up or a backward half-sweep)
   WalkerDev* dW = nullptr;          // device descriptors
   char* arena = nullptr;
   size_t arena_bytes = 0;
@@ -563,6 +572,7 @@ int dqmc_batch_destroy(dqmc_batch* b) {
       for (auto& m : v) { cudaEventDestroy(m.a); cudaEventDestroy(m.b); }
   if (b->h_uni) cudaFreeHost(b->h_uni);
   if (b->arena) cudaFree(b->arena);
+  if (b->dyn_arena) cudaFree(b->dyn_arena);
   if (b->own) cudaStreamDestroy(b->own);
   delete b;
   return DQMC_OK;
@@ -728,6 +738,7 @@ int dqmc_init_greens(dqmc_batch* b) {
   }
   CUDA_TRY(cudaStreamSynchronize(b->stream));
   b->initialised = true;
+  b->at_zero = true;
   b->trace_count = 0;
   if (b->any_general && (b->kd > 0 || b->mixed) && !b->tuned) {
     if (int r = autotune_delayed(b)) return r;
@@ -867,8 +878,136 @@ int dqmc_launch_count(dqmc_batch* b, int64_t* launches) {
   return DQMC_OK;
 }
 
-int dqmc_sweep_0_to_beta(dqmc_batch* b, int measure) { return half_sweep(b, MODE_FWD, measure); }
-int dqmc_sweep_beta_to_0(dqmc_batch* b, int measure) { return half_sweep(b, MODE_BWD, measure); }
+int dqmc_sweep_0_to_beta(dqmc_batch* b, int measure) {
+  const int r = half_sweep(b, MODE_FWD, measure);
+  if (r == DQMC_OK) b->at_zero = false;
+  return r;
+}
+int dqmc_sweep_beta_to_0(dqmc_batch* b, int measure) {
+  const int r = half_sweep(b, MODE_BWD, measure);
+  if (r == DQMC_OK) b->at_zero = true;
+  return r;
+}
+
+// ---- dynamic half-sweep ------------------------------------------------------------
+static constexpr int kMaxTau = 256;
+
+static int dyn_alloc(dqmc_batch* b) {
+  if (b->dyn_arena) return DQMC_OK;
+  size_t cur = 0;
+  auto take = [&](size_t bytes) { const size_t o = cur; cur = align256(cur + bytes); return o; };
+  const size_t taus_off = take(sizeof(int) * kMaxTau);
+  std::vector<size_t> off(b->nw * 6);
+  for (int w = 0; w < b->nw; ++w) {
+    const WalkerDev& h = b->hw[w];
+    const size_t NN = (size_t)h.N * h.N;
+    off[6 * w + 0] = take(sizeof(double) * 2 * h.S * NN);  // G(t,0)
+    off[6 * w + 1] = take(sizeof(double) * 2 * h.S * NN);  // G(0,t)
+    off[6 * w + 2] = take(sizeof(double) * h.S * NN);      // X1
+    off[6 * w + 3] = take(sizeof(int) * h.S * h.N);        // LU pivots
+    off[6 * w + 4] = take(sizeof(double) * kMaxTau);
+    off[6 * w + 5] = take(sizeof(long long) * kMaxTau);
+  }
+  cudaError_t e = cudaMalloc(&b->dyn_arena, cur);
+  if (e != cudaSuccess) {
+    b->dyn_arena = nullptr;
+    return fail(DQMC_ERR_CUDA, "dynamic buffers (%zu bytes): %s", cur, cudaGetErrorString(e));
+  }
+  CUDA_TRY(cudaMemsetAsync(b->dyn_arena, 0, cur, b->stream));
+  b->d_taus = reinterpret_cast<int*>(b->dyn_arena + taus_off);
+  for (int w = 0; w < b->nw; ++w) {
+    WalkerDev& h = b->hw[w];
+    h.gt0 = reinterpret_cast<double*>(b->dyn_arena + off[6 * w + 0]);
+    h.g0t = reinterpret_cast<double*>(b->dyn_arena + off[6 * w + 1]);
+    h.dynx = reinterpret_cast<double*>(b->dyn_arena + off[6 * w + 2]);
+    h.dpiv = reinterpret_cast<int*>(b->dyn_arena + off[6 * w + 3]);
+    h.dyn_sum = reinterpret_cast<double*>(b->dyn_arena + off[6 * w + 4]);
+    h.dyn_cnt = reinterpret_cast<long long*>(b->dyn_arena + off[6 * w + 5]);
+    h.dyn_taus = b->d_taus;
+    h.dyn_ntau = 0;
+  }
+  CUDA_TRY(cudaMemcpyAsync(b->dW, b->hw.data(), sizeof(WalkerDev) * b->nw, cudaMemcpyHostToDevice, b->stream));
+  return DQMC_OK;
+}
+
+int dqmc_clear_dynamic(dqmc_batch* b) {
+  if (!b) return fail(DQMC_ERR_ARG, "null batch");
+  if (!b->dyn_arena) return DQMC_OK;
+  for (int w = 0; w < b->nw; ++w) {
+    CUDA_TRY(cudaMemsetAsync(b->hw[w].dyn_sum, 0, sizeof(double) * kMaxTau, b->stream));
+    CUDA_TRY(cudaMemsetAsync(b->hw[w].dyn_cnt, 0, sizeof(long long) * kMaxTau, b->stream));
+  }
+  CUDA_TRY(cudaStreamSynchronize(b->stream));
+  return DQMC_OK;
+}
+
+int dqmc_sweep_dynamic(dqmc_batch* b, const int* taus, int ntau) {
+  if (!b) return fail(DQMC_ERR_ARG, "null batch");
+  if (!b->initialised) return fail(DQMC_ERR_STATE, "dynamic sweep before dqmc_init_greens");
+  if (!b->at_zero)
+    return fail(DQMC_ERR_STATE, "dynamic sweep needs the stacks of t = 0 (after set-up or a backward half-sweep)");
+  if (b->any_small)
+    return fail(DQMC_ERR_ARG, "dynamic sweep needs every walker on the HBM path (N > 64 or DQMC_MIXED)");
+  if (b->any_general_cb) return fail(DQMC_ERR_ARG, "dynamic sweep: checkerboard walkers are not supported");
+  if (ntau < 0 || ntau > kMaxTau || (ntau > 0 && !taus)) return fail(DQMC_ERR_ARG, "ntau must be in [0, 256]");
+  for (int k = 0; k < ntau; ++k)
+    for (int w = 0; w < b->nw; ++w)
+      if (taus[k] < 0 || taus[k] >= b->desc[w].Lt)
+        return fail(DQMC_ERR_ARG, "tau %d outside [0, Lt) of walker %d", taus[k], w);
+  if (int r = dyn_alloc(b)) return r;
+  const std::vector<int> tv(taus, taus + ntau);
+  if (tv != b->taus) {  // a new tau list restarts the accumulators
+    b->taus = tv;
+    if (ntau) CUDA_TRY(cudaMemcpyAsync(b->d_taus, b->taus.data(), sizeof(int) * ntau, cudaMemcpyHostToDevice, b->stream));
+    for (auto& h : b->hw) h.dyn_ntau = ntau;
+    if (int r = dqmc_clear_dynamic(b)) return r;
+  }
+  // the dynamic half-sweep stabilizes every walker with the FP64 kernels
+  std::vector<WalkerDev> hv = b->hw;
+  for (auto& h : hv) h.ozstab = 0;
+  CUDA_TRY(cudaMemcpyAsync(b->dW, hv.data(), sizeof(WalkerDev) * b->nw, cudaMemcpyHostToDevice, b->stream));
+  general_dynamic_begin(b->dW, b->nw, b->stream);
+  for (int j = 0; j < b->maxNs; ++j) {
+    general_chain_init(MODE_FWD, b->dW, b->nw, j, b->stream);
+    for (int q = 0; q < b->maxPace_general; ++q)
+      general_dynamic_slice(b->dW, b->nw, j, q, b->maxN_general, b->mixed, b->stream);
+    general_push(MODE_FWD, b->dW, b->nw, j, b->maxN_general, b->stream);
+    general_greens(MODE_FWD, b->dW, b->nw, j, -1, b->maxN_general, b->stream);
+    general_dynamic_stab(b->dW, b->nw, j, b->maxN_general, b->stream);
+  }
+  general_dynamic_end(b->dW, b->nw, b->stream);
+  CUDA_TRY(cudaMemcpyAsync(b->dW, b->hw.data(), sizeof(WalkerDev) * b->nw, cudaMemcpyHostToDevice, b->stream));
+  CUDA_TRY(cudaStreamSynchronize(b->stream));
+  if (int r = launch_check("dynamic sweep")) return r;
+  b->at_zero = false;
+  return DQMC_OK;
+}
+
+int dqmc_get_dynamic(dqmc_batch* b, int w, double* sums, int64_t* counts) {
+  if (int r = check_walker(b, w)) return r;
+  if (!b->dyn_arena || b->taus.empty()) return DQMC_OK;
+  const int n = (int)b->taus.size();
+  std::vector<long long> c(n);
+  if (sums) CUDA_TRY(cudaMemcpyAsync(sums, b->hw[w].dyn_sum, sizeof(double) * n, cudaMemcpyDeviceToHost, b->stream));
+  CUDA_TRY(cudaMemcpyAsync(c.data(), b->hw[w].dyn_cnt, sizeof(long long) * n, cudaMemcpyDeviceToHost, b->stream));
+  CUDA_TRY(cudaStreamSynchronize(b->stream));
+  if (counts)
+    for (int k = 0; k < n; ++k) counts[k] = c[k];
+  return DQMC_OK;
+}
+
+int dqmc_get_green_dynamic(dqmc_batch* b, int w, int which, int spin, double* out) {
+  if (int r = check_walker(b, w)) return r;
+  if (which < 0 || which > 1 || spin < 0 || spin > 1 || !out) return fail(DQMC_ERR_ARG, "bad which, spin or output");
+  if (!b->dyn_arena) return fail(DQMC_ERR_STATE, "no dynamic half-sweep has run");
+  const WalkerDev& h = b->hw[w];
+  const size_t NN = (size_t)h.N * h.N;
+  const int sp = spin < h.S ? spin : 0;
+  const double* src = (which == 0 ? h.gt0 : h.g0t) + ((size_t)(h.Lt & 1) * h.S + sp) * NN;
+  CUDA_TRY(cudaMemcpyAsync(out, src, sizeof(double) * NN, cudaMemcpyDeviceToHost, b->stream));
+  CUDA_TRY(cudaStreamSynchronize(b->stream));
+  return DQMC_OK;
+}
 
 int dqmc_get_green(dqmc_batch* b, int w, int spin, double* out) {
   if (int r = check_walker(b, w)) return r;

@@ -48,6 +48,18 @@ struct WalkerDev {
   // mixed walkers, submatrix Metropolis: per spin T [N][32] FP64, then the BF16
   // slices of T and of G0(:, accepted sites) [2][6][N][40] and their exponents [2][N]
   unsigned char* msub;
+  // time-displaced Green's functions (dynamic half-sweep), allocated on first use:
+  // G(t,0) and G(0,t) ping-pong [2][S][N*N], second right-hand side [S][N*N],
+  // LU pivots [S][N], G(k,tau) accumulators [dyn_ntau]
+  double* gt0;
+  double* g0t;
+  double* dynx;
+  int* dpiv;
+  double* dyn_sum;
+  long long* dyn_cnt;
+  const int* dyn_taus;
+  int dyn_ntau;
+  int pad2;
   // mixed walkers: BF16 slices of the operand being multiplied, [S][slices][N][ldk]
   unsigned short* sl;
   int* sle;                  // slice exponents [S][N]

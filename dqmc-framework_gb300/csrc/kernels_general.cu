@@ -72,6 +72,11 @@ enum GemmOp {
   OP_GA = 6,       // M  = Dlmax^-1 (U_L^T U_R) Drmax^-1
   OP_GB = 7,       // M += Dlmin (F_L F_R^T) Drmin
   OP_GG = 8,       // G  = (U_R Drmax^-1) X, wrap error, trace
+  // dynamic half-sweep (sweep_for_dynamic_greens, src/dqmc_walker.cpp:424-524)
+  OP_DT0 = 9,      // G(t,0) = diag(e+) expK G(t-1,0)          (mult_B_from_left)
+  OP_D0T = 10,     // G(0,t) = G(0,t-1) expK^-1 diag(e-)       (mult_invB_from_right)
+  OP_DT0_OUT = 11, // G(t,0) = (U_R Drmax^-1) X1, X1 = M^-1 Dlmin F_L; wrap error
+  OP_D0T_OUT = 12, // G(0,t) = -(F_R^T Drmin) X, X = M^-1 Dlmax^-1 U_L^T; wrap error
 };
 
 constexpr int kTile = 64, kTk = 16;
@@ -86,9 +91,12 @@ __global__ void __launch_bounds__(256) gemm_op_kernel(const WalkerDev* __restric
   const int r0 = blockIdx.y * kTile, c0 = blockIdx.x * kTile;
   if (r0 >= N || c0 >= N) return;
   int t = 0, nsl = 0, t_hi = 0;
-  const bool slice_op = OP <= OP_CH_BWD;
+  constexpr bool dyn_prop = OP == OP_DT0 || OP == OP_D0T;
+  constexpr bool dyn_out = OP == OP_DT0_OUT || OP == OP_D0T_OUT;
+  const bool slice_op = OP <= OP_CH_BWD || dyn_prop;
+  if ((dyn_prop || dyn_out) && !w.gt0) return;
   if (slice_op && w.cb) return;  // checkerboard walkers take cb_general_kernel (expK is null for them)
-  if (slice_op && w.path == 2) return;  // mixed walkers take the tensor-core products
+  if (slice_op && !dyn_prop && w.path == 2) return;  // mixed walkers take the tensor-core products
   if (slice_op && !slice_of(w, mode, j, q, t, nsl, t_hi)) return;
   if (!slice_op && j >= w.nstack) return;
   if (!slice_op && w.ozstab) return;  // stabilized by kernels_stab_oz.cu
@@ -112,6 +120,9 @@ __global__ void __launch_bounds__(256) gemm_op_kernel(const WalkerDev* __restric
   const double* DL = UL ? UL + 2 * NN : nullptr;
   const double* DR = UR ? UR + 2 * NN : nullptr;
   double* scr = w.scr + sp * 2 * NN;  // M (col-major), Y/X (row-major)
+  // dynamic buffers: [2][S][N*N], slot = parity of the slice
+  const int t_end = min((j + 1) * w.pace, w.Lt);  // forward step j ends at this slice
+  auto dbuf = [&](double* base, int par) { return base + ((long long)(par & 1) * w.S + sp) * NN; };
   switch (OP) {
     case OP_WL_FWD: A = w.expK; B = G; C = work; break;
     case OP_WR_FWD: A = work; B = w.invK; C = G; break;
@@ -122,15 +133,22 @@ __global__ void __launch_bounds__(256) gemm_op_kernel(const WalkerDev* __restric
     case OP_GA: A = UL; B = UR; C = scr; break;
     case OP_GB: A = UL + NN; B = UR + NN; C = scr; break;      // F_L, F_R
     case OP_GG: A = UR; B = scr + NN; C = G; break;           // U_R, X (row-major)
+    case OP_DT0: A = w.expK; B = dbuf(w.gt0, t - 1); C = dbuf(w.gt0, t); break;
+    case OP_D0T: A = dbuf(w.g0t, t - 1); B = w.invK; C = dbuf(w.g0t, t); break;
+    case OP_DT0_OUT: A = UR; B = w.dynx + sp * NN; C = dbuf(w.gt0, t_end); break;   // X1 row-major
+    case OP_D0T_OUT: A = UR + NN; B = scr + NN; C = dbuf(w.g0t, t_end); break;      // F_R, X row-major
   }
 
   __shared__ double As[kTk][kTile + 1];
   __shared__ double Bs[kTk][kTile + 1];
   __shared__ double s_red[8];
-  __shared__ double s_inv[OP == OP_GG ? kMaxN : 1];  // 1 / max(D_R, 1) along k
+  __shared__ double s_inv[(OP == OP_GG || dyn_out) ? kMaxN : 1];  // 1 / max(D_R, 1) or min(D_R, 1) along k
   const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
-  if (OP == OP_GG) {
+  if (OP == OP_GG || OP == OP_DT0_OUT) {
     for (int k = tid; k < N; k += 256) s_inv[k] = 1.0 / fmax(DR[k], 1.0);
+    __syncthreads();
+  } else if (OP == OP_D0T_OUT) {
+    for (int k = tid; k < N; k += 256) s_inv[k] = fmin(DR[k], 1.0);
     __syncthreads();
   }
   double acc[4][4];
@@ -157,6 +175,10 @@ __global__ void __launch_bounds__(256) gemm_op_kernel(const WalkerDev* __restric
           case OP_GA: v = A[(long long)r * N + k]; break;  // U_L^T (r,k) = U_L(k,r)
           case OP_GB: v = A[(long long)k * N + r]; break;
           case OP_GG: v = A[(long long)k * N + r] * s_inv[k]; break;  // U_R(r,k) / drmax_k
+          case OP_DT0: v = A[(long long)k * N + r] * bscale(w, t, sp, +1, r); break;
+          case OP_D0T: v = A[(long long)k * N + r]; break;
+          case OP_DT0_OUT: v = A[(long long)k * N + r] * s_inv[k]; break;
+          case OP_D0T_OUT: v = A[(long long)r * N + k] * s_inv[k]; break;  // F_R^T(r,k) drmin_k
         }
       }
       As[kk][rr] = v;
@@ -178,6 +200,10 @@ __global__ void __launch_bounds__(256) gemm_op_kernel(const WalkerDev* __restric
           case OP_GA: v = B[(long long)c * N + k]; break;
           case OP_GB: v = B[(long long)k * N + c]; break;  // F_R^T(k,c) = F_R(c,k)
           case OP_GG: v = B[(long long)k * N + c]; break;                     // X row-major
+          case OP_DT0: v = B[(long long)c * N + k]; break;
+          case OP_D0T: v = B[(long long)c * N + k]; break;
+          case OP_DT0_OUT: v = B[(long long)k * N + c]; break;  // X1 row-major
+          case OP_D0T_OUT: v = B[(long long)k * N + c]; break;  // X row-major
         }
       }
       Bs[kk][cc] = v;
@@ -214,12 +240,18 @@ __global__ void __launch_bounds__(256) gemm_op_kernel(const WalkerDev* __restric
       const long long o = (long long)c * N + r;
       switch (OP) {
         case OP_WR_FWD: v *= bscale(w, t, sp, -1, c); break;
+        case OP_D0T: v *= bscale(w, t, sp, -1, c); break;
+        case OP_D0T_OUT: v = -v; break;
         case OP_GA: v /= fmax(DL[r], 1.0) * fmax(DR[c], 1.0); break;
         case OP_GB: v *= fmin(DL[r], 1.0) * fmin(DR[c], 1.0); break;
         default: break;
       }
       if (OP == OP_GB) {
         C[o] += v;
+      } else if (dyn_out) {
+        err = fmax(err, fabs(v - C[o]));
+        if (!isfinite(v)) finite = false;
+        C[o] = v;
       } else if (OP == OP_GG) {
         if (check) err = fmax(err, fabs(v - C[o]));
         if (!isfinite(v)) finite = false;
@@ -233,9 +265,9 @@ __global__ void __launch_bounds__(256) gemm_op_kernel(const WalkerDev* __restric
         C[o] = v;
       }
     }
-  if (OP == OP_GG) {
+  if (OP == OP_GG || dyn_out) {
     if (!finite) atomicOr(w.status, ST_NONFINITE_G);
-    if (check) {
+    if (check || dyn_out) {
       for (int o = 16; o > 0; o >>= 1) err = fmax(err, __shfl_xor_sync(0xffffffffu, err, o));
       if ((tid & 31) == 0) s_red[tid >> 5] = err;
       __syncthreads();
@@ -795,6 +827,7 @@ __global__ void __launch_bounds__(1024) lu_solve_general_kernel(const WalkerDev*
     }
     __syncthreads();
     const int p = s_p;
+    if (w.dpiv && tid == 0) w.dpiv[sp * N + k] = p;  // kept for a second right-hand side
     if (p != k) {  // swap rows k and p of M (all columns) and Y
       for (int c = tid; c < N; c += nt) {
         double* mc = M + (long long)c * N;
@@ -928,6 +961,149 @@ __global__ void __launch_bounds__(1024) sign_general_kernel(const WalkerDev* __r
 }
 
 // --------------------------------------------------------------------------
+// Dynamic half-sweep (sweep_for_dynamic_greens, src/dqmc_walker.cpp:424-524):
+// the forward half-sweep with the fields fixed, carrying G(t,0) and G(0,t)
+// besides G(t,t).  At each stabilization, with M and X = M^-1 Dlmax^-1 U_L^T of
+// the equal-time assembly (LU pivots kept):
+//   G(t,0) = U_R Drmax^-1 M^-1 (Dlmin F_L)     (compute_dynamic_greens, :246-325)
+//   G(0,t) = -F_R^T Drmin X                     (push-through form of the second
+//            formula, exact for any right factor F; the reference's form needs an
+//            orthogonal V)
+// and at t = beta (right stack empty, H = Dmax^-1 U^T + Dmin F):
+//   G(beta,0) = H^-1 Dmin F,  G(0,beta) = -H^-1 Dmax^-1 U^T = -G(beta,beta).
+// --------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) dyn_init_kernel(const WalkerDev* __restrict__ W) {
+  const int wi = blockIdx.y >> 1, sp = blockIdx.y & 1;
+  const WalkerDev& w = W[wi];
+  if (!w.gt0 || sp >= w.S) return;
+  const long long NN = (long long)w.N * w.N;
+  const double* G = w.G + sp * NN;
+  double* t0 = w.gt0 + sp * NN;  // parity slot 0 (t = 0)
+  double* ot = w.g0t + sp * NN;
+  for (long long e = blockIdx.x * 256LL + threadIdx.x; e < NN; e += (long long)gridDim.x * 256) {
+    const int r = (int)(e % w.N), c = (int)(e / w.N);
+    t0[e] = G[e];
+    ot[e] = G[e] - ((r == c) ? 1.0 : 0.0);
+  }
+}
+
+// X1 = M^-1 (Dlmin F_L) with the LU factors and pivots left by lu_solve_general_kernel;
+// thread per column of the right-hand side (row-major, coalesced across threads)
+__global__ void __launch_bounds__(1024) dyn_resolve_kernel(const WalkerDev* __restrict__ W, int j) {
+  const int wi = blockIdx.x >> 1, sp = blockIdx.x & 1;
+  const WalkerDev& w = W[wi];
+  if (!w.gt0 || sp >= w.S || j >= w.nstack) return;
+  const int N = w.N;
+  const long long NN = (long long)N * N;
+  const int nl = j + 1;  // forward step j: left stack holds j + 1 levels
+  const double* lv = stack_level(w, 0, sp, nl - 1);
+  const double* F = lv + NN;
+  const double* D = lv + 2 * NN;
+  const double* M = w.scr + sp * 2 * NN;  // LU factors, col-major
+  const int* piv = w.dpiv + sp * N;
+  double* X = w.dynx + sp * NN;  // row-major
+  for (int c = threadIdx.x; c < N; c += blockDim.x) {
+    for (int r = 0; r < N; ++r) X[(long long)r * N + c] = fmin(D[r], 1.0) * F[(long long)c * N + r];
+    // the factorization swapped whole rows (multipliers included): all swaps first, then L and U
+    for (int k = 0; k < N; ++k) {
+      const int p = piv[k];
+      if (p != k) {
+        const double a = X[(long long)k * N + c];
+        X[(long long)k * N + c] = X[(long long)p * N + c];
+        X[(long long)p * N + c] = a;
+      }
+    }
+    for (int k = 0; k < N; ++k) {
+      const double yk = X[(long long)k * N + c];
+      if (yk != 0.0)
+        for (int r = k + 1; r < N; ++r) X[(long long)r * N + c] = fma(-M[(long long)k * N + r], yk, X[(long long)r * N + c]);
+    }
+    for (int k = N - 1; k >= 0; --k) {
+      const double yk = X[(long long)k * N + c] / M[(long long)k * N + k];
+      X[(long long)k * N + c] = yk;
+      for (int r = 0; r < k; ++r) X[(long long)r * N + c] = fma(-M[(long long)k * N + r], yk, X[(long long)r * N + c]);
+    }
+  }
+}
+
+// t = beta (forward step nstack - 1): G(beta,0) = X1, G(0,beta) = -X, with their wrap errors
+__global__ void __launch_bounds__(256) dyn_boundary_kernel(const WalkerDev* __restrict__ W, int j) {
+  const int wi = blockIdx.y >> 1, sp = blockIdx.y & 1;
+  const WalkerDev& w = W[wi];
+  if (!w.gt0 || sp >= w.S || j != w.nstack - 1) return;
+  const int N = w.N;
+  const long long NN = (long long)N * N;
+  const int par = w.Lt & 1;
+  double* t0 = w.gt0 + ((long long)par * w.S + sp) * NN;
+  double* ot = w.g0t + ((long long)par * w.S + sp) * NN;
+  const double* X1 = w.dynx + sp * NN;        // row-major
+  const double* X = w.scr + sp * 2 * NN + NN;  // row-major
+  double err = 0.0;
+  for (long long e = blockIdx.x * 256LL + threadIdx.x; e < NN; e += (long long)gridDim.x * 256) {
+    const int r = (int)(e % N), c = (int)(e / N);
+    const double a = X1[(long long)r * N + c], b = -X[(long long)r * N + c];
+    err = fmax(err, fmax(fabs(a - t0[e]), fabs(b - ot[e])));
+    t0[e] = a;
+    ot[e] = b;
+  }
+  for (int o = 16; o > 0; o >>= 1) err = fmax(err, __shfl_xor_sync(0xffffffffu, err, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(w.wrap_bits, (unsigned long long)__double_as_longlong(err));
+}
+
+// G(k,tau) += sign / N sum_ij FF(r_j - r_i) (G_up(t,0)(j,i) + G_dn(t,0)(j,i)) / 2 at the listed tau
+// (measure_greens_functions, src/measure/measure_methods.cpp:278-308).  phase 0: slices inside
+// the interval (after propagation); 1: the interval's last slice (after stabilization);
+// 2: tau = 0 from G(beta,beta) after the sweep.
+__global__ void __launch_bounds__(256) dyn_measure_kernel(const WalkerDev* __restrict__ W, int j, int q, int phase) {
+  const WalkerDev& w = W[blockIdx.x];
+  if (!w.gt0 || j >= w.nstack) return;
+  int t;
+  if (phase == 2) {
+    t = 0;
+  } else {
+    const int t_lo = j * w.pace + 1, t_hi = min((j + 1) * w.pace, w.Lt);
+    if (phase == 0) {
+      if (q >= t_hi - t_lo) return;  // the last slice of the interval is measured after stabilization
+      t = t_lo + q;
+    } else {
+      t = t_hi;
+    }
+    if (t >= w.Lt) return;  // tau = beta is not measured
+  }
+  int slot = -1;
+  for (int k = 0; k < w.dyn_ntau; ++k)
+    if (w.dyn_taus[k] == t) slot = k;
+  if (slot < 0) return;
+  const int N = w.N, L = w.L;
+  const long long NN = (long long)N * N;
+  const double* gu;
+  if (phase == 2) gu = w.G;
+  else gu = w.gt0 + ((long long)(t & 1) * w.S) * NN;
+  const double* gd = (w.S == 2) ? gu + NN : gu;
+  double v = 0.0;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for (int jj = wid; jj < N; jj += 8) {
+    const int xj = jj % L, yj = jj / L;
+    for (int i = lane; i < N; i += 32) {
+      int dx = xj - i % L, dy = yj - i / L;
+      dx += (dx < 0) ? L : 0;
+      dy += (dy < 0) ? L : 0;
+      v += w.ff[dx + dy * L] * (gu[(long long)i * N + jj] + gd[(long long)i * N + jj]);  // G(jj, i)
+    }
+  }
+  __shared__ double red[8];
+  v = warp_sum_g(v);
+  if (lane == 0) red[wid] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double tot = 0.0;
+    for (int k = 0; k < 8; ++k) tot += red[k];
+    w.dyn_sum[slot] += *w.sign * 0.5 * tot / N;
+    w.dyn_cnt[slot] += 1;
+  }
+}
+
+// --------------------------------------------------------------------------
 // host-side launchers for general walkers
 // --------------------------------------------------------------------------
 static dim3 gemm_grid(int maxN, int nw) {
@@ -979,6 +1155,40 @@ void general_slice(int mode, const WalkerDev* W, int nw, int j, int q, int maxN,
     if (mixed_dense) mixed_wrap_bwd(W, nw, maxN, j, q, st);
     if (any_cb) cb_general_kernel<<<2 * nw, 256, cb_sm, st>>>(W, mode, j, q, 1);
   }
+}
+
+// one slice of the dynamic half-sweep: wrap, G(t,0) and G(0,t) steps, B-chain, G(k,tau)
+void general_dynamic_slice(const WalkerDev* W, int nw, int j, int q, int maxN, bool mixed, cudaStream_t st) {
+  const dim3 g = gemm_grid(maxN, nw);
+  if (mixed) {
+    mixed_wrap_fwd(W, nw, maxN, j, q, st);
+  } else {
+    gemm_op_kernel<OP_WL_FWD><<<g, 256, 0, st>>>(W, MODE_FWD, j, q, -1);
+    gemm_op_kernel<OP_WR_FWD><<<g, 256, 0, st>>>(W, MODE_FWD, j, q, -1);
+  }
+  gemm_op_kernel<OP_DT0><<<g, 256, 0, st>>>(W, MODE_FWD, j, q, -1);
+  gemm_op_kernel<OP_D0T><<<g, 256, 0, st>>>(W, MODE_FWD, j, q, -1);
+  dyn_measure_kernel<<<nw, 256, 0, st>>>(W, j, q, 0);
+  if (mixed) mixed_chain(W, nw, maxN, MODE_FWD, j, q, st);
+  else gemm_op_kernel<OP_CH_FWD><<<g, 256, 0, st>>>(W, MODE_FWD, j, q, -1);
+}
+
+// stabilization of the dynamic pieces after general_greens of forward step j
+void general_dynamic_stab(const WalkerDev* W, int nw, int j, int maxN, cudaStream_t st) {
+  const dim3 g = gemm_grid(maxN, nw);
+  const int threads = std::min(1024, ((maxN + 31) / 32) * 32);
+  dyn_resolve_kernel<<<2 * nw, threads, 0, st>>>(W, j);
+  gemm_op_kernel<OP_DT0_OUT><<<g, 256, 0, st>>>(W, MODE_FWD, j, 0, -1);
+  gemm_op_kernel<OP_D0T_OUT><<<g, 256, 0, st>>>(W, MODE_FWD, j, 0, -1);
+  dyn_boundary_kernel<<<dim3(64, 2 * nw), 256, 0, st>>>(W, j);
+  dyn_measure_kernel<<<nw, 256, 0, st>>>(W, j, 0, 1);
+}
+
+void general_dynamic_begin(const WalkerDev* W, int nw, cudaStream_t st) {
+  dyn_init_kernel<<<dim3(64, 2 * nw), 256, 0, st>>>(W);
+}
+void general_dynamic_end(const WalkerDev* W, int nw, cudaStream_t st) {
+  dyn_measure_kernel<<<nw, 256, 0, st>>>(W, 0, 0, 2);
 }
 
 cudaError_t configure_general_kernels() {

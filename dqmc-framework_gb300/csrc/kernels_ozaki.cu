@@ -305,12 +305,18 @@ __global__ void __launch_bounds__(256, 1) oz_prod_tc_kernel(const WalkerDev* __r
   }
   extern __shared__ __align__(1024) unsigned char tsm[];
   __shared__ int eA[MT], eB[NT];
+  __shared__ double s_scale[MT];  // exp(+-alpha s) of the output rows (or columns)
   __shared__ __align__(8) unsigned long long mbar[2];
   __shared__ unsigned tbase;
   __shared__ int s_fail;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   if (tid < MT) eA[tid] = (r0 + tid < N) ? job.ea[r0 + tid] : -1100;
   if (tid < NT) eB[tid] = (c0 + tid < N) ? job.eb[c0 + tid] : -1100;
+  if (OP == OZ_WL_FWD || OP == OZ_CH_FWD) {
+    if (tid < MT) s_scale[tid] = (r0 + tid < N) ? oz_bscale(w, t, sp, +1, r0 + tid) : 0.0;
+  } else if (OP == OZ_WR_FWD) {
+    if (tid < NT) s_scale[tid] = (c0 + tid < N) ? oz_bscale(w, t, sp, -1, c0 + tid) : 0.0;
+  }
   if (tid == 0) {
     s_fail = 0;
     tc::mbar_init(&mbar[0]);
@@ -324,19 +330,26 @@ __global__ void __launch_bounds__(256, 1) oz_prod_tc_kernel(const WalkerDev* __r
   const unsigned taddr = tbase;
   constexpr uint32_t idesc = tc::idesc_bf16(MT, NT);
   const int nch = (ldk + KC - 1) / KC;
+  // this thread's 16-byte pieces per slice and chunk: two of A (lines tid % 128, k groups
+  // tid / 128 and tid / 128 + 2), one of B (line tid % 64, k group tid / 64)
+  const long long sstride = (long long)N * ldk;
+  const int la = tid & (MT - 1), kqa = tid >> 7, lb = tid & (NT - 1), kqb = tid >> 6;
+  const bool va = r0 + la < N, vb = c0 + lb < N;
+  const unsigned short* srcA = job.A + (long long)min(r0 + la, N - 1) * ldk + kqa * 8;
+  const unsigned short* srcB = job.B + (long long)min(c0 + lb, N - 1) * ldk + kqb * 8;
+  const int dA = (la & 7) * 16 + kqa * CM + (la >> 3) * RG;
+  const int dB = (lb & 7) * 16 + kqb * CM + (lb >> 3) * RG;
   auto load = [&](int c, int st) {
     unsigned char* sA = tsm + st * STAGE;
     unsigned char* sB = sA + S * A_SL;
     const int k0 = c * KC;
-    for (int gi = tid; gi < S * (MT + NT) * (KC / 8); gi += 256) {
-      const bool isA = gi < S * MT * (KC / 8);
-      const int g2 = isA ? gi : gi - S * MT * (KC / 8);
-      const int nl = isA ? MT : NT;
-      const int line = g2 % nl, rest = g2 / nl, kq = rest % (KC / 8), s = rest / (KC / 8);
-      const int gl = (isA ? r0 : c0) + line, k = k0 + kq * 8;
-      const unsigned short* src = (isA ? job.A : job.B) + ((long long)s * N + min(gl, N - 1)) * ldk + min(k, ldk - 8);
-      unsigned char* dst = (isA ? sA + s * A_SL : sB + s * B_SL) + (line & 7) * 16 + kq * CM + (line >> 3) * RG;
-      cp_async16(dst, src, gl < N && k < ldk);
+    const bool ka0 = k0 + kqa * 8 < ldk, ka1 = k0 + kqa * 8 + 16 < ldk, kb0 = k0 + kqb * 8 < ldk;
+    const int oa0 = ka0 ? k0 : 0, oa1 = ka1 ? k0 + 16 : 0, ob = kb0 ? k0 : 0;
+#pragma unroll
+    for (int s2 = 0; s2 < S; ++s2) {
+      cp_async16(sA + s2 * A_SL + dA, srcA + s2 * sstride + oa0, va && ka0);
+      cp_async16(sA + s2 * A_SL + dA + 2 * CM, srcA + s2 * sstride + oa1, va && ka1);
+      cp_async16(sB + s2 * B_SL + dB, srcB + s2 * sstride + ob, vb && kb0);
     }
     cp_async_commit();
   };
@@ -392,8 +405,8 @@ __global__ void __launch_bounds__(256, 1) oz_prod_tc_kernel(const WalkerDev* __r
 #pragma unroll
           for (int m = 0; m < S; ++m) sv = (sv << bits) + (long long)__float2int_rn(__uint_as_float(v[m][u]));
           double val = ozaki::ldexp_i64(sv, eA[rl] + eB[cl] - bits * (S + 1));
-          if (OP == OZ_WL_FWD || OP == OZ_CH_FWD) val *= oz_bscale(w, t, sp, +1, r);
-          if (OP == OZ_WR_FWD) val *= oz_bscale(w, t, sp, -1, col);
+          if (OP == OZ_WL_FWD || OP == OZ_CH_FWD) val *= s_scale[rl];
+          if (OP == OZ_WR_FWD) val *= s_scale[cl];
           out[(long long)col * N + r] = val;
         }
       }

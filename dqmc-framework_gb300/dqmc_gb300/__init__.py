@@ -36,6 +36,7 @@ EXPORTS = [
     "dqmc_clear_observables", "dqmc_trace_count", "dqmc_trace_get", "dqmc_trace_clear", "dqmc_batch_info",
     "dqmc_profile_enable", "dqmc_profile_read", "dqmc_microbench_fp64", "dqmc_get_observables_all",
     "dqmc_product_check", "dqmc_product_device_noalloc", "dqmc_launch_count", "dqmc_tuning",
+    "dqmc_sweep_dynamic", "dqmc_get_dynamic", "dqmc_clear_dynamic", "dqmc_get_green_dynamic",
 ]
 KCLASSES = ["segment", "push", "greens", "measure"]
 
@@ -91,6 +92,8 @@ def load() -> ctypes.CDLL:
         "dqmc_product_device_noalloc": (c, [c, vp, vp, vp, vp]),
         "dqmc_launch_count": (c, [vp, i64p]),
         "dqmc_tuning": (c, [vp, ip, ip, ip, ip, ip, ctypes.POINTER(ctypes.c_float)]),
+        "dqmc_sweep_dynamic": (c, [vp, ip, c]), "dqmc_get_dynamic": (c, [vp, c, dp, i64p]),
+        "dqmc_clear_dynamic": (c, [vp]), "dqmc_get_green_dynamic": (c, [vp, c, c, c, dp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -258,6 +261,30 @@ class Batch:
             _check(load().dqmc_profile_read(self.h, k, ctypes.byref(ms), ctypes.byref(n)))
             out[name] = (ms.value, n.value)
         return out
+
+    def sweep_dynamic(self, taus):
+        """DqmcWalker::sweep_for_dynamic_greens + G(k, tau) at the listed tau (fields fixed)."""
+        self._taus = [int(t) for t in taus]
+        arr = (ctypes.c_int * max(1, len(self._taus)))(*self._taus)
+        _check(load().dqmc_sweep_dynamic(self.h, arr, len(self._taus)))
+
+    def dynamic(self, w: int):
+        """(sums, counts) of sign * G(k, tau) per listed tau for walker w."""
+        n = len(getattr(self, "_taus", []))
+        s = np.zeros(max(n, 1))
+        c = (ctypes.c_int64 * max(n, 1))()
+        _check(load().dqmc_get_dynamic(self.h, w, s.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), c))
+        return s[:n], np.array(list(c))[:n]
+
+    def clear_dynamic(self):
+        _check(load().dqmc_clear_dynamic(self.h))
+
+    def green_dynamic(self, w: int, which: int, spin: int) -> np.ndarray:
+        """G(beta, 0) (which 0) or G(0, beta) (which 1) after the last dynamic half-sweep."""
+        N = self.walkers[w].N
+        g = np.zeros((N, N), order="F")
+        _check(load().dqmc_get_green_dynamic(self.h, w, which, spin, g.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
+        return g
 
     def tuning(self) -> dict:
         """The autotuner's pick (delayed block k, tensor-core flush) and every candidate's time."""

@@ -133,6 +133,27 @@ int dqmc_init_greens(dqmc_batch* b);
 int dqmc_sweep_0_to_beta(dqmc_batch* b, int measure);
 int dqmc_sweep_beta_to_0(dqmc_batch* b, int measure);
 
+/* Dynamic (time-displaced) half-sweep: DqmcWalker::sweep_for_dynamic_greens
+ * (src/dqmc_walker.cpp:424-524) with MeasureHandler::dynamic_measure's
+ * measure_greens_functions (src/measure/measure_methods.cpp:278-308).  Replaces
+ * a 0 -> beta half-sweep (src/dqmc.cpp:53-57): the fields stay fixed, G(t,0)
+ * and G(0,t) are carried besides G(t,t) and recomputed stably at every
+ * stabilization (their differences enter the wrap error, which here also
+ * includes the equal-time G), and G(k,tau) = sign/N sum_ij FF(r_j - r_i)
+ * (G_up(tau,0)(j,i) + G_dn(tau,0)(j,i))/2 is accumulated for the walker's
+ * momentum at each listed tau in [0, Lt) (tau = 0 from G(beta,beta)).  Needs
+ * the stacks of t = 0 (after dqmc_init_greens or dqmc_sweep_beta_to_0) and
+ * every walker on the HBM path (N > 64 or DQMC_MIXED), dense exp(-dtau K);
+ * stabilizes with the FP64 kernels.  A new tau list (at most 256 entries)
+ * restarts the accumulators. */
+int dqmc_sweep_dynamic(dqmc_batch* b, const int* taus, int ntau);
+/* Sums of sign * G(k,tau) and their counts, in the order of the last tau list. */
+int dqmc_get_dynamic(dqmc_batch* b, int walker, double* sums, int64_t* counts);
+int dqmc_clear_dynamic(dqmc_batch* b);
+/* G(beta,0) (which = 0) or G(0,beta) (which = 1) after the last dynamic half-sweep
+ * (DqmcWalker::Greent0Up/Dn, Green0tUp/Dn at t = Lt), column-major N x N. */
+int dqmc_get_green_dynamic(dqmc_batch* b, int walker, int which, int spin, double* out);
+
 /* Accessors: DqmcWalker::GreenttUp/GreenttDn, ConfigSign, WrapError
  * (include/dqmc_walker.h:150-184). spin 0 = up, 1 = down. */
 int dqmc_get_green(dqmc_batch* b, int walker, int spin, double* out);

@@ -128,6 +128,22 @@ class DqmcWalker {
   void initial_greens_functions() { check(dqmc_init_greens(b_)); }  // stacks + G(0) + sign
   void sweep_from_0_to_beta(bool measure = false) { check(dqmc_sweep_0_to_beta(b_, measure)); }
   void sweep_from_beta_to_0(bool measure = false) { check(dqmc_sweep_beta_to_0(b_, measure)); }
+  // sweep_for_dynamic_greens (include/dqmc_walker.h:131) + G(k,tau) at the listed tau
+  void sweep_for_dynamic_greens(const std::vector<int>& taus) {
+    check(dqmc_sweep_dynamic(b_, taus.data(), (int)taus.size()));
+  }
+  // G(k,tau) accumulators of walker w in the order of the last tau list
+  std::vector<double> DynamicGreens(int w, std::vector<int64_t>* counts = nullptr, int ntau = 0) const {
+    std::vector<double> s(ntau);
+    std::vector<int64_t> c(ntau);
+    check(dqmc_get_dynamic(b_, w, s.data(), c.data()));
+    if (counts) *counts = c;
+    return s;
+  }
+  std::vector<double> Greent0Up(int w) const { return green_dyn(w, 0, 0); }  // G(beta,0) after the last dynamic half-sweep
+  std::vector<double> Greent0Dn(int w) const { return green_dyn(w, 0, 1); }
+  std::vector<double> Green0tUp(int w) const { return green_dyn(w, 1, 0); }
+  std::vector<double> Green0tDn(int w) const { return green_dyn(w, 1, 1); }
 
   std::vector<double> GreenttUp(int w) const { return green(w, 0); }
   std::vector<double> GreenttDn(int w) const { return green(w, 1); }
@@ -139,6 +155,11 @@ class DqmcWalker {
   dqmc_batch* handle() const { return b_; }
 
  private:
+  std::vector<double> green_dyn(int w, int which, int spin) const {
+    std::vector<double> g((size_t)N_ * N_);
+    check(dqmc_get_green_dynamic(b_, w, which, spin, g.data()));
+    return g;
+  }
   std::vector<double> green(int w, int spin) const {
     std::vector<double> g((size_t)N_ * N_);
     check(dqmc_get_green(b_, w, spin, g.data()));

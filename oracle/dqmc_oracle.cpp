@@ -644,6 +644,11 @@ struct Oracle {
   bool trace_on = false;
   std::vector<Vec> trace;  // pairs (up, dn)
   int kidx = 0;
+  // time-displaced Green's functions (dqmc_walker.h:74-80) and G(k, tau) accumulators
+  Vec gt0[2], g0t[2];
+  std::vector<int> dyn_taus;
+  std::vector<double> dyn_sum;
+  std::vector<long long> dyn_cnt;
 
   double& s(int t, int i) { return field[(size_t)t * N + i]; }
   double s(int t, int i) const { return field[(size_t)t * N + i]; }
@@ -958,6 +963,175 @@ struct Oracle {
     }
   }
 
+
+  // --- time-displaced Green's functions ------------------------------------------
+  // compute_dynamic_greens (numerical_stable.hpp:246-325) for both stack kinds;
+  // the stack product is U diag(D) F with F = V^T (SVD) or the QRP right factor.
+  void dynamic_greens(int sp, Vec& t0, Vec& ot) const {
+    const Stack& L = left[sp];
+    const Stack& R = right[sp];
+    const Vec I = identity(N);
+    if (L.empty()) {  // gt0 = g00, g0t = -(1 - g00)  (:250-257)
+      t0 = equaltime_greens(N, L, R);
+      ot = t0;
+      for (size_t k = 0; k < ot.size(); ++k) ot[k] -= I[k];
+      return;
+    }
+    if (R.empty()) {  // gt0 = (1 + B)^-1 B (compute_greens_b0, :159-179), g0t = -(1 + B)^-1  (:260-270)
+      const Level& l = L.top();
+      Vec dmax, dmin;
+      split_max_min(l.D, dmax, dmin);
+      Vec H((size_t)N * N), r1((size_t)N * N), r2((size_t)N * N);
+      for (int c = 0; c < N; ++c)
+        for (int r = 0; r < N; ++r) {
+          const double ut = at(l.U, N, c, r) / dmax[r];  // (Dmax^-1 U^T)(r, c)
+          const double vf = dmin[r] * at(l.F, N, r, c);   // (Dmin V^T)(r, c)
+          at(H, N, r, c) = ut + vf;
+          at(r1, N, r, c) = vf;
+          at(r2, N, r, c) = ut;
+        }
+      if (L.kind == ORC_STACK_SVD) {  // the reference's fullPivHouseholderQr solves
+        t0 = fullpiv_qr_solve(N, H, r1);
+        ot = fullpiv_qr_solve(N, H, r2);
+      } else {
+        std::vector<int> piv;
+        int ns;
+        lu_factor(N, H, piv, ns);
+        lu_solve(N, H, piv, r1, N);
+        lu_solve(N, H, piv, r2, N);
+        t0 = r1;
+        ot = r2;
+      }
+      for (auto& x : ot) x = -x;
+      return;
+    }
+    const Level& l = L.top();
+    const Level& r = R.top();
+    Vec dlmax, dlmin, drmax, drmin;
+    split_max_min(l.D, dlmax, dlmin);
+    split_max_min(r.D, drmax, drmin);
+    // gt0 = U_R Drmax^-1 [Dlmax^-1 U_L^T U_R Drmax^-1 + Dlmin V_L^T V_R Drmin]^-1 Dlmin V_L^T
+    {
+      const Vec A = gemm('T', 'N', N, l.U, r.U);
+      const Vec B = gemm('N', 'T', N, l.F, r.F);
+      Vec M((size_t)N * N), rhs((size_t)N * N);
+      for (int j = 0; j < N; ++j)
+        for (int i = 0; i < N; ++i) {
+          at(M, N, i, j) = at(A, N, i, j) / (dlmax[i] * drmax[j]) + at(B, N, i, j) * dlmin[i] * drmin[j];
+          at(rhs, N, i, j) = dlmin[i] * at(l.F, N, i, j);
+        }
+      std::vector<int> piv;
+      int ns;
+      lu_factor(N, M, piv, ns);
+      lu_solve(N, M, piv, rhs, N);
+      Vec ur = r.U;
+      for (int c = 0; c < N; ++c)
+        for (int i = 0; i < N; ++i) at(ur, N, i, c) /= drmax[c];
+      t0 = gemm('N', 'N', N, ur, rhs);
+    }
+    if (L.kind != ORC_STACK_SVD) {
+      // the right factors of the QRP stack are not orthogonal, so the reference's
+      // second formula does not apply; by push-through, (1 + B_R B_L)^-1 B_R =
+      // B_R (1 + B_L B_R)^-1 with B_R = F_R^T D_R U_R^T gives
+      // g0t = -F_R^T Drmin M^-1 Dlmax^-1 U_L^T (the M of the equal-time form)
+      const Vec A = gemm('T', 'N', N, l.U, r.U);
+      const Vec B = gemm('N', 'T', N, l.F, r.F);
+      Vec M((size_t)N * N), rhs((size_t)N * N);
+      for (int j = 0; j < N; ++j)
+        for (int i = 0; i < N; ++i) {
+          at(M, N, i, j) = at(A, N, i, j) / (dlmax[i] * drmax[j]) + at(B, N, i, j) * dlmin[i] * drmin[j];
+          at(rhs, N, i, j) = at(l.U, N, j, i) / dlmax[i];
+        }
+      std::vector<int> piv;
+      int ns;
+      lu_factor(N, M, piv, ns);
+      lu_solve(N, M, piv, rhs, N);
+      Vec frt = transpose(r.F, N);
+      for (int c = 0; c < N; ++c)
+        for (int i = 0; i < N; ++i) at(frt, N, i, c) *= -drmin[c];
+      ot = gemm('N', 'N', N, frt, rhs);
+      return;
+    }
+    // g0t = -V_L Dlmax^-1 [Drmax^-1 V_R^T V_L Dlmax^-1 + Drmin U_R^T U_L Dlmin]^-1 Drmin U_R^T
+    {
+      const Vec X = gemm('N', 'T', N, r.F, l.F);
+      const Vec Y = gemm('T', 'N', N, r.U, l.U);
+      Vec M((size_t)N * N), rhs((size_t)N * N);
+      for (int j = 0; j < N; ++j)
+        for (int i = 0; i < N; ++i) {
+          at(M, N, i, j) = at(X, N, i, j) / (drmax[i] * dlmax[j]) + at(Y, N, i, j) * drmin[i] * dlmin[j];
+          at(rhs, N, i, j) = drmin[i] * at(r.U, N, j, i);
+        }
+      std::vector<int> piv;
+      int ns;
+      lu_factor(N, M, piv, ns);
+      lu_solve(N, M, piv, rhs, N);
+      Vec vl = transpose(l.F, N);
+      for (int c = 0; c < N; ++c)
+        for (int i = 0; i < N; ++i) at(vl, N, i, c) /= -dlmax[c];
+      ot = gemm('N', 'N', N, vl, rhs);
+    }
+  }
+  // measure_greens_functions (measure_methods.cpp:278-308) at one tau for this walker's momentum
+  void accumulate_dynamic(int slot, const Vec& gu, const Vec& gd) {
+    double sum = 0.0;
+    for (int i = 0; i < N; ++i)
+      for (int j = 0; j < N; ++j)
+        sum += sign * 0.5 * (at(gu, N, j, i) + at(gd, N, j, i)) / N * lat.fourier(lat.disp(i, j), kidx);
+    dyn_sum[slot] += sum;
+    dyn_cnt[slot] += 1;
+  }
+  // sweep_for_dynamic_greens (dqmc_walker.cpp:424-524): 0 -> beta with the fields fixed
+  void sweep_dynamic(const int* taus, int ntau) {
+    if (!left[0].empty() || right[0].len != nstack)
+      throw std::runtime_error("sweep_dynamic: needs the stacks of t = 0 (after init or a backward sweep)");
+    if ((int)dyn_taus.size() != ntau || !std::equal(dyn_taus.begin(), dyn_taus.end(), taus)) {
+      dyn_taus.assign(taus, taus + ntau);
+      dyn_sum.assign(ntau, 0.0);
+      dyn_cnt.assign(ntau, 0);
+    }
+    const Vec I = identity(N);
+    for (int sp = 0; sp < 2; ++sp) {
+      gt0[sp] = G[sp];
+      g0t[sp] = G[sp];
+      for (size_t k = 0; k < g0t[sp].size(); ++k) g0t[sp][k] -= I[k];
+    }
+    Vec tu = identity(N), td = identity(N);
+    for (int t = 1; t <= Lt; ++t) {
+      wrap_fwd(t - 1);
+      mult_B(0, gt0[0], t, +1);
+      mult_B(0, gt0[1], t, -1);
+      mult_B(3, g0t[0], t, +1);
+      mult_B(3, g0t[1], t, -1);
+      mult_B(0, tu, t, +1);
+      mult_B(0, td, t, -1);
+      if (t % pace == 0 || t == Lt) {
+        right[0].pop();
+        right[1].pop();
+        left[0].push(tu);
+        left[1].push(td);
+        for (int sp = 0; sp < 2; ++sp) {
+          G[sp] = equaltime_greens(N, left[sp], right[sp]);
+          Vec f0, f1;
+          dynamic_greens(sp, f0, f1);
+          wrap_err = std::max(wrap_err, std::max(matrix_compare_error(N, f0, gt0[sp]), matrix_compare_error(N, f1, g0t[sp])));
+          gt0[sp] = f0;
+          g0t[sp] = f1;
+        }
+        if (trace_on) {
+          trace.push_back(gt0[0]);
+          trace.push_back(gt0[1]);
+        }
+        tu = identity(N);
+        td = identity(N);
+      }
+      for (int k = 0; k < ntau; ++k)
+        if (taus[k] == t && t < Lt) accumulate_dynamic(k, gt0[0], gt0[1]);
+    }
+    for (int k = 0; k < ntau; ++k)
+      if (taus[k] == 0) accumulate_dynamic(k, G[0], G[1]);  // tau = 0: G(beta, beta) = G(0, 0)
+  }
+
   // --- equal-time measurements (measure_methods.cpp:22-255) ---------------------
   void measure() {
     if (!p.record_greens) throw std::runtime_error("measure() needs record_greens");
@@ -1060,6 +1234,24 @@ void orc_init(void* h) { O(h)->init(); }
 void orc_sweep_0_to_beta(void* h) { O(h)->sweep_fwd(); }
 void orc_sweep_beta_to_0(void* h) { O(h)->sweep_bwd(); }
 void orc_measure(void* h) { O(h)->measure(); }
+int orc_sweep_dynamic(void* h, const int* taus, int ntau) {
+  try {
+    O(h)->sweep_dynamic(taus, ntau);
+  } catch (const std::exception&) {
+    return -1;
+  }
+  return 0;
+}
+void orc_get_dynamic(void* h, double* sums, int64_t* counts) {
+  for (size_t k = 0; k < O(h)->dyn_sum.size(); ++k) {
+    sums[k] = O(h)->dyn_sum[k];
+    counts[k] = O(h)->dyn_cnt[k];
+  }
+}
+void orc_get_green_dynamic(void* h, int which, int spin, double* out) {
+  const Vec& g = which == 0 ? O(h)->gt0[spin] : O(h)->g0t[spin];
+  std::memcpy(out, g.data(), sizeof(double) * g.size());
+}
 void orc_write_bin(void* h, int, double* out) { O(h)->write_bin(out); }
 void orc_get_accumulators(void* h, double* sums, int* counts) {
   for (int k = 0; k < ORC_NUM_OBS; ++k) {

@@ -88,6 +88,15 @@ void orc_init(void* h);
 void orc_sweep_0_to_beta(void* h);
 void orc_sweep_beta_to_0(void* h);
 
+/* Dynamic half-sweep 0 -> beta with the fields fixed (src/dqmc_walker.cpp:424-524),
+ * accumulating G(k, tau) of the walker's momentum at the listed tau
+ * (measure_methods.cpp:278-308).  Needs the stacks of t = 0 (after init or a
+ * backward half-sweep); 0 on success, -1 otherwise.  The trace records G(t,0)
+ * after each stabilization. */
+int orc_sweep_dynamic(void* h, const int* taus, int ntau);
+void orc_get_dynamic(void* h, double* sums, int64_t* counts);          /* [ntau] */
+void orc_get_green_dynamic(void* h, int which, int spin, double* out); /* 0: G(t,0), 1: G(0,t) */
+
 /* Equal-time measurement over the recorded series (measure_handler.cpp:136-150). */
 void orc_measure(void* h);
 /* Normalise the temporaries into bin b and clear them (measure_handler.cpp:170-240,261-277). */

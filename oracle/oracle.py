@@ -82,6 +82,9 @@ def lib() -> ctypes.CDLL:
         "orc_fields_random": (None, [vp]), "orc_set_fields": (None, [vp, i8p]),
         "orc_get_fields": (None, [vp, i8p]), "orc_init": (None, [vp]),
         "orc_sweep_0_to_beta": (None, [vp]), "orc_sweep_beta_to_0": (None, [vp]),
+        "orc_sweep_dynamic": (ctypes.c_int, [vp, ctypes.POINTER(ctypes.c_int), ctypes.c_int]),
+        "orc_get_dynamic": (None, [vp, dp, ctypes.POINTER(ctypes.c_int64)]),
+        "orc_get_green_dynamic": (None, [vp, ctypes.c_int, ctypes.c_int, dp]),
         "orc_measure": (None, [vp]), "orc_write_bin": (None, [vp, ctypes.c_int, dp]),
         "orc_get_accumulators": (None, [vp, dp, ctypes.POINTER(ctypes.c_int)]),
         "orc_get_green": (None, [vp, ctypes.c_int, dp]),
@@ -192,6 +195,27 @@ class Walker:
 
     def measure(self):
         lib().orc_measure(self.h)
+
+    def sweep_dynamic(self, taus):
+        """sweep_for_dynamic_greens + G(k, tau) at the listed tau (fields fixed)."""
+        self._taus = [int(t) for t in taus]
+        arr = (ctypes.c_int * len(self._taus))(*self._taus)
+        if lib().orc_sweep_dynamic(self.h, arr, len(self._taus)) != 0:
+            raise RuntimeError("sweep_dynamic needs the stacks of t = 0 (after init or sweep_beta_to_0)")
+
+    def dynamic(self):
+        """(sums, counts) of sign * G(k, tau) per listed tau."""
+        n = len(self._taus)
+        s = np.zeros(n)
+        c = (ctypes.c_int64 * n)()
+        lib().orc_get_dynamic(self.h, _dp(s), c)
+        return s, np.array(list(c))
+
+    def green_dynamic(self, which: int, spin: int) -> np.ndarray:
+        """which 0: G(t, 0), 1: G(0, t) after the last dynamic sweep (t = beta)."""
+        g = np.zeros((self.N, self.N), order="F")
+        lib().orc_get_green_dynamic(self.h, which, spin, _dp(g))
+        return g
 
     def write_bin(self) -> np.ndarray:
         out = np.zeros(len(OBS_NAMES))

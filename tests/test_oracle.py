@@ -213,6 +213,73 @@ def test_svd_and_qrp_stacks_agree(oracle_mod):
     assert abs(ta - tb).max() < 1e-10
 
 
+# ---- time-displaced Green's functions (sweep_for_dynamic_greens) ----------------
+
+@pytest.mark.parametrize("stack", [0, 1])
+def test_dynamic_free_fermions_known_answer(oracle_mod, stack):
+    """U = 0: G(k, tau) = exp(-tau e_k) / (1 + exp(-beta e_k)), e_k = -2t(cos kx + cos ky) + mu;
+    the M point (pi, pi) gives e = 4t + mu."""
+    O = oracle_mod
+    mu, beta, Lt = 0.3, 2.0, 20
+    w = O.Walker(model=0, L=4, U=0.0, mu=mu, beta=beta, Lt=Lt, pace=5, stack=stack)
+    w.seed(5)
+    w.fields_random()
+    w.init()
+    taus = [0, 1, 5, 7, 10, 19]
+    w.sweep_dynamic(taus)
+    sums, counts = w.dynamic()
+    e = 4.0 + mu
+    for tau, s, c in zip(taus, sums, counts):
+        assert c == 1
+        assert abs(s - np.exp(-tau * beta / Lt * e) / (1 + np.exp(-beta * e))) < 1e-12
+    assert w.wrap_error < 1e-12
+
+
+@pytest.mark.parametrize("stack", [0, 1])
+@pytest.mark.parametrize("model", [0, 1])
+def test_dynamic_greens_at_beta_equal_direct_formula(oracle_mod, stack, model):
+    """After the dynamic sweep G(beta, 0) = (1 + B)^-1 B and G(0, beta) = -(1 + B)^-1 with
+    B = B(beta) ... B(1) of the spin (interacting, fixed fields)."""
+    O = oracle_mod
+    w = O.Walker(model=model, L=4, U=4.0, mu=-0.2 if model else 0.0, beta=2.0, Lt=20, pace=5, stack=stack)
+    w.seed(3)
+    w.fields_random()
+    w.init()
+    N = 16
+    B = [np.eye(N), np.eye(N)]
+    for t in range(1, 21):
+        for s, sg in ((0, +1), (1, -1)):
+            m = np.asfortranarray(np.eye(N))
+            O.lib().orc_mult_B(w.h, 0, O._dp(m), t, sg)
+            B[s] = m @ B[s]
+    w.sweep_dynamic([3])
+    for s in (0, 1):
+        assert abs(w.green_dynamic(0, s) - np.linalg.solve(np.eye(N) + B[s], B[s])).max() < 1e-10
+        assert abs(w.green_dynamic(1, s) + np.linalg.inv(np.eye(N) + B[s])).max() < 1e-10
+    assert w.wrap_error < 1e-9
+
+
+def test_dynamic_stacks_agree_and_alternate(oracle_mod):
+    """Both stack kinds give the same G(k, tau); dynamic and backward half-sweeps alternate."""
+    O = oracle_mod
+    res = []
+    for stack in (O.STACK_SVD, O.STACK_QRP):
+        w = O.Walker(model=1, L=4, U=4.0, mu=-0.5, beta=4.0, Lt=40, pace=8, stack=stack)
+        w.seed(11)
+        w.fields_random()
+        w.init()
+        taus = [0, 4, 8, 13, 39]
+        for _ in range(2):
+            w.sweep_dynamic(taus)
+            w.sweep_beta_to_0()
+        res.append((w.dynamic()[0], w.wrap_error))
+        with pytest.raises(RuntimeError):
+            w.sweep_0_to_beta()
+            w.sweep_dynamic(taus)  # stacks no longer at t = 0
+    assert abs(res[0][0] - res[1][0]).max() < 1e-10
+    assert res[0][1] < 1e-9 and res[1][1] < 1e-9
+
+
 def _pin_chain(args):
     import os
     import sys
