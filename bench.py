@@ -2,11 +2,17 @@
 """bench.py — HS-field updates/s of the DQMC sweep on GB300.
 
 Metric (the reference's sweep counting, src/dqmc.cpp:88-92): HS-field update
-attempts per second = walkers * N * Lt / half-sweep time.  One step = one
-half-sweep (alternating 0->beta and beta->0) of every walker, equal-time
-measurement fused.  Default workload: 256 independent FP64 walkers, repulsive
-Hubbard 8x8 (N=64), t=1, U=4, mu=0, beta=8, dtau=0.05 (Lt=160), checkerboard
-exp(-dtau K), stabilization every 10 slices, seeded +/-1 fields.
+attempts per second = walkers * N * Lt / half-sweep time, of the batched
+mixed-precision sweep against the FP64 path, with the mixed path's max |dG|
+against FP64 on the same fields.  One step = one half-sweep (alternating
+0->beta and beta->0) of every walker, equal-time measurement fused.  Default
+workload: 128 walkers, attractive Hubbard 16x16 (N=256), t=1, |U|=4,
+mu=-0.5, beta=10, dtau=0.1 (Lt=100), dense exp(-dtau K), stabilization every
+8 slices, seeded +/-1 fields; wraps, B-chain and stabilization products on the
+tensor cores (exact-slice BF16, tcgen05), FP64 elsewhere.  For this workload
+the line also carries the FP64 batch on the same configuration, the plain
+single-walker FP64 path, and max |dG| at every stabilization of a half-sweep
+(mixed against FP64 on the same fields and uniforms, a sample of walkers).
 
 Legs printed on one JSON line:
   value        device-timed throughput (CUDA events on the library's stream,
@@ -54,7 +60,7 @@ WORKLOADS = {
     "fp64_single_4x4_dense": dict(walkers=1, model=0, L=4, U=4.0, mu=0.0, beta=4.0, Lt=80, pace=10,
                                   checkerboard=False),
 }
-DEFAULT_WORKLOAD = "fp64_batch_8x8_checkerboard"
+DEFAULT_WORKLOAD = "mixed_batch_16x16_attractive"
 METRIC = "HS-field updates/s (walkers*N*Lt / half-sweep time)"
 
 
@@ -185,6 +191,73 @@ def flops_model(wl, accepts_per_walker_per_half):
     return {"segment": seg, "push": push, "greens": greens, "nominal_F": nominal}
 
 
+def stab_tensor_flops(N, TB=32):
+    """FP64-equivalent flops of the tensor-core products of one push and one
+    Green's assembly (blocked Householder, panel TB), per walker and spin."""
+    push = 2 * N ** 3  # F = D^-1 R P^T F_prev
+    greens = 3 * 2 * N ** 3  # M = ... U_L^T U_R ..., += F_L F_R^T, G = U_R X
+    for p in range(-(-N // TB)):
+        j0 = p * TB
+        m = N - j0
+        pb = min(TB, m)
+        nt = m - pb
+        qr = (2 * pb * nt * m + 2 * pb * nt * pb + 2 * m * nt * pb) if nt > 0 else 0
+        push += qr + 2 * pb * m * m + 2 * pb * m * pb + 2 * m * m * pb  # trailing update, forming Q
+        greens += qr + 2 * pb * N * m + 2 * pb * N * pb + 2 * m * N * pb  # trailing update, Q^T Y
+        if j0 + pb < N:
+            greens += 2 * pb * N * (N - j0 - pb)  # block back substitution
+    return push, greens
+
+
+def fp64_comparison(args, dq, wl, stream, sample=8):
+    """The FP64 path on the same configuration (throughput), the plain
+    single-walker FP64 path, and max |dG| of the mixed path against FP64 at
+    every stabilization of one half-sweep on the same fields and uniforms."""
+    import torch
+
+    def timed_rate(descs, steps):
+        b = dq.Batch(descs, rng=dq.RNG_PHILOX, precision=dq.FP64)
+        b.set_stream(stream.cuda_stream)
+        for w in range(len(descs)):
+            b.fields_random(w)
+        b.init_greens()
+        b.sweep_0_to_beta(measure=True)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for k in range(steps):
+            (b.sweep_beta_to_0 if k % 2 == 0 else b.sweep_0_to_beta)(measure=True)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        upd = b.updates_per_half_sweep()
+        b.close()
+        return upd * steps / (ms * 1e-3), ms / steps
+
+    descs = _descs(dq, wl)
+    fp64_value, fp64_ms = timed_rate(descs, 2)
+    single_value, single_ms = timed_rate(descs[:1], 1)
+    # accuracy gate on a sample of walkers: identical decisions, |dG| at every stabilization
+    sub = descs[:sample]
+    traces, fields = [], []
+    for prec in (dq.MIXED, dq.FP64):
+        b = dq.Batch(sub, rng=dq.RNG_PHILOX, precision=prec, trace=True)
+        for w in range(len(sub)):
+            b.fields_random(w)
+        b.init_greens()
+        b.sweep_0_to_beta(measure=True)
+        traces.append([b.trace(w) for w in range(len(sub))])
+        fields.append([b.fields(w) for w in range(len(sub))])
+        b.close()
+    same = [bool((fields[0][w] == fields[1][w]).all()) for w in range(len(sub))]
+    dg = max(float(abs(traces[0][w] - traces[1][w]).max()) for w in range(len(sub)) if same[w]) if any(same) else None
+    return {"fp64_batch_value": fp64_value, "fp64_batch_ms_per_step": fp64_ms,
+            "fp64_single_walker_value": single_value, "fp64_single_walker_ms_per_step": single_ms,
+            "max_abs_dG": dg, "dG_sample": f"{len(sub)} walkers, every stabilization of one 0->beta half-sweep, "
+                                            f"same fields and Philox uniforms",
+            "walkers_with_identical_decisions": int(sum(same))}
+
+
 def run_gpu(args, wl, rank, world):
     import torch
 
@@ -257,21 +330,51 @@ def run_gpu(args, wl, rank, world):
         ms = float(t.item())
     value = world * upd * args.steps / (ms * 1e-3)
 
-    # ---- roofline of the dominant kernel class
+    # ---- roofline of the dominant kernel class (algorithmic work of the class / its CUDA-event time)
     acc_per_walker_half = (acc1 - acc0) / len(descs) / args.steps
     fm = flops_model(wl, acc_per_walker_half)
-    dom = max(["segment", "push", "greens"], key=lambda k: prof[k][0])
+    N, S, Lt = wl["L"] ** 2, (1 if wl["model"] == 1 else 2), wl["Lt"]
+    ns = -(-Lt // wl["pace"])
+    units = len(descs) * args.steps  # walker half-sweeps in the timed region
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    bf16_peak = peaks.get("bf16_tflops_sustained") or 1700.0
+    bf16_src = ("MEASURED_PEAKS.json bf16_tflops_sustained (the class runs inside a long step)"
+                if "bf16_tflops_sustained" in peaks else "fallback 1.7 PFLOP/s sustained bf16")
+    fp64_src = "FP64 FMA probe measured in this run (dqmc_microbench_fp64); MEASURED_PEAKS.json holds no FP64 figure"
+    model = {}  # class -> (bound, algorithmic flops in the timed region, peak TFLOP/s, what is counted)
+    if wl.get("precision") == "mixed":
+        sl = 6 * 7 // 2 if N <= 256 else 7 * 8 // 2  # slice products of one wrap or chain product
+        model["product"] = ("tensor", units * S * Lt * 3 * sl * 2 * N ** 3, bf16_peak,
+                            f"BF16 flops of the exact-slice products: 3 per slice x {sl} slice pairs x 2N^3")
+        if N >= 128:
+            pf, gf = stab_tensor_flops(N)
+            pairs = 36 if N <= 256 else 45
+            model["push"] = ("tensor", units * S * ns * pf * pairs, bf16_peak,
+                             f"BF16 flops of the blocked-QR products ({pairs} slice pairs per FP64-class product)")
+            model["greens"] = ("tensor", units * S * ns * gf * pairs, bf16_peak,
+                               f"BF16 flops of the Green's-assembly products ({pairs} slice pairs)")
+        model["metropolis"] = ("fp64", units * S * acc_per_walker_half * 2 * N * N, fp64_peak / 1e3,
+                               "the reference's rank-1 update flops, 2 N^2 per accepted flip and spin")
+    else:
+        for k in ("segment", "push", "greens"):
+            model[k] = ("fp64", fm[k] * units, fp64_peak / 1e3, "FP64 flops of the class (see DESIGN.md)")
+    dom = max((k for k in model if prof.get(k, (0, 0))[1] > 0), key=lambda k: prof[k][0])
+    bound, flops, peak, what = model[dom]
     dom_ms, dom_n = prof[dom]
-    flops_per_launch = fm[dom] * len(descs) * args.steps / max(dom_n, 1)
-    avg_ms = dom_ms / max(dom_n, 1)
-    achieved = flops_per_launch / (avg_ms * 1e-3) / 1e12
-    roofline = {"bound": "fp64", "kernel": f"{dom}_kernel", "achieved": achieved, "peak": fp64_peak / 1e3,
-                "unit": "TFLOP/s", "frac": achieved / (fp64_peak / 1e3), "traffic": None,
-                "peak_source": "FP64 FMA probe measured in this run (dqmc_microbench_fp64); "
-                               "MEASURED_PEAKS.json holds no FP64 figure",
-                "avg_launch_ms": avg_ms,
-                "kernel_share": {k: prof[k][0] / ms for k in prof},
-                "sweep_nominal_F_tflops": fm["nominal_F"] * len(descs) * args.steps / (ms * 1e-3) / 1e12}
+    achieved = flops / (dom_ms * 1e-3) / 1e12
+    roofline = {"bound": bound, "kernel": f"{dom} kernel class", "achieved": achieved, "peak": peak,
+                "unit": "TFLOP/s", "frac": achieved / peak, "traffic": None,
+                "peak_source": bf16_src if bound == "tensor" else fp64_src, "counted": what,
+                "avg_launch_ms": dom_ms / max(dom_n, 1),
+                "kernel_share": {k: prof[k][0] / ms for k in prof if prof[k][1] > 0},
+                "classes": {k: {"bound": v[0], "achieved_tflops": v[1] / (prof[k][0] * 1e-3) / 1e12,
+                                "frac": v[1] / (prof[k][0] * 1e-3) / 1e12 / v[2]}
+                            for k, v in model.items() if prof.get(k, (0, 0))[0] > 0},
+                "sweep_nominal_F_tflops": fm["nominal_F"] * units / (ms * 1e-3) / 1e12}
     launches = batch.launch_count() - launches0
 
     # ---- e2e: reference RNG on the host, copies in and out every step
@@ -297,8 +400,11 @@ def run_gpu(args, wl, rank, world):
                "h2d_bytes_per_step": 8 * upd, "d2h_bytes_per_step": int(sums.nbytes + counts.nbytes),
                "steps": ek, "rng": "host minstd_rand0 (reference stream)"}
         eb.close()
+    cmp = None
+    if wl.get("precision") == "mixed" and rank == 0 and world == 1 and not args.no_compare:
+        cmp = fp64_comparison(args, dq, wl, stream)
     return dict(value=value, ms=ms, roofline=roofline, e2e=e2e, clocks=clk, launches=launches, status=status,
-                tuning=tuning,
+                tuning=tuning, fp64=cmp,
                 accept_rate=acc_per_walker_half / (wl["L"] ** 2 * wl["Lt"]), fp64_peak=fp64_peak)
 
 
@@ -311,6 +417,7 @@ def main():
     ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=sorted(WORKLOADS))
     ap.add_argument("--cpu-budget", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-compare", action="store_true", help="skip the FP64 comparison legs (profiling runs)")
     ap.add_argument("--walkers", type=int, default=0, help="override the walker count (profiling runs)")
     args = ap.parse_args()
     wl = dict(WORKLOADS[args.workload])
@@ -349,12 +456,18 @@ def main():
         cb = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
     line = {"metric": METRIC, "value": r["value"], "unit": "updates/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": r["ms"] / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded +/-1 fields)",
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64; products as exact bf16 slices" if wl.get("precision") == "mixed" else "f64",
+            "data": "synthetic (seeded +/-1 fields)",
             "config": config, "roofline": r["roofline"], "cpu_baseline": cb, "e2e": r["e2e"],
             "gpu_launches": r["launches"], "clocks": r["clocks"], "accept_rate": r["accept_rate"],
             "walker_status_nonzero": sum(1 for s in r["status"] if s)}
     if r["tuning"]["candidates"]:
         line["autotune"] = r["tuning"]
+    if r["fp64"]:
+        c = r["fp64"]
+        line["vs_fp64"] = dict(c, ratio_vs_fp64_batch=r["value"] / c["fp64_batch_value"],
+                               ratio_vs_fp64_single_walker=r["value"] / c["fp64_single_walker_value"])
     print(json.dumps(line))
 
 

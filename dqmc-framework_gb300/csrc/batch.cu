@@ -24,6 +24,7 @@
 
 #include "../../include/dqmc_gb300.h"
 #include "dqmc_device.cuh"
+#include "ozaki.cuh"
 
 namespace dqmc {
 cudaError_t configure_fp64_kernels(int maxN);
@@ -36,8 +37,12 @@ double run_fp64_probe(cudaError_t* err);
 void launch_bump(unsigned long long* ctr, cudaStream_t st);
 // general (N > 64) walkers, kernels_general.cu
 cudaError_t configure_general_kernels();
-void general_slice(int mode, const WalkerDev* W, int nw, int j, int q, int maxN, int measure, bool any_dense,
-                   bool any_cb, bool mixed, int kd, int smax, int tc_flush, cudaStream_t st);
+void general_slice_pre(int mode, const WalkerDev* W, int nw, int j, int q, int maxN, bool any_dense, bool any_cb,
+                       bool mixed, cudaStream_t st);
+void general_slice_metro(int mode, const WalkerDev* W, int nw, int j, int q, int maxN, int measure, bool mixed,
+                         int kd, int smax, int tc_flush, cudaStream_t st);
+void general_slice_post(int mode, const WalkerDev* W, int nw, int j, int q, int maxN, bool any_dense, bool any_cb,
+                        bool mixed, cudaStream_t st);
 void launch_metropolis_delayed(bool mixed, const WalkerDev* W, int nw, int mode, int j, int q, int maxN, int S_max,
                                int KD, int tc_flush, cudaStream_t st);
 size_t delayed_smem_bytes_host(int N, int S, int KD);
@@ -241,8 +246,8 @@ struct dqmc_batch {
   std::vector<Mark> marks;
   std::vector<Mark> pmarks[3][2];  // event nodes of the profiled graphs
   std::vector<cudaEvent_t> pool;
-  double prof_ms[DQMC_NUM_KCLASS] = {0, 0, 0, 0};
-  int64_t prof_n[DQMC_NUM_KCLASS] = {0, 0, 0, 0};
+  double prof_ms[DQMC_NUM_KCLASS] = {};
+  int64_t prof_n[DQMC_NUM_KCLASS] = {};
   cudaEvent_t ev() {
     if (pool.empty()) {
       cudaEvent_t e;
@@ -358,7 +363,7 @@ int dqmc_batch_create(const dqmc_walker_desc* descs, int n, const dqmc_batch_opt
     const size_t lvl = (2 * (size_t)N * N + N + 31) & ~(size_t)31;
     const bool general = N > kMaxSmemN || o.precision == DQMC_MIXED;
     const int ldk = (N + 15) / 16 * 16;
-    off[w].sl = (o.precision == DQMC_MIXED) ? take(sizeof(unsigned short) * S * 7 * (size_t)N * ldk) : 0;
+    off[w].sl = (o.precision == DQMC_MIXED) ? take(sizeof(unsigned short) * S * ozaki::kMaxSlices * (size_t)N * ldk) : 0;
     off[w].sle = (o.precision == DQMC_MIXED) ? take(sizeof(int) * S * (size_t)N) : 0;
     off[w].G = take(sizeof(double) * 2 * N * N);
     off[w].chain = take(sizeof(double) * (general ? 2 : 1) * S * N * N);
@@ -392,7 +397,7 @@ int dqmc_batch_create(const dqmc_walker_desc* descs, int n, const dqmc_batch_opt
     dense_off[i] = take(sizeof(double) * 2 * nn);
     if (o.precision == DQMC_MIXED) {  // 4 sliced copies: expK (A, B roles), invK (A, B roles)
       const int N = dense_n[i], ldk = (N + 15) / 16 * 16;
-      dense_sl[i] = take(sizeof(unsigned short) * 4 * 7 * (size_t)N * ldk);
+      dense_sl[i] = take(sizeof(unsigned short) * 4 * ozaki::kMaxSlices * (size_t)N * ldk);
       dense_sle[i] = take(sizeof(int) * 4 * (size_t)N);
     }
   }
@@ -436,8 +441,9 @@ int dqmc_batch_create(const dqmc_walker_desc* descs, int n, const dqmc_batch_opt
                     cudaMemcpyHostToDevice, b->stream);
     if (o.precision == DQMC_MIXED) {
       const int N = dense_n[i], ldk = (N + 15) / 16 * 16;
-      const auto cfg = N <= 256 ? std::make_pair(7, 6) : std::make_pair(6, 7);
-      const size_t one = 7 * (size_t)N * ldk;
+      const auto c = ozaki::cfg_for_k(N);
+      const auto cfg = std::make_pair(c.bits, c.slices);
+      const size_t one = ozaki::kMaxSlices * (size_t)N * ldk;
       auto* sl = reinterpret_cast<unsigned short*>(base + dense_sl[i]);
       auto* se = reinterpret_cast<int*>(base + dense_sle[i]);
       const double* ek = reinterpret_cast<const double*>(base + dense_off[i]);
@@ -502,13 +508,13 @@ int dqmc_batch_create(const dqmc_walker_desc* descs, int n, const dqmc_batch_opt
     h.ozstab = uses_ozstab(N, o.precision) ? 1 : 0;
     if (o.precision == DQMC_MIXED) {
       h.ldk = (N + 15) / 16 * 16;
-      h.slice_bits = N <= 256 ? 7 : 6;
-      h.slices = N <= 256 ? 6 : 7;
+      h.slice_bits = ozaki::cfg_for_k(N).bits;
+      h.slices = ozaki::cfg_for_k(N).slices;
       h.sl = reinterpret_cast<unsigned short*>(base + off[w].sl);
       h.sle = reinterpret_cast<int*>(base + off[w].sle);
       if (off[w].dense_id >= 0) {
         const int id = off[w].dense_id;
-        const size_t one = 7 * (size_t)N * h.ldk;
+        const size_t one = ozaki::kMaxSlices * (size_t)N * h.ldk;
         auto* sl = reinterpret_cast<const unsigned short*>(base + dense_sl[id]);
         auto* se = reinterpret_cast<const int*>(base + dense_sle[id]);
         h.kA = sl; h.kB = sl + one; h.iA = sl + 2 * one; h.iB = sl + 3 * one;
@@ -716,8 +722,8 @@ int dqmc_init_greens(dqmc_batch* b) {
     if (b->any_general) {
       general_chain_init(MODE_INIT, b->dW, b->nw, j, b->stream);
       for (int q = 0; q < b->maxPace_general; ++q)
-        general_slice(MODE_INIT, b->dW, b->nw, j, q, b->maxN_general, 0, b->any_general_dense, b->any_general_cb,
-                      b->mixed, b->kd, b->smax, b->tc_flush, b->stream);
+        general_slice_post(MODE_INIT, b->dW, b->nw, j, q, b->maxN_general, b->any_general_dense, b->any_general_cb,
+                           b->mixed, b->stream);  // the transposed B-chain of the initial right stack
       general_push(MODE_INIT, b->dW, b->nw, j, b->maxN_general, b->stream);
       if (b->any_ozstab) oz_push(MODE_INIT, b->dW, b->nw, j, b->maxN_oz, b->stream);
     }
@@ -764,12 +770,21 @@ static void issue_half_sweep(dqmc_batch* b, int mode, int measure) {
         b->timed(DQMC_KCLASS_MEASURE, [&] { launch_measure(mode, b->dW, b->nw, j, b->maxN_small, b->stream); });
     }
     if (b->any_general) {
-      b->timed(DQMC_KCLASS_SEGMENT, [&] {
-        general_chain_init(mode, b->dW, b->nw, j, b->stream);
-        for (int q = 0; q < b->maxPace_general; ++q)
-          general_slice(mode, b->dW, b->nw, j, q, b->maxN_general, measure, b->any_general_dense,
-                        b->any_general_cb, b->mixed, b->kd, b->smax, b->tc_flush, b->stream);
-      });
+      b->timed(DQMC_KCLASS_SEGMENT, [&] { general_chain_init(mode, b->dW, b->nw, j, b->stream); });
+      for (int q = 0; q < b->maxPace_general; ++q) {
+        b->timed(DQMC_KCLASS_PRODUCT, [&] {
+          general_slice_pre(mode, b->dW, b->nw, j, q, b->maxN_general, b->any_general_dense, b->any_general_cb,
+                            b->mixed, b->stream);
+        });
+        b->timed(DQMC_KCLASS_METROPOLIS, [&] {
+          general_slice_metro(mode, b->dW, b->nw, j, q, b->maxN_general, measure, b->mixed, b->kd, b->smax,
+                              b->tc_flush, b->stream);
+        });
+        b->timed(DQMC_KCLASS_PRODUCT, [&] {
+          general_slice_post(mode, b->dW, b->nw, j, q, b->maxN_general, b->any_general_dense, b->any_general_cb,
+                             b->mixed, b->stream);
+        });
+      }
       b->timed(DQMC_KCLASS_PUSH, [&] {
         general_push(mode, b->dW, b->nw, j, b->maxN_general, b->stream);
         if (b->any_ozstab) oz_push(mode, b->dW, b->nw, j, b->maxN_oz, b->stream);
@@ -1133,7 +1148,7 @@ int dqmc_product_check(int n, const double* a, const double* b, double* c) {
   // every piece 256-byte aligned (the product kernel copies slices in 16-byte chunks)
   const size_t o_b = align256(nn * sizeof(double)), o_c = o_b + align256(nn * sizeof(double));
   const size_t o_sa = o_c + align256(nn * sizeof(double));
-  const size_t sl_bytes = align256(7 * (size_t)n * ldk * sizeof(unsigned short));
+  const size_t sl_bytes = align256(ozaki::kMaxSlices * (size_t)n * ldk * sizeof(unsigned short));
   const size_t o_sb = o_sa + sl_bytes, o_ea = o_sb + sl_bytes, o_eb = o_ea + align256(n * sizeof(int));
   const size_t bytes = o_eb + align256(n * sizeof(int));
   char* buf = nullptr;

@@ -1119,28 +1119,40 @@ void launch_metropolis_delayed(bool mixed, const WalkerDev* W, int nw, int mode,
                                int KD, int tc_flush, cudaStream_t st);
 void launch_metropolis_sub(const WalkerDev* W, int nw, int mode, int j, int q, int maxN, int S_max, cudaStream_t st);
 
-void general_slice(int mode, const WalkerDev* W, int nw, int j, int q, int maxN, int measure, bool any_dense,
-                   bool any_cb, bool mixed, int kd, int smax, int tc_flush, cudaStream_t st) {
+// One slice of general walkers in three launch groups (timed separately by the
+// host): the dense products before the updates (forward wrap), the Metropolis
+// updates with the fused measurement, and the products after them (B-chain
+// step and backward wrap).
+void general_slice_pre(int mode, const WalkerDev* W, int nw, int j, int q, int maxN, bool any_dense, bool any_cb,
+                       bool mixed, cudaStream_t st) {
+  if (mode != MODE_FWD) return;
   // in a mixed batch the dense products go through the tensor cores (kernels_ozaki.cu)
+  const bool fp64_dense = any_dense && !mixed;
+  const dim3 g = gemm_grid(maxN, nw);
+  if (fp64_dense) {
+    gemm_op_kernel<OP_WL_FWD><<<g, 256, 0, st>>>(W, mode, j, q, -1);
+    gemm_op_kernel<OP_WR_FWD><<<g, 256, 0, st>>>(W, mode, j, q, -1);
+  }
+  if (any_dense && mixed) mixed_wrap_fwd(W, nw, maxN, j, q, st);
+  if (any_cb) cb_general_kernel<<<2 * nw, 256, sizeof(double) * 2 * maxN, st>>>(W, mode, j, q, 0);
+}
+
+void general_slice_metro(int mode, const WalkerDev* W, int nw, int j, int q, int maxN, int measure, bool mixed,
+                         int kd, int smax, int tc_flush, cudaStream_t st) {
+  if (mode == MODE_INIT) return;
+  const size_t met_sm = sizeof(double) * 6 * maxN + maxN + 16;
+  if (mixed && tc_flush == 2) launch_metropolis_sub(W, nw, mode, j, q, maxN, smax, st);
+  else if (kd > 0) launch_metropolis_delayed(mixed, W, nw, mode, j, q, maxN, smax, kd, tc_flush, st);
+  else metropolis_general_kernel<<<nw, kMetroThreads, met_sm, st>>>(W, mode, j, q);
+  if (measure) measure_general_kernel<<<nw, 256, sizeof(double) * 2 * maxN, st>>>(W, mode, j, q, 0);
+}
+
+void general_slice_post(int mode, const WalkerDev* W, int nw, int j, int q, int maxN, bool any_dense, bool any_cb,
+                        bool mixed, cudaStream_t st) {
   const bool fp64_dense = any_dense && !mixed;
   const bool mixed_dense = any_dense && mixed;
   const dim3 g = gemm_grid(maxN, nw);
   const size_t cb_sm = sizeof(double) * 2 * maxN;
-  const size_t met_sm = sizeof(double) * 6 * maxN + maxN + 16;
-  if (mode == MODE_FWD) {
-    if (fp64_dense) {
-      gemm_op_kernel<OP_WL_FWD><<<g, 256, 0, st>>>(W, mode, j, q, -1);
-      gemm_op_kernel<OP_WR_FWD><<<g, 256, 0, st>>>(W, mode, j, q, -1);
-    }
-    if (mixed_dense) mixed_wrap_fwd(W, nw, maxN, j, q, st);
-    if (any_cb) cb_general_kernel<<<2 * nw, 256, cb_sm, st>>>(W, mode, j, q, 0);
-  }
-  if (mode != MODE_INIT) {
-    if (mixed && tc_flush == 2) launch_metropolis_sub(W, nw, mode, j, q, maxN, smax, st);
-    else if (kd > 0) launch_metropolis_delayed(mixed, W, nw, mode, j, q, maxN, smax, kd, tc_flush, st);
-    else metropolis_general_kernel<<<nw, kMetroThreads, met_sm, st>>>(W, mode, j, q);
-    if (measure) measure_general_kernel<<<nw, 256, sizeof(double) * 2 * maxN, st>>>(W, mode, j, q, 0);
-  }
   if (fp64_dense) {
     if (mode == MODE_FWD) gemm_op_kernel<OP_CH_FWD><<<g, 256, 0, st>>>(W, mode, j, q, -1);
     else gemm_op_kernel<OP_CH_BWD><<<g, 256, 0, st>>>(W, mode, j, q, -1);

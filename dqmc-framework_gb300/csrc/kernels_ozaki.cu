@@ -1,5 +1,5 @@
 // kernels_ozaki.cu — the mixed-precision products of the sweep: FP64-accurate
-// (42-bit) matrix products on the BF16 tensor cores (see ozaki.cuh).
+// (49-bit) matrix products on the BF16 tensor cores (see ozaki.cuh).
 //
 // Slicing is integer work on the FP64 bit patterns; the product runs the
 // S(S+1)/2 slice pairs on the BF16 tensor cores (tcgen05, TMEM accumulators;
@@ -84,9 +84,9 @@ __device__ void slice_lines(const SliceJob& job, int N, int ldk, int role, int b
       const int line = line0 + ll, k = k0 + kk;
       if (line < N && k < ldk) {
         bool neg;
-        const unsigned long long q = ozaki::fixed42(s_t[ll][kk], s_e[0][ll], neg);
+        const unsigned long long q = ozaki::fixedq(s_t[ll][kk], s_e[0][ll], bits * slices, neg);
         for (int s = 0; s < slices; ++s)
-          job.out[((long long)s * N + line) * ldk + k] = ozaki::slice_bf16(q, s, bits, neg);
+          job.out[((long long)s * N + line) * ldk + k] = ozaki::slice_bf16q(q, s, bits, bits * slices, neg);
       }
     }
     __syncthreads();
@@ -202,11 +202,14 @@ __device__ void ozaki_product_tile(const ProdJob& job, int N, int ldk, int bits,
         const int r = r0 + wm * 32 + mt * 16 + g + ((v >> 1) << 3);
         const int c = c0 + wn * 16 + nt * 8 + 2 * t4 + (v & 1);
         if (r >= N || c >= N) continue;
-        // integer Horner: v = sum_m S_m 2^{bits (S-1-m)}, value = v 2^{ea+eb-bits (S+1)}
-        long long s = 0;
+        // integer Horner in two halves (groups 0-3 and 4..S-1), each exact in 64 bits
+        long long hi = 0, lo = 0;
 #pragma unroll
-        for (int m = 0; m < S; ++m) s = (s << bits) + (long long)__float2int_rn(acc[m][mt][nt][v]);
-        epi(r, c, ozaki::ldexp_i64(s, job.ea[r] + job.eb[c] - bits * (S + 1)));
+        for (int m = 0; m < 4; ++m) hi = (hi << bits) + (long long)__float2int_rn(acc[m][mt][nt][v]);
+#pragma unroll
+        for (int m = 4; m < S; ++m) lo = (lo << bits) + (long long)__float2int_rn(acc[m][mt][nt][v]);
+        const int e = job.ea[r] + job.eb[c];
+        epi(r, c, ozaki::ldexp_i64(hi, e - 5 * bits) + ozaki::ldexp_i64(lo, e - bits * (S + 1)));
       }
 }
 
@@ -401,10 +404,13 @@ __global__ void __launch_bounds__(256, 1) oz_prod_tc_kernel(const WalkerDev* __r
         for (int u = 0; u < 16; ++u) {
           const int cl = cc + u, col = c0 + cl;
           if (col >= N) continue;
-          long long sv = 0;
+          long long hi = 0, lo = 0;
 #pragma unroll
-          for (int m = 0; m < S; ++m) sv = (sv << bits) + (long long)__float2int_rn(__uint_as_float(v[m][u]));
-          double val = ozaki::ldexp_i64(sv, eA[rl] + eB[cl] - bits * (S + 1));
+          for (int m = 0; m < 4; ++m) hi = (hi << bits) + (long long)__float2int_rn(__uint_as_float(v[m][u]));
+#pragma unroll
+          for (int m = 4; m < S; ++m) lo = (lo << bits) + (long long)__float2int_rn(__uint_as_float(v[m][u]));
+          const int e = eA[rl] + eB[cl];
+          double val = ozaki::ldexp_i64(hi, e - 5 * bits) + ozaki::ldexp_i64(lo, e - bits * (S + 1));
           if (OP == OZ_WL_FWD || OP == OZ_CH_FWD) val *= s_scale[rl];
           if (OP == OZ_WR_FWD) val *= s_scale[cl];
           out[(long long)col * N + r] = val;
@@ -434,8 +440,8 @@ __global__ void __launch_bounds__(256) oz_selftest_prod_kernel(const unsigned sh
   ProdJob job{As, Bs, ea, eb};
   const int r0 = blockIdx.y * 64, c0 = blockIdx.x * 64;
   auto epi = [&](int r, int c, double v) { C[(long long)c * N + r] = v; };
-  if (S == 6) ozaki_product_tile<6>(job, N, ldk, bits, r0, c0, ozsm, epi);
-  else ozaki_product_tile<7>(job, N, ldk, bits, r0, c0, ozsm, epi);
+  if (S == 7) ozaki_product_tile<7>(job, N, ldk, bits, r0, c0, ozsm, epi);
+  else ozaki_product_tile<8>(job, N, ldk, bits, r0, c0, ozsm, epi);
 }
 
 static size_t oz_tc_smem(int S) { return 2ull * S * (128 + 64) * 32 * 2; }
@@ -443,14 +449,14 @@ size_t oz_prod_smem(int S) { return sizeof(unsigned short) * 2 * 2 * S * 64 * kO
 
 cudaError_t configure_ozaki_kernels() {
   cudaError_t e;
-#define OZCFG(...) if ((e = cudaFuncSetAttribute(__VA_ARGS__, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)oz_tc_smem(7)))) return e
-  OZCFG(oz_prod_tc_kernel<OZ_WL_FWD, 6>); OZCFG(oz_prod_tc_kernel<OZ_WR_FWD, 6>); OZCFG(oz_prod_tc_kernel<OZ_CH_FWD, 6>);
-  OZCFG(oz_prod_tc_kernel<OZ_CH_BWD, 6>); OZCFG(oz_prod_tc_kernel<OZ_WR_BWD, 6>); OZCFG(oz_prod_tc_kernel<OZ_WL_BWD, 6>);
+#define OZCFG(...) if ((e = cudaFuncSetAttribute(__VA_ARGS__, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)oz_tc_smem(8)))) return e
   OZCFG(oz_prod_tc_kernel<OZ_WL_FWD, 7>); OZCFG(oz_prod_tc_kernel<OZ_WR_FWD, 7>); OZCFG(oz_prod_tc_kernel<OZ_CH_FWD, 7>);
   OZCFG(oz_prod_tc_kernel<OZ_CH_BWD, 7>); OZCFG(oz_prod_tc_kernel<OZ_WR_BWD, 7>); OZCFG(oz_prod_tc_kernel<OZ_WL_BWD, 7>);
+  OZCFG(oz_prod_tc_kernel<OZ_WL_FWD, 8>); OZCFG(oz_prod_tc_kernel<OZ_WR_FWD, 8>); OZCFG(oz_prod_tc_kernel<OZ_CH_FWD, 8>);
+  OZCFG(oz_prod_tc_kernel<OZ_CH_BWD, 8>); OZCFG(oz_prod_tc_kernel<OZ_WR_BWD, 8>); OZCFG(oz_prod_tc_kernel<OZ_WL_BWD, 8>);
 #undef OZCFG
   if ((e = cudaFuncSetAttribute(oz_selftest_prod_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)oz_prod_smem(7))))
+                                (int)oz_prod_smem(8))))
     return e;
   return cudaSuccess;
 }
@@ -459,8 +465,8 @@ template <int OP>
 static void oz_op(const WalkerDev* W, int nw, int maxN, int mode, int j, int q, cudaStream_t st) {
   oz_slice_kernel<OP><<<dim3((maxN + 31) / 32, 2 * nw), 256, 0, st>>>(W, mode, j, q);
   const dim3 g((maxN + 63) / 64, (maxN + 127) / 128, 2 * nw);
-  oz_prod_tc_kernel<OP, 6><<<g, 256, oz_tc_smem(6), st>>>(W, mode, j, q);
-  if (maxN > 256) oz_prod_tc_kernel<OP, 7><<<g, 256, oz_tc_smem(7), st>>>(W, mode, j, q);
+  oz_prod_tc_kernel<OP, 7><<<g, 256, oz_tc_smem(7), st>>>(W, mode, j, q);
+  if (maxN > 256) oz_prod_tc_kernel<OP, 8><<<g, 256, oz_tc_smem(8), st>>>(W, mode, j, q);
 }
 
 // the slice work of mixed walkers (wraps and chain through the tensor cores)

@@ -17,7 +17,7 @@
 // After the block
 //     G = G0 - G0(:,I_A) Gamma R_A,   Gamma = sum_q a_q b_q^T   (m x m),
 // the Sherman-Morrison-Woodbury form of the m flips, applied as two products
-// on the BF16 tensor cores through exact 42-bit integer slices (ozaki.cuh):
+// on the BF16 tensor cores through exact 42-bit integer slices (ozaki.cuh; K <= 32 per flush):
 // T = Gamma R_A (m x N), then G -= G0(:,I_A) T (N x N, K = m).
 //
 // The decisions use the reference's ratio formula, evaluated with the same

@@ -7,7 +7,7 @@
 // embedding that forbids allocation inside its time loop), or a plugin whose
 // host grants it no allocation rights.  dqmc_product_device_noalloc serves
 // them: the caller passes device buffers for A, B and C, and the BF16 slice
-// scratch lives in the file-scope array below, a fixed 1.5 MB reserved in
+// scratch lives in the file-scope array below, a fixed 1.75 MB reserved in
 // every GPU that loads the library until the process exits.
 //
 // The array is shared by all calls on a device and keeps the last call's
@@ -31,8 +31,8 @@ int set_last_error(int code, const char* msg);
 
 namespace {
 
-constexpr int kNoAllocMaxN = 256;                        // 7-bit x 6 slices, ldk = N
-constexpr size_t kSliceElems = 6ull * kNoAllocMaxN * kNoAllocMaxN;
+constexpr int kNoAllocMaxN = 256;                        // 7-bit x 7 slices, ldk = N
+constexpr size_t kSliceElems = 7ull * kNoAllocMaxN * kNoAllocMaxN;
 constexpr size_t kScratchBytes = 2 * kSliceElems * sizeof(unsigned short)  // A and B slices
                                  + 2 * kNoAllocMaxN * sizeof(int);          // row / column exponents
 
@@ -49,7 +49,7 @@ bool g_ready[kMaxDevices] = {false};
 extern "C" int dqmc_product_device_noalloc(int n, const double* a, const double* b, double* c, void* stream) {
   if (n < 1 || n > kNoAllocMaxN)
     return dqmc::set_last_error(DQMC_ERR_ARG,
-                                "dqmc_product_device_noalloc: n must be in [1, 256] (fixed 1.5 MB scratch)");
+                                "dqmc_product_device_noalloc: n must be in [1, 256] (fixed 1.75 MB scratch)");
   if (!a || !b || !c) return dqmc::set_last_error(DQMC_ERR_ARG, "dqmc_product_device_noalloc: null pointer");
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);

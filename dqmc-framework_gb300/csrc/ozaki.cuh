@@ -10,27 +10,50 @@
 // groups m >= 4 carry weights 2^{-4B} and below, where FP32 rounding is far
 // under the kept precision.  The product is
 //     C(r,c) = 2^{e_r + f_c} sum_m 2^{-B(m+2)} S_m(r,c),   S_m = sum_{i+j=m} A_i B_j.
-// B = 7, S = 6 (42 bits, 21 slice products) for K <= 256; B = 6, S = 7
-// (42 bits, 28 products) for K <= 1024.  This is the splitting scheme of Ozaki,
-// Ogita, Oishi and Rump (Numer. Algorithms 2012) restated for BF16 inputs.
+// The sweep's wraps and B-chain use B = 7, S = 7 (49 bits, 28 slice products)
+// for K <= 256 and B = 6, S = 8 (48 bits, 36 products) for K <= 1024: at
+// beta = 10 the chain of a stabilization interval amplifies the truncation of
+// 42-bit products into |dG| of a few 1e-6, 49 bits keep it near 1e-8.  The
+// rank-k Metropolis flushes (K <= 32) use B = 7, S = 6.  This is the splitting
+// scheme of Ozaki, Ogita, Oishi and Rump (Numer. Algorithms 2012) restated for
+// BF16 inputs.
 #pragma once
 #include <cstdint>
 
 namespace dqmc {
 namespace ozaki {
 
-constexpr int kMaxSlices = 7;
+constexpr int kMaxSlices = 8;
 
 struct SliceCfg {
   int bits, slices;
 };
-__host__ __device__ inline SliceCfg cfg_for_k(int K) { return K <= 256 ? SliceCfg{7, 6} : SliceCfg{6, 7}; }
+__host__ __device__ inline SliceCfg cfg_for_k(int K) { return K <= 256 ? SliceCfg{7, 7} : SliceCfg{6, 8}; }
 
 // exponent e with |x| < 2^e (0 for x == 0); integer only
 __device__ __forceinline__ int exp_bound(double x) {
   const unsigned long long b = (unsigned long long)__double_as_longlong(x);
   const int ex = (int)((b >> 52) & 0x7ff);
   return ex == 0 ? -1100 : ex - 1022;  // normal: |x| in [2^(ex-1023), 2^(ex-1022))
+}
+
+// Q-bit truncated fixed-point magnitude of |x| / 2^e (e >= exp_bound(x), Q <= 62), and sign
+__device__ __forceinline__ unsigned long long fixedq(double x, int e, int Q, bool& neg) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  neg = (b >> 63) != 0;
+  const int ex = (int)((b >> 52) & 0x7ff);
+  if (ex == 0) return 0ULL;
+  const unsigned long long m = (b & 0xFFFFFFFFFFFFFULL) | 0x10000000000000ULL;
+  const int s = ex - 1075 - e + Q;  // |x| 2^{Q-e} = m 2^s, s <= Q - 53
+  if (s >= 0) return m << s;
+  if (s <= -64) return 0ULL;
+  return m >> (-s);
+}
+// slice i of a Q-bit magnitude with B bits per slice, as a signed BF16 bit pattern
+__device__ __forceinline__ unsigned short slice_bf16q(unsigned long long q, int i, int bits, int Q, bool neg) {
+  const unsigned v = (unsigned)((q >> (Q - bits * (i + 1))) & ((1u << bits) - 1));
+  const float f = neg ? -(float)v : (float)v;  // exact: v < 2^8
+  return (unsigned short)(__float_as_uint(f) >> 16);
 }
 
 // 42-bit truncated fixed-point magnitude of |x| / 2^e (e >= exp_bound(x)), and sign

@@ -38,7 +38,7 @@ EXPORTS = [
     "dqmc_product_check", "dqmc_product_device_noalloc", "dqmc_launch_count", "dqmc_tuning",
     "dqmc_sweep_dynamic", "dqmc_get_dynamic", "dqmc_clear_dynamic", "dqmc_get_green_dynamic",
 ]
-KCLASSES = ["segment", "push", "greens", "measure"]
+KCLASSES = ["segment", "push", "greens", "measure", "product", "metropolis"]
 
 
 class DqmcError(RuntimeError):

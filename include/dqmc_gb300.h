@@ -48,9 +48,12 @@ enum dqmc_rng {
 
 enum dqmc_precision {
   DQMC_FP64 = 0,  /* plain method: every product in FP64 */
-  DQMC_MIXED = 1  /* wraps and B-chain products on the BF16 tensor cores, split into exact
-                     integer slices and recombined to 42 bits; Metropolis ratios, rank-1
-                     updates, UDT stabilization and Green's assembly stay FP64 */
+  DQMC_MIXED = 1  /* tensor-core path: wraps and B-chain products on the BF16 tensor cores
+                     (tcgen05), split into exact integer slices and recombined to 49 bits
+                     (48 for N > 256); Metropolis by submatrix updates with 42-bit block
+                     flushes; for 128 <= N <= 768 the UDT push and Green's assembly by
+                     blocked Householder QR whose products carry 56 bits (FP64 class),
+                     FP64 panels; Metropolis ratios and all reductions in FP64 */
 };
 
 /* Observable slots, the equal-time list of src/measure/observable_handler.cpp:11-20
@@ -198,7 +201,9 @@ int dqmc_launch_count(dqmc_batch* b, int64_t* launches);
  * has only a whole-run wall-clock timer, src/dqmc.cpp:37-41).  Classes:
  * 0 segment, 1 push, 2 greens, 3 measure.  Enabling resets the totals. */
 enum { DQMC_KCLASS_SEGMENT = 0, DQMC_KCLASS_PUSH = 1, DQMC_KCLASS_GREENS = 2, DQMC_KCLASS_MEASURE = 3,
-       DQMC_NUM_KCLASS = 4 };
+       DQMC_KCLASS_PRODUCT = 4,     /* HBM walkers: dense products of a slice (wraps, B-chain step) */
+       DQMC_KCLASS_METROPOLIS = 5,  /* HBM walkers: Metropolis updates of a slice (+ fused measurement) */
+       DQMC_NUM_KCLASS = 6 };
 int dqmc_profile_enable(dqmc_batch* b, int on);
 int dqmc_profile_read(dqmc_batch* b, int kclass, double* total_ms, int64_t* launches);
 
@@ -210,7 +215,7 @@ int dqmc_product_check(int n, const double* a, const double* b, double* c);
 /* The same product for callers that cannot allocate device memory (inside a
  * CUDA-graph capture, or under a host framework that owns all device memory):
  * a, b, c are the caller's device buffers (column-major n x n doubles) and the
- * BF16 slice scratch is a fixed 1.5 MB array in the library's device image, so
+ * BF16 slice scratch is a fixed 1.75 MB array in the library's device image, so
  * the call allocates nothing.  Limit: n <= 256 (larger n is rejected with
  * DQMC_ERR_ARG).  All calls on a device share that scratch: calls that overlap
  * on the GPU race, so the caller serialises them.  The first call on a device

@@ -1,5 +1,5 @@
 """Mixed-precision path (DQMC_MIXED): wraps and B-chain products on the BF16
-tensor cores through exact integer slices (42-bit), FP64 everywhere else.
+tensor cores through exact integer slices (49-bit), FP64 everywhere else.
 
 Bars: the product engine agrees with FP64 to 2^-38 of |A||B| (normwise) and is
 exact on integer inputs; the mixed sweep keeps max|dG| <= 1e-6 against the FP64
@@ -61,6 +61,7 @@ def _run(dq, descs, precision, sweeps=1):
     (1, 16, 4.0, -0.5, 2.0, 20, 8),    # 16x16
     (0, 12, 4.0, 0.0, 2.0, 20, 5),     # repulsive N = 144: tensor-core QR, two spins, partial panel
     (1, 12, 3.0, -0.3, 2.0, 20, 10),   # attractive N = 144
+    (1, 16, 4.0, -0.5, 10.0, 100, 8),  # the mixed-precision configuration itself (beta = 10)
 ])
 def test_mixed_sweep_dG_against_fp64(dq, model, L, U, mu, beta, Lt, pace):
     descs = [dq.WalkerDesc(model=model, L=L, U=U, mu=mu, beta=beta, Lt=Lt, pace=pace, seed=100 + w) for w in range(2)]
