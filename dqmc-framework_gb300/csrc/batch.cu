@@ -345,7 +345,7 @@ int dqmc_batch_create(const dqmc_walker_desc* descs, int n, const dqmc_batch_opt
   if (b->mixed) b->tc_flush = 2;  // submatrix updates until the tuner has timed the candidates
 
   // ---- arena layout ----
-  struct Off { size_t G, chain, work, scr, sl, sle, stack, fields, ff, trace, msub; int dense_id; };
+  struct Off { size_t G, chain, work, scr, sl, sle, stack, fields, ff, trace, msub, zsl; int dense_id; };
   std::vector<Off> off(n);
   std::map<std::tuple<int, double, double, double>, int> dense_ids;  // (L, t, mu, dtau) -> id
   std::vector<std::pair<std::vector<double>, std::vector<double>>> dense;
@@ -373,6 +373,8 @@ int dqmc_batch_create(const dqmc_walker_desc* descs, int n, const dqmc_batch_opt
     off[w].fields = take((size_t)d.Lt * N);
     off[w].trace = b->trace_cap ? take(sizeof(double) * (size_t)b->trace_cap * 2 * N * N) : 0;
     off[w].msub = (o.precision == DQMC_MIXED) ? take((size_t)S * submatrix_scratch_bytes(N)) : 0;
+    off[w].zsl = uses_ozstab(N, o.precision)
+                     ? take(sizeof(unsigned short) * (size_t)S * 2 * 9 * N * (size_t)((N + 31) / 32 * 32)) : 0;
     off[w].dense_id = -1;
     if (!d.checkerboard) {
       auto key = std::make_tuple(d.L, d.hopping_t, d.mu, d.beta / d.Lt);
@@ -506,6 +508,8 @@ int dqmc_batch_create(const dqmc_walker_desc* descs, int n, const dqmc_batch_opt
     h.scr = gen ? reinterpret_cast<double*>(base + off[w].scr) : nullptr;
     h.msub = (o.precision == DQMC_MIXED) ? reinterpret_cast<unsigned char*>(base + off[w].msub) : nullptr;
     h.ozstab = uses_ozstab(N, o.precision) ? 1 : 0;
+    h.zld = (N + 31) / 32 * 32;
+    h.zsl = h.ozstab ? reinterpret_cast<unsigned short*>(base + off[w].zsl) : nullptr;
     if (o.precision == DQMC_MIXED) {
       h.ldk = (N + 15) / 16 * 16;
       h.slice_bits = ozaki::cfg_for_k(N).bits;

@@ -59,7 +59,10 @@ struct WalkerDev {
   long long* dyn_cnt;
   const int* dyn_taus;
   int dyn_ntau;
-  int pad2;
+  int zld;                   // line stride of zsl (N rounded up to 32)
+  // tensor-core stabilization: BF16 slices of both operands of the current product,
+  // [S][2 operands][9 slices][N][zld]
+  unsigned short* zsl;
   // mixed walkers: BF16 slices of the operand being multiplied, [S][slices][N][ldk]
   unsigned short* sl;
   int* sle;                  // slice exponents [S][N]

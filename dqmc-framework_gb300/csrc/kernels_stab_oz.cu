@@ -37,9 +37,6 @@ namespace dqmc {
 namespace {
 
 constexpr int TB = 32;           // Householder panel width
-constexpr int ZT = 64;           // product tile edge
-constexpr int ZK = 32;           // k chunk sliced at a time
-constexpr int ZKP = ZK + 8;      // padded BF16 row (80 bytes)
 
 __device__ __forceinline__ double zwarp_sum(double v) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -272,245 +269,103 @@ __device__ __forceinline__ unsigned long long zfixed(double x, int e, int Q, boo
   if (s <= -64) return 0ULL;
   return mant >> (-s);
 }
-__device__ __forceinline__ unsigned zslice2(unsigned long long q0, bool n0, unsigned long long q1, bool n1, int i,
-                                            int Bb, int Q) {
-  const int sh = Q - Bb * (i + 1);
-  const unsigned m = (1u << Bb) - 1;
-  const unsigned v0 = (unsigned)((q0 >> sh) & m), v1 = (unsigned)((q1 >> sh) & m);
-  const float f0 = n0 ? -(float)v0 : (float)v0, f1 = n1 ? -(float)v1 : (float)v1;
-  return (__float_as_uint(f0) >> 16) | (__float_as_uint(f1) & 0xFFFF0000u);
+
+__device__ __forceinline__ void cp16_async(void* dst, const void* src, bool pred) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  const int n = pred ? 16 : 0;  // 0: zero-fill, nothing is read
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(d), "l"(src), "r"(n));
 }
 
 }  // namespace
 
 // --------------------------------------------------------------------------
-// Batched product C (op)= alpha rs (A B) cs, 64 x 64 tile per CTA, operands
-// sliced in the kernel (S slices of B bits, fraction Q = S B), BF16 MMA.
+// Slicing of both operands of a product, once per product: blockIdx.y = 0 the
+// rows of op(A), 1 the columns of op(B); 32 lines per CTA.  Pass 1: the line
+// exponents (8 k groups per line); pass 2: 32 x 32 tiles staged through
+// shared memory so that loads run along the stored matrix and the BF16 writes
+// along k.  Output: [operand][S][N][zld], zero past K up to a multiple of 32.
 // --------------------------------------------------------------------------
 template <int S, int B>
-__global__ void __launch_bounds__(256) zgemm_kernel(const WalkerDev* __restrict__ W, int op, int mode, int j, int p,
-                                                    int trace_slot) {
+__global__ void __launch_bounds__(256) zslice_kernel(const WalkerDev* __restrict__ W, int op, int mode, int j, int p) {
   const int wi = blockIdx.z >> 1, sp = blockIdx.z & 1;
   const WalkerDev& w = W[wi];
   if (!w.ozstab || sp >= w.S) return;
   ZJob jb;
   if (!zjob(w, op, mode, j, p, sp, jb)) return;
   if ((jb.K <= 256) != (B == 7)) return;
-  const int r0 = blockIdx.y * ZT, c0 = blockIdx.x * ZT;
-  if (r0 >= jb.M || c0 >= jb.N) return;
-  constexpr int Q = S * B;
-  extern __shared__ __align__(16) unsigned short zsm[];
-  unsigned short* sa = zsm;                 // [S][64][ZKP]
-  unsigned short* sb = zsm + S * ZT * ZKP;  // [S][64][ZKP]
-  __shared__ int eA[ZT], eB[ZT];
-  __shared__ int etmp[2][4][ZT];
-  const int tid = threadIdx.x, ll = tid & 63, part = tid >> 6;
-  const int lane = tid & 31, wid = tid >> 5;
-  const int wm = wid >> 2, wn = wid & 3, g = lane >> 2, t4 = lane & 3;
-  {
-    int ea = -1100, eb = -1100;
-    const int r = r0 + ll, c = c0 + ll;
-    // 8 independent loads per operand in flight per step
-    for (int k0 = part * 8; k0 < jb.K; k0 += 32) {
-      double xa[8], xb[8];
-#pragma unroll
-      for (int u = 0; u < 8; ++u) {
-        const int k = k0 + u;
-        xa[u] = (r < jb.M && k < jb.K) ? zel(jb.a, r, k, false) : 0.0;
-        xb[u] = (c < jb.N && k < jb.K) ? zel(jb.b, c, k, true) : 0.0;
-      }
-#pragma unroll
-      for (int u = 0; u < 8; ++u) {
-        ea = max(ea, ozaki::exp_bound(xa[u]));
-        eb = max(eb, ozaki::exp_bound(xb[u]));
-      }
-    }
-    etmp[0][part][ll] = ea;
-    etmp[1][part][ll] = eb;
-  }
-  __syncthreads();
-  if (tid < 128) {
-    const int o = tid >> 6, l = tid & 63;
-    const int e = max(max(etmp[o][0][l], etmp[o][1][l]), max(etmp[o][2][l], etmp[o][3][l]));
-    (o ? eB : eA)[l] = e;
-  }
-  __syncthreads();
-
-  float acc[S][2][2][4];
-#pragma unroll
-  for (int m = 0; m < S; ++m)
-#pragma unroll
-    for (int a = 0; a < 2; ++a)
-#pragma unroll
-      for (int b = 0; b < 2; ++b)
-#pragma unroll
-        for (int v = 0; v < 4; ++v) acc[m][a][b][v] = 0.f;
-
-  for (int k0 = 0; k0 < jb.K; k0 += ZK) {
-#pragma unroll
-    for (int opd = 0; opd < 2; ++opd) {
-      const int line = (opd ? c0 : r0) + ll;
-      const bool ok = line < (opd ? jb.N : jb.M);
-      const int e = (opd ? eB : eA)[ll];
-      unsigned pk[S][4];
-#pragma unroll
-      for (int u = 0; u < 8; u += 2) {
-        const int k = k0 + part * 8 + u;
-        const double x0 = (ok && k < jb.K) ? zel(opd ? jb.b : jb.a, line, k, opd == 1) : 0.0;
-        const double x1 = (ok && k + 1 < jb.K) ? zel(opd ? jb.b : jb.a, line, k + 1, opd == 1) : 0.0;
-        bool n0, n1;
-        const unsigned long long q0 = zfixed(x0, e, Q, n0), q1 = zfixed(x1, e, Q, n1);
-#pragma unroll
-        for (int s = 0; s < S; ++s) pk[s][u >> 1] = zslice2(q0, n0, q1, n1, s, B, Q);
-      }
-      unsigned short* dst = opd ? sb : sa;
-#pragma unroll
-      for (int s = 0; s < S; ++s)
-        *reinterpret_cast<uint4*>(dst + (s * ZT + ll) * ZKP + part * 8) =
-            make_uint4(pk[s][0], pk[s][1], pk[s][2], pk[s][3]);
-    }
-    __syncthreads();
-#pragma unroll
-    for (int kk = 0; kk < ZK; kk += 16) {
-#pragma unroll
-      for (int i = 0; i < S; ++i) {
-        unsigned a[2][4];
-#pragma unroll
-        for (int mt = 0; mt < 2; ++mt) {
-          const unsigned short* pa = sa + (i * ZT + wm * 32 + mt * 16 + g) * ZKP + kk + 2 * t4;
-          a[mt][0] = *(const unsigned*)(pa);
-          a[mt][1] = *(const unsigned*)(pa + 8 * ZKP);
-          a[mt][2] = *(const unsigned*)(pa + 8);
-          a[mt][3] = *(const unsigned*)(pa + 8 * ZKP + 8);
-        }
-#pragma unroll
-        for (int jj = 0; jj < S - i; ++jj) {
-          unsigned bf[2][2];
-#pragma unroll
-          for (int nt = 0; nt < 2; ++nt) {
-            const unsigned short* pb2 = sb + (jj * ZT + wn * 16 + nt * 8 + g) * ZKP + kk + 2 * t4;
-            bf[nt][0] = *(const unsigned*)(pb2);
-            bf[nt][1] = *(const unsigned*)(pb2 + 8);
-          }
-#pragma unroll
-          for (int mt = 0; mt < 2; ++mt)
-#pragma unroll
-            for (int nt = 0; nt < 2; ++nt)
-              ozaki::mma16816(acc[i + jj][mt][nt], a[mt][0], a[mt][1], a[mt][2], a[mt][3], bf[nt][0], bf[nt][1]);
-        }
-      }
-    }
-    __syncthreads();
-  }
-
-  // epilogue: C = 2^{ea+eb} sum_m 2^{-B(m+2)} S_m, the groups summed exactly in two 64-bit halves
-  const long long NN = (long long)w.N * w.N;
-  double err = 0.0;
-  bool finite = true;
-  double* tr = (jb.out && w.trace && trace_slot >= 0 && trace_slot < w.trace_cap)
-                   ? w.trace + ((long long)trace_slot * 2 + sp) * NN : nullptr;
-  const bool check = jb.out && !(mode == MODE_INIT || (mode == MODE_BWD && j == w.nstack - 1));
-#pragma unroll
-  for (int mt = 0; mt < 2; ++mt)
-#pragma unroll
-    for (int nt = 0; nt < 2; ++nt)
-#pragma unroll
-      for (int v = 0; v < 4; ++v) {
-        const int rl = wm * 32 + mt * 16 + g + ((v >> 1) << 3), cl = wn * 16 + nt * 8 + 2 * t4 + (v & 1);
-        const int r = r0 + rl, c = c0 + cl;
-        if (r >= jb.M || c >= jb.N) continue;
-        long long hi = 0, lo = 0;
-#pragma unroll
-        for (int m = 0; m < 4; ++m) hi = (hi << B) + (long long)__float2int_rn(acc[m][mt][nt][v]);
-#pragma unroll
-        for (int m = 4; m < S; ++m) lo = (lo << B) + (long long)__float2int_rn(acc[m][mt][nt][v]);
-        const int e = eA[rl] + eB[cl];
-        double val = ozaki::ldexp_i64(hi, e - 5 * B) + ozaki::ldexp_i64(lo, e - B * (S + 1));
-        if (jb.rs) val *= jb.rs[r];
-        if (jb.cs) val *= jb.cs[c];
-        const long long o = (long long)c * jb.ldc + r;
-        if (!jb.out) {
-          val *= jb.alpha;
-          jb.c[o] = jb.beta ? jb.c[o] + val : val;
-        } else {
-          if (check) err = fmax(err, fabs(val - jb.c[o]));
-          if (!isfinite(val)) finite = false;
-          jb.c[o] = val;
-          if (tr) tr[o] = val;
-          if (w.S == 1) {
-            jb.c[NN + o] = val;
-            if (tr) tr[NN + o] = val;
-          }
-        }
-      }
-  if (jb.out) {
-    if (!finite) atomicOr(w.status, ST_NONFINITE_G);
-    if (check) {
-      for (int o = 16; o > 0; o >>= 1) err = fmax(err, __shfl_xor_sync(0xffffffffu, err, o));
-      if (lane == 0) atomicMax(w.wrap_bits, (unsigned long long)__double_as_longlong(err));
-    }
-  }
-}
-
-
-// --------------------------------------------------------------------------
-// Line exponents of both operands of a product (one pass over the operands,
-// shared by all output tiles): blockIdx.y = 0 rows of op(A), 1 columns of
-// op(B); 32 lines x 8 k groups per CTA.
-// --------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) zexp_kernel(const WalkerDev* __restrict__ W, int op, int mode, int j, int p) {
-  const int wi = blockIdx.z >> 1, sp = blockIdx.z & 1;
-  const WalkerDev& w = W[wi];
-  if (!w.ozstab || sp >= w.S) return;
-  ZJob jb;
-  if (!zjob(w, op, mode, j, p, sp, jb)) return;
   const bool isB = blockIdx.y == 1;
   const ZOpnd& o = isB ? jb.b : jb.a;
   const int nlines = isB ? jb.N : jb.M;
   const int l0 = blockIdx.x * 32;
   if (l0 >= nlines) return;
+  constexpr int Q = S * B;
+  const int N = w.N, ld = w.zld, Kp = (jb.K + 31) / 32 * 32;
+  const ZScr z = zscr(w, sp);
+  unsigned short* out = w.zsl + ((long long)(sp * 2 + (isB ? 1 : 0)) * 9) * N * ld;
   // lines contiguous in memory when the stored row index runs along the line
-  const bool line_fast = (o.tr != (int)isB) ? false : true;
-  const int ll = line_fast ? (threadIdx.x & 31) : (threadIdx.x >> 3);
-  const int kg = line_fast ? (threadIdx.x >> 5) : (threadIdx.x & 7);
-  const int line = l0 + ll;
-  int e = -1100;
-  if (line < nlines)
-    for (int k0 = kg; k0 < jb.K; k0 += 64) {
-      double x[8];
-#pragma unroll
-      for (int u = 0; u < 8; ++u) {
-        const int k = k0 + 8 * u;
-        x[u] = (k < jb.K) ? zel(o, line, k, isB) : 0.0;
-      }
-#pragma unroll
-      for (int u = 0; u < 8; ++u) e = max(e, ozaki::exp_bound(x[u]));
-    }
+  const bool line_fast = (o.tr == (int)isB);
   __shared__ int s_e[8][32];
-  s_e[kg][ll] = e;
+  __shared__ double s_t[32][33];
+  {
+    const int ll = line_fast ? (threadIdx.x & 31) : (threadIdx.x >> 3);
+    const int kg = line_fast ? (threadIdx.x >> 5) : (threadIdx.x & 7);
+    const int line = l0 + ll;
+    int e = -1100;
+    if (line < nlines)
+      for (int k0 = kg; k0 < jb.K; k0 += 64) {
+        double x[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          const int k = k0 + 8 * u;
+          x[u] = (k < jb.K) ? zel(o, line, k, isB) : 0.0;
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u) e = max(e, ozaki::exp_bound(x[u]));
+      }
+    s_e[kg][ll] = e;
+  }
   __syncthreads();
-  if (threadIdx.x < 32 && l0 + threadIdx.x < nlines) {
+  if (threadIdx.x < 32) {
     int m = s_e[0][threadIdx.x];
 #pragma unroll
     for (int q = 1; q < 8; ++q) m = max(m, s_e[q][threadIdx.x]);
-    const ZScr z = zscr(w, sp);
-    (isB ? z.expB : z.expA)[l0 + threadIdx.x] = m;
+    s_e[0][threadIdx.x] = m;
+    if (l0 + threadIdx.x < nlines) (isB ? z.expB : z.expA)[l0 + threadIdx.x] = m;
+  }
+  __syncthreads();
+  for (int k0 = 0; k0 < Kp; k0 += 32) {
+    for (int e = threadIdx.x; e < 32 * 32; e += 256) {
+      const int ll = line_fast ? (e & 31) : (e >> 5), kk = line_fast ? (e >> 5) : (e & 31);
+      const int line = l0 + ll, k = k0 + kk;
+      s_t[ll][kk] = (line < nlines && k < jb.K) ? zel(o, line, k, isB) : 0.0;
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < 32 * 32; e += 256) {
+      const int kk = e & 31, ll = e >> 5, line = l0 + ll;
+      if (line < nlines) {
+        bool neg;
+        const unsigned long long q = zfixed(s_t[ll][kk], s_e[0][ll], Q, neg);
+#pragma unroll
+        for (int s2 = 0; s2 < S; ++s2)
+          out[((long long)s2 * N + line) * ld + k0 + kk] = ozaki::slice_bf16q(q, s2, B, Q, neg);
+      }
+    }
+    __syncthreads();
   }
 }
 
 // --------------------------------------------------------------------------
-// The same product on the 5th-generation tensor cores (tcgen05): a 128 x NT
-// output tile per CTA, the S weight groups accumulated in TMEM (S NT columns).
-// Per 32-deep k chunk, all 256 threads slice both operands into one shared
-// stage (K-major, 8-row x 16-byte core matrices, no swizzle) while the MMAs
-// of the previous chunk run from the other stage; one thread issues the
-// S (S+1) / 2 x 2 MMAs of a chunk and commits them to the stage's mbarrier.
+// The product on the 5th-generation tensor cores (tcgen05): a 128 x NT output
+// tile per CTA, the S weight groups accumulated in TMEM (S NT columns).  The
+// pre-sliced operands stream 32 k at a time through two shared stages
+// (cp.async, 16-byte pieces placed as K-major core matrices, no swizzle); one
+// thread issues the S (S+1) / 2 x 2 MMAs of a chunk and commits them to the
+// stage's mbarrier, so the copies of chunk c+1 overlap the MMAs of chunk c.
 // --------------------------------------------------------------------------
 template <int S, int B, int NT>
 __global__ void __launch_bounds__(256, 1) zgemm_tc_kernel(const WalkerDev* __restrict__ W, int op, int mode, int j,
                                                           int p, int trace_slot) {
   constexpr int MT = 128, KC = 32;
-  constexpr int Q = S * B;
   constexpr int CM = 128;                 // bytes of one core matrix (8 rows x 16 bytes)
   constexpr int RG = (KC / 8) * CM;       // bytes between 8-row groups
   constexpr int A_SL = MT * KC * 2, B_SL = NT * KC * 2;
@@ -531,6 +386,7 @@ __global__ void __launch_bounds__(256, 1) zgemm_tc_kernel(const WalkerDev* __res
   __shared__ int s_fail;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const ZScr z = zscr(w, sp);
+  const int N = w.N, ld = w.zld;
   if (tid < MT) eA[tid] = (r0 + tid < jb.M) ? z.expA[r0 + tid] : -1100;
   if (tid < NT) eB[tid] = (c0 + tid < jb.N) ? z.expB[c0 + tid] : -1100;
   if (tid == 0) {
@@ -546,45 +402,46 @@ __global__ void __launch_bounds__(256, 1) zgemm_tc_kernel(const WalkerDev* __res
   const unsigned taddr = tbase;
   constexpr uint32_t idesc = tc::idesc_bf16(MT, NT);
   const int nch = (jb.K + KC - 1) / KC;
-
-  for (int c = 0; c < nch; ++c) {
-    const int st = c & 1;
+  // this thread's 16-byte pieces per slice and chunk: A lines tid % 128 (k groups tid / 128 and
+  // + 2), B line tid % NT (k group tid / NT, threads < 4 NT)
+  const long long sst = (long long)N * ld;
+  const unsigned short* zA = w.zsl + (long long)(sp * 2) * 9 * sst;
+  const unsigned short* zB = zA + 9 * sst;
+  const int la = tid & (MT - 1), kqa = tid >> 7;
+  const int lb = tid % NT, kqb = tid / NT;
+  const bool va = r0 + la < jb.M, vb = c0 + lb < jb.N && tid < 4 * NT;
+  const unsigned short* srcA = zA + (long long)min(r0 + la, N - 1) * ld + kqa * 8;
+  const unsigned short* srcB = zB + (long long)min(c0 + lb, N - 1) * ld + (kqb & 3) * 8;
+  const int dA = (la & 7) * 16 + kqa * CM + (la >> 3) * RG;
+  const int dB = (lb & 7) * 16 + (kqb & 3) * CM + (lb >> 3) * RG;
+  auto load = [&](int c, int st) {
     unsigned char* sA = tsm + st * STAGE;
     unsigned char* sB = sA + S * A_SL;
-    if (c >= 2 && !tc::mbar_wait(&mbar[st], ((c - 2) >> 1) & 1)) s_fail = 1;
     const int k0 = c * KC;
-    // each thread slices groups of 8 consecutive k of one line (lines fastest: coalesced)
 #pragma unroll
-    for (int opd = 0; opd < 2; ++opd) {
-      const int nl = opd ? NT : MT;
-      unsigned char* base = opd ? sB : sA;
-      for (int gi = tid; gi < nl * (KC / 8); gi += 256) {
-        const int line = gi % nl, kl = (gi / nl) * 8;
-        const int gline = (opd ? c0 : r0) + line;
-        const bool ok = gline < (opd ? jb.N : jb.M);
-        const int e = (opd ? eB : eA)[line];
-        unsigned pk[S][4];
-#pragma unroll
-        for (int u = 0; u < 8; u += 2) {
-          const int k = k0 + kl + u;
-          const double x0 = (ok && k < jb.K) ? zel(opd ? jb.b : jb.a, gline, k, opd == 1) : 0.0;
-          const double x1 = (ok && k + 1 < jb.K) ? zel(opd ? jb.b : jb.a, gline, k + 1, opd == 1) : 0.0;
-          bool n0, n1;
-          const unsigned long long q0 = zfixed(x0, e, Q, n0), q1 = zfixed(x1, e, Q, n1);
-#pragma unroll
-          for (int s2 = 0; s2 < S; ++s2) pk[s2][u >> 1] = zslice2(q0, n0, q1, n1, s2, B, Q);
-        }
-        const int off = (line & 7) * 16 + (kl >> 3) * CM + (line >> 3) * RG;
-#pragma unroll
-        for (int s2 = 0; s2 < S; ++s2)
-          *reinterpret_cast<uint4*>(base + s2 * (opd ? B_SL : A_SL) + off) =
-              make_uint4(pk[s2][0], pk[s2][1], pk[s2][2], pk[s2][3]);
-      }
+    for (int s2 = 0; s2 < S; ++s2) {
+      cp16_async(sA + s2 * A_SL + dA, srcA + s2 * sst + k0, va);
+      cp16_async(sA + s2 * A_SL + dA + 2 * CM, srcA + s2 * sst + k0 + 16, va);
+      if (tid < 4 * NT) cp16_async(sB + s2 * B_SL + dB, srcB + s2 * sst + k0, vb);
+    }
+    asm volatile("cp.async.commit_group;\n" ::);
+  };
+  load(0, 0);
+  for (int c = 0; c < nch; ++c) {
+    const int st = c & 1;
+    if (c + 1 < nch) {
+      if (c >= 1 && !tc::mbar_wait(&mbar[(c + 1) & 1], ((c - 1) >> 1) & 1)) s_fail = 1;
+      load(c + 1, (c + 1) & 1);
+      asm volatile("cp.async.wait_group 1;\n" ::: "memory");
+    } else {
+      asm volatile("cp.async.wait_group 0;\n" ::: "memory");
     }
     tc::fence_proxy_async();
     __syncthreads();
     if (tid == 0) {
       tc::fence_after();
+      const unsigned char* sA = tsm + st * STAGE;
+      const unsigned char* sB = sA + S * A_SL;
 #pragma unroll
       for (int kk = 0; kk < KC / 16; ++kk) {
 #pragma unroll
@@ -941,7 +798,6 @@ __global__ void __launch_bounds__(256) zgreens_out_kernel(const WalkerDev* __res
 // --------------------------------------------------------------------------
 // host side
 // --------------------------------------------------------------------------
-static size_t zgemm_smem(int S) { return 2ull * S * ZT * ZKP * sizeof(unsigned short); }
 static size_t ztc_smem(int S, int NT) { return 2ull * S * (128 + NT) * 32 * 2; }
 static size_t zpanel_smem(int maxN) { return sizeof(double) * ((size_t)TB * maxN + 2 * TB * TB); }
 
@@ -953,10 +809,6 @@ cudaError_t configure_stab_oz_kernels(int maxN) {
   if ((e = cudaFuncSetAttribute(zgemm_tc_kernel<9, 6, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)ztc_smem(9, 32))))
     return e;
-  if ((e = cudaFuncSetAttribute(zgemm_kernel<8, 7>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)zgemm_smem(8))))
-    return e;
-  if ((e = cudaFuncSetAttribute(zgemm_kernel<9, 6>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)zgemm_smem(9))))
-    return e;
   if ((e = cudaFuncSetAttribute(zqr_panel_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)zpanel_smem(maxN > 0 ? maxN : 1))))
     return e;
@@ -965,7 +817,9 @@ cudaError_t configure_stab_oz_kernels(int maxN) {
 
 static void zgemm(const WalkerDev* W, int nw, int maxN, int op, int mode, int j, int p, int rows_max, int cols_max,
                   int trace_slot, cudaStream_t st) {
-  zexp_kernel<<<dim3((std::max(rows_max, cols_max) + 31) / 32, 2, 2 * nw), 256, 0, st>>>(W, op, mode, j, p);
+  const dim3 gs((std::max(rows_max, cols_max) + 31) / 32, 2, 2 * nw);
+  zslice_kernel<8, 7><<<gs, 256, 0, st>>>(W, op, mode, j, p);
+  if (maxN > 256) zslice_kernel<9, 6><<<gs, 256, 0, st>>>(W, op, mode, j, p);
   const dim3 g8((cols_max + 63) / 64, (rows_max + 127) / 128, 2 * nw);
   zgemm_tc_kernel<8, 7, 64><<<g8, 256, ztc_smem(8, 64), st>>>(W, op, mode, j, p, trace_slot);
   if (maxN > 256) {
