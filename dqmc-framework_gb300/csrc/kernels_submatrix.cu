@@ -72,10 +72,6 @@ __device__ __forceinline__ void cp16(void* dst, const void* src, bool pred) {
   const int n = pred ? 16 : 0;  // 0: zero-fill, nothing is read
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(d), "l"(src), "r"(n));
 }
-__device__ __forceinline__ void cp_commit_wait() {
-  asm volatile("cp.async.commit_group;\n" ::);
-  asm volatile("cp.async.wait_group 0;\n" ::);
-}
 
 // Slices nlines lines x K (<= KB) of an operand into dst[s][line][KP] with one
 // exponent per line (ex[line]); get(line, k) is the FP64 element.  Lines of a
@@ -189,14 +185,15 @@ constexpr int kEOff = -OZB * (OZS + 1);
 
 size_t submatrix_scratch_bytes(int N) { return sub_offsets(N).total; }
 
-size_t submatrix_smem_bytes(int N, int S) {
+// nbuf: flush tile buffers (2 overlaps the copies of tile i+1 with tile i)
+size_t submatrix_smem_bytes(int N, int S, int nbuf) {
   const size_t Nu = (size_t)((N + 1) & ~1);
-  return sizeof(double) * (Nu + 6ull * S * KK) + 2ull * OZS * 64 * KP * sizeof(unsigned short) +
+  return sizeof(double) * (Nu + 6ull * S * KK) + 2ull * nbuf * OZS * 64 * KP * sizeof(unsigned short) +
          256 * sizeof(int) + (size_t)N;
 }
 
 __global__ void __launch_bounds__(kSubThreads) metropolis_sub_kernel(const WalkerDev* __restrict__ W, int mode, int j,
-                                                                     int q) {
+                                                                     int q, int nbuf) {
   const WalkerDev& w = W[blockIdx.x];
   if (w.path != 2) return;
   int t;
@@ -211,11 +208,12 @@ __global__ void __launch_bounds__(kSubThreads) metropolis_sub_kernel(const Walke
   double* Ut = Bc + S * KK;              // [S][q][l] u~_q at block position l
   double* Wt = Ut + S * KK;              // [S][q][l] w~_q
   double* Gam = Wt + S * KK;             // [S][KK] Gamma(x, y) at y * KB + x
-  unsigned short* sa = reinterpret_cast<unsigned short*>(Gam + S * KK);  // [6][64][KP]
-  unsigned short* sb = sa + OZS * 64 * KP;
-  int* etmp = reinterpret_cast<int*>(sb + OZS * 64 * KP);  // [256]
+  unsigned short* sa = reinterpret_cast<unsigned short*>(Gam + S * KK);  // [nbuf][6][64][KP] left operand tiles
+  unsigned short* sb = sa + nbuf * OZS * 64 * KP;                         // [nbuf][6][64][KP] right operand tiles
+  int* etmp = reinterpret_cast<int*>(sb + nbuf * OZS * 64 * KP);  // [256]
   int8_t* s_field = reinterpret_cast<int8_t*>(etmp + 256);  // [N]
   __shared__ int eA[64], eB[64];
+  __shared__ int fA[2][64], fB[2][64];  // exponents of the flush tiles (per buffer)
   __shared__ int s_next, s_pos[KB];
   __shared__ double s_f[2];
 
@@ -355,30 +353,74 @@ __global__ void __launch_bounds__(kSubThreads) metropolis_sub_kernel(const Walke
       }
       // T as the right operand (lines = columns c, k = x)
       slice_lines([&](int line, int k) { return Tg[(long long)line * KB + k]; }, N, m, sT, N, eT, etmp);
-      // G -= G0(:, I_A) T
-      for (int r0 = 0; r0 < N; r0 += 64)
-        for (int c0 = 0; c0 < N; c0 += 64) {
-          for (int e = tid; e < 2 * OZS * 64 * 4; e += kSubThreads) {
-            const int ch = e & 3, line = (e >> 2) & 63, s = (e >> 8) % OZS, op = (e >> 8) / OZS;
-            const int gl = (op == 0 ? r0 : c0) + line;
-            const unsigned short* src = (op == 0 ? sG : sT) + ((long long)s * N + min(gl, N - 1)) * KP + ch * 8;
-            cp16((op == 0 ? sa : sb) + (s * 64 + line) * KP + ch * 8, src, gl < N);
-          }
-          if (tid < 128) {
-            const int op = tid >> 6, l = tid & 63, gl = (op ? c0 : r0) + l;
-            (op ? eB : eA)[l] = (gl < N) ? (op ? eT : eG)[gl] : -1100;
-          }
-          cp_commit_wait();
-          __syncthreads();
-          float acc[OZS][2][2][4];
-          mma_tile(sa, sb, acc);
-          tile_epilogue(acc, [&](int rl, int cl, long long v) {
-            const int r = r0 + rl, c = c0 + cl;
-            if (v != 0 && r < N && c < N)
-              Gs[(long long)c * N + r] -= ozaki::ldexp_i64(v, eA[rl] + eB[cl] + kEOff);
-          });
-          __syncthreads();
+      // G -= G0(:, I_A) T, tile by tile: the slices of tile i+1 are copied (cp.async) while
+      // tile i multiplies, and each tile's G values are loaded before its MMAs
+      const int ntl = (N + 63) / 64, ntiles = ntl * ntl;
+      auto issue = [&](int ti, int b) {
+        const int r0 = (ti / ntl) * 64, c0 = (ti % ntl) * 64;
+        unsigned short* ta = sa + b * OZS * 64 * KP;
+        unsigned short* tb = sb + b * OZS * 64 * KP;
+        for (int e = tid; e < 2 * OZS * 64 * 4; e += kSubThreads) {
+          const int ch = e & 3, line = (e >> 2) & 63, s = (e >> 8) % OZS, op = (e >> 8) / OZS;
+          const int gl = (op == 0 ? r0 : c0) + line;
+          const unsigned short* src = (op == 0 ? sG : sT) + ((long long)s * N + min(gl, N - 1)) * KP + ch * 8;
+          cp16((op == 0 ? ta : tb) + (s * 64 + line) * KP + ch * 8, src, gl < N);
         }
+        if (tid < 128) {
+          const int op = tid >> 6, l = tid & 63, gl = (op ? c0 : r0) + l;
+          (op ? fB : fA)[b][l] = (gl < N) ? (op ? eT : eG)[gl] : -1100;
+        }
+        asm volatile("cp.async.commit_group;\n" ::);
+      };
+      issue(0, 0);
+      for (int ti = 0; ti < ntiles; ++ti) {
+        const int b = (nbuf == 2) ? (ti & 1) : 0;
+        const int r0 = (ti / ntl) * 64, c0 = (ti % ntl) * 64;
+        if (nbuf == 2 && ti + 1 < ntiles) {
+          issue(ti + 1, b ^ 1);
+          asm volatile("cp.async.wait_group 1;\n" ::: "memory");
+        } else {
+          asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+        }
+        __syncthreads();
+        double gv[2][2][4];
+        {
+          const int lane = tid & 31, wid = tid >> 5;
+          const int wm = wid >> 2, wn = wid & 3, g = lane >> 2, t4 = lane & 3;
+#pragma unroll
+          for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+            for (int nt = 0; nt < 2; ++nt)
+#pragma unroll
+              for (int v = 0; v < 4; ++v) {
+                const int r = r0 + wm * 32 + mt * 16 + g + ((v >> 1) << 3);
+                const int c = c0 + wn * 16 + nt * 8 + 2 * t4 + (v & 1);
+                gv[mt][nt][v] = (r < N && c < N) ? Gs[(long long)c * N + r] : 0.0;
+              }
+        }
+        float acc[OZS][2][2][4];
+        mma_tile(sa + b * OZS * 64 * KP, sb + b * OZS * 64 * KP, acc);
+        {
+          const int lane = tid & 31, wid = tid >> 5;
+          const int wm = wid >> 2, wn = wid & 3, g = lane >> 2, t4 = lane & 3;
+#pragma unroll
+          for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+            for (int nt = 0; nt < 2; ++nt)
+#pragma unroll
+              for (int v = 0; v < 4; ++v) {
+                const int rl = wm * 32 + mt * 16 + g + ((v >> 1) << 3), cl = wn * 16 + nt * 8 + 2 * t4 + (v & 1);
+                const int r = r0 + rl, c = c0 + cl;
+                long long sv = 0;
+#pragma unroll
+                for (int m = 0; m < OZS; ++m) sv = (sv << OZB) + (long long)ozaki::f2i_small(acc[m][mt][nt][v]);
+                if (sv != 0 && r < N && c < N)
+                  Gs[(long long)c * N + r] = gv[mt][nt][v] - ozaki::ldexp_i64(sv, fA[b][rl] + fB[b][cl] + kEOff);
+              }
+        }
+        __syncthreads();
+        if (nbuf == 1 && ti + 1 < ntiles) issue(ti + 1, 0);
+      }
     }
   }
 
@@ -391,20 +433,25 @@ __global__ void __launch_bounds__(kSubThreads) metropolis_sub_kernel(const Walke
   }
 }
 
+static size_t g_sub_smem_limit = 0;  // dynamic shared memory the kernel may use
+
 cudaError_t configure_submatrix_kernel() {
   int dev = 0, optin = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
   cudaFuncAttributes fa{};
   if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, metropolis_sub_kernel);
-  if (e == cudaSuccess)
+  if (e == cudaSuccess) {
+    g_sub_smem_limit = (size_t)(optin - (int)fa.sharedSizeBytes);
     e = cudaFuncSetAttribute(metropolis_sub_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             optin - (int)fa.sharedSizeBytes);
+                             (int)g_sub_smem_limit);
+  }
   return e;
 }
 
 void launch_metropolis_sub(const WalkerDev* W, int nw, int mode, int j, int q, int maxN, int S_max, cudaStream_t st) {
-  metropolis_sub_kernel<<<nw, kSubThreads, submatrix_smem_bytes(maxN, S_max), st>>>(W, mode, j, q);
+  const int nbuf = submatrix_smem_bytes(maxN, S_max, 2) <= g_sub_smem_limit ? 2 : 1;
+  metropolis_sub_kernel<<<nw, kSubThreads, submatrix_smem_bytes(maxN, S_max, nbuf), st>>>(W, mode, j, q, nbuf);
 }
 
 }  // namespace dqmc
