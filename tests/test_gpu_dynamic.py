@@ -94,6 +94,22 @@ def test_dynamic_mixed_against_fp64(dq):
         assert stm[w] == 0 and stf[w] == 0
 
 
+def test_dynamic_mixed_large_n(dq):
+    """N = 289 (> 256 slice configuration) on the tensor-core path against FP64."""
+    descs = [dq.WalkerDesc(model=0, L=17, U=4.0, beta=1.0, Lt=10, pace=5, seed=90)]
+    taus = [0, 3, 5, 9]
+    res = []
+    for prec in (dq.MIXED, dq.FP64):
+        b = dq.Batch(descs, rng=dq.RNG_MINSTD, precision=prec)
+        b.fields_random(0)
+        b.init_greens()
+        b.sweep_dynamic(taus)
+        res.append((b.dynamic(0)[0], b.green_dynamic(0, 0, 0), b.status(0)))
+    assert _close(res[0][0], res[1][0], 1e-6)
+    assert abs(res[0][1] - res[1][1]).max() <= 1e-6
+    assert res[0][2] == 0 and res[1][2] == 0
+
+
 def test_dynamic_sweep_state_and_arguments(dq):
     d = dq.WalkerDesc(model=0, L=9, U=4.0, beta=1.0, Lt=10, pace=5, seed=1)
     b = dq.Batch([d], rng=dq.RNG_PHILOX)

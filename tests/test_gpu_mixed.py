@@ -62,6 +62,7 @@ def _run(dq, descs, precision, sweeps=1):
     (0, 12, 4.0, 0.0, 2.0, 20, 5),     # repulsive N = 144: tensor-core QR, two spins, partial panel
     (1, 12, 3.0, -0.3, 2.0, 20, 10),   # attractive N = 144
     (1, 16, 4.0, -0.5, 10.0, 100, 8),  # the mixed-precision configuration itself (beta = 10)
+    (0, 17, 4.0, 0.0, 1.0, 10, 5),     # N = 289 > 256: 8 x 6-bit wrap slices, 9 x 6-bit stabilization slices
 ])
 def test_mixed_sweep_dG_against_fp64(dq, model, L, U, mu, beta, Lt, pace):
     descs = [dq.WalkerDesc(model=model, L=L, U=U, mu=mu, beta=beta, Lt=Lt, pace=pace, seed=100 + w) for w in range(2)]
