@@ -69,7 +69,7 @@ void mixed_wrap_fwd(const WalkerDev* W, int nw, int maxN, int j, int q, cudaStre
 void mixed_wrap_bwd(const WalkerDev* W, int nw, int maxN, int j, int q, cudaStream_t st);
 void mixed_chain(const WalkerDev* W, int nw, int maxN, int mode, int j, int q, cudaStream_t st);
 void oz_slice_const(const double* X, unsigned short* out, int* exps, int N, int ldk, int role, int bits, int slices,
-                    cudaStream_t st);
+                    int layout, cudaStream_t st);
 void oz_selftest(const double* A, const double* B, double* C, unsigned short* sa, int* ea, unsigned short* sb, int* eb,
                  int N, cudaStream_t st);
 }  // namespace dqmc
@@ -363,7 +363,8 @@ int dqmc_batch_create(const dqmc_walker_desc* descs, int n, const dqmc_batch_opt
     const size_t lvl = (2 * (size_t)N * N + N + 31) & ~(size_t)31;
     const bool general = N > kMaxSmemN || o.precision == DQMC_MIXED;
     const int ldk = (N + 15) / 16 * 16;
-    off[w].sl = (o.precision == DQMC_MIXED) ? take(sizeof(unsigned short) * S * ozaki::kMaxSlices * (size_t)N * ldk) : 0;
+    off[w].sl = (o.precision == DQMC_MIXED)
+                    ? take(sizeof(unsigned short) * S * ozaki::kMaxSlices * ozaki::tc_slice_elems(N, ldk)) : 0;
     off[w].sle = (o.precision == DQMC_MIXED) ? take(sizeof(int) * S * (size_t)N) : 0;
     off[w].G = take(sizeof(double) * 2 * N * N);
     off[w].chain = take(sizeof(double) * (general ? 2 : 1) * S * N * N);
@@ -399,7 +400,7 @@ int dqmc_batch_create(const dqmc_walker_desc* descs, int n, const dqmc_batch_opt
     dense_off[i] = take(sizeof(double) * 2 * nn);
     if (o.precision == DQMC_MIXED) {  // 4 sliced copies: expK (A, B roles), invK (A, B roles)
       const int N = dense_n[i], ldk = (N + 15) / 16 * 16;
-      dense_sl[i] = take(sizeof(unsigned short) * 4 * ozaki::kMaxSlices * (size_t)N * ldk);
+      dense_sl[i] = take(sizeof(unsigned short) * 4 * ozaki::kMaxSlices * ozaki::tc_slice_elems(N, ldk));
       dense_sle[i] = take(sizeof(int) * 4 * (size_t)N);
     }
   }
@@ -445,15 +446,15 @@ int dqmc_batch_create(const dqmc_walker_desc* descs, int n, const dqmc_batch_opt
       const int N = dense_n[i], ldk = (N + 15) / 16 * 16;
       const auto c = ozaki::cfg_for_k(N);
       const auto cfg = std::make_pair(c.bits, c.slices);
-      const size_t one = ozaki::kMaxSlices * (size_t)N * ldk;
+      const size_t one = ozaki::kMaxSlices * ozaki::tc_slice_elems(N, ldk);
       auto* sl = reinterpret_cast<unsigned short*>(base + dense_sl[i]);
       auto* se = reinterpret_cast<int*>(base + dense_sle[i]);
       const double* ek = reinterpret_cast<const double*>(base + dense_off[i]);
       const double* ik = ek + nn;
-      oz_slice_const(ek, sl + 0 * one, se + 0 * N, N, ldk, 0, cfg.first, cfg.second, b->stream);  // expK as A
-      oz_slice_const(ek, sl + 1 * one, se + 1 * N, N, ldk, 1, cfg.first, cfg.second, b->stream);  // expK as B
-      oz_slice_const(ik, sl + 2 * one, se + 2 * N, N, ldk, 0, cfg.first, cfg.second, b->stream);  // invK as A
-      oz_slice_const(ik, sl + 3 * one, se + 3 * N, N, ldk, 1, cfg.first, cfg.second, b->stream);  // invK as B
+      oz_slice_const(ek, sl + 0 * one, se + 0 * N, N, ldk, 0, cfg.first, cfg.second, 1, b->stream);  // expK as A
+      oz_slice_const(ek, sl + 1 * one, se + 1 * N, N, ldk, 1, cfg.first, cfg.second, 1, b->stream);  // expK as B
+      oz_slice_const(ik, sl + 2 * one, se + 2 * N, N, ldk, 0, cfg.first, cfg.second, 1, b->stream);  // invK as A
+      oz_slice_const(ik, sl + 3 * one, se + 3 * N, N, ldk, 1, cfg.first, cfg.second, 1, b->stream);  // invK as B
     }
   }
   std::vector<std::vector<double>> fftabs;
@@ -518,7 +519,7 @@ int dqmc_batch_create(const dqmc_walker_desc* descs, int n, const dqmc_batch_opt
       h.sle = reinterpret_cast<int*>(base + off[w].sle);
       if (off[w].dense_id >= 0) {
         const int id = off[w].dense_id;
-        const size_t one = ozaki::kMaxSlices * (size_t)N * h.ldk;
+        const size_t one = ozaki::kMaxSlices * ozaki::tc_slice_elems(N, h.ldk);
         auto* sl = reinterpret_cast<const unsigned short*>(base + dense_sl[id]);
         auto* se = reinterpret_cast<const int*>(base + dense_sle[id]);
         h.kA = sl; h.kB = sl + one; h.iA = sl + 2 * one; h.iB = sl + 3 * one;

@@ -23,14 +23,16 @@ namespace dqmc {
 using ozaki::kMaxSlices;
 
 // --------------------------------------------------------------------------
-// Slicing.  role 0 (left operand, A): lines are rows r, k runs over columns,
-// out[s][r][k].  role 1 (right operand, B): lines are columns c, k runs over
-// rows, out[s][c][k].  X is column-major N x N (ld N).  pre (may be null)
-// scales element k of every line before slicing.  One CTA per 32 lines.
+// Slicing.  role 0 (left operand, A): lines are rows r, k runs over columns.
+// role 1 (right operand, B): lines are columns c, k runs over rows.  X is
+// column-major N x N (ld N).  pre (may be null) scales element k of every line
+// before slicing.  layout 0 writes out[s][line][k] (row-major, ld ldk); layout
+// 1 writes the tensor-core image (ozaki::tc_index, slice stride
+// ozaki::tc_slice_elems).  One CTA of 256 threads per 32 lines.
 // --------------------------------------------------------------------------
 struct SliceJob {
   const double* X;
-  unsigned short* out;  // [S][N][ldk] BF16 bits
+  unsigned short* out;  // BF16 bits, S slices
   int* exps;            // [N]
   const double* pre;    // along k, or null
 };
@@ -39,7 +41,8 @@ __device__ __forceinline__ double xelem(const double* X, int N, int role, int li
   return role == 0 ? X[(long long)k * N + line] : X[(long long)line * N + k];
 }
 
-__device__ void slice_lines(const SliceJob& job, int N, int ldk, int role, int bits, int slices, int line0) {
+__device__ void slice_lines(const SliceJob& job, int N, int ldk, int role, int bits, int slices, int line0,
+                            int layout) {
   __shared__ int s_e[8][32];
   __shared__ double s_t[32][33];
   const int tid = threadIdx.x;
@@ -79,14 +82,37 @@ __device__ void slice_lines(const SliceJob& job, int N, int ldk, int role, int b
       s_t[ll][kk] = x;
     }
     __syncthreads();
-    for (int e2 = tid; e2 < 32 * 32; e2 += blockDim.x) {
-      const int kk = e2 & 31, ll = e2 >> 5;
-      const int line = line0 + ll, k = k0 + kk;
+    const int Q = bits * slices;
+    if (layout == 0) {
+      for (int e2 = tid; e2 < 32 * 32; e2 += blockDim.x) {
+        const int kk = e2 & 31, ll = e2 >> 5;
+        const int line = line0 + ll, k = k0 + kk;
+        if (line < N && k < ldk) {
+          bool neg;
+          const unsigned long long q = ozaki::fixedq(s_t[ll][kk], s_e[0][ll], Q, neg);
+          for (int s = 0; s < slices; ++s)
+            job.out[((long long)s * N + line) * ldk + k] = ozaki::slice_bf16q(q, s, bits, Q, neg);
+        }
+      }
+    } else {
+      // one line and 4 consecutive k per thread: one 8-byte store per slice
+      const int kq = tid & 7, ll = tid >> 3;
+      const int line = line0 + ll, k = k0 + kq * 4;
       if (line < N && k < ldk) {
-        bool neg;
-        const unsigned long long q = ozaki::fixedq(s_t[ll][kk], s_e[0][ll], bits * slices, neg);
-        for (int s = 0; s < slices; ++s)
-          job.out[((long long)s * N + line) * ldk + k] = ozaki::slice_bf16q(q, s, bits, bits * slices, neg);
+        unsigned long long q[4];
+        bool ng[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) q[u] = ozaki::fixedq(s_t[ll][kq * 4 + u], s_e[0][ll], Q, ng[u]);
+        const long long sstride = (long long)ozaki::tc_slice_elems(N, ldk);
+        unsigned short* o = job.out + ozaki::tc_index(line, k, ozaki::tc_lines(N) / 8);
+        for (int s = 0; s < slices; ++s) {
+          ushort4 v;
+          v.x = ozaki::slice_bf16q(q[0], s, bits, Q, ng[0]);
+          v.y = ozaki::slice_bf16q(q[1], s, bits, Q, ng[1]);
+          v.z = ozaki::slice_bf16q(q[2], s, bits, Q, ng[2]);
+          v.w = ozaki::slice_bf16q(q[3], s, bits, Q, ng[3]);
+          *reinterpret_cast<ushort4*>(o + s * sstride) = v;
+        }
       }
     }
     __syncthreads();
@@ -269,22 +295,30 @@ __global__ void __launch_bounds__(256) oz_slice_kernel(const WalkerDev* __restri
   if (sgn)
     for (int k = threadIdx.x; k < N; k += blockDim.x) s_pre[k] = oz_bscale(w, t, sp, sgn, k);
   __syncthreads();
-  SliceJob job{X, w.sl + (long long)sp * w.slices * N * w.ldk, w.sle + (long long)sp * N, sgn ? s_pre : nullptr};
-  slice_lines(job, N, w.ldk, role, w.slice_bits, w.slices, blockIdx.x * 32);
+  SliceJob job{X, w.sl + (long long)sp * w.slices * ozaki::tc_slice_elems(N, w.ldk), w.sle + (long long)sp * N,
+               sgn ? s_pre : nullptr};
+  slice_lines(job, N, w.ldk, role, w.slice_bits, w.slices, blockIdx.x * 32, 1);
 }
 
 // Product of op OP on the 5th-generation tensor cores: a 128 x 64 output
 // tile per CTA with the S weight groups accumulated in TMEM (S x 64 columns).
-// The pre-sliced operands stream 32 k at a time through two shared stages
-// (cp.async, 16-byte pieces placed as K-major core matrices); one thread
-// issues the S (S+1) / 2 x 2 MMAs of a chunk and commits them to the stage's
-// mbarrier, so the copies of chunk c+1 overlap the MMAs of chunk c.
+// The operands' slices are stored as the tensor core's shared-memory image
+// (ozaki::tc_index), so a tile's 16-deep k chunk of one slice is one
+// contiguous range (4 KB of A, 2 KB of B).  One thread streams the chunks with
+// bulk asynchronous copies into a ring of NS stages, each completing on its
+// mbarrier's byte count, issues the S (S+1) / 2 MMAs of a chunk as soon as it
+// lands, and refills a stage once the MMAs that read it have completed (their
+// commit mbarrier), so NS - 1 chunks are in flight under the MMAs.
+__host__ __device__ constexpr int oz_tc_stages(int S) { return S <= 7 ? 5 : 4; }
+__host__ __device__ constexpr int oz_tc_stage_bytes(int S) { return S * (128 + 64) * 16 * 2; }
+
 template <int OP, int S>
 __global__ void __launch_bounds__(256, 1) oz_prod_tc_kernel(const WalkerDev* __restrict__ W, int mode, int j,
                                                             int q) {
-  constexpr int MT = 128, NT = 64, KC = 32, CM = 128, RG = (KC / 8) * CM;
-  constexpr int A_SL = MT * KC * 2, B_SL = NT * KC * 2, STAGE = S * (A_SL + B_SL);
+  constexpr int MT = 128, NT = 64, KC = 16;
+  constexpr int A_SL = MT * KC * 2, B_SL = NT * KC * 2, STAGE = oz_tc_stage_bytes(S), NS = oz_tc_stages(S);
   constexpr unsigned TCOLS = (S * NT <= 256) ? 256u : 512u;
+  static_assert(STAGE == S * (A_SL + B_SL), "stage size");
   const int wi = blockIdx.z >> 1, sp = blockIdx.z & 1;
   const WalkerDev& w = W[wi];
   if (w.path != 2 || w.cb || sp >= w.S || w.slices != S) return;
@@ -294,7 +328,8 @@ __global__ void __launch_bounds__(256, 1) oz_prod_tc_kernel(const WalkerDev* __r
   const int r0 = blockIdx.y * MT, c0 = blockIdx.x * NT;
   if (r0 >= N || c0 >= N) return;
   const long long NN = (long long)N * N;
-  const unsigned short* ws = w.sl + (long long)sp * w.slices * N * ldk;
+  const long long sstride = (long long)ozaki::tc_slice_elems(N, ldk);
+  const unsigned short* ws = w.sl + (long long)sp * w.slices * sstride;
   const int* we = w.sle + (long long)sp * N;
   ProdJob job{};
   double* out = nullptr;
@@ -309,9 +344,9 @@ __global__ void __launch_bounds__(256, 1) oz_prod_tc_kernel(const WalkerDev* __r
   extern __shared__ __align__(1024) unsigned char tsm[];
   __shared__ int eA[MT], eB[NT];
   __shared__ double s_scale[MT];  // exp(+-alpha s) of the output rows (or columns)
-  __shared__ __align__(8) unsigned long long mbar[2];
+  __shared__ __align__(8) unsigned long long full[NS], done[NS];
   __shared__ unsigned tbase;
-  __shared__ int s_fail;
+  __shared__ int s_fail, s_last;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   if (tid < MT) eA[tid] = (r0 + tid < N) ? job.ea[r0 + tid] : -1100;
   if (tid < NT) eB[tid] = (c0 + tid < N) ? job.eb[c0 + tid] : -1100;
@@ -322,8 +357,11 @@ __global__ void __launch_bounds__(256, 1) oz_prod_tc_kernel(const WalkerDev* __r
   }
   if (tid == 0) {
     s_fail = 0;
-    tc::mbar_init(&mbar[0]);
-    tc::mbar_init(&mbar[1]);
+    s_last = -1;
+    for (int i = 0; i < NS; ++i) {
+      tc::mbar_init(&full[i]);
+      tc::mbar_init(&done[i]);
+    }
     tc::mbar_fence_init();
   }
   if (warp == 0) tc::alloc(&tbase, TCOLS);
@@ -332,68 +370,62 @@ __global__ void __launch_bounds__(256, 1) oz_prod_tc_kernel(const WalkerDev* __r
   tc::fence_after();
   const unsigned taddr = tbase;
   constexpr uint32_t idesc = tc::idesc_bf16(MT, NT);
-  const int nch = (ldk + KC - 1) / KC;
-  // this thread's 16-byte pieces per slice and chunk: two of A (lines tid % 128, k groups
-  // tid / 128 and tid / 128 + 2), one of B (line tid % 64, k group tid / 64)
-  const long long sstride = (long long)N * ldk;
-  const int la = tid & (MT - 1), kqa = tid >> 7, lb = tid & (NT - 1), kqb = tid >> 6;
-  const bool va = r0 + la < N, vb = c0 + lb < N;
-  const unsigned short* srcA = job.A + (long long)min(r0 + la, N - 1) * ldk + kqa * 8;
-  const unsigned short* srcB = job.B + (long long)min(c0 + lb, N - 1) * ldk + kqb * 8;
-  const int dA = (la & 7) * 16 + kqa * CM + (la >> 3) * RG;
-  const int dB = (lb & 7) * 16 + kqb * CM + (lb >> 3) * RG;
-  auto load = [&](int c, int st) {
-    unsigned char* sA = tsm + st * STAGE;
-    unsigned char* sB = sA + S * A_SL;
-    const int k0 = c * KC;
-    const bool ka0 = k0 + kqa * 8 < ldk, ka1 = k0 + kqa * 8 + 16 < ldk, kb0 = k0 + kqb * 8 < ldk;
-    const int oa0 = ka0 ? k0 : 0, oa1 = ka1 ? k0 + 16 : 0, ob = kb0 ? k0 : 0;
+  if (tid == 0) {
+    // chunk c of slice s of the tile: (c * nlb + line0 / 8) 8-line blocks of 128 elements in
+    const long long cstep = (long long)(ozaki::tc_lines(N) / 8) * 128;
+    const unsigned short* a0 = job.A + (long long)(r0 / 8) * 128;
+    const unsigned short* b0 = job.B + (long long)(c0 / 8) * 128;
+    const int nch = ldk / KC;
+    auto produce = [&](int c, int st) {
+      unsigned char* sA = tsm + st * STAGE;
+      unsigned char* sB = sA + S * A_SL;
+      tc::mbar_expect_tx(&full[st], STAGE);
 #pragma unroll
-    for (int s2 = 0; s2 < S; ++s2) {
-      cp_async16(sA + s2 * A_SL + dA, srcA + s2 * sstride + oa0, va && ka0);
-      cp_async16(sA + s2 * A_SL + dA + 2 * CM, srcA + s2 * sstride + oa1, va && ka1);
-      cp_async16(sB + s2 * B_SL + dB, srcB + s2 * sstride + ob, vb && kb0);
-    }
-    cp_async_commit();
-  };
-  load(0, 0);
-  for (int c = 0; c < nch; ++c) {
-    const int st = c & 1;
-    if (c + 1 < nch) {
-      if (c >= 1 && !tc::mbar_wait(&mbar[(c + 1) & 1], ((c - 1) >> 1) & 1)) s_fail = 1;
-      load(c + 1, (c + 1) & 1);
-      asm volatile("cp.async.wait_group 1;\n" ::: "memory");
-    } else {
-      asm volatile("cp.async.wait_group 0;\n" ::: "memory");
-    }
-    tc::fence_proxy_async();
-    __syncthreads();
-    if (tid == 0) {
-      tc::fence_after();
-      const unsigned char* sA = tsm + st * STAGE;
-      const unsigned char* sB = sA + S * A_SL;
-#pragma unroll
-      for (int kk = 0; kk < KC / 16; ++kk) {
-#pragma unroll
-        for (int i = 0; i < S; ++i) {
-          const uint64_t ad = tc::desc(tc::su32(sA + i * A_SL) + kk * 2 * CM, CM, RG);
-#pragma unroll
-          for (int jj = 0; jj < S - i; ++jj) {
-            const uint64_t bd = tc::desc(tc::su32(sB + jj * B_SL) + kk * 2 * CM, CM, RG);
-            tc::mma(taddr + (unsigned)((i + jj) * NT), ad, bd, idesc, c > 0 || kk > 0 || i > 0);
-          }
-        }
+      for (int s2 = 0; s2 < S; ++s2) {
+        tc::bulk_g2s(sA + s2 * A_SL, a0 + s2 * sstride + c * cstep, A_SL, &full[st]);
+        tc::bulk_g2s(sB + s2 * B_SL, b0 + s2 * sstride + c * cstep, B_SL, &full[st]);
       }
-      tc::commit(&mbar[st]);
+    };
+    int produced = 0, landed = 0, last = -1;
+    bool ok = true;
+    for (; produced < min(NS, nch); ++produced) produce(produced, produced);
+    for (int c = 0; c < nch; ++c) {
+      const int st = c % NS;
+      if (!tc::mbar_wait(&full[st], (c / NS) & 1)) { ok = false; break; }
+      landed = c + 1;
+      tc::fence_after();
+      const unsigned sa = tc::su32(tsm + st * STAGE), sb = sa + S * A_SL;
+#pragma unroll
+      for (int i = 0; i < S; ++i) {
+        const uint64_t ad = tc::desc(sa + i * A_SL, 128, 256);
+#pragma unroll
+        for (int jj = 0; jj < S - i; ++jj)
+          tc::mma(taddr + (unsigned)((i + jj) * NT), ad, tc::desc(sb + jj * B_SL, 128, 256), idesc, c > 0 || i > 0);
+      }
+      tc::commit(&done[st]);
+      last = c;
+      if (c >= 1 && c - 1 + NS < nch) {  // stage of chunk c - 1 is free once its MMAs completed
+        const int pc = c - 1;
+        if (!tc::mbar_wait(&done[pc % NS], (pc / NS) & 1)) { ok = false; break; }
+        produce(pc + NS, pc % NS);
+        ++produced;
+      }
     }
+    if (!ok || last != nch - 1) {
+      s_fail = 1;
+      for (int c = landed; c < produced; ++c) tc::mbar_wait(&full[c % NS], (c / NS) & 1);  // copies in flight
+    }
+    s_last = last;
   }
-  if (!tc::mbar_wait(&mbar[(nch - 1) & 1], ((nch - 1) >> 1) & 1)) s_fail = 1;
-  tc::fence_after();
   __syncthreads();
+  const int last = s_last;
+  const bool mma_done = last >= 0 && tc::mbar_wait(&done[last % NS], (last / NS) & 1);
+  const int failed = __syncthreads_or(!mma_done || s_fail);
+  tc::fence_after();
   const int bits = w.slice_bits;
   const int q4 = warp & 3, half = warp >> 2;
   const int rl = q4 * 32 + lane, r = r0 + rl;
-  if (!s_fail) {
+  if (!failed) {
     for (int cc = half * (NT / 2); cc < (half + 1) * (NT / 2); cc += 16) {
       uint32_t v[S][16];
 #pragma unroll
@@ -427,9 +459,9 @@ __global__ void __launch_bounds__(256, 1) oz_prod_tc_kernel(const WalkerDev* __r
 
 // constant operands (exp(-dtau K), exp(+dtau K)), sliced once per batch
 __global__ void __launch_bounds__(256) oz_const_slice_kernel(const double* X, unsigned short* out, int* exps, int N,
-                                                             int ldk, int role, int bits, int slices) {
+                                                             int ldk, int role, int bits, int slices, int layout) {
   SliceJob job{X, out, exps, nullptr};
-  slice_lines(job, N, ldk, role, bits, slices, blockIdx.x * 32);
+  slice_lines(job, N, ldk, role, bits, slices, blockIdx.x * 32, layout);
 }
 
 // stand-alone product C = A B (test hook): A, B column-major N x N on the device
@@ -444,16 +476,16 @@ __global__ void __launch_bounds__(256) oz_selftest_prod_kernel(const unsigned sh
   else ozaki_product_tile<8>(job, N, ldk, bits, r0, c0, ozsm, epi);
 }
 
-static size_t oz_tc_smem(int S) { return 2ull * S * (128 + 64) * 32 * 2; }
+static size_t oz_tc_smem(int S) { return (size_t)oz_tc_stages(S) * oz_tc_stage_bytes(S); }
 size_t oz_prod_smem(int S) { return sizeof(unsigned short) * 2 * 2 * S * 64 * kOzRow; }
 
 cudaError_t configure_ozaki_kernels() {
   cudaError_t e;
-#define OZCFG(...) if ((e = cudaFuncSetAttribute(__VA_ARGS__, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)oz_tc_smem(8)))) return e
-  OZCFG(oz_prod_tc_kernel<OZ_WL_FWD, 7>); OZCFG(oz_prod_tc_kernel<OZ_WR_FWD, 7>); OZCFG(oz_prod_tc_kernel<OZ_CH_FWD, 7>);
-  OZCFG(oz_prod_tc_kernel<OZ_CH_BWD, 7>); OZCFG(oz_prod_tc_kernel<OZ_WR_BWD, 7>); OZCFG(oz_prod_tc_kernel<OZ_WL_BWD, 7>);
-  OZCFG(oz_prod_tc_kernel<OZ_WL_FWD, 8>); OZCFG(oz_prod_tc_kernel<OZ_WR_FWD, 8>); OZCFG(oz_prod_tc_kernel<OZ_CH_FWD, 8>);
-  OZCFG(oz_prod_tc_kernel<OZ_CH_BWD, 8>); OZCFG(oz_prod_tc_kernel<OZ_WR_BWD, 8>); OZCFG(oz_prod_tc_kernel<OZ_WL_BWD, 8>);
+#define OZCFG(S, ...) if ((e = cudaFuncSetAttribute(__VA_ARGS__, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)oz_tc_smem(S)))) return e
+  OZCFG(7, oz_prod_tc_kernel<OZ_WL_FWD, 7>); OZCFG(7, oz_prod_tc_kernel<OZ_WR_FWD, 7>); OZCFG(7, oz_prod_tc_kernel<OZ_CH_FWD, 7>);
+  OZCFG(7, oz_prod_tc_kernel<OZ_CH_BWD, 7>); OZCFG(7, oz_prod_tc_kernel<OZ_WR_BWD, 7>); OZCFG(7, oz_prod_tc_kernel<OZ_WL_BWD, 7>);
+  OZCFG(8, oz_prod_tc_kernel<OZ_WL_FWD, 8>); OZCFG(8, oz_prod_tc_kernel<OZ_WR_FWD, 8>); OZCFG(8, oz_prod_tc_kernel<OZ_CH_FWD, 8>);
+  OZCFG(8, oz_prod_tc_kernel<OZ_CH_BWD, 8>); OZCFG(8, oz_prod_tc_kernel<OZ_WR_BWD, 8>); OZCFG(8, oz_prod_tc_kernel<OZ_WL_BWD, 8>);
 #undef OZCFG
   if ((e = cudaFuncSetAttribute(oz_selftest_prod_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)oz_prod_smem(8))))
@@ -484,16 +516,16 @@ void mixed_wrap_bwd(const WalkerDev* W, int nw, int maxN, int j, int q, cudaStre
 }
 
 void oz_slice_const(const double* X, unsigned short* out, int* exps, int N, int ldk, int role, int bits, int slices,
-                    cudaStream_t st) {
-  oz_const_slice_kernel<<<(N + 31) / 32, 256, 0, st>>>(X, out, exps, N, ldk, role, bits, slices);
+                    int layout, cudaStream_t st) {
+  oz_const_slice_kernel<<<(N + 31) / 32, 256, 0, st>>>(X, out, exps, N, ldk, role, bits, slices, layout);
 }
 
 void oz_selftest(const double* A, const double* B, double* C, unsigned short* sa, int* ea, unsigned short* sb, int* eb,
                  int N, cudaStream_t st) {
   const ozaki::SliceCfg cfg = ozaki::cfg_for_k(N);
   const int ldk = (N + 15) / 16 * 16;
-  oz_slice_const(A, sa, ea, N, ldk, 0, cfg.bits, cfg.slices, st);
-  oz_slice_const(B, sb, eb, N, ldk, 1, cfg.bits, cfg.slices, st);
+  oz_slice_const(A, sa, ea, N, ldk, 0, cfg.bits, cfg.slices, 0, st);
+  oz_slice_const(B, sb, eb, N, ldk, 1, cfg.bits, cfg.slices, 0, st);
   const int t = (N + 63) / 64;
   oz_selftest_prod_kernel<<<dim3(t, t), 256, oz_prod_smem(cfg.slices), st>>>(sa, ea, sb, eb, C, N, ldk, cfg.bits,
                                                                              cfg.slices);

@@ -30,6 +30,17 @@ struct SliceCfg {
 };
 __host__ __device__ inline SliceCfg cfg_for_k(int K) { return K <= 256 ? SliceCfg{7, 7} : SliceCfg{6, 8}; }
 
+// The tensor-core image of a slice (the sweep's operands): k in chunks of 16,
+// 8-line blocks of 256 bytes in core-matrix order ((k / 8) * 128 + (line % 8) * 16
+// + (k % 8) * 2 bytes), the blocks of one chunk side by side, lines padded to a
+// multiple of 128.  A tile's chunk (128 or 64 consecutive lines) is then one
+// contiguous range, the layout the tensor core reads from shared memory.
+__host__ __device__ inline int tc_lines(int N) { return (N + 127) / 128 * 128; }
+__host__ __device__ inline size_t tc_slice_elems(int N, int ldk) { return (size_t)ldk * tc_lines(N); }
+__host__ __device__ inline long long tc_index(int line, int k, int nlb) {
+  return ((long long)(k >> 4) * nlb + (line >> 3)) * 128 + ((k >> 3) & 1) * 64 + (line & 7) * 8 + (k & 7);
+}
+
 // exponent e with |x| < 2^e (0 for x == 0); integer only
 __device__ __forceinline__ int exp_bound(double x) {
   const unsigned long long b = (unsigned long long)__double_as_longlong(x);

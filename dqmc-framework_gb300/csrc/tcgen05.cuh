@@ -41,6 +41,19 @@ __device__ __forceinline__ bool mbar_wait(unsigned long long* mbar, unsigned par
   return done != 0;
 }
 
+// arm the mbarrier for `bytes` of bulk copies (this thread's arrival counts as the one expected)
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long* mbar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(su32(mbar)), "r"(bytes) : "memory");
+}
+// bulk copy of `bytes` (multiple of 16, both addresses 16-byte aligned) global -> shared,
+// completing on the mbarrier's transaction count
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes, unsigned long long* mbar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   su32(dst)),
+               "l"(src), "r"(bytes), "r"(su32(mbar))
+               : "memory");
+}
+
 // one warp: allocate ncols TMEM columns (power of two >= 32), address into *dst
 __device__ __forceinline__ void alloc(unsigned* dst, unsigned ncols) {
   asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(su32(dst)), "r"(ncols));
