@@ -375,7 +375,8 @@ int dqmc_batch_create(const dqmc_walker_desc* descs, int n, const dqmc_batch_opt
     off[w].trace = b->trace_cap ? take(sizeof(double) * (size_t)b->trace_cap * 2 * N * N) : 0;
     off[w].msub = (o.precision == DQMC_MIXED) ? take((size_t)S * submatrix_scratch_bytes(N)) : 0;
     off[w].zsl = uses_ozstab(N, o.precision)
-                     ? take(sizeof(unsigned short) * (size_t)S * 2 * 9 * N * (size_t)((N + 31) / 32 * 32)) : 0;
+                     ? take(sizeof(unsigned short) * (size_t)S * 2 * 9 * ozaki::tc_lines(N) * (size_t)((N + 31) / 32 * 32))
+                     : 0;
     off[w].dense_id = -1;
     if (!d.checkerboard) {
       auto key = std::make_tuple(d.L, d.hopping_t, d.mu, d.beta / d.Lt);

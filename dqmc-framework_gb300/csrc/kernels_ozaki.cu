@@ -16,6 +16,7 @@
 
 #include "dqmc_device.cuh"
 #include "ozaki.cuh"
+#include "oz_tc.cuh"
 #include "tcgen05.cuh"
 
 namespace dqmc {
@@ -301,24 +302,17 @@ __global__ void __launch_bounds__(256) oz_slice_kernel(const WalkerDev* __restri
 }
 
 // Product of op OP on the 5th-generation tensor cores: a 128 x 64 output
-// tile per CTA with the S weight groups accumulated in TMEM (S x 64 columns).
-// The operands' slices are stored as the tensor core's shared-memory image
-// (ozaki::tc_index), so a tile's 16-deep k chunk of one slice is one
-// contiguous range (4 KB of A, 2 KB of B).  One thread streams the chunks with
-// bulk asynchronous copies into a ring of NS stages, each completing on its
-// mbarrier's byte count, issues the S (S+1) / 2 MMAs of a chunk as soon as it
-// lands, and refills a stage once the MMAs that read it have completed (their
-// commit mbarrier), so NS - 1 chunks are in flight under the MMAs.
+// tile per CTA with the S weight groups accumulated in TMEM (S x 64 columns),
+// the operands streamed by oztc::mainloop (bulk copies through a ring of
+// 4 or 5 stages of 16-deep k chunks).
 __host__ __device__ constexpr int oz_tc_stages(int S) { return S <= 7 ? 5 : 4; }
-__host__ __device__ constexpr int oz_tc_stage_bytes(int S) { return S * (128 + 64) * 16 * 2; }
+__host__ __device__ constexpr int oz_tc_stage_bytes(int S) { return oztc::stage_bytes(S, 128, 64); }
 
 template <int OP, int S>
 __global__ void __launch_bounds__(256, 1) oz_prod_tc_kernel(const WalkerDev* __restrict__ W, int mode, int j,
                                                             int q) {
-  constexpr int MT = 128, NT = 64, KC = 16;
-  constexpr int A_SL = MT * KC * 2, B_SL = NT * KC * 2, STAGE = oz_tc_stage_bytes(S), NS = oz_tc_stages(S);
+  constexpr int MT = 128, NT = 64, NS = oz_tc_stages(S);
   constexpr unsigned TCOLS = (S * NT <= 256) ? 256u : 512u;
-  static_assert(STAGE == S * (A_SL + B_SL), "stage size");
   const int wi = blockIdx.z >> 1, sp = blockIdx.z & 1;
   const WalkerDev& w = W[wi];
   if (w.path != 2 || w.cb || sp >= w.S || w.slices != S) return;
@@ -369,53 +363,13 @@ __global__ void __launch_bounds__(256, 1) oz_prod_tc_kernel(const WalkerDev* __r
   __syncthreads();
   tc::fence_after();
   const unsigned taddr = tbase;
-  constexpr uint32_t idesc = tc::idesc_bf16(MT, NT);
   if (tid == 0) {
-    // chunk c of slice s of the tile: (c * nlb + line0 / 8) 8-line blocks of 128 elements in
+    // chunk c of the tile: (c * nlb + line0 / 8) 8-line blocks of 128 elements into each slice
     const long long cstep = (long long)(ozaki::tc_lines(N) / 8) * 128;
-    const unsigned short* a0 = job.A + (long long)(r0 / 8) * 128;
-    const unsigned short* b0 = job.B + (long long)(c0 / 8) * 128;
-    const int nch = ldk / KC;
-    auto produce = [&](int c, int st) {
-      unsigned char* sA = tsm + st * STAGE;
-      unsigned char* sB = sA + S * A_SL;
-      tc::mbar_expect_tx(&full[st], STAGE);
-#pragma unroll
-      for (int s2 = 0; s2 < S; ++s2) {
-        tc::bulk_g2s(sA + s2 * A_SL, a0 + s2 * sstride + c * cstep, A_SL, &full[st]);
-        tc::bulk_g2s(sB + s2 * B_SL, b0 + s2 * sstride + c * cstep, B_SL, &full[st]);
-      }
-    };
-    int produced = 0, landed = 0, last = -1;
-    bool ok = true;
-    for (; produced < min(NS, nch); ++produced) produce(produced, produced);
-    for (int c = 0; c < nch; ++c) {
-      const int st = c % NS;
-      if (!tc::mbar_wait(&full[st], (c / NS) & 1)) { ok = false; break; }
-      landed = c + 1;
-      tc::fence_after();
-      const unsigned sa = tc::su32(tsm + st * STAGE), sb = sa + S * A_SL;
-#pragma unroll
-      for (int i = 0; i < S; ++i) {
-        const uint64_t ad = tc::desc(sa + i * A_SL, 128, 256);
-#pragma unroll
-        for (int jj = 0; jj < S - i; ++jj)
-          tc::mma(taddr + (unsigned)((i + jj) * NT), ad, tc::desc(sb + jj * B_SL, 128, 256), idesc, c > 0 || i > 0);
-      }
-      tc::commit(&done[st]);
-      last = c;
-      if (c >= 1 && c - 1 + NS < nch) {  // stage of chunk c - 1 is free once its MMAs completed
-        const int pc = c - 1;
-        if (!tc::mbar_wait(&done[pc % NS], (pc / NS) & 1)) { ok = false; break; }
-        produce(pc + NS, pc % NS);
-        ++produced;
-      }
-    }
-    if (!ok || last != nch - 1) {
-      s_fail = 1;
-      for (int c = landed; c < produced; ++c) tc::mbar_wait(&full[c % NS], (c / NS) & 1);  // copies in flight
-    }
-    s_last = last;
+    bool ok;
+    s_last = oztc::mainloop<S, MT, NT, NS>(tsm, full, done, taddr, job.A + (long long)(r0 / 8) * 128,
+                                            job.B + (long long)(c0 / 8) * 128, sstride, cstep, ldk / 16, ok);
+    s_fail = ok ? 0 : 1;
   }
   __syncthreads();
   const int last = s_last;

@@ -30,6 +30,7 @@
 
 #include "dqmc_device.cuh"
 #include "ozaki.cuh"
+#include "oz_tc.cuh"
 #include "tcgen05.cuh"
 
 namespace dqmc {
@@ -114,19 +115,20 @@ __device__ __forceinline__ double zel(const ZOpnd& o, int i, int k, bool isB) {
   return v;
 }
 
+// The block reflector of panel p is I - V_p T_p V_p^T.  Its T factor is folded
+// into the reflectors once per panel in FP64, Vt = V_p T_p (applying Q_p^T:
+// T_p^T V_p^T A = Vt^T A) or Vt = V_p T_p^T (applying Q_p), so that every
+// application is two products: Wb = Vt^T A, A -= V_p Wb.
 enum ZOp {
-  Z_QR_W = 0,    // Wb = V_p^T X(j0:, j0+pb:)
-  Z_QR_W2,       // W2 = T_p^T Wb
-  Z_QR_UPD,      // X(j0:, j0+pb:) -= V_p W2
-  Z_Q_W,         // Wb = V_p^T U(j0:, j0:)        (forming Q, backward)
-  Z_Q_W2,        // W2 = T_p Wb
-  Z_Q_UPD,       // U(j0:, j0:) -= V_p W2
+  Z_QR_W = 0,    // Wb = (V_p T_p)^T X(j0:, j0+pb:)
+  Z_QR_UPD,      // X(j0:, j0+pb:) -= V_p Wb
+  Z_Q_W,         // Wb = (V_p T_p^T)^T U(j0:, j0:)   (forming Q, backward)
+  Z_Q_UPD,       // U(j0:, j0:) -= V_p Wb
   Z_F,           // F = D^-1 R P^T F_prev
   Z_GA,          // M = Dlmax^-1 U_L^T U_R Drmax^-1
   Z_GB,          // M += Dlmin F_L F_R^T Drmin
-  Z_AQ_W,        // Wb = V_p^T Y(j0:, :)
-  Z_AQ_W2,       // W2 = T_p^T Wb
-  Z_AQ_UPD,      // Y(j0:, :) -= V_p W2
+  Z_AQ_W,        // Wb = (V_p T_p)^T Y(j0:, :)
+  Z_AQ_UPD,      // Y(j0:, :) -= V_p Wb
   Z_TR_UPD,      // Y(j0:j0+pb, :) -= R(j0:j0+pb, j0+pb:) Y(j0+pb:, :)
   Z_GG,          // G = U_R Drmax^-1 X
 };
@@ -143,51 +145,38 @@ __device__ bool zjob(const WalkerDev& w, int op, int mode, int j, int p, int sp,
   const bool panel_op = op != Z_F && op != Z_GA && op != Z_GB && op != Z_GG;
   if (panel_op && j0 >= N) return false;
   const ZOpnd Vp{z.X + (long long)j0 * N + j0, N, 0, 1, nullptr, nullptr};
-  ZOpnd VpT = Vp;
-  VpT.tr = 1;
-  const ZOpnd Tp{z.Tb + (long long)p * TB * TB, TB, 0, 2, nullptr, nullptr};
-  ZOpnd TpT = Tp;
-  TpT.tr = 1;
+  const ZOpnd VtT{z.W2, N, 1, 0, nullptr, nullptr};  // Vt^T (Vt: m x pb, ld N, in W2)
+  const ZOpnd Wbo{z.Wb, TB, 0, 0, nullptr, nullptr};
   int nl = 0, nr = 0;
   zstack_tops(w, mode, j, nl, nr);
   const int side = (mode == MODE_FWD) ? 0 : 1;
   switch (op) {
     case Z_QR_W:
-    case Z_QR_W2:
     case Z_QR_UPD: {
       const int nt = m - pb;
       if (nt <= 0) return false;
       if (op == Z_QR_W) {
-        jb.a = VpT;
+        jb.a = VtT;
         jb.b = ZOpnd{z.X + (long long)(j0 + pb) * N + j0, N, 0, 0, nullptr, nullptr};
         jb.c = z.Wb; jb.ldc = TB; jb.M = pb; jb.N = nt; jb.K = m;
-      } else if (op == Z_QR_W2) {
-        jb.a = TpT;
-        jb.b = ZOpnd{z.Wb, TB, 0, 0, nullptr, nullptr};
-        jb.c = z.W2; jb.ldc = TB; jb.M = pb; jb.N = nt; jb.K = pb;
       } else {
         jb.a = Vp;
-        jb.b = ZOpnd{z.W2, TB, 0, 0, nullptr, nullptr};
+        jb.b = Wbo;
         jb.c = z.X + (long long)(j0 + pb) * N + j0; jb.ldc = N; jb.M = m; jb.N = nt; jb.K = pb;
         jb.beta = 1; jb.alpha = -1.0;
       }
       return true;
     }
     case Z_Q_W:
-    case Z_Q_W2:
     case Z_Q_UPD: {
       double* Uo = stack_level(w, side, sp, j);
       if (op == Z_Q_W) {
-        jb.a = VpT;
+        jb.a = VtT;
         jb.b = ZOpnd{Uo + (long long)j0 * N + j0, N, 0, 0, nullptr, nullptr};
         jb.c = z.Wb; jb.ldc = TB; jb.M = pb; jb.N = m; jb.K = m;
-      } else if (op == Z_Q_W2) {
-        jb.a = Tp;
-        jb.b = ZOpnd{z.Wb, TB, 0, 0, nullptr, nullptr};
-        jb.c = z.W2; jb.ldc = TB; jb.M = pb; jb.N = m; jb.K = pb;
       } else {
         jb.a = Vp;
-        jb.b = ZOpnd{z.W2, TB, 0, 0, nullptr, nullptr};
+        jb.b = Wbo;
         jb.c = Uo + (long long)j0 * N + j0; jb.ldc = N; jb.M = m; jb.N = m; jb.K = pb;
         jb.beta = 1; jb.alpha = -1.0;
       }
@@ -227,19 +216,14 @@ __device__ bool zjob(const WalkerDev& w, int op, int mode, int j, int p, int sp,
       return true;
     }
     case Z_AQ_W:
-    case Z_AQ_W2:
     case Z_AQ_UPD: {
       if (op == Z_AQ_W) {
-        jb.a = VpT;
+        jb.a = VtT;
         jb.b = ZOpnd{z.Y + j0, N, 0, 0, nullptr, nullptr};
         jb.c = z.Wb; jb.ldc = TB; jb.M = pb; jb.N = N; jb.K = m;
-      } else if (op == Z_AQ_W2) {
-        jb.a = TpT;
-        jb.b = ZOpnd{z.Wb, TB, 0, 0, nullptr, nullptr};
-        jb.c = z.W2; jb.ldc = TB; jb.M = pb; jb.N = N; jb.K = pb;
       } else {
         jb.a = Vp;
-        jb.b = ZOpnd{z.W2, TB, 0, 0, nullptr, nullptr};
+        jb.b = Wbo;
         jb.c = z.Y + j0; jb.ldc = N; jb.M = m; jb.N = N; jb.K = pb;
         jb.beta = 1; jb.alpha = -1.0;
       }
@@ -282,8 +266,9 @@ __device__ __forceinline__ void cp16_async(void* dst, const void* src, bool pred
 // Slicing of both operands of a product, once per product: blockIdx.y = 0 the
 // rows of op(A), 1 the columns of op(B); 32 lines per CTA.  Pass 1: the line
 // exponents (8 k groups per line); pass 2: 32 x 32 tiles staged through
-// shared memory so that loads run along the stored matrix and the BF16 writes
-// along k.  Output: [operand][S][N][zld], zero past K up to a multiple of 32.
+// shared memory so that loads run along the stored matrix.  Output: per
+// operand S slices of tc_lines(N) x zld in the tensor core's shared-memory
+// image (ozaki::tc_index), zero past K up to a multiple of 32.
 // --------------------------------------------------------------------------
 template <int S, int B>
 __global__ void __launch_bounds__(256) zslice_kernel(const WalkerDev* __restrict__ W, int op, int mode, int j, int p) {
@@ -299,9 +284,10 @@ __global__ void __launch_bounds__(256) zslice_kernel(const WalkerDev* __restrict
   const int l0 = blockIdx.x * 32;
   if (l0 >= nlines) return;
   constexpr int Q = S * B;
-  const int N = w.N, ld = w.zld, Kp = (jb.K + 31) / 32 * 32;
+  const int N = w.N, Kp = (jb.K + 31) / 32 * 32, nlb = ozaki::tc_lines(N) / 8;
+  const long long sst = (long long)ozaki::tc_lines(N) * w.zld;
   const ZScr z = zscr(w, sp);
-  unsigned short* out = w.zsl + ((long long)(sp * 2 + (isB ? 1 : 0)) * 9) * N * ld;
+  unsigned short* out = w.zsl + ((long long)(sp * 2 + (isB ? 1 : 0)) * 9) * sst;
   // lines contiguous in memory when the stored row index runs along the line
   const bool line_fast = (o.tr == (int)isB);
   __shared__ int s_e[8][32];
@@ -340,14 +326,23 @@ __global__ void __launch_bounds__(256) zslice_kernel(const WalkerDev* __restrict
       s_t[ll][kk] = (line < nlines && k < jb.K) ? zel(o, line, k, isB) : 0.0;
     }
     __syncthreads();
-    for (int e = threadIdx.x; e < 32 * 32; e += 256) {
-      const int kk = e & 31, ll = e >> 5, line = l0 + ll;
+    {  // one line and 4 consecutive k per thread: one 8-byte store per slice
+      const int kq = threadIdx.x & 7, ll = threadIdx.x >> 3, line = l0 + ll;
       if (line < nlines) {
-        bool neg;
-        const unsigned long long q = zfixed(s_t[ll][kk], s_e[0][ll], Q, neg);
+        unsigned long long q[4];
+        bool ng[4];
 #pragma unroll
-        for (int s2 = 0; s2 < S; ++s2)
-          out[((long long)s2 * N + line) * ld + k0 + kk] = ozaki::slice_bf16q(q, s2, B, Q, neg);
+        for (int u = 0; u < 4; ++u) q[u] = zfixed(s_t[ll][kq * 4 + u], s_e[0][ll], Q, ng[u]);
+        unsigned short* o = out + ozaki::tc_index(line, k0 + kq * 4, nlb);
+#pragma unroll
+        for (int s2 = 0; s2 < S; ++s2) {
+          ushort4 v;
+          v.x = ozaki::slice_bf16q(q[0], s2, B, Q, ng[0]);
+          v.y = ozaki::slice_bf16q(q[1], s2, B, Q, ng[1]);
+          v.z = ozaki::slice_bf16q(q[2], s2, B, Q, ng[2]);
+          v.w = ozaki::slice_bf16q(q[3], s2, B, Q, ng[3]);
+          *reinterpret_cast<ushort4*>(o + s2 * sst) = v;
+        }
       }
     }
     __syncthreads();
@@ -356,20 +351,16 @@ __global__ void __launch_bounds__(256) zslice_kernel(const WalkerDev* __restrict
 
 // --------------------------------------------------------------------------
 // The product on the 5th-generation tensor cores (tcgen05): a 128 x NT output
-// tile per CTA, the S weight groups accumulated in TMEM (S NT columns).  The
-// pre-sliced operands stream 32 k at a time through two shared stages
-// (cp.async, 16-byte pieces placed as K-major core matrices, no swizzle); one
-// thread issues the S (S+1) / 2 x 2 MMAs of a chunk and commits them to the
-// stage's mbarrier, so the copies of chunk c+1 overlap the MMAs of chunk c.
+// tile per CTA, the S weight groups accumulated in TMEM (S NT columns), the
+// pre-sliced operands streamed by oztc::mainloop (bulk copies through a ring
+// of 4 stages of 16-deep k chunks).
 // --------------------------------------------------------------------------
+constexpr int kZStages = 4;
+
 template <int S, int B, int NT>
 __global__ void __launch_bounds__(256, 1) zgemm_tc_kernel(const WalkerDev* __restrict__ W, int op, int mode, int j,
                                                           int p, int trace_slot) {
-  constexpr int MT = 128, KC = 32;
-  constexpr int CM = 128;                 // bytes of one core matrix (8 rows x 16 bytes)
-  constexpr int RG = (KC / 8) * CM;       // bytes between 8-row groups
-  constexpr int A_SL = MT * KC * 2, B_SL = NT * KC * 2;
-  constexpr int STAGE = S * (A_SL + B_SL);
+  constexpr int MT = 128, NS = kZStages;
   constexpr unsigned TCOLS = (S * NT <= 256) ? 256u : 512u;
   const int wi = blockIdx.z >> 1, sp = blockIdx.z & 1;
   const WalkerDev& w = W[wi];
@@ -381,18 +372,21 @@ __global__ void __launch_bounds__(256, 1) zgemm_tc_kernel(const WalkerDev* __res
   if (r0 >= jb.M || c0 >= jb.N) return;
   extern __shared__ __align__(1024) unsigned char tsm[];
   __shared__ int eA[MT], eB[NT];
-  __shared__ __align__(8) unsigned long long mbar[2];
+  __shared__ __align__(8) unsigned long long full[NS], done[NS];
   __shared__ unsigned tbase;
-  __shared__ int s_fail;
+  __shared__ int s_fail, s_last;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const ZScr z = zscr(w, sp);
-  const int N = w.N, ld = w.zld;
+  const int N = w.N;
   if (tid < MT) eA[tid] = (r0 + tid < jb.M) ? z.expA[r0 + tid] : -1100;
   if (tid < NT) eB[tid] = (c0 + tid < jb.N) ? z.expB[c0 + tid] : -1100;
   if (tid == 0) {
     s_fail = 0;
-    tc::mbar_init(&mbar[0]);
-    tc::mbar_init(&mbar[1]);
+    s_last = -1;
+    for (int i = 0; i < NS; ++i) {
+      tc::mbar_init(&full[i]);
+      tc::mbar_init(&done[i]);
+    }
     tc::mbar_fence_init();
   }
   if (warp == 0) tc::alloc(&tbase, TCOLS);
@@ -400,64 +394,22 @@ __global__ void __launch_bounds__(256, 1) zgemm_tc_kernel(const WalkerDev* __res
   __syncthreads();
   tc::fence_after();
   const unsigned taddr = tbase;
-  constexpr uint32_t idesc = tc::idesc_bf16(MT, NT);
-  const int nch = (jb.K + KC - 1) / KC;
-  // this thread's 16-byte pieces per slice and chunk: A lines tid % 128 (k groups tid / 128 and
-  // + 2), B line tid % NT (k group tid / NT, threads < 4 NT)
-  const long long sst = (long long)N * ld;
-  const unsigned short* zA = w.zsl + (long long)(sp * 2) * 9 * sst;
-  const unsigned short* zB = zA + 9 * sst;
-  const int la = tid & (MT - 1), kqa = tid >> 7;
-  const int lb = tid % NT, kqb = tid / NT;
-  const bool va = r0 + la < jb.M, vb = c0 + lb < jb.N && tid < 4 * NT;
-  const unsigned short* srcA = zA + (long long)min(r0 + la, N - 1) * ld + kqa * 8;
-  const unsigned short* srcB = zB + (long long)min(c0 + lb, N - 1) * ld + (kqb & 3) * 8;
-  const int dA = (la & 7) * 16 + kqa * CM + (la >> 3) * RG;
-  const int dB = (lb & 7) * 16 + (kqb & 3) * CM + (lb >> 3) * RG;
-  auto load = [&](int c, int st) {
-    unsigned char* sA = tsm + st * STAGE;
-    unsigned char* sB = sA + S * A_SL;
-    const int k0 = c * KC;
-#pragma unroll
-    for (int s2 = 0; s2 < S; ++s2) {
-      cp16_async(sA + s2 * A_SL + dA, srcA + s2 * sst + k0, va);
-      cp16_async(sA + s2 * A_SL + dA + 2 * CM, srcA + s2 * sst + k0 + 16, va);
-      if (tid < 4 * NT) cp16_async(sB + s2 * B_SL + dB, srcB + s2 * sst + k0, vb);
-    }
-    asm volatile("cp.async.commit_group;\n" ::);
-  };
-  load(0, 0);
-  for (int c = 0; c < nch; ++c) {
-    const int st = c & 1;
-    if (c + 1 < nch) {
-      if (c >= 1 && !tc::mbar_wait(&mbar[(c + 1) & 1], ((c - 1) >> 1) & 1)) s_fail = 1;
-      load(c + 1, (c + 1) & 1);
-      asm volatile("cp.async.wait_group 1;\n" ::: "memory");
-    } else {
-      asm volatile("cp.async.wait_group 0;\n" ::: "memory");
-    }
-    tc::fence_proxy_async();
-    __syncthreads();
-    if (tid == 0) {
-      tc::fence_after();
-      const unsigned char* sA = tsm + st * STAGE;
-      const unsigned char* sB = sA + S * A_SL;
-#pragma unroll
-      for (int kk = 0; kk < KC / 16; ++kk) {
-#pragma unroll
-        for (int i = 0; i < S; ++i) {
-          const uint64_t ad = tc::desc(tc::su32(sA + i * A_SL) + kk * 2 * CM, CM, RG);
-#pragma unroll
-          for (int jj = 0; jj < S - i; ++jj) {
-            const uint64_t bd = tc::desc(tc::su32(sB + jj * B_SL) + kk * 2 * CM, CM, RG);
-            tc::mma(taddr + (unsigned)((i + jj) * NT), ad, bd, idesc, c > 0 || kk > 0 || i > 0);
-          }
-        }
-      }
-      tc::commit(&mbar[st]);
-    }
+  if (tid == 0) {
+    const long long sst = (long long)ozaki::tc_lines(N) * w.zld;
+    const unsigned short* zA = w.zsl + (long long)(sp * 2) * 9 * sst;
+    const unsigned short* zB = zA + 9 * sst;
+    const long long cstep = (long long)(ozaki::tc_lines(N) / 8) * 128;
+    bool ok;
+    s_last = oztc::mainloop<S, MT, NT, NS>(tsm, full, done, taddr, zA + (long long)(r0 / 8) * 128,
+                                            zB + (long long)(c0 / 8) * 128, sst, cstep, (jb.K + 15) / 16, ok);
+    s_fail = ok ? 0 : 1;
   }
-  if (!tc::mbar_wait(&mbar[(nch - 1) & 1], ((nch - 1) >> 1) & 1)) s_fail = 1;
+  __syncthreads();
+  {
+    const int last = s_last;
+    const bool mma_done = last >= 0 && tc::mbar_wait(&done[last % NS], (last / NS) & 1);
+    if (__syncthreads_or(!mma_done || s_fail) && tid == 0) s_fail = 1;
+  }
   tc::fence_after();
   __syncthreads();
 
@@ -657,6 +609,13 @@ __global__ void __launch_bounds__(256) zqr_panel_kernel(const WalkerDev* __restr
   }
   for (int c = 0; c < pb; ++c)
     for (int r = tid; r < m; r += 256) z.X[(long long)(j0 + c) * N + j0 + r] = P[c * m + r];
+  // Vt = V_p T_p (m x pb, ld N) for the trailing updates: Vt(r, c) = sum_{q <= min(r, c)} V(r, q) T(q, c)
+  for (int e = tid; e < m * pb; e += 256) {
+    const int r = e % m, c = e / m;
+    double s = 0.0;
+    for (int q = 0; q <= min(r, c); ++q) s = fma((q == r) ? 1.0 : P[q * m + r], T[c * TB + q], s);
+    z.W2[(long long)c * N + r] = s;
+  }
   double* Tg = z.Tb + (long long)p * TB * TB;
   for (int e = tid; e < TB * TB; e += 256) {
     const int r = e % TB, c = e / TB;
@@ -669,6 +628,36 @@ __global__ void __launch_bounds__(256) zqr_panel_kernel(const WalkerDev* __restr
     Do[j0 + tid] = d;
     z.invd[j0 + tid] = (d != 0.0) ? 1.0 / d : 0.0;
     if (d == 0.0 || !isfinite(d)) atomicOr(w.status, ST_SINGULAR);
+  }
+}
+
+// Vt = V_p T_p^T (m x pb, ld N) for forming Q: Vt(r, c) = sum_{c <= q <= r} V(r, q) T(c, q).
+// 32 rows per CTA, V and T staged in shared memory.
+__global__ void __launch_bounds__(256) zvt_kernel(const WalkerDev* __restrict__ W, int mode, int j, int p) {
+  const int wi = blockIdx.y >> 1, sp = blockIdx.y & 1;
+  const WalkerDev& w = W[wi];
+  if (!w.ozstab || sp >= w.S || j >= w.nstack) return;
+  const int N = w.N, j0 = p * TB;
+  if (j0 >= N) return;
+  const int m = N - j0, pb = min(TB, m), r0 = blockIdx.x * 32;
+  if (r0 >= m) return;
+  const ZScr z = zscr(w, sp);
+  __shared__ double sV[TB][33], sT[TB][33];  // sV[q][rl] = V(r0 + rl, q), sT[q][c] = T(c, q)
+  const double* Tg = z.Tb + (long long)p * TB * TB;
+  for (int e = threadIdx.x; e < TB * TB; e += 256) {
+    const int rl = e & 31, q = e >> 5, r = r0 + rl;
+    double v = 0.0;
+    if (q < pb && r < m) v = (r > q) ? z.X[(long long)(j0 + q) * N + j0 + r] : (r == q ? 1.0 : 0.0);
+    sV[q][rl] = v;
+    sT[q][rl] = (q < pb && rl < pb) ? Tg[q * TB + rl] : 0.0;  // T(rl, q), zero below the diagonal
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < 32 * pb; e += 256) {
+    const int rl = e & 31, c = e >> 5, r = r0 + rl;
+    if (r >= m) continue;
+    double s = 0.0;
+    for (int q = c; q < pb; ++q) s = fma(sV[q][rl], sT[q][c], s);
+    z.W2[(long long)c * N + r] = s;
   }
 }
 
@@ -807,7 +796,7 @@ __global__ void __launch_bounds__(256) zgreens_out_kernel(const WalkerDev* __res
 // --------------------------------------------------------------------------
 // host side
 // --------------------------------------------------------------------------
-static size_t ztc_smem(int S, int NT) { return 2ull * S * (128 + NT) * 32 * 2; }
+static size_t ztc_smem(int S, int NT) { return (size_t)kZStages * oztc::stage_bytes(S, 128, NT); }
 static size_t zpanel_smem(int maxN) { return sizeof(double) * ((size_t)TB * maxN + 2 * TB * TB); }
 
 cudaError_t configure_stab_oz_kernels(int maxN) {
@@ -843,14 +832,13 @@ void oz_push(int mode, const WalkerDev* W, int nw, int j, int maxN, cudaStream_t
   for (int p = 0; p < np; ++p) {
     zqr_panel_kernel<<<2 * nw, 256, zpanel_smem(maxN), st>>>(W, mode, j, p, 1);
     zgemm(W, nw, maxN, Z_QR_W, mode, j, p, TB, maxN, -1, st);
-    zgemm(W, nw, maxN, Z_QR_W2, mode, j, p, TB, maxN, -1, st);
     zgemm(W, nw, maxN, Z_QR_UPD, mode, j, p, maxN, maxN, -1, st);
   }
   zpush_fin_kernel<<<dim3(64, 2 * nw), 256, 0, st>>>(W, mode, j);
   zgemm(W, nw, maxN, Z_F, mode, j, 0, maxN, maxN, -1, st);
   for (int p = np - 1; p >= 0; --p) {
+    zvt_kernel<<<dim3((maxN + 31) / 32, 2 * nw), 256, 0, st>>>(W, mode, j, p);
     zgemm(W, nw, maxN, Z_Q_W, mode, j, p, TB, maxN, -1, st);
-    zgemm(W, nw, maxN, Z_Q_W2, mode, j, p, TB, maxN, -1, st);
     zgemm(W, nw, maxN, Z_Q_UPD, mode, j, p, maxN, maxN, -1, st);
   }
 }
@@ -863,10 +851,8 @@ void oz_greens(int mode, const WalkerDev* W, int nw, int j, int trace_slot, int 
   for (int p = 0; p < np; ++p) {
     zqr_panel_kernel<<<2 * nw, 256, zpanel_smem(maxN), st>>>(W, mode, j, p, 0);
     zgemm(W, nw, maxN, Z_QR_W, mode, j, p, TB, maxN, -1, st);
-    zgemm(W, nw, maxN, Z_QR_W2, mode, j, p, TB, maxN, -1, st);
     zgemm(W, nw, maxN, Z_QR_UPD, mode, j, p, maxN, maxN, -1, st);
     zgemm(W, nw, maxN, Z_AQ_W, mode, j, p, TB, maxN, -1, st);
-    zgemm(W, nw, maxN, Z_AQ_W2, mode, j, p, TB, maxN, -1, st);
     zgemm(W, nw, maxN, Z_AQ_UPD, mode, j, p, maxN, maxN, -1, st);
   }
   for (int p = np - 1; p >= 0; --p) {
