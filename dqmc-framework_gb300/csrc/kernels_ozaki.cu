@@ -301,17 +301,23 @@ __global__ void __launch_bounds__(256) oz_slice_kernel(const WalkerDev* __restri
   slice_lines(job, N, w.ldk, role, w.slice_bits, w.slices, blockIdx.x * 32, 1);
 }
 
-// Product of op OP on the 5th-generation tensor cores: a 128 x 64 output
-// tile per CTA with the S weight groups accumulated in TMEM (S x 64 columns),
-// the operands streamed by oztc::mainloop (bulk copies through a ring of
-// 4 or 5 stages of 16-deep k chunks).
-__host__ __device__ constexpr int oz_tc_stages(int S) { return S <= 7 ? 5 : 4; }
-__host__ __device__ constexpr int oz_tc_stage_bytes(int S) { return oztc::stage_bytes(S, 128, 64); }
+// Product of op OP on the 5th-generation tensor cores: a 128 x NT output
+// tile per CTA with the S weight groups accumulated in TMEM (S x NT columns),
+// the operands streamed by oztc::mainloop (bulk copies through a ring of NS
+// stages of 16-deep k chunks).  The 49-bit configuration (7 slices) runs
+// 128 x 32 tiles with 3 stages so that two CTAs share an SM (256 TMEM columns,
+// 105 KB of shared memory, at most 128 registers each); the 48-bit one (8
+// slices, K > 256) 128 x 64 tiles with 4 stages, one CTA per SM.
+__host__ __device__ constexpr int oz_tc_nt(int S) { return S <= 7 ? 32 : 64; }
+__host__ __device__ constexpr int oz_tc_stages(int S) { return S <= 7 ? 3 : 4; }
+__host__ __device__ constexpr int oz_tc_minb(int S) { return S <= 7 ? 2 : 1; }
+__host__ __device__ constexpr int oz_tc_stage_bytes(int S) { return oztc::stage_bytes(S, 128, oz_tc_nt(S)); }
 
 template <int OP, int S>
-__global__ void __launch_bounds__(256, 1) oz_prod_tc_kernel(const WalkerDev* __restrict__ W, int mode, int j,
-                                                            int q) {
-  constexpr int MT = 128, NT = 64, NS = oz_tc_stages(S);
+__global__ void __launch_bounds__(256, oz_tc_minb(S)) oz_prod_tc_kernel(const WalkerDev* __restrict__ W, int mode,
+                                                                        int j, int q) {
+  constexpr int MT = 128, NT = oz_tc_nt(S), NS = oz_tc_stages(S);
+  constexpr int CW = (oz_tc_minb(S) > 1) ? 8 : 16;  // TMEM columns per load in the epilogue
   constexpr unsigned TCOLS = (S * NT <= 256) ? 256u : 512u;
   const int wi = blockIdx.z >> 1, sp = blockIdx.z & 1;
   const WalkerDev& w = W[wi];
@@ -380,14 +386,14 @@ __global__ void __launch_bounds__(256, 1) oz_prod_tc_kernel(const WalkerDev* __r
   const int q4 = warp & 3, half = warp >> 2;
   const int rl = q4 * 32 + lane, r = r0 + rl;
   if (!failed) {
-    for (int cc = half * (NT / 2); cc < (half + 1) * (NT / 2); cc += 16) {
-      uint32_t v[S][16];
+    for (int cc = half * (NT / 2); cc < (half + 1) * (NT / 2); cc += CW) {
+      uint32_t v[S][CW];
 #pragma unroll
-      for (int m = 0; m < S; ++m) tc::ld16(v[m], taddr + ((unsigned)(q4 * 32) << 16) + (unsigned)(m * NT + cc));
+      for (int m = 0; m < S; ++m) tc::ldw<CW>(v[m], taddr + ((unsigned)(q4 * 32) << 16) + (unsigned)(m * NT + cc));
       tc::wait_ld();
       if (r < N) {
 #pragma unroll
-        for (int u = 0; u < 16; ++u) {
+        for (int u = 0; u < CW; ++u) {
           const int cl = cc + u, col = c0 + cl;
           if (col >= N) continue;
           long long hi = 0, lo = 0;
@@ -450,9 +456,12 @@ cudaError_t configure_ozaki_kernels() {
 template <int OP>
 static void oz_op(const WalkerDev* W, int nw, int maxN, int mode, int j, int q, cudaStream_t st) {
   oz_slice_kernel<OP><<<dim3((maxN + 31) / 32, 2 * nw), 256, 0, st>>>(W, mode, j, q);
-  const dim3 g((maxN + 63) / 64, (maxN + 127) / 128, 2 * nw);
-  oz_prod_tc_kernel<OP, 7><<<g, 256, oz_tc_smem(7), st>>>(W, mode, j, q);
-  if (maxN > 256) oz_prod_tc_kernel<OP, 8><<<g, 256, oz_tc_smem(8), st>>>(W, mode, j, q);
+  const dim3 g7((maxN + oz_tc_nt(7) - 1) / oz_tc_nt(7), (maxN + 127) / 128, 2 * nw);
+  oz_prod_tc_kernel<OP, 7><<<g7, 256, oz_tc_smem(7), st>>>(W, mode, j, q);
+  if (maxN > 256) {
+    const dim3 g8((maxN + oz_tc_nt(8) - 1) / oz_tc_nt(8), (maxN + 127) / 128, 2 * nw);
+    oz_prod_tc_kernel<OP, 8><<<g8, 256, oz_tc_smem(8), st>>>(W, mode, j, q);
+  }
 }
 
 // the slice work of mixed walkers (wraps and chain through the tensor cores)

@@ -353,15 +353,18 @@ __global__ void __launch_bounds__(256) zslice_kernel(const WalkerDev* __restrict
 // The product on the 5th-generation tensor cores (tcgen05): a 128 x NT output
 // tile per CTA, the S weight groups accumulated in TMEM (S NT columns), the
 // pre-sliced operands streamed by oztc::mainloop (bulk copies through a ring
-// of 4 stages of 16-deep k chunks).
+// of NS stages of 16-deep k chunks).  The 56-bit configuration runs 128 x 32
+// tiles with 2 stages so that two CTAs share an SM (256 TMEM columns, 80 KB of
+// shared memory and at most 128 registers each): one CTA's epilogue overlaps
+// the other's copies and MMAs.
 // --------------------------------------------------------------------------
-constexpr int kZStages = 4;
-
-template <int S, int B, int NT>
-__global__ void __launch_bounds__(256, 1) zgemm_tc_kernel(const WalkerDev* __restrict__ W, int op, int mode, int j,
-                                                          int p, int trace_slot) {
-  constexpr int MT = 128, NS = kZStages;
+template <int S, int B, int NT, int NS, int MINB>
+__global__ void __launch_bounds__(256, MINB) zgemm_tc_kernel(const WalkerDev* __restrict__ W, int op, int mode, int j,
+                                                             int p, int trace_slot) {
+  constexpr int MT = 128;
+  constexpr int CW = (MINB > 1) ? 8 : 16;  // TMEM columns per load in the epilogue
   constexpr unsigned TCOLS = (S * NT <= 256) ? 256u : 512u;
+  static_assert(MINB == 1 || S * NT <= 256, "two CTAs per SM need at most 256 TMEM columns each");
   const int wi = blockIdx.z >> 1, sp = blockIdx.z & 1;
   const WalkerDev& w = W[wi];
   if (!w.ozstab || sp >= w.S) return;
@@ -426,13 +429,13 @@ __global__ void __launch_bounds__(256, 1) zgemm_tc_kernel(const WalkerDev* __res
   // unit does ~15 per clock per SM); warps whose 32 rows are all past M skip the epilogue
   const bool small_k = jb.K <= 32;
   if (!s_fail && r0 + q4 * 32 < jb.M) {
-    for (int cc = half * (NT / 2); cc < (half + 1) * (NT / 2); cc += 16) {
-      uint32_t v[S][16];
+    for (int cc = half * (NT / 2); cc < (half + 1) * (NT / 2); cc += CW) {
+      uint32_t v[S][CW];
 #pragma unroll
-      for (int m = 0; m < S; ++m) tc::ld16(v[m], taddr + ((unsigned)(q4 * 32) << 16) + (unsigned)(m * NT + cc));
+      for (int m = 0; m < S; ++m) tc::ldw<CW>(v[m], taddr + ((unsigned)(q4 * 32) << 16) + (unsigned)(m * NT + cc));
       tc::wait_ld();
 #pragma unroll
-      for (int u = 0; u < 16; ++u) {
+      for (int u = 0; u < CW; ++u) {
         const int cl = cc + u, col = c0 + cl;
         if (r >= jb.M || col >= jb.N) continue;
         long long hi = 0, lo = 0;
@@ -796,16 +799,17 @@ __global__ void __launch_bounds__(256) zgreens_out_kernel(const WalkerDev* __res
 // --------------------------------------------------------------------------
 // host side
 // --------------------------------------------------------------------------
-static size_t ztc_smem(int S, int NT) { return (size_t)kZStages * oztc::stage_bytes(S, 128, NT); }
+// the two product configurations: 56 bits (K <= 256) and 54 bits (K <= 1024)
+#define ZGEMM56 zgemm_tc_kernel<8, 7, 32, 2, 2>
+#define ZGEMM54 zgemm_tc_kernel<9, 6, 32, 4, 1>
+static size_t ztc_smem(int S, int NT, int NS) { return (size_t)NS * oztc::stage_bytes(S, 128, NT); }
 static size_t zpanel_smem(int maxN) { return sizeof(double) * ((size_t)TB * maxN + 2 * TB * TB); }
 
 cudaError_t configure_stab_oz_kernels(int maxN) {
   cudaError_t e;
-  if ((e = cudaFuncSetAttribute(zgemm_tc_kernel<8, 7, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)ztc_smem(8, 64))))
+  if ((e = cudaFuncSetAttribute(ZGEMM56, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ztc_smem(8, 32, 2))))
     return e;
-  if ((e = cudaFuncSetAttribute(zgemm_tc_kernel<9, 6, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)ztc_smem(9, 32))))
+  if ((e = cudaFuncSetAttribute(ZGEMM54, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ztc_smem(9, 32, 4))))
     return e;
   if ((e = cudaFuncSetAttribute(zqr_panel_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)zpanel_smem(maxN > 0 ? maxN : 1))))
@@ -818,12 +822,9 @@ static void zgemm(const WalkerDev* W, int nw, int maxN, int op, int mode, int j,
   const dim3 gs((std::max(rows_max, cols_max) + 31) / 32, 2, 2 * nw);
   zslice_kernel<8, 7><<<gs, 256, 0, st>>>(W, op, mode, j, p);
   if (maxN > 256) zslice_kernel<9, 6><<<gs, 256, 0, st>>>(W, op, mode, j, p);
-  const dim3 g8((cols_max + 63) / 64, (rows_max + 127) / 128, 2 * nw);
-  zgemm_tc_kernel<8, 7, 64><<<g8, 256, ztc_smem(8, 64), st>>>(W, op, mode, j, p, trace_slot);
-  if (maxN > 256) {
-    const dim3 g9((cols_max + 31) / 32, (rows_max + 127) / 128, 2 * nw);
-    zgemm_tc_kernel<9, 6, 32><<<g9, 256, ztc_smem(9, 32), st>>>(W, op, mode, j, p, trace_slot);
-  }
+  const dim3 g((cols_max + 31) / 32, (rows_max + 127) / 128, 2 * nw);
+  ZGEMM56<<<g, 256, ztc_smem(8, 32, 2), st>>>(W, op, mode, j, p, trace_slot);
+  if (maxN > 256) ZGEMM54<<<g, 256, ztc_smem(9, 32, 4), st>>>(W, op, mode, j, p, trace_slot);
 }
 
 void oz_push(int mode, const WalkerDev* W, int nw, int j, int maxN, cudaStream_t st) {

@@ -87,6 +87,17 @@ __device__ __forceinline__ void ld16(uint32_t (&v)[16], unsigned taddr) {
         "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
       : "r"(taddr));
 }
+// 8 consecutive FP32 columns of this thread's TMEM lane
+__device__ __forceinline__ void ld8(uint32_t (&v)[8], unsigned taddr) {
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+               : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7])
+               : "r"(taddr));
+}
+template <int W>
+__device__ __forceinline__ void ldw(uint32_t (&v)[W], unsigned taddr) {
+  if constexpr (W == 16) ld16(v, taddr);
+  else ld8(v, taddr);
+}
 __device__ __forceinline__ void wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
 }  // namespace tc
