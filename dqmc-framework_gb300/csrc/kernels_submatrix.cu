@@ -17,8 +17,14 @@
 // After the block
 //     G = G0 - G0(:,I_A) Gamma R_A,   Gamma = sum_q a_q b_q^T   (m x m),
 // the Sherman-Morrison-Woodbury form of the m flips, applied as two products
-// on the BF16 tensor cores through exact 42-bit integer slices (ozaki.cuh; K <= 32 per flush):
-// T = Gamma R_A (m x N), then G -= G0(:,I_A) T (N x N, K = m).
+// on the 5th-generation tensor cores through exact 42-bit integer slices
+// (ozaki.cuh; K <= 32 per flush): T = Gamma R_A (m x N), then
+// G -= G0(:,I_A) T (N x N, K = m).  Both run as a pipelined tile loop: one
+// thread stages the slices (bulk copies into shared memory, B tiles two
+// ahead) and issues the MMAs of tile t+1 into one of two TMEM accumulators
+// while all warps run the epilogue of tile t from the other.  The epilogue of
+// T slices T directly (per-column exponents by warp reductions), so T never
+// exists in FP64 outside registers.
 //
 // The decisions use the reference's ratio formula, evaluated with the same
 // rounded operations, and the same uniform per site; G reaches them through
@@ -30,6 +36,7 @@
 
 #include "dqmc_device.cuh"
 #include "ozaki.cuh"
+#include "tcgen05.cuh"
 
 namespace dqmc {
 
@@ -38,23 +45,35 @@ namespace {
 constexpr int kSubThreads = 256;
 constexpr int KB = 32;           // sites per block
 constexpr int KK = KB * KB;
-constexpr int KP = KB + 8;       // padded BF16 row of a slice tile (80 bytes)
 constexpr int OZS = 6, OZB = 7;  // 6 slices of 7 bits; group sums < 2^22 for K <= 32
+// tensor-core tiles: 128 rows x 32 columns, K = 32 in two chunks of 16
+constexpr int TM = 128, TN = 32;
+constexpr int A_BYTES = OZS * 2 * TM * 32;  // A operand: [slice][chunk][128 lines x 16 k]
+constexpr int B_BYTES = OZS * 2 * TN * 32;  // one B tile: [slice][chunk][32 lines x 16 k]
+constexpr int NBB = 3;                      // B tiles in flight (loads run two tiles ahead)
+constexpr int ACC_COLS = OZS * TN;          // TMEM columns of one accumulator (6 weight groups)
+constexpr unsigned TMEM_COLS = 512;         // two accumulators
 
 __host__ __device__ inline size_t al256(size_t x) { return (x + 255) & ~(size_t)255; }
 
-// per-spin scratch in HBM (WalkerDev::msub)
+// per-spin scratch in HBM (WalkerDev::msub): the operands' slices as tensor-core
+// images (ozaki::tc_index, k stride 32) and the line exponents
 struct SubOff {
-  size_t T, sT, sG, eT, eG, total;
+  size_t sGm, sG, sR, sT, eGm, eG, eR, eT, total;
 };
+__host__ __device__ inline size_t sub_sst(int N) { return (size_t)ozaki::tc_lines(N) * KB; }
 __host__ __device__ inline SubOff sub_offsets(int N) {
   SubOff o;
-  o.T = 0;                                                          // T(x, c) at c * KB + x
-  o.sT = al256((size_t)N * KB * sizeof(double));                    // slices of T, lines = columns c
-  o.sG = o.sT + al256((size_t)OZS * N * KP * sizeof(unsigned short));  // slices of G0(:, I_A), lines = rows
-  o.eT = o.sG + al256((size_t)OZS * N * KP * sizeof(unsigned short));
-  o.eG = o.eT + al256((size_t)N * sizeof(int));
-  o.total = o.eG + al256((size_t)N * sizeof(int));
+  const size_t img = al256(OZS * sub_sst(N) * sizeof(unsigned short));
+  o.sGm = 0;                                             // Gamma, lines = rows x (128-line image)
+  o.sG = al256(OZS * sub_sst(1) * sizeof(unsigned short));  // G0(:, I_A), lines = rows
+  o.sR = o.sG + img;                                     // R_A, lines = columns c
+  o.sT = o.sR + img;                                     // T, lines = columns c
+  o.eGm = o.sT + img;
+  o.eG = o.eGm + al256(KB * sizeof(int));
+  o.eR = o.eG + al256((size_t)N * sizeof(int));
+  o.eT = o.eR + al256((size_t)N * sizeof(int));
+  o.total = o.eT + al256((size_t)N * sizeof(int));
   return o;
 }
 
@@ -67,18 +86,13 @@ __device__ __forceinline__ bool sub_slice_of(const WalkerDev& w, int mode, int j
   return true;
 }
 
-__device__ __forceinline__ void cp16(void* dst, const void* src, bool pred) {
-  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
-  const int n = pred ? 16 : 0;  // 0: zero-fill, nothing is read
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(d), "l"(src), "r"(n));
-}
-
-// Slices nlines lines x K (<= KB) of an operand into dst[s][line][KP] with one
-// exponent per line (ex[line]); get(line, k) is the FP64 element.  Lines of a
-// 64-line chunk past nlines (up to dst_lines) are written as zeros.  All
-// threads take part; 4 threads per line, 8 k each.
+// Slices nlines lines x K (<= KB) of an operand into the tensor-core image
+// dst (slice stride sst, nlb 8-line blocks per k chunk; k past K written as
+// zeros) with one exponent per line (ex[line]); get(line, k) is the FP64
+// element.  All threads take part; 4 threads per line, 8 k each.
 template <class Get>
-__device__ void slice_lines(Get get, int nlines, int K, unsigned short* dst, int dst_lines, int* ex, int* etmp) {
+__device__ void slice_lines(Get get, int nlines, int K, unsigned short* dst, long long sst, int nlb, int* ex,
+                            int* etmp) {
   const int tid = threadIdx.x, ll = tid & 63, part = tid >> 6;
   for (int l0 = 0; l0 < nlines; l0 += 64) {
     const int line = l0 + ll;
@@ -93,7 +107,7 @@ __device__ void slice_lines(Get get, int nlines, int K, unsigned short* dst, int
     etmp[part * 64 + ll] = e;
     __syncthreads();
     e = max(max(etmp[ll], etmp[64 + ll]), max(etmp[128 + ll], etmp[192 + ll]));
-    if (line < dst_lines) {
+    if (line < nlines) {
       if (part == 0) ex[line] = e;
       unsigned pk[OZS][4];
 #pragma unroll
@@ -105,78 +119,114 @@ __device__ void slice_lines(Get get, int nlines, int K, unsigned short* dst, int
           pk[s][u >> 1] = (unsigned)ozaki::slice_bf16(q0, s, OZB, n0) |
                           ((unsigned)ozaki::slice_bf16(q1, s, OZB, n1) << 16);
       }
+      unsigned short* o = dst + ozaki::tc_index(line, part * 8, nlb);
 #pragma unroll
       for (int s = 0; s < OZS; ++s)
-        *reinterpret_cast<uint4*>(dst + ((long long)s * dst_lines + line) * KP + part * 8) =
-            make_uint4(pk[s][0], pk[s][1], pk[s][2], pk[s][3]);
+        *reinterpret_cast<uint4*>(o + s * sst) = make_uint4(pk[s][0], pk[s][1], pk[s][2], pk[s][3]);
     }
     __syncthreads();
   }
 }
 
-// 64 x 64 product tile, K = 32, from sa[s][row][KP] and sb[s][col][KP]: weight groups in acc
-__device__ __forceinline__ void mma_tile(const unsigned short* sa, const unsigned short* sb,
-                                         float (&acc)[OZS][2][2][4]) {
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const int wm = wid >> 2, wn = wid & 3, g = lane >> 2, t4 = lane & 3;
+// The integer value sum_m S_m 2^(7 (5 - m)) of this thread's element of column u
+// from the six weight-group sums S_m (exact FP32 integers, |S_m| < 2^22): the
+// groups are read as integers through the 1.5 2^23 bias, combined in pairs
+// P = 128 S_a + S_b (|P| < 2^30) in 32 bits, and the three pairs in 64.
+__device__ __forceinline__ long long group_sum(const uint32_t (&v)[OZS][8], int u) {
+  static_assert(OZS == 6 && OZB == 7, "pairing assumes six 7-bit groups");
+  constexpr unsigned kBias = 0x4B400000u;  // bits of 1.5 2^23
+  unsigned b[OZS];
 #pragma unroll
-  for (int m = 0; m < OZS; ++m)
-#pragma unroll
-    for (int a = 0; a < 2; ++a)
-#pragma unroll
-      for (int b = 0; b < 2; ++b)
-#pragma unroll
-        for (int v = 0; v < 4; ++v) acc[m][a][b][v] = 0.f;
-#pragma unroll
-  for (int k0 = 0; k0 < KB; k0 += 16) {
-#pragma unroll
-    for (int i = 0; i < OZS; ++i) {
-      unsigned a[2][4];
-#pragma unroll
-      for (int mt = 0; mt < 2; ++mt) {
-        const unsigned short* p = sa + (i * 64 + wm * 32 + mt * 16 + g) * KP + k0 + 2 * t4;
-        a[mt][0] = *(const unsigned*)(p);
-        a[mt][1] = *(const unsigned*)(p + 8 * KP);
-        a[mt][2] = *(const unsigned*)(p + 8);
-        a[mt][3] = *(const unsigned*)(p + 8 * KP + 8);
-      }
-#pragma unroll
-      for (int jj = 0; jj < OZS - i; ++jj) {
-        unsigned b[2][2];
-#pragma unroll
-        for (int nt = 0; nt < 2; ++nt) {
-          const unsigned short* p = sb + (jj * 64 + wn * 16 + nt * 8 + g) * KP + k0 + 2 * t4;
-          b[nt][0] = *(const unsigned*)(p);
-          b[nt][1] = *(const unsigned*)(p + 8);
-        }
-#pragma unroll
-        for (int mt = 0; mt < 2; ++mt)
-#pragma unroll
-          for (int nt = 0; nt < 2; ++nt)
-            ozaki::mma16816(acc[i + jj][mt][nt], a[mt][0], a[mt][1], a[mt][2], a[mt][3], b[nt][0], b[nt][1]);
-      }
-    }
-  }
+  for (int m = 0; m < OZS; ++m) b[m] = __float_as_uint(__uint_as_float(v[m][u]) + 12582912.0f);
+  const int p01 = (int)(b[0] * 128u + b[1] - 129u * kBias);
+  const int p23 = (int)(b[2] * 128u + b[3] - 129u * kBias);
+  const int p45 = (int)(b[4] * 128u + b[5] - 129u * kBias);
+  return ((long long)p01 << 28) + ((long long)p23 << 14) + (long long)p45;
 }
 
-// calls f(rl, cl, v, e_offset) for this thread's 16 elements of a 64 x 64 tile;
-// value = v * 2^(eA[rl] + eB[cl] + e_offset)
-template <class F>
-__device__ __forceinline__ void tile_epilogue(const float (&acc)[OZS][2][2][4], F f) {
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const int wm = wid >> 2, wn = wid & 3, g = lane >> 2, t4 = lane & 3;
+// The tile loop of one product, C = A B with A: nrb row blocks of 128 lines, B:
+// nct column tiles of 32 lines, K = 16 nk, both as tensor-core images in
+// global memory (slice stride a_sst / b_sst, a_nlb / b_nlb line blocks per k
+// chunk).  Tile u (global count across products) uses B buffer u % NBB and TMEM
+// accumulator u & 1; thread 0 copies the B tile of t+2 and issues the MMAs of
+// t+1 while every thread runs pre(row block, column tile) (loads that do not
+// need the product) and then epi(row block, column tile, TMEM address) on tile
+// t.  A is reloaded (after the MMAs of the previous tile) at each row block.
+struct SubTC {
+  unsigned char* A;            // A_BYTES
+  unsigned char* B;            // NBB x B_BYTES
+  unsigned long long* ldA;     // [1]
+  unsigned long long* ldB;     // [NBB]
+  unsigned long long* mmab;    // [2]
+  unsigned tmem;
+  volatile int* fail;          // shared flag: a bounded wait ran out
+};
+
+template <class Pre, class Epi>
+__device__ void sub_gemm(const SubTC& tc, unsigned& gt, unsigned& nA, const unsigned short* aG, long long a_sst,
+                         int a_nlb, int nrb, const unsigned short* bG, long long b_sst, int b_nlb, int nct, int nk,
+                         Pre pre, Epi epi) {
+  const int tid = threadIdx.x;
+  const int ntiles = nrb * nct;
+  constexpr uint32_t idesc = tc::idesc_bf16(TM, TN);
+  auto load_b = [&](int t) {  // thread 0
+    const unsigned u = gt + t;
+    const int cb = t % nct, bb = (int)(u % NBB);
+    unsigned char* dst = tc.B + bb * B_BYTES;
+    tc::mbar_expect_tx(&tc.ldB[bb], OZS * nk * TN * 32);
+    for (int s2 = 0; s2 < OZS; ++s2)
+      for (int kk = 0; kk < nk; ++kk)
+        tc::bulk_g2s(dst + (s2 * 2 + kk) * TN * 32, bG + s2 * b_sst + ((long long)kk * b_nlb + cb * (TN / 8)) * 128,
+                     TN * 32, &tc.ldB[bb]);
+  };
+  auto issue = [&](int t) {  // thread 0: A if a new row block, then the MMAs of tile t
+    const unsigned u = gt + t;
+    const int rb = t / nct, bb = (int)(u % NBB), acc = (int)(u & 1);
+    if (*tc.fail) return;
+    if (t % nct == 0) {
+      // the A buffer is free once the MMAs of the previous tile (all earlier ones) completed
+      if (t > 0 && !tc::mbar_wait(&tc.mmab[(u - 1) & 1], ((u - 1) >> 1) & 1)) { *tc.fail = 1; return; }
+      tc::mbar_expect_tx(tc.ldA, OZS * nk * TM * 32);
+      for (int s2 = 0; s2 < OZS; ++s2)
+        for (int kk = 0; kk < nk; ++kk)
+          tc::bulk_g2s(tc.A + (s2 * 2 + kk) * TM * 32, aG + s2 * a_sst + ((long long)kk * a_nlb + rb * (TM / 8)) * 128,
+                       TM * 32, tc.ldA);
+      if (!tc::mbar_wait(tc.ldA, nA & 1)) { *tc.fail = 1; return; }
+      ++nA;
+    }
+    if (!tc::mbar_wait(&tc.ldB[bb], (u / NBB) & 1)) { *tc.fail = 1; return; }
+    tc::fence_after();
+    const unsigned sa = tc::su32(tc.A), sb = tc::su32(tc.B + bb * B_BYTES);
+    for (int kk = 0; kk < nk; ++kk)
 #pragma unroll
-  for (int mt = 0; mt < 2; ++mt)
+      for (int i = 0; i < OZS; ++i) {
+        const uint64_t ad = tc::desc(sa + (i * 2 + kk) * TM * 32, 128, 256);
 #pragma unroll
-    for (int nt = 0; nt < 2; ++nt)
-#pragma unroll
-      for (int v = 0; v < 4; ++v) {
-        const int rl = wm * 32 + mt * 16 + g + ((v >> 1) << 3), cl = wn * 16 + nt * 8 + 2 * t4 + (v & 1);
-        long long s = 0;
-#pragma unroll
-        for (int m = 0; m < OZS; ++m) s = (s << OZB) + (long long)ozaki::f2i_small(acc[m][mt][nt][v]);
-        f(rl, cl, s);
+        for (int jj = 0; jj < OZS - i; ++jj)
+          tc::mma(tc.tmem + (unsigned)(acc * ACC_COLS + (i + jj) * TN), ad,
+                  tc::desc(sb + (jj * 2 + kk) * TN * 32, 128, 256), idesc, kk > 0 || i > 0);
       }
+    tc::commit(&tc.mmab[acc]);
+  };
+  if (tid == 0 && !*tc.fail) {
+    load_b(0);
+    if (ntiles > 1) load_b(1);
+    issue(0);
+  }
+  for (int t = 0; t < ntiles; ++t) {
+    const unsigned u = gt + t;
+    if (tid == 0 && !*tc.fail) {
+      if (t + 2 < ntiles) load_b(t + 2);  // its buffer held tile t - 1, whose epilogue is done
+      if (t + 1 < ntiles) issue(t + 1);
+    }
+    pre(t / nct, t % nct);
+    if (!*tc.fail && !tc::mbar_wait(&tc.mmab[u & 1], (u >> 1) & 1)) *tc.fail = 1;
+    tc::fence_after();
+    epi(t / nct, t % nct, tc.tmem + (unsigned)((u & 1) * ACC_COLS), !*tc.fail);
+    tc::fence_before();
+    __syncthreads();
+  }
+  gt += ntiles;
 }
 
 constexpr int kEOff = -OZB * (OZS + 1);
@@ -185,22 +235,24 @@ constexpr int kEOff = -OZB * (OZS + 1);
 
 size_t submatrix_scratch_bytes(int N) { return sub_offsets(N).total; }
 
-// nbuf: flush tile buffers (2 overlaps the copies of tile i+1 with tile i)
-size_t submatrix_smem_bytes(int N, int S, int nbuf) {
+// dynamic shared memory: tensor-core operand buffers first (1024-byte aligned
+// base), then the FP64 block state, the exponent scratch and the fields
+size_t submatrix_smem_bytes(int N, int S) {
   const size_t Nu = (size_t)((N + 1) & ~1);
-  return sizeof(double) * (Nu + 6ull * S * KK) + 2ull * nbuf * OZS * 64 * KP * sizeof(unsigned short) +
-         256 * sizeof(int) + (size_t)N;
+  return (size_t)A_BYTES + (size_t)NBB * B_BYTES + sizeof(double) * (Nu + 6ull * S * KK) + 256 * sizeof(int) +
+         (size_t)N;
 }
 
 __global__ void __launch_bounds__(kSubThreads) metropolis_sub_kernel(const WalkerDev* __restrict__ W, int mode, int j,
-                                                                     int q, int nbuf) {
+                                                                     int q) {
   const WalkerDev& w = W[blockIdx.x];
   if (w.path != 2) return;
   int t;
   if (!sub_slice_of(w, mode, j, q, t)) return;
   const int N = w.N, S = w.S, Lt = w.Lt, tid = threadIdx.x;
   const long long NN = (long long)N * N;
-  extern __shared__ __align__(16) double sh[];
+  extern __shared__ __align__(1024) unsigned char smem[];
+  double* sh = reinterpret_cast<double*>(smem + A_BYTES + NBB * B_BYTES);
   double* uni = sh;                      // [N] uniforms of the slice
   double* Gb = uni + ((N + 1) & ~1);     // [S][KK] diagonal block, (r, c) at c * KB + r
   double* Ac = Gb + S * KK;              // [S][q][x] a_q at compact index x
@@ -208,14 +260,13 @@ __global__ void __launch_bounds__(kSubThreads) metropolis_sub_kernel(const Walke
   double* Ut = Bc + S * KK;              // [S][q][l] u~_q at block position l
   double* Wt = Ut + S * KK;              // [S][q][l] w~_q
   double* Gam = Wt + S * KK;             // [S][KK] Gamma(x, y) at y * KB + x
-  unsigned short* sa = reinterpret_cast<unsigned short*>(Gam + S * KK);  // [nbuf][6][64][KP] left operand tiles
-  unsigned short* sb = sa + nbuf * OZS * 64 * KP;                         // [nbuf][6][64][KP] right operand tiles
-  int* etmp = reinterpret_cast<int*>(sb + nbuf * OZS * 64 * KP);  // [256]
+  int* etmp = reinterpret_cast<int*>(Gam + S * KK);         // [256]
   int8_t* s_field = reinterpret_cast<int8_t*>(etmp + 256);  // [N]
-  __shared__ int eA[64], eB[64];
-  __shared__ int fA[2][64], fB[2][64];  // exponents of the flush tiles (per buffer)
   __shared__ int s_next, s_pos[KB];
   __shared__ double s_f[2];
+  __shared__ __align__(8) unsigned long long bar_ldA, bar_ldB[NBB], bar_mma[2];
+  __shared__ unsigned s_tmem;
+  __shared__ int s_tcfail;
 
   const SubOff so = sub_offsets(N);
   double* G[2] = {w.G, (S == 2) ? w.G + NN : w.G};
@@ -228,8 +279,23 @@ __global__ void __launch_bounds__(kSubThreads) metropolis_sub_kernel(const Walke
   }
   double sign = 0.0;
   long long acc_count = 0;
-  if (tid == 0) sign = *w.sign;
+  if (tid == 0) {
+    sign = *w.sign;
+    s_tcfail = 0;
+    tc::mbar_init(&bar_ldA);
+    for (int i = 0; i < NBB; ++i) tc::mbar_init(&bar_ldB[i]);
+    tc::mbar_init(&bar_mma[0]);
+    tc::mbar_init(&bar_mma[1]);
+    tc::mbar_fence_init();
+  }
+  if (tid < 32) tc::alloc(&s_tmem, TMEM_COLS);
+  tc::fence_before();
   __syncthreads();
+  tc::fence_after();
+  const SubTC tcs{smem, smem + A_BYTES, &bar_ldA, bar_ldB, bar_mma, s_tmem, &s_tcfail};
+  unsigned gt = 0, nA = 0;  // tiles and A loads so far (mbarrier phases)
+  const int nlbN = ozaki::tc_lines(N) / 8;
+  const long long sstN = (long long)sub_sst(N), sstG = (long long)sub_sst(1);
 
   for (int i0 = 0; i0 < N; i0 += KB) {
     const int kb = min(KB, N - i0);
@@ -321,112 +387,131 @@ __global__ void __launch_bounds__(kSubThreads) metropolis_sub_kernel(const Walke
     }
     __syncthreads();
 
+    const int nk = (m + 15) / 16;  // k chunks of 16 (slices are zero past m)
     for (int sp = 0; sp < S; ++sp) {
       unsigned char* ms = w.msub + (size_t)sp * so.total;
-      double* Tg = reinterpret_cast<double*>(ms + so.T);
-      unsigned short* sT = reinterpret_cast<unsigned short*>(ms + so.sT);
+      unsigned short* sGm = reinterpret_cast<unsigned short*>(ms + so.sGm);
       unsigned short* sG = reinterpret_cast<unsigned short*>(ms + so.sG);
-      int* eT = reinterpret_cast<int*>(ms + so.eT);
+      unsigned short* sR = reinterpret_cast<unsigned short*>(ms + so.sR);
+      unsigned short* sT = reinterpret_cast<unsigned short*>(ms + so.sT);
+      int* eGm = reinterpret_cast<int*>(ms + so.eGm);
       int* eG = reinterpret_cast<int*>(ms + so.eG);
+      int* eR = reinterpret_cast<int*>(ms + so.eR);
+      int* eT = reinterpret_cast<int*>(ms + so.eT);
       const double* gam = Gam + sp * KK;
       double* Gs = G[sp];
-      // Gamma as the left operand (lines = rows x, k = y)
-      slice_lines([&](int line, int k) { return gam[k * KB + line]; }, m, m, sa, 64, eA, etmp);
-      // G0(:, I_A) as the left operand of the flush, taken before G changes
-      slice_lines([&](int line, int k) { return Gs[(long long)(i0 + s_pos[k]) * N + line]; }, N, m, sG, N, eG,
-                  etmp);
-      // T = Gamma R_A, 64 columns at a time
-      for (int c0 = 0; c0 < N; c0 += 64) {
-        slice_lines(
-            [&](int line, int k) {
-              const int c = c0 + line, i = i0 + s_pos[k];
-              return ((c == i) ? 1.0 : 0.0) - Gs[(long long)c * N + i];
-            },
-            min(64, N - c0), m, sb, 64, eB, etmp);
-        float acc[OZS][2][2][4];
-        mma_tile(sa, sb, acc);
-        tile_epilogue(acc, [&](int rl, int cl, long long v) {
-          const int c = c0 + cl;
-          if (rl < m && c < N) Tg[(long long)c * KB + rl] = ozaki::ldexp_i64(v, eA[rl] + eB[cl] + kEOff);
-        });
-        __syncthreads();
-      }
-      // T as the right operand (lines = columns c, k = x)
-      slice_lines([&](int line, int k) { return Tg[(long long)line * KB + k]; }, N, m, sT, N, eT, etmp);
-      // G -= G0(:, I_A) T, tile by tile: the slices of tile i+1 are copied (cp.async) while
-      // tile i multiplies, and each tile's G values are loaded before its MMAs
-      const int ntl = (N + 63) / 64, ntiles = ntl * ntl;
-      auto issue = [&](int ti, int b) {
-        const int r0 = (ti / ntl) * 64, c0 = (ti % ntl) * 64;
-        unsigned short* ta = sa + b * OZS * 64 * KP;
-        unsigned short* tb = sb + b * OZS * 64 * KP;
-        for (int e = tid; e < 2 * OZS * 64 * 4; e += kSubThreads) {
-          const int ch = e & 3, line = (e >> 2) & 63, s = (e >> 8) % OZS, op = (e >> 8) / OZS;
-          const int gl = (op == 0 ? r0 : c0) + line;
-          const unsigned short* src = (op == 0 ? sG : sT) + ((long long)s * N + min(gl, N - 1)) * KP + ch * 8;
-          cp16((op == 0 ? ta : tb) + (s * 64 + line) * KP + ch * 8, src, gl < N);
-        }
-        if (tid < 128) {
-          const int op = tid >> 6, l = tid & 63, gl = (op ? c0 : r0) + l;
-          (op ? fB : fA)[b][l] = (gl < N) ? (op ? eT : eG)[gl] : -1100;
-        }
-        asm volatile("cp.async.commit_group;\n" ::);
-      };
-      issue(0, 0);
-      for (int ti = 0; ti < ntiles; ++ti) {
-        const int b = (nbuf == 2) ? (ti & 1) : 0;
-        const int r0 = (ti / ntl) * 64, c0 = (ti % ntl) * 64;
-        if (nbuf == 2 && ti + 1 < ntiles) {
-          issue(ti + 1, b ^ 1);
-          asm volatile("cp.async.wait_group 1;\n" ::: "memory");
-        } else {
-          asm volatile("cp.async.wait_group 0;\n" ::: "memory");
-        }
-        __syncthreads();
-        double gv[2][2][4];
-        {
-          const int lane = tid & 31, wid = tid >> 5;
-          const int wm = wid >> 2, wn = wid & 3, g = lane >> 2, t4 = lane & 3;
+      // Gamma (lines = rows x, k = y), G0(:, I_A) (lines = rows, k = accept) and
+      // R_A = E_A^T - G0(I_A, :) (lines = columns c, k = accept), taken before G changes
+      slice_lines([&](int line, int k) { return gam[k * KB + line]; }, m, m, sGm, sstG, TM / 8, eGm, etmp);
+      slice_lines([&](int line, int k) { return Gs[(long long)(i0 + s_pos[k]) * N + line]; }, N, m, sG, sstN, nlbN,
+                  eG, etmp);
+      slice_lines(
+          [&](int line, int k) {
+            const int i = i0 + s_pos[k];
+            return ((line == i) ? 1.0 : 0.0) - Gs[(long long)line * N + i];
+          },
+          N, m, sR, sstN, nlbN, eR, etmp);
+      asm volatile("fence.proxy.async.global;" ::: "memory");  // generic writes -> bulk-copy reads
+      __syncthreads();
+      // T^T = R_A^T Gamma^T (rows c, columns x): warp w and w + 4 share TMEM lanes 32 (w & 3)..
+      // (columns c) and take x in [0, 16) and [16, 32); the column exponent max over x goes
+      // through shared memory, and the epilogue slices T straight into the B image of the
+      // flush (line c, k = x)
+      sub_gemm(tcs, gt, nA, sR, sstN, nlbN, (N + TM - 1) / TM, sGm, sstG, TM / 8, 1, nk, [&](int, int) {},
+               [&](int rb, int, unsigned tacc, bool ok) {
+                 const int wq = (tid >> 5) & 3, xh = tid >> 7;
+                 const int c = rb * TM + wq * 32 + (tid & 31);
+                 const int ec = (c < N) ? eR[c] : 0;
+                 double tv[16];
+                 int e = -1100;
+                 if (ok) {
 #pragma unroll
-          for (int mt = 0; mt < 2; ++mt)
+                   for (int h = 0; h < 2; ++h) {
+                     uint32_t v[OZS][8];
 #pragma unroll
-            for (int nt = 0; nt < 2; ++nt)
+                     for (int g = 0; g < OZS; ++g)
+                       tc::ld8(v[g], tacc + ((unsigned)(wq * 32) << 16) + (unsigned)(g * TN + xh * 16 + h * 8));
+                     tc::wait_ld();
 #pragma unroll
-              for (int v = 0; v < 4; ++v) {
-                const int r = r0 + wm * 32 + mt * 16 + g + ((v >> 1) << 3);
-                const int c = c0 + wn * 16 + nt * 8 + 2 * t4 + (v & 1);
-                gv[mt][nt][v] = (r < N && c < N) ? Gs[(long long)c * N + r] : 0.0;
-              }
-        }
-        float acc[OZS][2][2][4];
-        mma_tile(sa + b * OZS * 64 * KP, sb + b * OZS * 64 * KP, acc);
-        {
-          const int lane = tid & 31, wid = tid >> 5;
-          const int wm = wid >> 2, wn = wid & 3, g = lane >> 2, t4 = lane & 3;
+                     for (int u = 0; u < 8; ++u) {
+                       const int x = xh * 16 + h * 8 + u;
+                       tv[h * 8 + u] = (x < m && c < N) ? ozaki::ldexp_i64(group_sum(v, u), ec + eGm[x] + kEOff) : 0.0;
+                       e = max(e, ozaki::exp_bound(tv[h * 8 + u]));
+                     }
+                   }
+                 }
+                 etmp[tid] = e;
+                 __syncthreads();
+                 e = max(e, etmp[tid ^ 128]);
+                 if (ok && c < N) {
+                   if (xh == 0) eT[c] = e;
+                   unsigned pk[OZS][8];
 #pragma unroll
-          for (int mt = 0; mt < 2; ++mt)
+                   for (int u = 0; u < 16; u += 2) {
+                     bool n0, n1;
+                     const unsigned long long q0 = ozaki::fixed42(tv[u], e, n0), q1 = ozaki::fixed42(tv[u + 1], e, n1);
 #pragma unroll
-            for (int nt = 0; nt < 2; ++nt)
+                     for (int s2 = 0; s2 < OZS; ++s2)
+                       pk[s2][u >> 1] = (unsigned)ozaki::slice_bf16(q0, s2, OZB, n0) |
+                                        ((unsigned)ozaki::slice_bf16(q1, s2, OZB, n1) << 16);
+                   }
+                   unsigned short* o = sT + ozaki::tc_index(c, xh * 16, nlbN);
 #pragma unroll
-              for (int v = 0; v < 4; ++v) {
-                const int rl = wm * 32 + mt * 16 + g + ((v >> 1) << 3), cl = wn * 16 + nt * 8 + 2 * t4 + (v & 1);
-                const int r = r0 + rl, c = c0 + cl;
-                long long sv = 0;
+                   for (int s2 = 0; s2 < OZS; ++s2) {
+                     *reinterpret_cast<uint4*>(o + s2 * sstN) = make_uint4(pk[s2][0], pk[s2][1], pk[s2][2], pk[s2][3]);
+                     *reinterpret_cast<uint4*>(o + s2 * sstN + 64) =
+                         make_uint4(pk[s2][4], pk[s2][5], pk[s2][6], pk[s2][7]);
+                   }
+                 }
+               });
+      asm volatile("fence.proxy.async.global;" ::: "memory");
+      __syncthreads();
+      // G -= G0(:, I_A) T: warp w reads TMEM lanes 32 (w & 3) .. (rows), columns 16 (w >> 2) ..;
+      // the G values and column exponents of a tile are loaded before its MMAs are waited on
+      double gv[16];
+      int ecol[16];
+      const int wq = (tid >> 5) & 3, half = tid >> 7;
+      sub_gemm(tcs, gt, nA, sG, sstN, nlbN, (N + TM - 1) / TM, sT, sstN, nlbN, (N + TN - 1) / TN, nk,
+               [&](int rb, int cb) {
+                 const int r = rb * TM + wq * 32 + (tid & 31), c0 = cb * TN + half * 16;
 #pragma unroll
-                for (int m = 0; m < OZS; ++m) sv = (sv << OZB) + (long long)ozaki::f2i_small(acc[m][mt][nt][v]);
-                if (sv != 0 && r < N && c < N)
-                  Gs[(long long)c * N + r] = gv[mt][nt][v] - ozaki::ldexp_i64(sv, fA[b][rl] + fB[b][cl] + kEOff);
-              }
-        }
-        __syncthreads();
-        if (nbuf == 1 && ti + 1 < ntiles) issue(ti + 1, 0);
-      }
+                 for (int u = 0; u < 16; ++u) {
+                   const int c = c0 + u;
+                   gv[u] = (r < N && c < N) ? Gs[(long long)c * N + r] : 0.0;
+                   ecol[u] = (c < N) ? eT[c] : 0;
+                 }
+               },
+               [&](int rb, int cb, unsigned tacc, bool ok) {
+                 if (!ok) return;
+                 const int r = rb * TM + wq * 32 + (tid & 31), c0 = cb * TN + half * 16;
+                 const int er = (r < N) ? eG[r] : 0;
+                 const unsigned ta = tacc + ((unsigned)(wq * 32) << 16);
+#pragma unroll
+                 for (int h = 0; h < 2; ++h) {
+                   uint32_t v[OZS][8];
+#pragma unroll
+                   for (int g = 0; g < OZS; ++g) tc::ld8(v[g], ta + (unsigned)(g * TN + half * 16 + h * 8));
+                   tc::wait_ld();
+#pragma unroll
+                   for (int u = 0; u < 8; ++u) {
+                     const int c = c0 + h * 8 + u;
+                     const long long sv = group_sum(v, u);
+                     if (sv != 0 && r < N && c < N)
+                       Gs[(long long)c * N + r] = gv[h * 8 + u] - ozaki::ldexp_i64(sv, er + ecol[h * 8 + u] + kEOff);
+                   }
+                 }
+               });
     }
   }
 
   int8_t* frw = w.fields + (long long)eff * N;
   for (int i = tid; i < N; i += kSubThreads) frw[i] = s_field[i];
+  // TMEM back: every committed MMA has completed (each tile's commit was waited on)
+  tc::fence_before();
+  __syncthreads();
+  if (tid < 32) tc::dealloc(s_tmem, TMEM_COLS);
   if (tid == 0) {
+    if (s_tcfail) atomicOr(w.status, ST_TIMEOUT);
     *w.sign = sign;
     *w.accepts += acc_count;
     if (mode == MODE_BWD && t == Lt) *w.sign_Lt = sign;
@@ -450,8 +535,7 @@ cudaError_t configure_submatrix_kernel() {
 }
 
 void launch_metropolis_sub(const WalkerDev* W, int nw, int mode, int j, int q, int maxN, int S_max, cudaStream_t st) {
-  const int nbuf = submatrix_smem_bytes(maxN, S_max, 2) <= g_sub_smem_limit ? 2 : 1;
-  metropolis_sub_kernel<<<nw, kSubThreads, submatrix_smem_bytes(maxN, S_max, nbuf), st>>>(W, mode, j, q, nbuf);
+  metropolis_sub_kernel<<<nw, kSubThreads, submatrix_smem_bytes(maxN, S_max), st>>>(W, mode, j, q);
 }
 
 }  // namespace dqmc
