@@ -15,6 +15,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <random>
@@ -217,6 +218,13 @@ struct dqmc_batch {
   char* arena = nullptr;
   size_t arena_bytes = 0;
   cudaStream_t own = nullptr, stream = nullptr;
+  // the general walkers' half-sweep runs as ngroups independent branches (walker
+  // ranges on their own streams, forked from and joined to `stream`), so that the
+  // latency-bound kernels of one group overlap the other groups' work
+  static constexpr int kMaxGroups = 16;
+  int ngroups = 1;
+  cudaStream_t gst[kMaxGroups] = {};
+  cudaEvent_t ev_fork = nullptr, ev_join[kMaxGroups] = {};
   std::vector<std::minstd_rand0> eng;
   double* h_uni = nullptr;          // pinned [nw][maxLt*maxN]
   double* d_uni = nullptr;
@@ -427,6 +435,22 @@ int dqmc_batch_create(const dqmc_walker_desc* descs, int n, const dqmc_batch_opt
     return fail(DQMC_ERR_CUDA, "stream/kernel set-up: %s", cudaGetErrorString(e));
   }
   b->stream = b->own;
+  {
+    // walker groups of the general path: tensor-core-path batches run one branch per 16
+    // walkers, up to 8 (DQMC_STREAM_GROUPS=1..16 overrides)
+    int ng = b->mixed ? std::min(8, std::max(1, n / 16)) : 1;
+    if (const char* env = std::getenv("DQMC_STREAM_GROUPS")) ng = std::atoi(env);
+    b->ngroups = std::max(1, std::min(ng, dqmc_batch::kMaxGroups));
+    for (int g = 0; g < b->ngroups && e == cudaSuccess; ++g) {
+      e = cudaStreamCreateWithFlags(&b->gst[g], cudaStreamNonBlocking);
+      if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->ev_join[g], cudaEventDisableTiming);
+    }
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming);
+    if (e != cudaSuccess) {
+      dqmc_batch_destroy(b);
+      return fail(DQMC_ERR_CUDA, "stream groups: %s", cudaGetErrorString(e));
+    }
+  }
   cudaMemsetAsync(b->arena, 0, b->arena_bytes, b->stream);
 
   char* base = b->arena;
@@ -546,6 +570,7 @@ int dqmc_batch_create(const dqmc_walker_desc* descs, int n, const dqmc_batch_opt
     h.status = &sc->status;
     h.uni = b->d_uni ? b->d_uni + b->uni_stride * w : nullptr;
     h.seed = d.seed;
+    h.widx = w;
     h.sweep_ctr = b->d_sweep;
     h.trace = b->trace_cap ? reinterpret_cast<double*>(base + off[w].trace) : nullptr;
     h.trace_cap = b->trace_cap;
@@ -585,6 +610,11 @@ int dqmc_batch_destroy(dqmc_batch* b) {
   if (b->h_uni) cudaFreeHost(b->h_uni);
   if (b->arena) cudaFree(b->arena);
   if (b->dyn_arena) cudaFree(b->dyn_arena);
+  for (int g = 0; g < dqmc_batch::kMaxGroups; ++g) {
+    if (b->gst[g]) cudaStreamDestroy(b->gst[g]);
+    if (b->ev_join[g]) cudaEventDestroy(b->ev_join[g]);
+  }
+  if (b->ev_fork) cudaEventDestroy(b->ev_fork);
   if (b->own) cudaStreamDestroy(b->own);
   delete b;
   return DQMC_OK;
@@ -758,14 +788,57 @@ int dqmc_init_greens(dqmc_batch* b) {
   return DQMC_OK;
 }
 
+// Level j of the general walkers W[0..nw) on stream st (kernel classes timed when profiling).
+static void issue_general_level(dqmc_batch* b, int mode, int measure, int j, int slot, const WalkerDev* W, int nw,
+                                cudaStream_t st) {
+  b->timed(DQMC_KCLASS_SEGMENT, [&] { general_chain_init(mode, W, nw, j, st); });
+  for (int q = 0; q < b->maxPace_general; ++q) {
+    b->timed(DQMC_KCLASS_PRODUCT, [&] {
+      general_slice_pre(mode, W, nw, j, q, b->maxN_general, b->any_general_dense, b->any_general_cb, b->mixed, st);
+    });
+    b->timed(DQMC_KCLASS_METROPOLIS, [&] {
+      general_slice_metro(mode, W, nw, j, q, b->maxN_general, measure, b->mixed, b->kd, b->smax, b->tc_flush, st);
+    });
+    b->timed(DQMC_KCLASS_PRODUCT, [&] {
+      general_slice_post(mode, W, nw, j, q, b->maxN_general, b->any_general_dense, b->any_general_cb, b->mixed, st);
+    });
+  }
+  b->timed(DQMC_KCLASS_PUSH, [&] {
+    general_push(mode, W, nw, j, b->maxN_general, st);
+    if (b->any_ozstab) oz_push(mode, W, nw, j, b->maxN_oz, st);
+  });
+  b->timed(DQMC_KCLASS_GREENS, [&] {
+    general_greens(mode, W, nw, j, slot, b->maxN_general, st);
+    if (b->any_ozstab) oz_greens(mode, W, nw, j, slot, b->maxN_oz, st);
+  });
+  if (measure) b->timed(DQMC_KCLASS_MEASURE, [&] { general_measure_after(mode, W, nw, j, b->maxN_general, st); });
+}
+
+static int trace_slot(const dqmc_batch* b, int j) {
+  return (b->trace_cap && b->trace_count + j < b->trace_cap) ? b->trace_count + j : -1;
+}
+
 // All device work of one half-sweep, in stream order (captured into a graph).
+// Profiled replays keep one branch (class events on one stream); otherwise the
+// general walkers run as b->ngroups forked branches.
 static void issue_half_sweep(dqmc_batch* b, int mode, int measure) {
   if (b->opt.rng == DQMC_RNG_MINSTD)
     cudaMemcpyAsync(b->d_uni, b->h_uni, sizeof(double) * b->uni_stride * b->nw, cudaMemcpyHostToDevice, b->stream);
   else
     launch_bump(b->d_sweep, b->stream);  // Philox counter: the half-sweep index
+  const int ng = (b->any_general && !b->prof) ? std::min(b->ngroups, b->nw) : 1;
+  if (ng > 1) {
+    cudaEventRecord(b->ev_fork, b->stream);
+    for (int g = 0; g < ng; ++g) {
+      const int w0 = (int)((long long)b->nw * g / ng), w1 = (int)((long long)b->nw * (g + 1) / ng);
+      cudaStreamWaitEvent(b->gst[g], b->ev_fork, 0);
+      for (int j = 0; j < b->maxNs; ++j)
+        issue_general_level(b, mode, measure, j, trace_slot(b, j), b->dW + w0, w1 - w0, b->gst[g]);
+      cudaEventRecord(b->ev_join[g], b->gst[g]);
+    }
+  }
   for (int j = 0; j < b->maxNs; ++j) {
-    const int slot = (b->trace_cap && b->trace_count + j < b->trace_cap) ? b->trace_count + j : -1;
+    const int slot = trace_slot(b, j);
     if (b->any_small) {
       b->timed(DQMC_KCLASS_SEGMENT,
                [&] { launch_segment(mode, b->dW, b->nw, j, measure, b->maxN_small, b->stream); });
@@ -775,36 +848,10 @@ static void issue_half_sweep(dqmc_batch* b, int mode, int measure) {
       if (measure)
         b->timed(DQMC_KCLASS_MEASURE, [&] { launch_measure(mode, b->dW, b->nw, j, b->maxN_small, b->stream); });
     }
-    if (b->any_general) {
-      b->timed(DQMC_KCLASS_SEGMENT, [&] { general_chain_init(mode, b->dW, b->nw, j, b->stream); });
-      for (int q = 0; q < b->maxPace_general; ++q) {
-        b->timed(DQMC_KCLASS_PRODUCT, [&] {
-          general_slice_pre(mode, b->dW, b->nw, j, q, b->maxN_general, b->any_general_dense, b->any_general_cb,
-                            b->mixed, b->stream);
-        });
-        b->timed(DQMC_KCLASS_METROPOLIS, [&] {
-          general_slice_metro(mode, b->dW, b->nw, j, q, b->maxN_general, measure, b->mixed, b->kd, b->smax,
-                              b->tc_flush, b->stream);
-        });
-        b->timed(DQMC_KCLASS_PRODUCT, [&] {
-          general_slice_post(mode, b->dW, b->nw, j, q, b->maxN_general, b->any_general_dense, b->any_general_cb,
-                             b->mixed, b->stream);
-        });
-      }
-      b->timed(DQMC_KCLASS_PUSH, [&] {
-        general_push(mode, b->dW, b->nw, j, b->maxN_general, b->stream);
-        if (b->any_ozstab) oz_push(mode, b->dW, b->nw, j, b->maxN_oz, b->stream);
-      });
-      b->timed(DQMC_KCLASS_GREENS,
-               [&] {
-                 general_greens(mode, b->dW, b->nw, j, slot, b->maxN_general, b->stream);
-                 if (b->any_ozstab) oz_greens(mode, b->dW, b->nw, j, slot, b->maxN_oz, b->stream);
-               });
-      if (measure)
-        b->timed(DQMC_KCLASS_MEASURE,
-                 [&] { general_measure_after(mode, b->dW, b->nw, j, b->maxN_general, b->stream); });
-    }
+    if (b->any_general && ng == 1) issue_general_level(b, mode, measure, j, slot, b->dW, b->nw, b->stream);
   }
+  if (ng > 1)
+    for (int g = 0; g < ng; ++g) cudaStreamWaitEvent(b->stream, b->ev_join[g], 0);
 }
 
 static int half_sweep(dqmc_batch* b, int mode, int measure) {

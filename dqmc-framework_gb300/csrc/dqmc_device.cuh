@@ -91,6 +91,7 @@ struct WalkerDev {
   double* trace;             // [trace_cap][2][N*N] or null
   int trace_cap;
   int ozstab;                // 1: stabilization by the tensor-core blocked QR (kernels_stab_oz.cu)
+  int widx;                  // index of the walker in its batch (Philox counter word)
 };
 
 // Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11): uniform double in [0,1)

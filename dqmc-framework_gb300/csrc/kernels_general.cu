@@ -418,7 +418,7 @@ __global__ void __launch_bounds__(kMetroThreads) metropolis_general_kernel(const
       const double r = (w.model == 0) ? __dmul_rn(ru, rd) : __dmul_rn(__dmul_rn(w.ex2[si], ru), rd);
       const int attempt = (mode == MODE_FWD) ? (eff * N + i) : ((Lt - t) * N + i);
       const double u = (w.rng == 0) ? w.uni[attempt]
-                                    : philox_uniform(w.seed, blockIdx.x, sweep, (unsigned)(eff * N + i));
+                                    : philox_uniform(w.seed, (unsigned)w.widx, sweep, (unsigned)(eff * N + i));
       const double prob = fmin(1.0, fabs(r));
       if (!isfinite(r)) atomicOr(w.status, ST_NONFINITE_RATIO);
       if (u < prob) {

@@ -254,12 +254,6 @@ __device__ __forceinline__ unsigned long long zfixed(double x, int e, int Q, boo
   return mant >> (-s);
 }
 
-__device__ __forceinline__ void cp16_async(void* dst, const void* src, bool pred) {
-  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
-  const int n = pred ? 16 : 0;  // 0: zero-fill, nothing is read
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(d), "l"(src), "r"(n));
-}
-
 }  // namespace
 
 // --------------------------------------------------------------------------

@@ -275,7 +275,7 @@ __global__ void __launch_bounds__(kSubThreads) metropolis_sub_kernel(const Walke
   for (int i = tid; i < N; i += kSubThreads) {
     s_field[i] = w.fields[(long long)eff * N + i];
     const int attempt = (mode == MODE_FWD) ? (eff * N + i) : ((Lt - t) * N + i);
-    uni[i] = (w.rng == 0) ? w.uni[attempt] : philox_uniform(w.seed, blockIdx.x, sweep, (unsigned)(eff * N + i));
+    uni[i] = (w.rng == 0) ? w.uni[attempt] : philox_uniform(w.seed, (unsigned)w.widx, sweep, (unsigned)(eff * N + i));
   }
   double sign = 0.0;
   long long acc_count = 0;

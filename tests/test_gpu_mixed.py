@@ -93,3 +93,31 @@ def test_autotuner_picks_a_timed_candidate(dq):
     for w in range(len(descs)):
         np.testing.assert_array_equal(om[0][w][0], of[0][w][0])
         assert float(np.abs(om[0][w][1] - of[0][w][1]).max()) <= 1e-6
+
+
+def test_walker_groups_give_identical_walkers(dq, monkeypatch):
+    """The half-sweep of 16 tensor-core-path walkers as one branch and as four
+    forked walker groups (DQMC_STREAM_GROUPS): every walker's fields, Green's
+    function and observables are bitwise the same (Philox keyed by the walker's
+    batch index, no work shared between walkers)."""
+    descs = [dq.WalkerDesc(model=1, L=12, U=4.0, mu=-0.5, beta=2.0, Lt=20, pace=5, seed=300 + w) for w in range(16)]
+    res = []
+    for groups in ("1", "4"):
+        monkeypatch.setenv("DQMC_STREAM_GROUPS", groups)
+        b = dq.Batch(descs, rng=dq.RNG_PHILOX, precision=dq.MIXED)
+        for w in range(16):
+            b.fields_random(w)
+        b.init_greens()
+        for k in range(2):
+            b.sweep_0_to_beta(measure=True)
+            b.sweep_beta_to_0(measure=True)
+        res.append(([b.fields(w) for w in range(16)], [b.green(w, 0) for w in range(16)],
+                    b.observables_all(), [b.status(w) for w in range(16)]))
+        b.close()
+    (f1, g1, o1, s1), (f4, g4, o4, s4) = res
+    for w in range(16):
+        np.testing.assert_array_equal(f1[w], f4[w])
+        np.testing.assert_array_equal(g1[w], g4[w])
+        assert s1[w] == 0 and s4[w] == 0
+    np.testing.assert_array_equal(o1[0], o4[0])
+    np.testing.assert_array_equal(o1[1], o4[1])
