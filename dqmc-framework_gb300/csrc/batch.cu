@@ -436,9 +436,9 @@ int dqmc_batch_create(const dqmc_walker_desc* descs, int n, const dqmc_batch_opt
   }
   b->stream = b->own;
   {
-    // walker groups of the general path: tensor-core-path batches run one branch per 16
-    // walkers, up to 8 (DQMC_STREAM_GROUPS=1..16 overrides)
-    int ng = b->mixed ? std::min(8, std::max(1, n / 16)) : 1;
+    // walker groups of the general path: one branch per 8 walkers, up to 16
+    // (DQMC_STREAM_GROUPS=1..16 overrides)
+    int ng = std::min(16, std::max(1, n / 8));
     if (const char* env = std::getenv("DQMC_STREAM_GROUPS")) ng = std::atoi(env);
     b->ngroups = std::max(1, std::min(ng, dqmc_batch::kMaxGroups));
     for (int g = 0; g < b->ngroups && e == cudaSuccess; ++g) {
