@@ -382,7 +382,7 @@ __global__ void __launch_bounds__(256, oz_tc_minb(S)) oz_prod_tc_kernel(const Wa
   const bool mma_done = last >= 0 && tc::mbar_wait(&done[last % NS], (last / NS) & 1);
   const int failed = __syncthreads_or(!mma_done || s_fail);
   tc::fence_after();
-  const int bits = w.slice_bits;
+  constexpr int SB = (S <= 7) ? 7 : 6;  // bits per slice of the configuration (ozaki::cfg_for_k)
   const int q4 = warp & 3, half = warp >> 2;
   const int rl = q4 * 32 + lane, r = r0 + rl;
   if (!failed) {
@@ -398,11 +398,11 @@ __global__ void __launch_bounds__(256, oz_tc_minb(S)) oz_prod_tc_kernel(const Wa
           if (col >= N) continue;
           long long hi = 0, lo = 0;
 #pragma unroll
-          for (int m = 0; m < 4; ++m) hi = (hi << bits) + (long long)__float2int_rn(__uint_as_float(v[m][u]));
+          for (int m = 0; m < 4; ++m) hi = (hi << SB) + (long long)__float2int_rn(__uint_as_float(v[m][u]));
 #pragma unroll
-          for (int m = 4; m < S; ++m) lo = (lo << bits) + (long long)__float2int_rn(__uint_as_float(v[m][u]));
+          for (int m = 4; m < S; ++m) lo = (lo << SB) + (long long)__float2int_rn(__uint_as_float(v[m][u]));
           const int e = eA[rl] + eB[cl];
-          double val = ozaki::ldexp_i64(hi, e - 5 * bits) + ozaki::ldexp_i64(lo, e - bits * (S + 1));
+          double val = ozaki::combine_hilo<S, (S <= 7 ? 7 : 6)>(hi, lo, e);
           if (OP == OZ_WL_FWD || OP == OZ_CH_FWD) val *= s_scale[rl];
           if (OP == OZ_WR_FWD) val *= s_scale[cl];
           out[(long long)col * N + r] = val;

@@ -445,7 +445,7 @@ __global__ void __launch_bounds__(256, MINB) zgemm_tc_kernel(const WalkerDev* __
           for (int m = 4; m < S; ++m) lo = (lo << B) + (long long)__float2int_rn(__uint_as_float(v[m][u]));
         }
         const int e = eA[rl] + eB[cl];
-        double val = ozaki::ldexp_i64(hi, e - 5 * B) + ozaki::ldexp_i64(lo, e - B * (S + 1));
+        double val = ozaki::combine_hilo<S, B>(hi, lo, e);
         if (jb.rs) val *= jb.rs[r];
         if (jb.cs) val *= jb.cs[col];
         const long long o = (long long)col * jb.ldc + r;

@@ -120,6 +120,21 @@ __device__ __forceinline__ double ldexp_i64(long long v, int e) {
   return __longlong_as_double((long long)(sgn | ((unsigned long long)ex << 52) | (a & 0xFFFFFFFFFFFFFULL)));
 }
 
+// The S weight-group sums of an element, read as hi = groups 0..3 (|hi| < 2^44 for
+// the configurations used: B = 7 with K <= 256, B = 6 with K <= 1024) and lo =
+// groups 4..S-1, as one FP64 value 2^e sum_m S_m 2^(-B (m + 2)): hi and the
+// rounded top of lo form one 63-bit integer hi 2^(B (S - 4) - D) + round(lo / 2^D)
+// with D = B (S - 4) - 19, so a single conversion replaces two and an FP64 add.
+// The 2^D units of lo dropped lie below the slices' own truncation (at most
+// 2^(e - 2B - 37) against K 2^(e - B S) for the products that use it).
+template <int S, int B>
+__device__ __forceinline__ double combine_hilo(long long hi, long long lo, int e) {
+  constexpr int D = B * (S - 4) - 19;
+  static_assert(D >= 1 && D < 32, "hi/lo split");
+  const long long v = (hi << (B * (S - 4) - D)) + ((lo + (1LL << (D - 1))) >> D);
+  return ldexp_i64(v, e - B * (S + 1) + D);
+}
+
 // one BF16 tensor-core MMA m16n8k16, FP32 accumulate in place
 __device__ __forceinline__ void mma16816(float (&c)[4], unsigned a0, unsigned a1, unsigned a2, unsigned a3,
                                          unsigned b0, unsigned b1) {
