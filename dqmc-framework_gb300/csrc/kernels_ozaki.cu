@@ -126,8 +126,8 @@ __device__ void slice_lines(const SliceJob& job, int N, int ldk, int role, int b
 // double buffered).  The epilogue functor receives (r, c, value).
 // --------------------------------------------------------------------------
 struct ProdJob {
-  const unsigned short* A;  // [S][N][ldk]
-  const unsigned short* B;  // [S][N][ldk]
+  const unsigned short* A;  // S slices: [S][N][ldk] (test hook) or tensor-core images (sweep)
+  const unsigned short* B;
   const int* ea;
   const int* eb;
 };

@@ -17,10 +17,13 @@
 //           R^-1 Q^T Y by blocked reflector application and blocked back
 //           substitution (FP64 diagonal blocks); G = U_R Drmax^-1 X.  Boundary
 //           steps (one stack empty) form M = Y + Dmin F and G = X or X^T.
-// Every product slices its FP64 operands in the kernel into 8 integer slices
-// of 7 bits (56 significant bits, K <= 256) or 9 of 6 (54 bits, K <= 1024) and
-// multiplies them on the BF16 tensor cores with FP32 accumulation (exact for
-// the leading weight groups): an FP64-class GEMM.  Panels, diagonal solves,
+// Every product slices its two FP64 operands once (zslice_kernel, tensor-core
+// images) into 8 integer slices of 7 bits (56 significant bits, K <= 256) or 9
+// of 6 (54 bits, K <= 1024) and multiplies them on the BF16 tensor cores with
+// FP32 accumulation (exact for the leading weight groups; zgemm_tc_kernel
+// streams the slices through oztc::mainloop): an FP64-class GEMM.  The panel
+// folds its T factor into the reflectors (Vt = V T, or V T^T when forming Q),
+// so applying a block reflector is two products.  Panels, diagonal solves,
 // reflectors and reductions are native FP64.  G equals the pivoted-QR path's
 // mathematically; the UDT factors differ only in the column order of the QR.
 #include <cuda_runtime.h>
@@ -97,8 +100,8 @@ struct ZJob {
   double* c;
   long long ldc;
   int M, N, K;
-  int beta;            // 1: C += alpha AB
-  double alpha;
+  int beta;            // 1: C += (-1)^neg AB
+  int neg;             // 1: the product enters negated (an operand modifier, no FP64 multiply)
   const double* rs;    // row multiplier of the product, or null
   const double* cs;    // column multiplier, or null
   int out;             // 1: Green's function output (wrap error, trace, spin copy)
@@ -141,7 +144,6 @@ __device__ bool zjob(const WalkerDev& w, int op, int mode, int j, int p, int sp,
   const int j0 = p * TB;
   const int m = N - j0, pb = min(TB, m);
   jb = ZJob{};
-  jb.alpha = 1.0;
   const bool panel_op = op != Z_F && op != Z_GA && op != Z_GB && op != Z_GG;
   if (panel_op && j0 >= N) return false;
   const ZOpnd Vp{z.X + (long long)j0 * N + j0, N, 0, 1, nullptr, nullptr};
@@ -163,7 +165,7 @@ __device__ bool zjob(const WalkerDev& w, int op, int mode, int j, int p, int sp,
         jb.a = Vp;
         jb.b = Wbo;
         jb.c = z.X + (long long)(j0 + pb) * N + j0; jb.ldc = N; jb.M = m; jb.N = nt; jb.K = pb;
-        jb.beta = 1; jb.alpha = -1.0;
+        jb.beta = 1; jb.neg = 1;
       }
       return true;
     }
@@ -178,7 +180,7 @@ __device__ bool zjob(const WalkerDev& w, int op, int mode, int j, int p, int sp,
         jb.a = Vp;
         jb.b = Wbo;
         jb.c = Uo + (long long)j0 * N + j0; jb.ldc = N; jb.M = m; jb.N = m; jb.K = pb;
-        jb.beta = 1; jb.alpha = -1.0;
+        jb.beta = 1; jb.neg = 1;
       }
       return true;
     }
@@ -225,7 +227,7 @@ __device__ bool zjob(const WalkerDev& w, int op, int mode, int j, int p, int sp,
         jb.a = Vp;
         jb.b = Wbo;
         jb.c = z.Y + j0; jb.ldc = N; jb.M = m; jb.N = N; jb.K = pb;
-        jb.beta = 1; jb.alpha = -1.0;
+        jb.beta = 1; jb.neg = 1;
       }
       return true;
     }
@@ -234,7 +236,7 @@ __device__ bool zjob(const WalkerDev& w, int op, int mode, int j, int p, int sp,
       jb.a = ZOpnd{z.X + (long long)(j0 + pb) * N + j0, N, 0, 0, nullptr, nullptr};
       jb.b = ZOpnd{z.Y + j0 + pb, N, 0, 0, nullptr, nullptr};
       jb.c = z.Y + j0; jb.ldc = N; jb.M = pb; jb.N = N; jb.K = N - j0 - pb;
-      jb.beta = 1; jb.alpha = -1.0;
+      jb.beta = 1; jb.neg = 1;
       return true;
     }
   }
@@ -450,7 +452,7 @@ __global__ void __launch_bounds__(256, MINB) zgemm_tc_kernel(const WalkerDev* __
         if (jb.cs) val *= jb.cs[col];
         const long long o = (long long)col * jb.ldc + r;
         if (!jb.out) {
-          val *= jb.alpha;
+          if (jb.neg) val = -val;
           jb.c[o] = jb.beta ? jb.c[o] + val : val;
         } else {
           if (check) err = fmax(err, fabs(val - jb.c[o]));
