@@ -57,7 +57,7 @@ void general_push(int mode, const WalkerDev* W, int nw, int j, int maxN, cudaStr
 void general_dynamic_slice(const WalkerDev* W, int nw, int j, int q, int maxN, bool mixed, cudaStream_t st);
 void general_dynamic_stab(const WalkerDev* W, int nw, int j, int maxN, cudaStream_t st);
 void general_dynamic_begin(const WalkerDev* W, int nw, cudaStream_t st);
-void general_dynamic_end(const WalkerDev* W, int nw, cudaStream_t st);
+void general_dynamic_end(const WalkerDev* W, int nw, int maxN, cudaStream_t st);
 void oz_push(int mode, const WalkerDev* W, int nw, int j, int maxN, cudaStream_t st);
 void oz_greens(int mode, const WalkerDev* W, int nw, int j, int trace_slot, int maxN, cudaStream_t st);
 cudaError_t configure_stab_oz_kernels(int maxN);
@@ -965,16 +965,20 @@ static int dyn_alloc(dqmc_batch* b) {
   size_t cur = 0;
   auto take = [&](size_t bytes) { const size_t o = cur; cur = align256(cur + bytes); return o; };
   const size_t taus_off = take(sizeof(int) * kMaxTau);
-  std::vector<size_t> off(b->nw * 6);
+  constexpr int kOff = 9;
+  std::vector<size_t> off(b->nw * kOff);
   for (int w = 0; w < b->nw; ++w) {
     const WalkerDev& h = b->hw[w];
     const size_t NN = (size_t)h.N * h.N;
-    off[6 * w + 0] = take(sizeof(double) * 2 * h.S * NN);  // G(t,0)
-    off[6 * w + 1] = take(sizeof(double) * 2 * h.S * NN);  // G(0,t)
-    off[6 * w + 2] = take(sizeof(double) * h.S * NN);      // X1
-    off[6 * w + 3] = take(sizeof(int) * h.S * h.N);        // LU pivots
-    off[6 * w + 4] = take(sizeof(double) * kMaxTau);
-    off[6 * w + 5] = take(sizeof(long long) * kMaxTau);
+    off[kOff * w + 0] = take(sizeof(double) * 2 * h.S * NN);  // G(t,0)
+    off[kOff * w + 1] = take(sizeof(double) * 2 * h.S * NN);  // G(0,t)
+    off[kOff * w + 2] = take(sizeof(double) * h.S * NN);      // X1
+    off[kOff * w + 3] = take(sizeof(int) * h.S * h.N);        // LU pivots
+    off[kOff * w + 4] = take(sizeof(double) * kMaxTau);
+    off[kOff * w + 5] = take(sizeof(long long) * kMaxTau);
+    off[kOff * w + 6] = take(sizeof(double) * 3 * kMaxTau);           // DOS, chi, stiffness sums
+    off[kOff * w + 7] = take(sizeof(double) * 2 * kMaxTau * h.N);     // parts awaiting G(beta,beta)
+    off[kOff * w + 8] = take(sizeof(double) * 2 * kMaxTau);
   }
   cudaError_t e = cudaMalloc(&b->dyn_arena, cur);
   if (e != cudaSuccess) {
@@ -985,12 +989,15 @@ static int dyn_alloc(dqmc_batch* b) {
   b->d_taus = reinterpret_cast<int*>(b->dyn_arena + taus_off);
   for (int w = 0; w < b->nw; ++w) {
     WalkerDev& h = b->hw[w];
-    h.gt0 = reinterpret_cast<double*>(b->dyn_arena + off[6 * w + 0]);
-    h.g0t = reinterpret_cast<double*>(b->dyn_arena + off[6 * w + 1]);
-    h.dynx = reinterpret_cast<double*>(b->dyn_arena + off[6 * w + 2]);
-    h.dpiv = reinterpret_cast<int*>(b->dyn_arena + off[6 * w + 3]);
-    h.dyn_sum = reinterpret_cast<double*>(b->dyn_arena + off[6 * w + 4]);
-    h.dyn_cnt = reinterpret_cast<long long*>(b->dyn_arena + off[6 * w + 5]);
+    h.gt0 = reinterpret_cast<double*>(b->dyn_arena + off[kOff * w + 0]);
+    h.g0t = reinterpret_cast<double*>(b->dyn_arena + off[kOff * w + 1]);
+    h.dynx = reinterpret_cast<double*>(b->dyn_arena + off[kOff * w + 2]);
+    h.dpiv = reinterpret_cast<int*>(b->dyn_arena + off[kOff * w + 3]);
+    h.dyn_sum = reinterpret_cast<double*>(b->dyn_arena + off[kOff * w + 4]);
+    h.dyn_cnt = reinterpret_cast<long long*>(b->dyn_arena + off[kOff * w + 5]);
+    h.dyn_obs = reinterpret_cast<double*>(b->dyn_arena + off[kOff * w + 6]);
+    h.dyn_vec = reinterpret_cast<double*>(b->dyn_arena + off[kOff * w + 7]);
+    h.dyn_part = reinterpret_cast<double*>(b->dyn_arena + off[kOff * w + 8]);
     h.dyn_taus = b->d_taus;
     h.dyn_ntau = 0;
   }
@@ -1004,6 +1011,7 @@ int dqmc_clear_dynamic(dqmc_batch* b) {
   for (int w = 0; w < b->nw; ++w) {
     CUDA_TRY(cudaMemsetAsync(b->hw[w].dyn_sum, 0, sizeof(double) * kMaxTau, b->stream));
     CUDA_TRY(cudaMemsetAsync(b->hw[w].dyn_cnt, 0, sizeof(long long) * kMaxTau, b->stream));
+    CUDA_TRY(cudaMemsetAsync(b->hw[w].dyn_obs, 0, sizeof(double) * 3 * kMaxTau, b->stream));
   }
   CUDA_TRY(cudaStreamSynchronize(b->stream));
   return DQMC_OK;
@@ -1043,7 +1051,7 @@ int dqmc_sweep_dynamic(dqmc_batch* b, const int* taus, int ntau) {
     general_greens(MODE_FWD, b->dW, b->nw, j, -1, b->maxN_general, b->stream);
     general_dynamic_stab(b->dW, b->nw, j, b->maxN_general, b->stream);
   }
-  general_dynamic_end(b->dW, b->nw, b->stream);
+  general_dynamic_end(b->dW, b->nw, b->maxN_general, b->stream);
   CUDA_TRY(cudaMemcpyAsync(b->dW, b->hw.data(), sizeof(WalkerDev) * b->nw, cudaMemcpyHostToDevice, b->stream));
   CUDA_TRY(cudaStreamSynchronize(b->stream));
   if (int r = launch_check("dynamic sweep")) return r;
@@ -1061,6 +1069,21 @@ int dqmc_get_dynamic(dqmc_batch* b, int w, double* sums, int64_t* counts) {
   CUDA_TRY(cudaStreamSynchronize(b->stream));
   if (counts)
     for (int k = 0; k < n; ++k) counts[k] = c[k];
+  return DQMC_OK;
+}
+
+int dqmc_get_dynamic_obs(dqmc_batch* b, int w, double* dos, double* chi, double* rho) {
+  if (int r = check_walker(b, w)) return r;
+  if (!b->dyn_arena || b->taus.empty()) return DQMC_OK;
+  const int n = (int)b->taus.size();
+  std::vector<double> v(3 * (size_t)n);
+  CUDA_TRY(cudaMemcpyAsync(v.data(), b->hw[w].dyn_obs, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, b->stream));
+  CUDA_TRY(cudaStreamSynchronize(b->stream));
+  for (int k = 0; k < n; ++k) {
+    if (dos) dos[k] = v[3 * k + 0];
+    if (chi) chi[k] = v[3 * k + 1];
+    if (rho) rho[k] = v[3 * k + 2];
+  }
   return DQMC_OK;
 }
 

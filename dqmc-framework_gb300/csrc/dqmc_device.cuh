@@ -59,6 +59,11 @@ struct WalkerDev {
   long long* dyn_cnt;
   const int* dyn_taus;
   int dyn_ntau;
+  // dynamic observables: sums [tau][3] (density of states, spin susceptibility, stiffness),
+  // per-half-sweep parts awaiting G(beta,beta): vectors [tau][2][N] and scalars [tau][2]
+  double* dyn_obs;
+  double* dyn_vec;
+  double* dyn_part;
   int zld;                   // line stride of zsl (N rounded up to 32)
   // tensor-core stabilization: BF16 slices of both operands of the current product,
   // [S][2 operands][9 slices][N][zld]

@@ -1099,33 +1099,126 @@ __global__ void __launch_bounds__(256) dyn_measure_kernel(const WalkerDev* __res
   int slot = -1;
   for (int k = 0; k < w.dyn_ntau; ++k)
     if (w.dyn_taus[k] == t) slot = k;
-  if (slot < 0) return;
-  const int N = w.N, L = w.L;
+  const int N = w.N, L = w.L, S = w.S;
   const long long NN = (long long)N * N;
-  const double* gu;
-  if (phase == 2) gu = w.G;
-  else gu = w.gt0 + ((long long)(t & 1) * w.S) * NN;
-  const double* gd = (w.S == 2) ? gu + NN : gu;
-  double v = 0.0;
+  const double sg = *w.sign;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  for (int jj = wid; jj < N; jj += 8) {
-    const int xj = jj % L, yj = jj / L;
-    for (int i = lane; i < N; i += 32) {
-      int dx = xj - i % L, dy = yj - i / L;
-      dx += (dx < 0) ? L : 0;
-      dy += (dy < 0) ? L : 0;
-      v += w.ff[dx + dy * L] * (gu[(long long)i * N + jj] + gd[(long long)i * N + jj]);  // G(jj, i)
+  extern __shared__ double dsh[];  // [L] cos(-r kx1), phase 2 also [N] e_i and [N] B_i
+  __shared__ double red[8][4];
+  // FourierFactor(r, 1) of the reference's k-star 1 = (2 pi / L, 0) on the site (r, 0)
+  const double kx1 = (double)((L + 1) / 2 + 1) / L * 2 * M_PI - M_PI;
+  for (int r = threadIdx.x; r < L; r += blockDim.x) dsh[r] = cos(-r * kx1);
+  __syncthreads();
+  if (slot >= 0) {
+    // G(t,t), G(t,0), G(0,t); at tau = 0 the reference's index Lt-1: G(beta,beta), G(beta,0), G(0,beta)
+    const int tb = (phase == 2) ? (w.Lt & 1) : (t & 1);
+    const double* gtt[2] = {w.G, w.G + (S == 2 ? NN : 0)};
+    const double* gt0[2] = {w.gt0 + (long long)tb * S * NN, w.gt0 + ((long long)tb * S + (S == 2)) * NN};
+    const double* g0t[2] = {w.g0t + (long long)tb * S * NN, w.g0t + ((long long)tb * S + (S == 2)) * NN};
+    // G(k,tau) and the density of states read G(beta,beta) at tau = 0 (Greentt(Lt-1))
+    const double* gk[2] = {phase == 2 ? gtt[0] : gt0[0], phase == 2 ? gtt[1] : gt0[1]};
+    double v = 0.0, tr = 0.0, cpart = 0.0, rcor = 0.0;
+    for (int jj = wid; jj < N; jj += 8) {
+      const int xj = jj % L, yj = jj / L;
+      const int jpx = (xj + 1) % L + L * yj;
+      for (int i = lane; i < N; i += 32) {
+        const int xi = i % L, yi = i / L;
+        int dx = xj - xi, dy = yj - yi;
+        dx += (dx < 0) ? L : 0;
+        dy += (dy < 0) ? L : 0;
+        v += w.ff[dx + dy * L] * (gk[0][(long long)i * N + jj] + gk[1][(long long)i * N + jj]);  // G(jj, i)
+        // correlated current-current term of the stiffness (i, jj): measure_methods.cpp:400-407
+        const int ipx = (xi + 1) % L + L * yi;
+        const double fq = dsh[dx] - dsh[dy];
+        double c = 0.0;
+        for (int sp = 0; sp < S; ++sp) {
+          const double* a = g0t[sp];
+          const double* b = gt0[sp];
+          c += -a[(long long)jpx * N + ipx] * b[(long long)i * N + jj] + a[(long long)jpx * N + i] * b[(long long)ipx * N + jj] +
+               a[(long long)jj * N + ipx] * b[(long long)i * N + jpx] - a[(long long)jj * N + i] * b[(long long)ipx * N + jpx];
+        }
+        rcor += fq * ((S == 1) ? 2.0 * c : c);
+      }
+    }
+    for (int i = threadIdx.x; i < N; i += blockDim.x) {
+      const long long d = (long long)i * N + i;
+      const int xi = i % L, yi = i / L, ipx = (xi + 1) % L + L * yi;
+      tr += gk[0][d] + gk[1][d];
+      cpart += g0t[0][d] * gt0[0][d] + g0t[1][d] * gt0[1][d];
+      // parts that wait for G(beta,beta): d_i of the spin susceptibility, A_i of the stiffness
+      double* dv = w.dyn_vec + (long long)slot * 2 * N;
+      dv[i] = (1.0 - gtt[0][d]) - (1.0 - gtt[1][d]);
+      dv[N + i] = (gtt[0][(long long)ipx * N + i] - gtt[0][(long long)i * N + ipx]) +
+                  (gtt[1][(long long)ipx * N + i] - gtt[1][(long long)i * N + ipx]);
+    }
+    v = warp_sum_g(v);
+    tr = warp_sum_g(tr);
+    cpart = warp_sum_g(cpart);
+    rcor = warp_sum_g(rcor);
+    if (lane == 0) {
+      red[wid][0] = v;
+      red[wid][1] = tr;
+      red[wid][2] = cpart;
+      red[wid][3] = rcor;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double tot[4] = {0.0, 0.0, 0.0, 0.0};
+      for (int k = 0; k < 8; ++k)
+        for (int m = 0; m < 4; ++m) tot[m] += red[k][m];
+      w.dyn_sum[slot] += sg * 0.5 * tot[0] / N;
+      w.dyn_cnt[slot] += 1;
+      w.dyn_obs[slot * 3 + 0] += sg * 0.5 * tot[1] / N;
+      w.dyn_part[slot * 2 + 0] = tot[2];
+      w.dyn_part[slot * 2 + 1] = tot[3];
     }
   }
-  __shared__ double red[8];
-  v = warp_sum_g(v);
-  if (lane == 0) red[wid] = v;
+  if (phase != 2) return;
+  // end of the half-sweep: g00 = G(beta,beta) completes the spin susceptibility and the
+  // uncorrelated stiffness term of every listed tau (measure_methods.cpp:345-461)
   __syncthreads();
-  if (threadIdx.x == 0) {
-    double tot = 0.0;
-    for (int k = 0; k < 8; ++k) tot += red[k];
-    w.dyn_sum[slot] += *w.sign * 0.5 * tot / N;
-    w.dyn_cnt[slot] += 1;
+  double* e = dsh + L;
+  double* B = e + N;
+  for (int i = threadIdx.x; i < N; i += blockDim.x) {
+    const long long d = (long long)i * N + i;
+    const int ipx = (i % L + 1) % L + L * (i / L);
+    const double* g0 = w.G;
+    const double* g1 = w.G + (S == 2 ? NN : 0);
+    e[i] = (1.0 - g0[d]) - (1.0 - g1[d]);
+    B[i] = (g0[(long long)ipx * N + i] - g0[(long long)i * N + ipx]) + (g1[(long long)ipx * N + i] - g1[(long long)i * N + ipx]);
+  }
+  __syncthreads();
+  for (int k = 0; k < w.dyn_ntau; ++k) {
+    const double* dv = w.dyn_vec + (long long)k * 2 * N;
+    double ch = 0.0, un = 0.0;
+    for (int i = threadIdx.x; i < N; i += blockDim.x) ch += dv[i] * e[i];
+    for (int jj = wid; jj < N; jj += 8) {
+      const int xj = jj % L, yj = jj / L;
+      for (int i = lane; i < N; i += 32) {
+        int dx = xj - i % L, dy = yj - i / L;
+        dx += (dx < 0) ? L : 0;
+        dy += (dy < 0) ? L : 0;
+        un += (dsh[dx] - dsh[dy]) * dv[N + jj] * B[i];
+      }
+    }
+    ch = warp_sum_g(ch);
+    un = warp_sum_g(un);
+    if (lane == 0) {
+      red[wid][0] = ch;
+      red[wid][1] = un;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double c2 = 0.0, u2 = 0.0;
+      for (int q2 = 0; q2 < 8; ++q2) {
+        c2 += red[q2][0];
+        u2 += red[q2][1];
+      }
+      const double n = (double)N;
+      w.dyn_obs[k * 3 + 1] += 0.25 * sg / n * (c2 - w.dyn_part[k * 2 + 0]);
+      w.dyn_obs[k * 3 + 2] += 0.25 * w.hop_t * w.hop_t * sg * (w.dyn_part[k * 2 + 1] - u2) / (n * n);
+    }
+    __syncthreads();
   }
 }
 
@@ -1206,7 +1299,7 @@ void general_dynamic_slice(const WalkerDev* W, int nw, int j, int q, int maxN, b
   }
   gemm_op_kernel<OP_DT0><<<g, 256, 0, st>>>(W, MODE_FWD, j, q, -1);
   gemm_op_kernel<OP_D0T><<<g, 256, 0, st>>>(W, MODE_FWD, j, q, -1);
-  dyn_measure_kernel<<<nw, 256, 0, st>>>(W, j, q, 0);
+  dyn_measure_kernel<<<nw, 256, sizeof(double) * 32, st>>>(W, j, q, 0);
   if (mixed) mixed_chain(W, nw, maxN, MODE_FWD, j, q, st);
   else gemm_op_kernel<OP_CH_FWD><<<g, 256, 0, st>>>(W, MODE_FWD, j, q, -1);
 }
@@ -1219,14 +1312,14 @@ void general_dynamic_stab(const WalkerDev* W, int nw, int j, int maxN, cudaStrea
   gemm_op_kernel<OP_DT0_OUT><<<g, 256, 0, st>>>(W, MODE_FWD, j, 0, -1);
   gemm_op_kernel<OP_D0T_OUT><<<g, 256, 0, st>>>(W, MODE_FWD, j, 0, -1);
   dyn_boundary_kernel<<<dim3(64, 2 * nw), 256, 0, st>>>(W, j);
-  dyn_measure_kernel<<<nw, 256, 0, st>>>(W, j, 0, 1);
+  dyn_measure_kernel<<<nw, 256, sizeof(double) * 32, st>>>(W, j, 0, 1);
 }
 
 void general_dynamic_begin(const WalkerDev* W, int nw, cudaStream_t st) {
   dyn_init_kernel<<<dim3(64, 2 * nw), 256, 0, st>>>(W);
 }
-void general_dynamic_end(const WalkerDev* W, int nw, cudaStream_t st) {
-  dyn_measure_kernel<<<nw, 256, 0, st>>>(W, 0, 0, 2);
+void general_dynamic_end(const WalkerDev* W, int nw, int maxN, cudaStream_t st) {
+  dyn_measure_kernel<<<nw, 256, sizeof(double) * (32 + 2 * maxN), st>>>(W, 0, 0, 2);
 }
 
 cudaError_t configure_general_kernels() {

@@ -36,7 +36,7 @@ EXPORTS = [
     "dqmc_clear_observables", "dqmc_trace_count", "dqmc_trace_get", "dqmc_trace_clear", "dqmc_batch_info",
     "dqmc_profile_enable", "dqmc_profile_read", "dqmc_microbench_fp64", "dqmc_get_observables_all",
     "dqmc_product_check", "dqmc_product_device_noalloc", "dqmc_launch_count", "dqmc_tuning",
-    "dqmc_sweep_dynamic", "dqmc_get_dynamic", "dqmc_clear_dynamic", "dqmc_get_green_dynamic",
+    "dqmc_sweep_dynamic", "dqmc_get_dynamic", "dqmc_clear_dynamic", "dqmc_get_green_dynamic", "dqmc_get_dynamic_obs",
 ]
 KCLASSES = ["segment", "push", "greens", "measure", "product", "metropolis"]
 
@@ -94,6 +94,7 @@ def load() -> ctypes.CDLL:
         "dqmc_tuning": (c, [vp, ip, ip, ip, ip, ip, ctypes.POINTER(ctypes.c_float)]),
         "dqmc_sweep_dynamic": (c, [vp, ip, c]), "dqmc_get_dynamic": (c, [vp, c, dp, i64p]),
         "dqmc_clear_dynamic": (c, [vp]), "dqmc_get_green_dynamic": (c, [vp, c, c, c, dp]),
+        "dqmc_get_dynamic_obs": (c, [vp, c, dp, dp, dp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -275,6 +276,15 @@ class Batch:
         c = (ctypes.c_int64 * max(n, 1))()
         _check(load().dqmc_get_dynamic(self.h, w, s.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), c))
         return s[:n], np.array(list(c))[:n]
+
+    def dynamic_obs(self, w: int):
+        """(dos, chi, rho) sums per listed tau for walker w: density of states, local
+        dynamic spin susceptibility and the superfluid-stiffness contribution of that tau."""
+        n = len(getattr(self, "_taus", []))
+        d, c, r = (np.zeros(max(n, 1)) for _ in range(3))
+        P = ctypes.POINTER(ctypes.c_double)
+        _check(load().dqmc_get_dynamic_obs(self.h, w, d.ctypes.data_as(P), c.ctypes.data_as(P), r.ctypes.data_as(P)))
+        return d[:n], c[:n], r[:n]
 
     def clear_dynamic(self):
         _check(load().dqmc_clear_dynamic(self.h))

@@ -153,6 +153,14 @@ int dqmc_sweep_dynamic(dqmc_batch* b, const int* taus, int ntau);
 /* Sums of sign * G(k,tau) and their counts, in the order of the last tau list. */
 int dqmc_get_dynamic(dqmc_batch* b, int walker, double* sums, int64_t* counts);
 int dqmc_clear_dynamic(dqmc_batch* b);
+/* Sums per listed tau of the other dynamic observables of the reference
+ * (src/measure/measure_methods.cpp:315-461): the density of states D(tau)
+ * (measure_density_of_states), the local dynamic spin susceptibility
+ * (measure_dynamic_spin_susceptibility) and the superfluid-stiffness
+ * contribution of that tau (measure_superfluid_stiffness sums it over all tau),
+ * each sign-weighted like the reference's tmp_value; counts as dqmc_get_dynamic.
+ * Any output may be null. */
+int dqmc_get_dynamic_obs(dqmc_batch* b, int walker, double* dos, double* chi, double* rho);
 /* G(beta,0) (which = 0) or G(0,beta) (which = 1) after the last dynamic half-sweep
  * (DqmcWalker::Greent0Up/Dn, Green0tUp/Dn at t = Lt), column-major N x N. */
 int dqmc_get_green_dynamic(dqmc_batch* b, int walker, int which, int spin, double* out);

@@ -140,6 +140,15 @@ class DqmcWalker {
     if (counts) *counts = c;
     return s;
   }
+  // measure_density_of_states, measure_dynamic_spin_susceptibility and the per-tau terms of
+  // measure_superfluid_stiffness (src/measure/measure_methods.cpp:315-461), sums per listed tau
+  struct DynamicObservables { std::vector<double> density_of_states, spin_susceptibility, stiffness_terms; };
+  DynamicObservables DynamicObs(int w, int ntau) const {
+    DynamicObservables o{std::vector<double>(ntau), std::vector<double>(ntau), std::vector<double>(ntau)};
+    check(dqmc_get_dynamic_obs(b_, w, o.density_of_states.data(), o.spin_susceptibility.data(),
+                               o.stiffness_terms.data()));
+    return o;
+  }
   std::vector<double> Greent0Up(int w) const { return green_dyn(w, 0, 0); }  // G(beta,0) after the last dynamic half-sweep
   std::vector<double> Greent0Dn(int w) const { return green_dyn(w, 0, 1); }
   std::vector<double> Green0tUp(int w) const { return green_dyn(w, 1, 0); }

@@ -21,6 +21,7 @@
 #include "dqmc_oracle.h"
 
 #include <algorithm>
+#include <array>
 #include <cassert>
 #include <cmath>
 #include <cstring>
@@ -649,6 +650,11 @@ struct Oracle {
   std::vector<int> dyn_taus;
   std::vector<double> dyn_sum;
   std::vector<long long> dyn_cnt;
+  // density of states, dynamic spin susceptibility and superfluid-stiffness contribution
+  // per listed tau (sums over dynamic half-sweeps, sign-weighted as the reference's)
+  std::vector<double> dyn_dos, dyn_chi, dyn_rho;
+  // G(t,t), G(t,0), G(0,t) per spin at the listed tau of the current half-sweep
+  std::vector<std::array<Vec, 6>> dyn_rec;
 
   double& s(int t, int i) { return field[(size_t)t * N + i]; }
   double s(int t, int i) const { return field[(size_t)t * N + i]; }
@@ -1081,6 +1087,56 @@ struct Oracle {
     dyn_sum[slot] += sum;
     dyn_cnt[slot] += 1;
   }
+  // The dynamic observables of measure_methods.cpp:315-461 for the listed tau, from the
+  // recorded G(t,t), G(t,0), G(0,t) (tau >= 1: slice tau; tau = 0: the reference's
+  // index Lt-1, i.e. G(beta,beta), G(beta,0), G(0,beta)) and g00 = G(beta,beta):
+  //   density of states (316-332): sign tr(G(t,0) spin-averaged) / N, G(beta,beta) at tau = 0;
+  //   dynamic spin susceptibility (422-461): 0.25 sign / N sum_i (Gc(t,t)_ii Gc00_ii - G(0,t)_ii G(t,0)_ii
+  //     for both spins - Gc(t,t)up_ii Gc00dn_ii - Gc00up_ii Gc(t,t)dn_ii), Gc = I - G^T;
+  //   superfluid stiffness (345-416): 0.25 t^2 sign / N^2 sum_ij (cos kx rx - cos kx ry) (uncorrelated
+  //     and correlated current terms), one contribution per tau (the reference sums them over all tau).
+  void measure_dynamic_obs(int ntau) {
+    const double s = sign, invN = 1.0 / N, kx1 = lat.kx[1];
+    const Vec& g00u = G[0];
+    const Vec& g00d = G[1];
+    for (int k = 0; k < ntau; ++k) {
+      const int t = dyn_taus[k];
+      const auto& r = dyn_rec[k];
+      const Vec &gttu = r[0], &gttd = r[1], &gt0u = r[2], &gt0d = r[3], &g0tu = r[4], &g0td = r[5];
+      // density of states: G(beta,beta) at tau = 0 (the reference's Greentt(Lt-1))
+      const Vec& du = (t == 0) ? gttu : gt0u;
+      const Vec& dd = (t == 0) ? gttd : gt0d;
+      double tr = 0.0;
+      for (int i = 0; i < N; ++i) tr += 0.5 * (at(du, N, i, i) + at(dd, N, i, i));
+      dyn_dos[k] += s * tr * invN;
+      double chi = 0.0;
+      for (int i = 0; i < N; ++i) {
+        const double gcttu = 1.0 - at(gttu, N, i, i), gcttd = 1.0 - at(gttd, N, i, i);
+        const double gc00u = 1.0 - at(g00u, N, i, i), gc00d = 1.0 - at(g00d, N, i, i);
+        chi += 0.25 * s * invN *
+               (+gcttu * gc00u - at(g0tu, N, i, i) * at(gt0u, N, i, i) + gcttd * gc00d -
+                at(g0td, N, i, i) * at(gt0d, N, i, i) - gcttu * gc00d - gc00u * gcttd);
+      }
+      dyn_chi[k] += chi;
+      double rho = 0.0;
+      for (int i = 0; i < N; ++i) {
+        const int ipx = lat.nn[i * 4 + 0];
+        for (int j = 0; j < N; ++j) {
+          const int jpx = lat.nn[j * 4 + 0];
+          const int d = lat.disp(i, j), rx = d % lat.L, ry = d / lat.L;
+          const double ff = std::cos(-rx * kx1) - std::cos(-ry * kx1);  // FourierFactor(rx,1) - (ry,1)
+          rho += p.hopping_t * p.hopping_t * s * ff *
+                 (-(at(gttu, N, j, jpx) - at(gttu, N, jpx, j) + at(gttd, N, j, jpx) - at(gttd, N, jpx, j)) *
+                      (at(g00u, N, i, ipx) - at(g00u, N, ipx, i) + at(g00d, N, i, ipx) - at(g00d, N, ipx, i)) -
+                  at(g0tu, N, ipx, jpx) * at(gt0u, N, j, i) - at(g0td, N, ipx, jpx) * at(gt0d, N, j, i) +
+                  at(g0tu, N, i, jpx) * at(gt0u, N, j, ipx) + at(g0td, N, i, jpx) * at(gt0d, N, j, ipx) +
+                  at(g0tu, N, ipx, j) * at(gt0u, N, jpx, i) + at(g0td, N, ipx, j) * at(gt0d, N, jpx, i) -
+                  at(g0tu, N, i, j) * at(gt0u, N, jpx, ipx) - at(g0td, N, i, j) * at(gt0d, N, jpx, ipx));
+        }
+      }
+      dyn_rho[k] += 0.25 * rho / ((double)N * N);
+    }
+  }
   // sweep_for_dynamic_greens (dqmc_walker.cpp:424-524): 0 -> beta with the fields fixed
   void sweep_dynamic(const int* taus, int ntau) {
     if (!left[0].empty() || right[0].len != nstack)
@@ -1089,7 +1145,11 @@ struct Oracle {
       dyn_taus.assign(taus, taus + ntau);
       dyn_sum.assign(ntau, 0.0);
       dyn_cnt.assign(ntau, 0);
+      dyn_dos.assign(ntau, 0.0);
+      dyn_chi.assign(ntau, 0.0);
+      dyn_rho.assign(ntau, 0.0);
     }
+    dyn_rec.assign(ntau, {});
     const Vec I = identity(N);
     for (int sp = 0; sp < 2; ++sp) {
       gt0[sp] = G[sp];
@@ -1126,10 +1186,18 @@ struct Oracle {
         td = identity(N);
       }
       for (int k = 0; k < ntau; ++k)
-        if (taus[k] == t && t < Lt) accumulate_dynamic(k, gt0[0], gt0[1]);
+        if (taus[k] == t && t < Lt) {
+          accumulate_dynamic(k, gt0[0], gt0[1]);
+          dyn_rec[k] = {G[0], G[1], gt0[0], gt0[1], g0t[0], g0t[1]};
+        }
     }
     for (int k = 0; k < ntau; ++k)
-      if (taus[k] == 0) accumulate_dynamic(k, G[0], G[1]);  // tau = 0: G(beta, beta) = G(0, 0)
+      if (taus[k] == 0) {
+        accumulate_dynamic(k, G[0], G[1]);  // tau = 0: G(beta, beta) = G(0, 0)
+        dyn_rec[k] = {G[0], G[1], gt0[0], gt0[1], g0t[0], g0t[1]};  // index Lt-1: t = beta
+      }
+    measure_dynamic_obs(ntau);
+    dyn_rec.clear();
   }
 
   // --- equal-time measurements (measure_methods.cpp:22-255) ---------------------
@@ -1246,6 +1314,13 @@ void orc_get_dynamic(void* h, double* sums, int64_t* counts) {
   for (size_t k = 0; k < O(h)->dyn_sum.size(); ++k) {
     sums[k] = O(h)->dyn_sum[k];
     counts[k] = O(h)->dyn_cnt[k];
+  }
+}
+void orc_get_dynamic_obs(void* h, double* dos, double* chi, double* rho) {
+  for (size_t k = 0; k < O(h)->dyn_dos.size(); ++k) {
+    dos[k] = O(h)->dyn_dos[k];
+    chi[k] = O(h)->dyn_chi[k];
+    rho[k] = O(h)->dyn_rho[k];
   }
 }
 void orc_get_green_dynamic(void* h, int which, int spin, double* out) {

@@ -85,6 +85,7 @@ def lib() -> ctypes.CDLL:
         "orc_sweep_dynamic": (ctypes.c_int, [vp, ctypes.POINTER(ctypes.c_int), ctypes.c_int]),
         "orc_get_dynamic": (None, [vp, dp, ctypes.POINTER(ctypes.c_int64)]),
         "orc_get_green_dynamic": (None, [vp, ctypes.c_int, ctypes.c_int, dp]),
+        "orc_get_dynamic_obs": (None, [vp, dp, dp, dp]),
         "orc_measure": (None, [vp]), "orc_write_bin": (None, [vp, ctypes.c_int, dp]),
         "orc_get_accumulators": (None, [vp, dp, ctypes.POINTER(ctypes.c_int)]),
         "orc_get_green": (None, [vp, ctypes.c_int, dp]),
@@ -210,6 +211,14 @@ class Walker:
         c = (ctypes.c_int64 * n)()
         lib().orc_get_dynamic(self.h, _dp(s), c)
         return s, np.array(list(c))
+
+    def dynamic_obs(self):
+        """(dos, chi, rho) sums per listed tau: density of states, dynamic spin
+        susceptibility and the superfluid-stiffness contribution of that tau."""
+        n = len(self._taus)
+        d, c, r = np.zeros(n), np.zeros(n), np.zeros(n)
+        lib().orc_get_dynamic_obs(self.h, _dp(d), _dp(c), _dp(r))
+        return d, c, r
 
     def green_dynamic(self, which: int, spin: int) -> np.ndarray:
         """which 0: G(t, 0), 1: G(0, t) after the last dynamic sweep (t = beta)."""

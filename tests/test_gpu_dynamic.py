@@ -129,3 +129,47 @@ def test_dynamic_sweep_state_and_arguments(dq):
     small.init_greens()
     with pytest.raises(dq.DqmcError):
         small.sweep_dynamic([0])      # shared-memory walkers
+
+
+@pytest.mark.parametrize("model,L,mu,Lt,pace", [
+    (0, 10, 0.0, 20, 5),    # repulsive, N = 100
+    (1, 10, -0.5, 24, 8),   # attractive
+])
+def test_dynamic_observables_against_oracle(dq, oracle_mod, model, L, mu, Lt, pace):
+    """Density of states, local dynamic spin susceptibility and the superfluid-stiffness
+    terms per tau (measure_methods.cpp:315-461) on the FP64 path against the oracle,
+    over two dynamic half-sweeps separated by a backward half-sweep."""
+    O = oracle_mod
+    O.use_scipy_lapack(False)
+    d = dq.WalkerDesc(model=model, L=L, U=4.0, mu=mu, beta=2.0, Lt=Lt, pace=pace, seed=17)
+    b = dq.Batch([d], rng=dq.RNG_MINSTD)
+    r = O.Walker(model=model, L=L, U=4.0, mu=mu, beta=2.0, Lt=Lt, pace=pace, stack=O.STACK_QRP)
+    r.seed(17)
+    b.fields_random(0)
+    r.fields_random()
+    b.init_greens()
+    r.init()
+    taus = [0, 1, pace - 1, pace, pace + 3, Lt - 1]
+    for rnd in range(2):
+        b.sweep_dynamic(taus)
+        r.sweep_dynamic(taus)
+        for dev, ref in zip(b.dynamic_obs(0), r.dynamic_obs()):
+            assert _close(dev, ref), (rnd, dev, ref)
+        b.sweep_beta_to_0(measure=False)
+        r.sweep_beta_to_0()
+    assert b.status(0) == 0
+
+
+def test_dynamic_observables_mixed_against_fp64(dq):
+    """The tensor-core path (N = 144) against the FP64 path on the same fields."""
+    descs = [dq.WalkerDesc(model=0, L=12, U=4.0, beta=2.0, Lt=20, pace=5, seed=80)]
+    taus = [0, 2, 5, 11, 19]
+    res = []
+    for prec in (dq.MIXED, dq.FP64):
+        b = dq.Batch(descs, rng=dq.RNG_MINSTD, precision=prec)
+        b.fields_random(0)
+        b.init_greens()
+        b.sweep_dynamic(taus)
+        res.append(b.dynamic_obs(0))
+    for m, f in zip(res[0], res[1]):
+        assert _close(m, f, 1e-6), (m, f)

@@ -330,3 +330,75 @@ def test_statistical_pin_against_reference_example(oracle_mod, example_fixture):
             assert abs(mean[k] - ref) < 4 * sigma, (name, mean[k], err[k], ref, ref_err)
     wrap = max(r[1] for r in res)
     assert 1e-11 < wrap < 1e-6  # published maximum wrap error 1.085e-8
+
+
+def _free_fermion_dynamic_obs(L, t, mu, beta, Lt, taus):
+    """U = 0 restatement of measure_methods.cpp:315-461 with the analytic Green's functions
+    G0 = (1 + e^{-beta K})^-1, G(tau,0) = e^{-tau K} G0, G(0,tau) = -(1 - G0) e^{tau K},
+    G(tau,tau) = G0 (the reference's index Lt-1 at tau = 0: G(beta,0), G(0,beta))."""
+    N = L * L
+    H = np.zeros((N, N))
+    for i in range(N):
+        x, y = i % L, i // L
+        for j in ((x + 1) % L + L * y, x + L * ((y + 1) % L)):
+            H[i, j] += 1.0
+            H[j, i] += 1.0
+    K = -t * H + mu * np.eye(N)
+    ev, U = np.linalg.eigh(K)
+    ex = lambda s: (U * np.exp(s * ev)) @ U.T
+    I = np.eye(N)
+    G0 = np.linalg.inv(I + ex(-beta))
+    dt = beta / Lt
+    kx1 = ((L + 1) // 2 + 1) / L * 2 * np.pi - np.pi
+    cf = np.cos(-np.arange(L) * kx1)
+    nn = [(i % L + 1) % L + L * (i // L) for i in range(N)]
+    out = []
+    for tau in taus:
+        s = beta if tau == 0 else tau * dt
+        gtt, g00 = G0, G0
+        gt0 = ex(-s) @ G0
+        g0t = -(I - G0) @ ex(s)
+        dos = np.trace(G0 if tau == 0 else gt0) / N
+        chi = sum(0.25 / N * (2 * (1 - gtt[i, i]) * (1 - g00[i, i]) - 2 * g0t[i, i] * gt0[i, i]
+                              - 2 * (1 - gtt[i, i]) * (1 - g00[i, i])) for i in range(N))
+        rho = 0.0
+        for i in range(N):
+            ipx = nn[i]
+            for j in range(N):
+                jpx = nn[j]
+                rx, ry = (j % L - i % L) % L, (j // L - i // L) % L
+                ff = cf[rx] - cf[ry]
+                rho += t * t * ff * (
+                    -(2 * (gtt[j, jpx] - gtt[jpx, j])) * (2 * (g00[i, ipx] - g00[ipx, i]))
+                    + 2 * (-g0t[ipx, jpx] * gt0[j, i] + g0t[i, jpx] * gt0[j, ipx]
+                           + g0t[ipx, j] * gt0[jpx, i] - g0t[i, j] * gt0[jpx, ipx]))
+        out.append((dos, chi, 0.25 * rho / N ** 2))
+    return np.array(out)
+
+
+@pytest.mark.parametrize("stack", [0, 1])
+def test_dynamic_observables_free_fermions_known_answer(oracle_mod, stack):
+    """U = 0: density of states, local dynamic spin susceptibility and the stiffness terms
+    of the oracle's dynamic half-sweep equal the analytic free-fermion values."""
+    O = oracle_mod
+    L, mu, beta, Lt = 4, 0.3, 2.0, 20
+    w = O.Walker(model=0, L=L, U=0.0, mu=mu, beta=beta, Lt=Lt, pace=5, stack=stack)
+    w.seed(5)
+    w.fields_random()
+    w.init()
+    taus = [0, 1, 5, 7, 10, 19]
+    w.sweep_dynamic(taus)
+    dos, chi, rho = w.dynamic_obs()
+    ref = _free_fermion_dynamic_obs(L, 1.0, mu, beta, Lt, taus)
+    np.testing.assert_allclose(dos, ref[:, 0], atol=1e-12)
+    np.testing.assert_allclose(chi, ref[:, 1], atol=1e-12)
+    np.testing.assert_allclose(rho, ref[:, 2], atol=1e-12)
+    # particle-hole symmetric point: D(tau) = D(beta - tau), chi(tau) = chi(beta - tau)
+    w0 = O.Walker(model=0, L=L, U=0.0, mu=0.0, beta=beta, Lt=Lt, pace=5, stack=stack)
+    w0.seed(5)
+    w0.fields_random()
+    w0.init()
+    w0.sweep_dynamic([1, 19, 0])
+    d0, c0, _ = w0.dynamic_obs()
+    assert abs(d0[0] - d0[1]) < 1e-12 and abs(c0[0] - c0[1]) < 1e-12
+    assert abs(d0[2] - 0.5) < 1e-12 and abs(c0[2] - 0.125) < 1e-12  # half filling, U = 0
