@@ -327,7 +327,7 @@ int dqmc_batch_create(const dqmc_walker_desc* descs, int n, const dqmc_batch_opt
   b->desc.assign(descs, descs + n);
   for (auto& d : b->desc) {
     const int N = d.L * d.L;
-    if (N > kMaxSmemN || o.precision == DQMC_MIXED) {
+    if (N > kMaxSmemN || o.precision == DQMC_MIXED || o.hbm) {
       b->any_general = true;
       b->maxN_general = std::max(b->maxN_general, N);
       b->maxPace_general = std::max(b->maxPace_general, d.pace);
@@ -369,7 +369,7 @@ int dqmc_batch_create(const dqmc_walker_desc* descs, int n, const dqmc_batch_opt
     const int S = (d.model == DQMC_ATTRACTIVE_HUBBARD) ? 1 : 2;
     const int ns = (d.Lt % d.pace == 0) ? d.Lt / d.pace : d.Lt / d.pace + 1;
     const size_t lvl = (2 * (size_t)N * N + N + 31) & ~(size_t)31;
-    const bool general = N > kMaxSmemN || o.precision == DQMC_MIXED;
+    const bool general = N > kMaxSmemN || o.precision == DQMC_MIXED || o.hbm;
     const int ldk = (N + 15) / 16 * 16;
     off[w].sl = (o.precision == DQMC_MIXED)
                     ? take(sizeof(unsigned short) * S * ozaki::kMaxSlices * ozaki::tc_slice_elems(N, ldk)) : 0;
@@ -528,7 +528,7 @@ int dqmc_batch_create(const dqmc_walker_desc* descs, int n, const dqmc_batch_opt
     plaq(h.cbI, std::cosh(-dtau * d.hopping_t), std::sinh(-dtau * d.hopping_t), std::exp(-0.5 * dtau * d.mu));
     h.G = reinterpret_cast<double*>(base + off[w].G);
     h.chain = reinterpret_cast<double*>(base + off[w].chain);
-    const bool gen = N > kMaxSmemN || o.precision == DQMC_MIXED;
+    const bool gen = N > kMaxSmemN || o.precision == DQMC_MIXED || o.hbm;
     h.path = (o.precision == DQMC_MIXED) ? 2 : (gen ? 1 : 0);
     h.work = gen ? reinterpret_cast<double*>(base + off[w].work) : nullptr;
     h.scr = gen ? reinterpret_cast<double*>(base + off[w].scr) : nullptr;

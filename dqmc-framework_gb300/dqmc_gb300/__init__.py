@@ -56,7 +56,7 @@ class _Desc(ctypes.Structure):
 
 class _Opts(ctypes.Structure):
     _fields_ = [("rng", ctypes.c_int), ("precision", ctypes.c_int), ("trace", ctypes.c_int),
-                ("graphs", ctypes.c_int)]
+                ("graphs", ctypes.c_int), ("hbm", ctypes.c_int)]
 
 
 _lib = None
@@ -136,11 +136,11 @@ class WalkerDesc:
 class Batch:
     """A batch of independent walkers on the current CUDA device."""
 
-    def __init__(self, walkers, rng=RNG_MINSTD, precision=FP64, trace=False, graphs=True):
+    def __init__(self, walkers, rng=RNG_MINSTD, precision=FP64, trace=False, graphs=True, hbm=False):
         L = load()
         self.walkers = list(walkers)
         arr = (_Desc * len(self.walkers))(*[w._c() for w in self.walkers])
-        opts = _Opts(rng, precision, int(trace), int(graphs))
+        opts = _Opts(rng, precision, int(trace), int(graphs), int(hbm))
         h = ctypes.c_void_p()
         _check(L.dqmc_batch_create(arr, len(self.walkers), ctypes.byref(opts), ctypes.byref(h)))
         self.h = h

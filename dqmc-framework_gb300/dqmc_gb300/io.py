@@ -1,0 +1,233 @@
+"""Reference-compatible configuration and text output.
+
+Reads the reference's TOML configuration (DqmcInitializer::parse_toml_config,
+src/dqmc_initializer.cpp:27-338: the same tables, keys and defaults) and writes
+its text files (DqmcIO, include/dqmc_io.h:267-629: observables as means and
+errors or raw bins, k stars, imaginary-time grids, bosonic fields) in the same
+formats, so that existing configurations and analysis scripts work unchanged.
+Host code only: nothing here touches the device.
+"""
+from __future__ import annotations
+
+import math
+import tomllib
+from dataclasses import dataclass, field
+
+# MeasureHandler::ObservableAll (src/measure/measure_handler.cpp), equal-time then dynamic
+EQUALTIME_OBSERVABLES = [
+    "filling_number", "double_occupancy", "kinetic_energy", "momentum_distribution", "local_spin_corr",
+    "spin_density_structure_factor", "charge_density_structure_factor", "s_wave_pairing_corr",
+]
+DYNAMIC_OBSERVABLES = ["greens_functions", "density_of_states", "superfluid_stiffness",
+                       "dynamic_spin_susceptibility"]
+ALL_OBSERVABLES = EQUALTIME_OBSERVABLES + DYNAMIC_OBSERVABLES
+
+
+@dataclass
+class RunConfig:
+    """The parsed configuration (reference defaults where a key is absent)."""
+    model: str = "RepulsiveHubbard"
+    hopping_t: float = 1.0
+    onsite_u: float = 4.0
+    chemical_potential: float = 0.0
+    lattice: str = "Square"
+    cell: tuple = (4, 4)
+    momentum: str = ""
+    momentum_list: str = ""
+    checkerboard: bool = False
+    beta: float = 4.0
+    time_size: int = 80
+    stabilization_pace: int = 10
+    sweeps_warmup: int = 512
+    bin_num: int = 20
+    bin_size: int = 100
+    sweeps_between_bins: int = 20
+    observables: list = field(default_factory=list)
+
+    @property
+    def L(self) -> int:
+        return self.cell[0]
+
+    @property
+    def equaltime(self) -> list:
+        return [o for o in self.observables if o in EQUALTIME_OBSERVABLES]
+
+    @property
+    def dynamic(self) -> list:
+        return [o for o in self.observables if o in DYNAMIC_OBSERVABLES]
+
+
+def parse_config(text: str) -> RunConfig:
+    """DqmcInitializer::parse_toml_config on a TOML string.  Raises ValueError where the
+    reference exits (unknown model or lattice, bad cell, missing observable list)."""
+    c = tomllib.loads(text)
+    m, lat = c.get("Model", {}), c.get("Lattice", {})
+    p, mc, me = m.get("Params", {}), c.get("MonteCarlo", {}), c.get("Measure", {})
+    cfg = RunConfig()
+    cfg.model = m.get("type", "RepulsiveHubbard")
+    if cfg.model not in ("RepulsiveHubbard", "AttractiveHubbard"):
+        raise ValueError(f"undefined model type '{cfg.model}'")
+    cfg.hopping_t = float(p.get("hopping_t", 1.0))
+    cfg.onsite_u = float(p.get("onsite_u", 4.0))
+    cfg.chemical_potential = float(p.get("chemical_potential", 0.0))
+    cfg.lattice = lat.get("type", "Square")
+    if cfg.lattice != "Square":
+        raise ValueError(f"lattice type '{cfg.lattice}' is not supported (the square lattice is)")
+    cell = lat.get("cell")
+    if not isinstance(cell, list) or len(cell) != 2 or any((not isinstance(v, int)) or v < 1 for v in cell):
+        raise ValueError("the input cell of 2d square lattice should be a vector containing two positive integers")
+    if cell[0] != cell[1]:
+        raise ValueError("the square lattice must have equal sides")
+    cfg.cell = (cell[0], cell[1])
+    cfg.momentum = lat.get("momentum", "")
+    cfg.momentum_list = lat.get("momentum_list", "")
+    cfg.checkerboard = bool(c.get("CheckerBoard", {}).get("whether_or_not", False))
+    cfg.beta = float(mc.get("beta", 4.0))
+    cfg.time_size = int(mc.get("time_size", 80))
+    cfg.stabilization_pace = int(mc.get("stabilization_pace", 10))
+    cfg.sweeps_warmup = int(me.get("sweeps_warmup", 512))
+    cfg.bin_num = int(me.get("bin_num", 20))
+    cfg.bin_size = int(me.get("bin_size", 100))
+    cfg.sweeps_between_bins = int(me.get("sweeps_between_bins", 20))
+    obs = me.get("observables")
+    if not isinstance(obs, list) or not all(isinstance(o, str) for o in obs):
+        raise ValueError("undefined observables, please check the config")
+    if len(obs) == 1 and obs[0] in ("all", "All"):
+        obs = list(ALL_OBSERVABLES)
+    elif len(obs) == 1 and obs[0] in ("none", "None"):
+        obs = []
+    for o in obs:
+        if o not in ALL_OBSERVABLES:
+            raise ValueError(f"unsupported observable '{o}'")
+    cfg.observables = obs
+    return cfg
+
+
+def load_config(path: str) -> RunConfig:
+    with open(path, encoding="utf-8") as f:
+        return parse_config(f.read())
+
+
+# ---- lattice tables (src/lattice/square.cpp:42-145) ------------------------------
+def kstars(L: int) -> list:
+    """The inequivalent momenta (k stars) of the L x L square lattice, in the reference's order."""
+    out = []
+    for i in range(math.ceil(L / 2), L + 1):
+        for j in range(math.ceil(L / 2), i + 1):
+            out.append((i / L * 2 * math.pi - math.pi, j / L * 2 * math.pi - math.pi))
+    return out
+
+
+def momentum_index(L: int, name: str) -> int:
+    """Index of a high-symmetry point among the k stars (Square::initial_symmetry_points)."""
+    nk = len(kstars(L))
+    table = {"GammaPoint": 0, "XPoint": nk - L // 2 - 1, "MPoint": nk - 1}
+    if name not in table:
+        raise ValueError(f"unsupported momentum '{name}' (GammaPoint, XPoint, MPoint)")
+    return table[name]
+
+
+# ---- text formats (boost::format "%| 20.10f|" etc. of include/dqmc_io.h) ------------
+def _f(v: float, prec: int = 10) -> str:
+    return f"{v:20.{prec}f}"
+
+
+def _d(v: int) -> str:
+    return f"{v:20d}"
+
+
+def format_scalar(mean: float, err: float) -> str:
+    rel = err / mean if mean != 0 else math.inf
+    return _f(mean) + _f(err) + _f(rel) + "\n"
+
+
+def format_vector(mean, err) -> str:
+    lines = [_d(len(mean)) + "\n"]
+    for i, (m, e) in enumerate(zip(mean, err)):
+        rel = e / m if m != 0 else math.inf
+        lines.append(_d(i) + _f(m) + _f(e) + _f(rel) + "\n")
+    return "".join(lines)
+
+
+def format_matrix(mean, err) -> str:
+    rows, cols = len(mean), len(mean[0])
+    lines = [_d(rows) + _d(cols) + "\n"]
+    for i in range(rows):
+        for j in range(cols):
+            m, e = mean[i][j], err[i][j]
+            rel = e / m if m != 0 else math.inf
+            lines.append(_d(i) + _d(j) + _f(m) + _f(e) + _f(rel) + "\n")
+    return "".join(lines)
+
+
+def format_bins_scalar(bins) -> str:
+    return _d(len(bins)) + "\n" + "".join(_d(b) + _f(v) + "\n" for b, v in enumerate(bins))
+
+
+def format_bins_vector(bins) -> str:
+    out = [_d(len(bins)) + _d(len(bins[0])) + "\n"]
+    for b, row in enumerate(bins):
+        out.extend(_d(b) + _d(i) + _f(v) + "\n" for i, v in enumerate(row))
+    return "".join(out)
+
+
+def format_bins_matrix(bins) -> str:
+    out = [_d(len(bins)) + _d(len(bins[0])) + _d(len(bins[0][0])) + "\n"]
+    for b, mat in enumerate(bins):
+        for i, row in enumerate(mat):
+            out.extend(_d(b) + _d(i) + _d(j) + _f(v) + "\n" for j, v in enumerate(row))
+    return "".join(out)
+
+
+def format_kstars(L: int) -> str:
+    ks = kstars(L)
+    return _d(len(ks)) + "\n" + "".join(_d(i) + _f(kx) + _f(ky) + "\n" for i, (kx, ky) in enumerate(ks))
+
+
+def format_tgrids(beta: float, time_size: int) -> str:
+    dt = beta / time_size
+    return (_d(time_size) + _f(beta, 5) + _f(dt, 5) + "\n" +
+            "".join(_d(t) + _f(t * dt) + "\n" for t in range(time_size)))
+
+
+def format_fields(fields) -> str:
+    """DqmcIO::output_bosonic_fields: 'Lt N' then 't i s' lines, fields[t][i] = +-1."""
+    lt, n = len(fields), len(fields[0])
+    out = [_d(lt) + _d(n) + "\n"]
+    for t in range(lt):
+        out.extend(_d(t) + _d(i) + _f(float(fields[t][i]), 1) + "\n" for i in range(n))
+    return "".join(out)
+
+
+def parse_fields(text: str):
+    """DqmcIO::read_bosonic_fields_from_file: returns (Lt, N, fields[t][i] in {+1, -1})."""
+    tok = text.split()
+    lt, n = int(tok[0]), int(tok[1])
+    f = [[1] * n for _ in range(lt)]
+    vals = tok[2:]
+    if len(vals) % 3:
+        raise ValueError("fields file: expected 't i s' triples")
+    for k in range(0, len(vals), 3):
+        t, i, s = int(vals[k]), int(vals[k + 1]), float(vals[k + 2])
+        if not (0 <= t < lt and 0 <= i < n):
+            raise ValueError(f"fields file: site ({t}, {i}) outside {lt} x {n}")
+        f[t][i] = 1 if s > 0 else -1
+    return lt, n, f
+
+
+def format_summary_line(description: str, mean: float, err: float) -> str:
+    """DqmcIO::output_observable to the terminal: '%| 30s|%| 7s|%| 20.12f|  pm  %.12f'."""
+    return f"{description:>30s}{'->':>7s}{mean:20.12f}  pm  {err:.12f}\n"
+
+
+def analyse_bins(bins):
+    """Observable::analyse (include/measure/observable.h:169-211): mean over bins and
+    sqrt(<x^2> - <x>^2) / sqrt(nbins - 1), elementwise for vectors and matrices."""
+    import numpy as np
+
+    b = np.asarray(bins, dtype=np.float64)
+    n = b.shape[0]
+    mean = b.sum(axis=0) / n
+    var = (b ** 2).sum(axis=0) / n - mean ** 2
+    err = np.sqrt(np.maximum(var, 0.0)) / math.sqrt(n - 1) if n > 1 else np.zeros_like(mean)
+    return mean, err

@@ -1,0 +1,164 @@
+"""Run a reference configuration on the GPU and write the reference's output files.
+
+    python -m dqmc_gb300.run config.toml --out DIR [--walkers W] [--seed S]
+                            [--fields FILE] [--precision fp64|mixed] [--rng minstd|philox]
+
+Follows the reference's driver (src/dqmc_main.cpp, src/dqmc.cpp:48-158): each walker
+is one of the reference's MPI ranks (one Markov chain); warm-up of
+sweeps_warmup / 2 forth-and-back sweeps; then ceil(bin_num / W) bins per walker,
+each bin_size / 2 forth-and-back sweeps with measurements (with dynamic
+observables the forward half-sweep is sweep_for_dynamic_greens and the equal-time
+measurement is taken on the backward one), the normalisation of
+MeasureHandler::normalize_stats, and sweeps_between_bins / 2 unmeasured sweeps
+between bins; the bins of all walkers are pooled (the reference's MPI gather) and
+analysed as Observable::analyse.  Output: the terminal summary of the scalar
+observables and fields.out, kstars.out, tgrids.out, swave(.bins).out,
+dos(.bins).out, greens(.bins).out, dss(.bins).out in the reference's formats.
+G(k, tau) is measured for the configured `momentum` (one row of greens.out).
+"""
+from __future__ import annotations
+
+import argparse
+import math
+import os
+import sys
+
+import numpy as np
+
+from . import io as dio
+
+DESCRIPTIONS = {
+    "filling_number": "Filling number", "double_occupancy": "Double occupation", "kinetic_energy": "Kinetic energy",
+    "momentum_distribution": "Momentum distribution", "local_spin_corr": "Local spin correlation",
+    "spin_density_structure_factor": "SDW order parameter", "charge_density_structure_factor": "CDW order parameter",
+    "s_wave_pairing_corr": "S-wave pairing correlation", "superfluid_stiffness": "Superfluid stiffness",
+    "equaltime_sign": "Averaged sign (equal-time)", "dynamic_sign": "Averaged sign (dynamic)",
+}
+
+
+def run(cfg: dio.RunConfig, out_dir: str, walkers: int = 1, seed: int = 12345, fields_file: str | None = None,
+        precision: str = "fp64", rng: str = "minstd", log=sys.stdout) -> dict:
+    """Run the configuration; returns {name: (mean, error)} and writes the output files."""
+    import dqmc_gb300 as dq
+
+    L, lt = cfg.L, cfg.time_size
+    kidx = dio.momentum_index(L, cfg.momentum) if cfg.momentum else -1
+    model = dq.ATTRACTIVE if cfg.model == "AttractiveHubbard" else dq.REPULSIVE
+    descs = [dq.WalkerDesc(model=model, L=L, t=cfg.hopping_t, U=cfg.onsite_u, mu=cfg.chemical_potential,
+                           beta=cfg.beta, Lt=lt, pace=cfg.stabilization_pace, checkerboard=cfg.checkerboard,
+                           momentum_index=kidx, seed=seed + w) for w in range(walkers)]
+    # the dynamic half-sweep runs on the HBM path, which walkers with N <= 64 take only when asked
+    b = dq.Batch(descs, rng=dq.RNG_PHILOX if rng == "philox" else dq.RNG_MINSTD,
+                 precision=dq.MIXED if precision == "mixed" else dq.FP64, hbm=bool(cfg.dynamic))
+    try:
+        if fields_file:
+            with open(fields_file, encoding="utf-8") as f:
+                flt, fn, fields = dio.parse_fields(f.read())
+            if flt != lt or fn != L * L:
+                raise ValueError("fields file size does not match the configuration")
+            for w in range(walkers):
+                b.set_fields(w, np.array(fields, dtype=np.int8))
+        else:
+            for w in range(walkers):
+                b.fields_random(w)
+        b.init_greens()
+        for _ in range(cfg.sweeps_warmup // 2):
+            b.sweep_0_to_beta()
+            b.sweep_beta_to_0()
+        eqt, dyn = bool(cfg.equaltime), bool(cfg.dynamic)
+        taus = list(range(lt))
+        nbins = math.ceil(cfg.bin_num / walkers) if (eqt or dyn) else 0
+        eq_bins = [[] for _ in range(walkers)]
+        dyn_bins = {k: [[] for _ in range(walkers)] for k in ("greens", "dos", "dss", "rho", "sign")}
+        for _ in range(nbins):
+            b.clear_observables()
+            if dyn:
+                b.clear_dynamic()
+            sgn = np.zeros(walkers)
+            for _ in range(cfg.bin_size // 2):
+                if dyn:
+                    b.sweep_dynamic(taus)
+                    sgn += [b.config_sign(w) for w in range(walkers)]
+                else:
+                    b.sweep_0_to_beta(measure=eqt)
+                b.sweep_beta_to_0(measure=eqt)
+            if eqt:
+                sums, counts = b.observables_all()
+                for w in range(walkers):
+                    eq_bins[w].append(dq.write_bin(sums[w], counts[w]))
+            if dyn:
+                for w in range(walkers):
+                    g, cnt = b.dynamic(w)
+                    dos, dss, rho = b.dynamic_obs(w)
+                    ms = sgn[w] / max(cnt[0], 1)  # the dynamic sign, one count per dynamic sweep
+                    norm = cnt * ms
+                    dyn_bins["greens"][w].append(g / norm)
+                    dyn_bins["dos"][w].append(dos / norm)
+                    dyn_bins["dss"][w].append(dss / norm)
+                    dyn_bins["rho"][w].append(rho.sum() / (cnt[0] * ms))
+                    dyn_bins["sign"][w].append(abs(ms))
+            for _ in range(cfg.sweeps_between_bins // 2):
+                b.sweep_0_to_beta()
+                b.sweep_beta_to_0()
+        fields0 = b.fields(0)
+    finally:
+        b.close()
+
+    os.makedirs(out_dir, exist_ok=True)
+    results = {}
+
+    def write(name, text):
+        with open(os.path.join(out_dir, name), "w", encoding="utf-8") as f:
+            f.write(text)
+
+    if eqt:
+        pooled = np.array([bb for wb in eq_bins for bb in wb])
+        mean, err = dio.analyse_bins(pooled)
+        for i, name in enumerate(dq.OBS_NAMES):
+            if name == "equaltime_sign" or name in cfg.equaltime:
+                results[name] = (float(mean[i]), float(err[i]))
+        if "s_wave_pairing_corr" in cfg.equaltime:
+            i = dq.OBS_NAMES.index("s_wave_pairing_corr")
+            write("swave.out", dio.format_scalar(mean[i], err[i]))
+            write("swave.bins.out", dio.format_bins_scalar(pooled[:, i]))
+    if dyn:
+        pool = {k: np.array([x for wb in v for x in wb]) for k, v in dyn_bins.items()}
+        results["dynamic_sign"] = tuple(float(x) for x in dio.analyse_bins(pool["sign"]))
+        for name, key, fname in (("density_of_states", "dos", "dos"), ("dynamic_spin_susceptibility", "dss", "dss")):
+            if name in cfg.dynamic:
+                mean, err = dio.analyse_bins(pool[key])
+                write(f"{fname}.out", dio.format_vector(mean, err))
+                write(f"{fname}.bins.out", dio.format_bins_vector(pool[key]))
+        if "greens_functions" in cfg.dynamic:
+            mean, err = dio.analyse_bins(pool["greens"])
+            write("greens.out", dio.format_matrix([mean], [err]))
+            write("greens.bins.out", dio.format_bins_matrix(pool["greens"][:, None, :]))
+        if "superfluid_stiffness" in cfg.dynamic:
+            mean, err = dio.analyse_bins(pool["rho"])
+            results["superfluid_stiffness"] = (float(mean), float(err))
+    write("fields.out", dio.format_fields(fields0))
+    write("kstars.out", dio.format_kstars(L))
+    write("tgrids.out", dio.format_tgrids(cfg.beta, lt))
+    for name in ["equaltime_sign"] + cfg.equaltime + ["dynamic_sign", "superfluid_stiffness"]:
+        if name in results:
+            log.write(dio.format_summary_line(DESCRIPTIONS[name], *results[name]))
+    return results
+
+
+def main(argv=None) -> int:
+    ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
+    ap.add_argument("config")
+    ap.add_argument("--out", default="output")
+    ap.add_argument("--walkers", type=int, default=1)
+    ap.add_argument("--seed", type=int, default=12345)
+    ap.add_argument("--fields", default=None)
+    ap.add_argument("--precision", choices=["fp64", "mixed"], default="fp64")
+    ap.add_argument("--rng", choices=["minstd", "philox"], default="minstd")
+    a = ap.parse_args(argv)
+    cfg = dio.load_config(a.config)
+    run(cfg, a.out, walkers=a.walkers, seed=a.seed, fields_file=a.fields, precision=a.precision, rng=a.rng)
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

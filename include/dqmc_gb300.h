@@ -27,7 +27,7 @@
 extern "C" {
 #endif
 
-#define DQMC_ABI_VERSION 1
+#define DQMC_ABI_VERSION 2
 
 enum dqmc_status {
   DQMC_OK = 0,
@@ -98,6 +98,8 @@ typedef struct dqmc_batch_options {
                           (parity tests; costs device memory) */
   int graphs;          /* 1: capture each kind of half-sweep once into a CUDA graph and replay
                           it (ignored while tracing or profiling) */
+  int hbm;             /* 1: every walker on the HBM path, whatever its size (N <= 64 walkers
+                          otherwise live in shared memory; dqmc_sweep_dynamic needs this) */
 } dqmc_batch_options;
 
 typedef struct dqmc_batch dqmc_batch;

@@ -116,7 +116,7 @@ class DqmcWalker {
       d[w] = dqmc_walker_desc{model.type, lat.side, model.hopping_t, model.onsite_u, model.chemical_potential,
                               beta_, lt_, pace_, model.checkerboard ? 1 : 0, lat.momentum_index, seeds[w]};
     }
-    dqmc_batch_options o{rng, DQMC_FP64, 0, 1};
+    dqmc_batch_options o{rng, DQMC_FP64, 0, 1, 0};
     if (b_) dqmc_batch_destroy(b_);
     b_ = nullptr;
     check(dqmc_batch_create(d.data(), (int)d.size(), &o, &b_));

@@ -36,7 +36,7 @@ def test_exports_every_declared_symbol(dq):
 
 
 def test_abi_version(dq):
-    assert dq.load().dqmc_abi_version() == 1
+    assert dq.load().dqmc_abi_version() == 2
 
 
 @pytest.mark.parametrize(

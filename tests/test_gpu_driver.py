@@ -1,0 +1,92 @@
+"""The reference-style driver (python -m dqmc_gb300.run) end to end on the GPU, and
+the HBM path at shared-memory sizes (the dynamic half-sweep needs it there)."""
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+CONFIG = """
+[Model]
+    type = "RepulsiveHubbard"
+    [Model.Params]
+    hopping_t = 1.0
+    onsite_u = 4.0
+    chemical_potential = 0.0
+[Lattice]
+    type = "Square"
+    cell = [ 4, 4 ]
+    momentum = "MPoint"
+[MonteCarlo]
+    beta = 1.0
+    time_size = 10
+    stabilization_pace = 5
+[Measure]
+    sweeps_warmup = 4
+    bin_num = 4
+    bin_size = 4
+    sweeps_between_bins = 2
+    observables = [ "all" ]
+"""
+
+
+@pytest.fixture(scope="module")
+def dq():
+    import __graft_entry__ as g
+
+    g.build()
+    import dqmc_gb300
+
+    return dqmc_gb300
+
+
+def test_hbm_path_equals_shared_memory_path(dq):
+    """N = 16 walkers on the HBM path (hbm option) against the shared-memory path:
+    identical decisions and G within 1e-10 after full sweeps with measurements."""
+    descs = [dq.WalkerDesc(model=m, L=4, U=4.0, mu=-0.3 * m, beta=1.0, Lt=10, pace=5, seed=40 + m) for m in (0, 1)]
+    out = []
+    for hbm in (False, True):
+        b = dq.Batch(descs, rng=dq.RNG_MINSTD, hbm=hbm)
+        for w in range(2):
+            b.fields_random(w)
+        b.init_greens()
+        for _ in range(2):
+            b.sweep_0_to_beta(measure=True)
+            b.sweep_beta_to_0(measure=True)
+        out.append(([b.fields(w) for w in range(2)], [b.green(w, s) for w in range(2) for s in (0, 1)],
+                    b.observables_all()[0]))
+        b.close()
+    (f0, g0, o0), (f1, g1, o1) = out
+    for w in range(2):
+        np.testing.assert_array_equal(f0[w], f1[w])
+    for a, c in zip(g0, g1):
+        assert abs(a - c).max() < 1e-10
+    np.testing.assert_allclose(o0, o1, rtol=1e-10, atol=1e-12)
+
+
+def test_driver_runs_a_reference_config(dq, tmp_path):
+    from dqmc_gb300 import io as dio
+    from dqmc_gb300.run import run
+
+    cfg = dio.parse_config(CONFIG)
+    log = tmp_path / "log.txt"
+    with open(log, "w") as fh:
+        res = run(cfg, str(tmp_path), walkers=2, seed=7, log=fh)
+    for name in ("fields.out", "kstars.out", "tgrids.out", "swave.out", "swave.bins.out", "dos.out",
+                 "dos.bins.out", "greens.out", "greens.bins.out", "dss.out", "dss.bins.out"):
+        assert os.path.getsize(tmp_path / name) > 0, name
+    dos = open(tmp_path / "dos.out").read().splitlines()
+    assert int(dos[0]) == 10 and len(dos) == 11
+    bins = open(tmp_path / "dos.bins.out").read().splitlines()
+    assert bins[0].split() == ["4", "10"]  # 2 walkers x ceil(4 / 2) bins, 10 tau
+    lt, n, _ = dio.parse_fields(open(tmp_path / "fields.out").read())
+    assert (lt, n) == (10, 16)
+    # half filling without a sign problem: <n> = 1, sign 1; D(0) = tr G / N near 1/2
+    assert res["equaltime_sign"][0] == pytest.approx(1.0) and res["dynamic_sign"][0] == pytest.approx(1.0)
+    assert abs(res["filling_number"][0] - 1.0) < 0.05
+    d0 = float(dos[1].split()[1])
+    assert abs(d0 - 0.5) < 0.05
+    assert np.isfinite(res["superfluid_stiffness"][0])
+    text = open(log).read()
+    assert "Filling number" in text and "Superfluid stiffness" in text

@@ -1,0 +1,140 @@
+"""Reference-compatible configuration parsing and text output (dqmc_gb300.io).
+
+The writers are pinned to the reference's own example output (fixture
+tests/golden/io_formats.json, made by make_io_fixture.py from
+example/output/*.out): kstars.out, tgrids.out and fields.out are rebuilt from the
+example's parameters and field configuration and must be byte-identical; the
+rows of the observable files are re-formatted field by field.
+"""
+import hashlib
+import json
+import os
+import sys
+
+import numpy as np
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(os.path.dirname(HERE), "dqmc-framework_gb300"))
+
+from dqmc_gb300 import io as dio  # noqa: E402  (host code only; no device library needed)
+
+FIX = json.load(open(os.path.join(HERE, "golden", "io_formats.json")))["files"]
+EX = json.load(open(os.path.join(HERE, "golden", "example_8x8.json")))
+
+
+def _sha(text: str) -> str:
+    return hashlib.sha256(text.encode()).hexdigest()
+
+
+def test_kstars_and_tgrids_are_byte_identical():
+    assert _sha(dio.format_kstars(EX["L"])) == FIX["kstars.out"]["sha256"]
+    assert _sha(dio.format_tgrids(EX["beta"], EX["Lt"])) == FIX["tgrids.out"]["sha256"]
+
+
+def test_fields_file_round_trip_is_byte_identical():
+    bits = np.unpackbits(np.frombuffer(bytes.fromhex(EX["fields_packed_hex"]), dtype=np.uint8))
+    fields = np.where(bits[: EX["Lt"] * EX["N"]].reshape(EX["Lt"], EX["N"]) > 0, 1, -1)
+    text = dio.format_fields(fields.tolist())
+    assert _sha(text) == FIX["fields.out"]["sha256"]
+    lt, n, back = dio.parse_fields(text)
+    assert (lt, n) == (EX["Lt"], EX["N"]) and (np.array(back) == fields).all()
+
+
+@pytest.mark.parametrize("name", ["dos.out", "dss.out", "greens.out", "swave.out", "dos.bins.out",
+                                  "greens.bins.out", "swave.bins.out"])
+def test_observable_rows_reformat_identically(name):
+    for line in FIX[name]["head"]:
+        if not line:
+            continue
+        assert len(line) % 20 == 0
+        fields = [line[k:k + 20] for k in range(0, len(line), 20)]
+        for f in fields:
+            tok = f.strip()
+            if "." in tok:
+                assert dio._f(float(tok)) == f
+            else:
+                assert dio._d(int(tok)) == f
+
+
+def test_writers_layout():
+    mean, err = np.array([0.5, 0.25]), np.array([0.01, 0.02])
+    v = dio.format_vector(mean, err).splitlines()
+    assert v[0] == dio._d(2) and v[2] == dio._d(1) + dio._f(0.25) + dio._f(0.02) + dio._f(0.08)
+    m = dio.format_matrix([[1.0, 2.0]], [[0.1, 0.2]]).splitlines()
+    assert m[0] == dio._d(1) + dio._d(2) and m[2].startswith(dio._d(0) + dio._d(1) + dio._f(2.0))
+    bins = np.arange(6.0).reshape(3, 2)
+    bv = dio.format_bins_vector(bins).splitlines()
+    assert bv[0] == dio._d(3) + dio._d(2) and bv[-1] == dio._d(2) + dio._d(1) + dio._f(5.0)
+    bm = dio.format_bins_matrix(bins[:, None, :]).splitlines()
+    assert bm[0] == dio._d(3) + dio._d(1) + dio._d(2) and len(bm) == 7
+    assert dio.format_summary_line("Filling number", 0.5, 0.01) == \
+        f"{'Filling number':>30s}{'->':>7s}{0.5:20.12f}  pm  {0.01:.12f}\n"
+
+
+def test_analyse_bins_matches_the_reference_formula():
+    rng = np.random.default_rng(1)
+    b = rng.standard_normal((20, 3))
+    mean, err = dio.analyse_bins(b)
+    np.testing.assert_allclose(mean, b.mean(axis=0), rtol=1e-14)
+    ref = np.sqrt((b ** 2).mean(axis=0) - b.mean(axis=0) ** 2) / np.sqrt(19)
+    np.testing.assert_allclose(err, ref, rtol=1e-12)
+
+
+CONFIG = """
+[Model]
+    type = "AttractiveHubbard"
+    [Model.Params]
+    hopping_t = 1.0
+    onsite_u = 4.0
+    chemical_potential = -0.5
+[Lattice]
+    type = "Square"
+    cell = [ 6, 6 ]
+    momentum = "XPoint"
+    momentum_list = "KstarsAll"
+[CheckerBoard]
+    whether_or_not = false
+[MonteCarlo]
+    beta = 4.0
+    time_size = 80
+    stabilization_pace = 8
+[Measure]
+    sweeps_warmup = 100
+    bin_num = 10
+    bin_size = 20
+    sweeps_between_bins = 4
+    observables = [ "all" ]
+"""
+
+
+def test_parse_config_keys_defaults_and_keywords():
+    c = dio.parse_config(CONFIG)
+    assert (c.model, c.hopping_t, c.onsite_u, c.chemical_potential) == ("AttractiveHubbard", 1.0, 4.0, -0.5)
+    assert (c.L, c.momentum, c.checkerboard) == (6, "XPoint", False)
+    assert (c.beta, c.time_size, c.stabilization_pace) == (4.0, 80, 8)
+    assert (c.sweeps_warmup, c.bin_num, c.bin_size, c.sweeps_between_bins) == (100, 10, 20, 4)
+    assert c.observables == dio.ALL_OBSERVABLES
+    assert c.equaltime == dio.EQUALTIME_OBSERVABLES and c.dynamic == dio.DYNAMIC_OBSERVABLES
+    # defaults of DqmcInitializer::parse_toml_config where a key is absent
+    d = dio.parse_config('[Lattice]\ncell = [4, 4]\n[Measure]\nobservables = ["none"]\n')
+    assert (d.model, d.onsite_u, d.beta, d.time_size, d.stabilization_pace) == ("RepulsiveHubbard", 4.0, 4.0, 80, 10)
+    assert (d.sweeps_warmup, d.bin_num, d.bin_size, d.sweeps_between_bins) == (512, 20, 100, 20)
+    assert d.observables == []
+    # k stars and high-symmetry points of the 6x6 lattice (Square::initial_symmetry_points)
+    ks = dio.kstars(6)
+    assert len(ks) == 10 and ks[0] == (0.0, 0.0)
+    assert dio.momentum_index(6, "MPoint") == 9 and dio.momentum_index(6, "XPoint") == 6
+    assert ks[6] == pytest.approx((np.pi, 0.0)) and ks[9] == pytest.approx((np.pi, np.pi))
+
+
+@pytest.mark.parametrize("bad", [
+    '[Model]\ntype = "Kondo"\n[Lattice]\ncell = [4, 4]\n[Measure]\nobservables = ["all"]\n',
+    '[Lattice]\ncell = [4, 0]\n[Measure]\nobservables = ["all"]\n',
+    '[Lattice]\ncell = [4, 4]\n',
+    '[Lattice]\ncell = [4, 4]\n[Measure]\nobservables = ["magic"]\n',
+    '[Lattice]\ntype = "Honeycomb"\ncell = [4, 4]\n[Measure]\nobservables = ["all"]\n',
+])
+def test_parse_config_rejects_what_the_reference_rejects(bad):
+    with pytest.raises(ValueError):
+        dio.parse_config(bad)
