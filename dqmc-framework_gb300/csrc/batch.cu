@@ -965,7 +965,7 @@ static int dyn_alloc(dqmc_batch* b) {
   size_t cur = 0;
   auto take = [&](size_t bytes) { const size_t o = cur; cur = align256(cur + bytes); return o; };
   const size_t taus_off = take(sizeof(int) * kMaxTau);
-  constexpr int kOff = 9;
+  constexpr int kOff = 10;
   std::vector<size_t> off(b->nw * kOff);
   for (int w = 0; w < b->nw; ++w) {
     const WalkerDev& h = b->hw[w];
@@ -979,6 +979,7 @@ static int dyn_alloc(dqmc_batch* b) {
     off[kOff * w + 6] = take(sizeof(double) * 3 * kMaxTau);           // DOS, chi, stiffness sums
     off[kOff * w + 7] = take(sizeof(double) * 2 * kMaxTau * h.N);     // parts awaiting G(beta,beta)
     off[kOff * w + 8] = take(sizeof(double) * 2 * kMaxTau);
+    off[kOff * w + 9] = take(sizeof(double) * kMaxTau * h.N);        // per-displacement G sums
   }
   cudaError_t e = cudaMalloc(&b->dyn_arena, cur);
   if (e != cudaSuccess) {
@@ -998,6 +999,7 @@ static int dyn_alloc(dqmc_batch* b) {
     h.dyn_obs = reinterpret_cast<double*>(b->dyn_arena + off[kOff * w + 6]);
     h.dyn_vec = reinterpret_cast<double*>(b->dyn_arena + off[kOff * w + 7]);
     h.dyn_part = reinterpret_cast<double*>(b->dyn_arena + off[kOff * w + 8]);
+    h.dyn_r = reinterpret_cast<double*>(b->dyn_arena + off[kOff * w + 9]);
     h.dyn_taus = b->d_taus;
     h.dyn_ntau = 0;
   }
@@ -1012,6 +1014,7 @@ int dqmc_clear_dynamic(dqmc_batch* b) {
     CUDA_TRY(cudaMemsetAsync(b->hw[w].dyn_sum, 0, sizeof(double) * kMaxTau, b->stream));
     CUDA_TRY(cudaMemsetAsync(b->hw[w].dyn_cnt, 0, sizeof(long long) * kMaxTau, b->stream));
     CUDA_TRY(cudaMemsetAsync(b->hw[w].dyn_obs, 0, sizeof(double) * 3 * kMaxTau, b->stream));
+    CUDA_TRY(cudaMemsetAsync(b->hw[w].dyn_r, 0, sizeof(double) * kMaxTau * b->hw[w].N, b->stream));
   }
   CUDA_TRY(cudaStreamSynchronize(b->stream));
   return DQMC_OK;
@@ -1084,6 +1087,16 @@ int dqmc_get_dynamic_obs(dqmc_batch* b, int w, double* dos, double* chi, double*
     if (chi) chi[k] = v[3 * k + 1];
     if (rho) rho[k] = v[3 * k + 2];
   }
+  return DQMC_OK;
+}
+
+int dqmc_get_dynamic_r(dqmc_batch* b, int w, double* out) {
+  if (int r = check_walker(b, w)) return r;
+  if (!out) return fail(DQMC_ERR_ARG, "null output");
+  if (!b->dyn_arena || b->taus.empty()) return DQMC_OK;
+  const size_t n = b->taus.size() * (size_t)b->hw[w].N;
+  CUDA_TRY(cudaMemcpyAsync(out, b->hw[w].dyn_r, sizeof(double) * n, cudaMemcpyDeviceToHost, b->stream));
+  CUDA_TRY(cudaStreamSynchronize(b->stream));
   return DQMC_OK;
 }
 

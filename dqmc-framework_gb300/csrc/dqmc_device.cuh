@@ -64,6 +64,7 @@ struct WalkerDev {
   double* dyn_obs;
   double* dyn_vec;
   double* dyn_part;
+  double* dyn_r;  // [tau][N] sign * 0.5 sum_i (G_up + G_dn)(i + r, i) / N: G(k,tau) of any k
   int zld;                   // line stride of zsl (N rounded up to 32)
   // tensor-core stabilization: BF16 slices of both operands of the current product,
   // [S][2 operands][9 slices][N][zld]

@@ -1140,6 +1140,17 @@ __global__ void __launch_bounds__(256) dyn_measure_kernel(const WalkerDev* __res
         rcor += fq * ((S == 1) ? 2.0 * c : c);
       }
     }
+    // per-displacement sums S(r) = sum_i G(i + r, i) (both spins): G(k,tau) = sum_r cos(k r) S(r)
+    for (int r = wid; r < N; r += 8) {
+      const int rx = r % L, ry = r / L;
+      double sr = 0.0;
+      for (int i = lane; i < N; i += 32) {
+        const int jj = (i % L + rx) % L + L * ((i / L + ry) % L);
+        sr += gk[0][(long long)i * N + jj] + gk[1][(long long)i * N + jj];
+      }
+      sr = warp_sum_g(sr);
+      if (lane == 0) w.dyn_r[(long long)slot * N + r] += sg * 0.5 * sr / N;
+    }
     for (int i = threadIdx.x; i < N; i += blockDim.x) {
       const long long d = (long long)i * N + i;
       const int xi = i % L, yi = i / L, ipx = (xi + 1) % L + L * yi;

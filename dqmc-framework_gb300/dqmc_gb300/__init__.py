@@ -37,6 +37,7 @@ EXPORTS = [
     "dqmc_profile_enable", "dqmc_profile_read", "dqmc_microbench_fp64", "dqmc_get_observables_all",
     "dqmc_product_check", "dqmc_product_device_noalloc", "dqmc_launch_count", "dqmc_tuning",
     "dqmc_sweep_dynamic", "dqmc_get_dynamic", "dqmc_clear_dynamic", "dqmc_get_green_dynamic", "dqmc_get_dynamic_obs",
+    "dqmc_get_dynamic_r",
 ]
 KCLASSES = ["segment", "push", "greens", "measure", "product", "metropolis"]
 
@@ -95,6 +96,7 @@ def load() -> ctypes.CDLL:
         "dqmc_sweep_dynamic": (c, [vp, ip, c]), "dqmc_get_dynamic": (c, [vp, c, dp, i64p]),
         "dqmc_clear_dynamic": (c, [vp]), "dqmc_get_green_dynamic": (c, [vp, c, c, c, dp]),
         "dqmc_get_dynamic_obs": (c, [vp, c, dp, dp, dp]),
+        "dqmc_get_dynamic_r": (c, [vp, c, dp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -285,6 +287,22 @@ class Batch:
         P = ctypes.POINTER(ctypes.c_double)
         _check(load().dqmc_get_dynamic_obs(self.h, w, d.ctypes.data_as(P), c.ctypes.data_as(P), r.ctypes.data_as(P)))
         return d[:n], c[:n], r[:n]
+
+    def dynamic_r(self, w: int) -> np.ndarray:
+        """[tau][r] sums of sign * 0.5 sum_i (G_up + G_dn)(i + r, i) / N per displacement r."""
+        n = len(getattr(self, "_taus", []))
+        out = np.zeros((max(n, 1), self.walkers[w].N))
+        _check(load().dqmc_get_dynamic_r(self.h, w, out.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
+        return out[:n]
+
+    def dynamic_greens_k(self, w: int, momenta) -> np.ndarray:
+        """G(k,tau) sums [k][tau] for the momenta (kx, ky) (measure_greens_functions):
+        sum_r cos(-(rx kx + ry ky)) S(r)."""
+        L = self.walkers[w].L
+        r = np.arange(L * L)
+        rx, ry = r % L, r // L
+        ff = np.array([np.cos(-(rx * kx + ry * ky)) for kx, ky in momenta])  # [k][r]
+        return ff @ self.dynamic_r(w).T
 
     def clear_dynamic(self):
         _check(load().dqmc_clear_dynamic(self.h))

@@ -127,6 +127,27 @@ def momentum_index(L: int, name: str) -> int:
     return table[name]
 
 
+def momentum_list_indices(L: int, name: str) -> list:
+    """k-star indices of a momentum list (Square::initial_symmetry_points and the
+    initializer's momentum_list options): KstarsAll, DeltaLine, ZLine, SigmaLine,
+    Gamma2X2M2GammaLoop, or a single point."""
+    nk = len(kstars(L))
+    h = L // 2
+    xp = nk - h - 1
+    if name == "KstarsAll":
+        return list(range(nk))
+    if name == "DeltaLine":
+        return [i * (i + 1) // 2 for i in range(h + 1)]
+    if name == "ZLine":
+        return [xp + i for i in range(h + 1)]
+    if name == "SigmaLine":
+        return [i * (i + 3) // 2 for i in range(h + 1)]
+    if name == "Gamma2X2M2GammaLoop":
+        return ([i * (i + 1) // 2 for i in range(h)] + [xp + i for i in range(h)] +
+                [i * (i + 3) // 2 for i in range(h, 0, -1)])
+    return [momentum_index(L, name)]
+
+
 # ---- text formats (boost::format "%| 20.10f|" etc. of include/dqmc_io.h) ------------
 def _f(v: float, prec: int = 10) -> str:
     return f"{v:20.{prec}f}"

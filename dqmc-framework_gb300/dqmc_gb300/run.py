@@ -14,7 +14,8 @@ between bins; the bins of all walkers are pooled (the reference's MPI gather) an
 analysed as Observable::analyse.  Output: the terminal summary of the scalar
 observables and fields.out, kstars.out, tgrids.out, swave(.bins).out,
 dos(.bins).out, greens(.bins).out, dss(.bins).out in the reference's formats.
-G(k, tau) is measured for the configured `momentum` (one row of greens.out).
+G(k, tau) covers the configured `momentum_list` (rows of greens.out in the
+reference's k-star order).
 """
 from __future__ import annotations
 
@@ -70,6 +71,8 @@ def run(cfg: dio.RunConfig, out_dir: str, walkers: int = 1, seed: int = 12345, f
         nbins = math.ceil(cfg.bin_num / walkers) if (eqt or dyn) else 0
         eq_bins = [[] for _ in range(walkers)]
         dyn_bins = {k: [[] for _ in range(walkers)] for k in ("greens", "dos", "dss", "rho", "sign")}
+        ks = dio.kstars(L)
+        klist = [ks[i] for i in dio.momentum_list_indices(L, cfg.momentum_list or "KstarsAll")]
         for _ in range(nbins):
             b.clear_observables()
             if dyn:
@@ -88,11 +91,12 @@ def run(cfg: dio.RunConfig, out_dir: str, walkers: int = 1, seed: int = 12345, f
                     eq_bins[w].append(dq.write_bin(sums[w], counts[w]))
             if dyn:
                 for w in range(walkers):
-                    g, cnt = b.dynamic(w)
+                    _, cnt = b.dynamic(w)
+                    g = b.dynamic_greens_k(w, klist)  # [k][tau]
                     dos, dss, rho = b.dynamic_obs(w)
                     ms = sgn[w] / max(cnt[0], 1)  # the dynamic sign, one count per dynamic sweep
                     norm = cnt * ms
-                    dyn_bins["greens"][w].append(g / norm)
+                    dyn_bins["greens"][w].append(g / norm[None, :])
                     dyn_bins["dos"][w].append(dos / norm)
                     dyn_bins["dss"][w].append(dss / norm)
                     dyn_bins["rho"][w].append(rho.sum() / (cnt[0] * ms))
@@ -131,8 +135,8 @@ def run(cfg: dio.RunConfig, out_dir: str, walkers: int = 1, seed: int = 12345, f
                 write(f"{fname}.bins.out", dio.format_bins_vector(pool[key]))
         if "greens_functions" in cfg.dynamic:
             mean, err = dio.analyse_bins(pool["greens"])
-            write("greens.out", dio.format_matrix([mean], [err]))
-            write("greens.bins.out", dio.format_bins_matrix(pool["greens"][:, None, :]))
+            write("greens.out", dio.format_matrix(mean, err))
+            write("greens.bins.out", dio.format_bins_matrix(pool["greens"]))
         if "superfluid_stiffness" in cfg.dynamic:
             mean, err = dio.analyse_bins(pool["rho"])
             results["superfluid_stiffness"] = (float(mean), float(err))

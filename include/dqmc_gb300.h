@@ -163,6 +163,10 @@ int dqmc_clear_dynamic(dqmc_batch* b);
  * each sign-weighted like the reference's tmp_value; counts as dqmc_get_dynamic.
  * Any output may be null. */
 int dqmc_get_dynamic_obs(dqmc_batch* b, int walker, double* dos, double* chi, double* rho);
+/* Sums per listed tau of sign * 0.5 * sum_i (G_up + G_dn)(i + r, i) / N for every
+ * displacement r (site index of the displacement vector), out[tau][r]: G(k,tau) of
+ * measure_greens_functions for any momentum k is sum_r FourierFactor(r, k) out[tau][r]. */
+int dqmc_get_dynamic_r(dqmc_batch* b, int walker, double* out);
 /* G(beta,0) (which = 0) or G(0,beta) (which = 1) after the last dynamic half-sweep
  * (DqmcWalker::Greent0Up/Dn, Green0tUp/Dn at t = Lt), column-major N x N. */
 int dqmc_get_green_dynamic(dqmc_batch* b, int walker, int which, int spin, double* out);

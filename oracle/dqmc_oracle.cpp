@@ -653,6 +653,8 @@ struct Oracle {
   // density of states, dynamic spin susceptibility and superfluid-stiffness contribution
   // per listed tau (sums over dynamic half-sweeps, sign-weighted as the reference's)
   std::vector<double> dyn_dos, dyn_chi, dyn_rho;
+  // per displacement r: sign * 0.5 sum_i (G_up + G_dn)(i + r, i) / N, [tau][r]
+  std::vector<double> dyn_r;
   // G(t,t), G(t,0), G(0,t) per spin at the listed tau of the current half-sweep
   std::vector<std::array<Vec, 6>> dyn_rec;
 
@@ -1086,6 +1088,15 @@ struct Oracle {
         sum += sign * 0.5 * (at(gu, N, j, i) + at(gd, N, j, i)) / N * lat.fourier(lat.disp(i, j), kidx);
     dyn_sum[slot] += sum;
     dyn_cnt[slot] += 1;
+    for (int r = 0; r < N; ++r) {
+      const int rx = r % lat.L, ry = r / lat.L;
+      double sr = 0.0;
+      for (int i = 0; i < N; ++i) {
+        const int j = (i % lat.L + rx) % lat.L + lat.L * ((i / lat.L + ry) % lat.L);  // disp(i, j) = r
+        sr += sign * 0.5 * (at(gu, N, j, i) + at(gd, N, j, i)) / N;
+      }
+      dyn_r[(size_t)slot * N + r] += sr;
+    }
   }
   // The dynamic observables of measure_methods.cpp:315-461 for the listed tau, from the
   // recorded G(t,t), G(t,0), G(0,t) (tau >= 1: slice tau; tau = 0: the reference's
@@ -1148,6 +1159,7 @@ struct Oracle {
       dyn_dos.assign(ntau, 0.0);
       dyn_chi.assign(ntau, 0.0);
       dyn_rho.assign(ntau, 0.0);
+      dyn_r.assign((size_t)ntau * N, 0.0);
     }
     dyn_rec.assign(ntau, {});
     const Vec I = identity(N);
@@ -1315,6 +1327,9 @@ void orc_get_dynamic(void* h, double* sums, int64_t* counts) {
     sums[k] = O(h)->dyn_sum[k];
     counts[k] = O(h)->dyn_cnt[k];
   }
+}
+void orc_get_dynamic_r(void* h, double* out) {
+  std::copy(O(h)->dyn_r.begin(), O(h)->dyn_r.end(), out);
 }
 void orc_get_dynamic_obs(void* h, double* dos, double* chi, double* rho) {
   for (size_t k = 0; k < O(h)->dyn_dos.size(); ++k) {

@@ -98,6 +98,8 @@ void orc_get_dynamic(void* h, double* sums, int64_t* counts);          /* [ntau]
 void orc_get_green_dynamic(void* h, int which, int spin, double* out); /* 0: G(t,0), 1: G(0,t) */
 /* density of states, dynamic spin susceptibility, superfluid-stiffness contribution [ntau] each */
 void orc_get_dynamic_obs(void* h, double* dos, double* chi, double* rho);
+/* per-displacement sums [ntau][N] (see dqmc_get_dynamic_r) */
+void orc_get_dynamic_r(void* h, double* out);
 
 /* Equal-time measurement over the recorded series (measure_handler.cpp:136-150). */
 void orc_measure(void* h);

@@ -86,6 +86,7 @@ def lib() -> ctypes.CDLL:
         "orc_get_dynamic": (None, [vp, dp, ctypes.POINTER(ctypes.c_int64)]),
         "orc_get_green_dynamic": (None, [vp, ctypes.c_int, ctypes.c_int, dp]),
         "orc_get_dynamic_obs": (None, [vp, dp, dp, dp]),
+        "orc_get_dynamic_r": (None, [vp, dp]),
         "orc_measure": (None, [vp]), "orc_write_bin": (None, [vp, ctypes.c_int, dp]),
         "orc_get_accumulators": (None, [vp, dp, ctypes.POINTER(ctypes.c_int)]),
         "orc_get_green": (None, [vp, ctypes.c_int, dp]),
@@ -219,6 +220,12 @@ class Walker:
         d, c, r = np.zeros(n), np.zeros(n), np.zeros(n)
         lib().orc_get_dynamic_obs(self.h, _dp(d), _dp(c), _dp(r))
         return d, c, r
+
+    def dynamic_r(self) -> np.ndarray:
+        """[tau][r] sums of sign * 0.5 sum_i (G_up + G_dn)(i + r, i) / N."""
+        out = np.zeros((len(self._taus), self.N))
+        lib().orc_get_dynamic_r(self.h, _dp(out))
+        return out
 
     def green_dynamic(self, which: int, spin: int) -> np.ndarray:
         """which 0: G(t, 0), 1: G(0, t) after the last dynamic sweep (t = beta)."""

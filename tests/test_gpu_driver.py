@@ -80,6 +80,8 @@ def test_driver_runs_a_reference_config(dq, tmp_path):
     assert int(dos[0]) == 10 and len(dos) == 11
     bins = open(tmp_path / "dos.bins.out").read().splitlines()
     assert bins[0].split() == ["4", "10"]  # 2 walkers x ceil(4 / 2) bins, 10 tau
+    greens = open(tmp_path / "greens.out").read().splitlines()
+    assert greens[0].split() == ["6", "10"]  # every k star of the 4 x 4 lattice, 10 tau
     lt, n, _ = dio.parse_fields(open(tmp_path / "fields.out").read())
     assert (lt, n) == (10, 16)
     # half filling without a sign problem: <n> = 1, sign 1; D(0) = tr G / N near 1/2

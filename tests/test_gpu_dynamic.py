@@ -155,6 +155,10 @@ def test_dynamic_observables_against_oracle(dq, oracle_mod, model, L, mu, Lt, pa
         r.sweep_dynamic(taus)
         for dev, ref in zip(b.dynamic_obs(0), r.dynamic_obs()):
             assert _close(dev, ref), (rnd, dev, ref)
+        assert _close(b.dynamic_r(0), r.dynamic_r())
+        # G(k,tau) of the walker's momentum from the per-displacement sums
+        # the M point (pi, pi) is the walker's default momentum
+        assert _close(b.dynamic_greens_k(0, [(np.pi, np.pi)])[0], b.dynamic(0)[0], 1e-12)
         b.sweep_beta_to_0(measure=False)
         r.sweep_beta_to_0()
     assert b.status(0) == 0

@@ -402,3 +402,27 @@ def test_dynamic_observables_free_fermions_known_answer(oracle_mod, stack):
     d0, c0, _ = w0.dynamic_obs()
     assert abs(d0[0] - d0[1]) < 1e-12 and abs(c0[0] - c0[1]) < 1e-12
     assert abs(d0[2] - 0.5) < 1e-12 and abs(c0[2] - 0.125) < 1e-12  # half filling, U = 0
+
+
+def test_dynamic_displacement_sums_give_g_of_every_k(oracle_mod):
+    """The per-displacement sums reproduce G(k, tau) of the walker's momentum and, at
+    U = 0, exp(-tau e_k) / (1 + exp(-beta e_k)) for every k star."""
+    O = oracle_mod
+    L, mu, beta, Lt = 4, 0.3, 2.0, 20
+    w = O.Walker(model=0, L=L, U=0.0, mu=mu, beta=beta, Lt=Lt, pace=5, stack=1)
+    w.seed(5)
+    w.fields_random()
+    w.init()
+    taus = [0, 1, 5, 7, 10, 19]
+    w.sweep_dynamic(taus)
+    S = w.dynamic_r()
+    sums, _ = w.dynamic()
+    r = np.arange(L * L)
+    rx, ry = r % L, r // L
+    ks = [(i / L * 2 * np.pi - np.pi, j / L * 2 * np.pi - np.pi)
+          for i in range(L // 2, L + 1) for j in range(L // 2, i + 1)]
+    G = np.array([[np.cos(-(rx * kx + ry * ky)) @ S[t] for t in range(len(taus))] for kx, ky in ks])
+    np.testing.assert_allclose(G[-1], sums, atol=1e-12)  # the M point, the walker's momentum
+    for (kx, ky), row in zip(ks, G):
+        e = -2.0 * (np.cos(kx) + np.cos(ky)) + mu
+        np.testing.assert_allclose(row, np.exp(-np.array(taus) * beta / Lt * e) / (1 + np.exp(-beta * e)), atol=1e-12)
