@@ -36,6 +36,7 @@ void launch_measure(int mode, const WalkerDev* W, int nw, int j, int maxN, cudaS
 void launch_sign(const WalkerDev* W, int nw, int maxN, cudaStream_t st);
 double run_fp64_probe(cudaError_t* err);
 void launch_bump(unsigned long long* ctr, cudaStream_t st);
+void launch_bin_close(const WalkerDev* W, int nw, double* bins, int nbins, int bin, cudaStream_t st);
 // general (N > 64) walkers, kernels_general.cu
 cudaError_t configure_general_kernels();
 void general_slice_pre(int mode, const WalkerDev* W, int nw, int j, int q, int maxN, bool any_dense, bool any_cb,
@@ -1179,6 +1180,41 @@ int dqmc_get_observables_all(dqmc_batch* b, double* sums, int64_t* counts) {
       counts[(size_t)w * kNumObs + k] = s[w].obs_cnt[k];
     }
   return DQMC_OK;
+}
+
+int dqmc_measure_bins(dqmc_batch* b, int nbins, int bin_size, int sweeps_between, double* out) {
+  if (!b || !out) return fail(DQMC_ERR_ARG, "null argument");
+  if (nbins <= 0 || bin_size < 2 || sweeps_between < 0) return fail(DQMC_ERR_ARG, "bad bin counts");
+  if (!b->initialised) return fail(DQMC_ERR_STATE, "measurement before dqmc_init_greens");
+  const size_t n = (size_t)b->nw * nbins * kNumObs;
+  double* d_bins = nullptr;
+  CUDA_TRY(cudaMalloc(&d_bins, sizeof(double) * n));
+  int r = DQMC_OK;
+  for (int w = 0; w < b->nw && r == DQMC_OK; ++w) {
+    if (cudaMemsetAsync(b->d_scal[w].obs, 0, sizeof(double) * kNumObs, b->stream) != cudaSuccess ||
+        cudaMemsetAsync(b->d_scal[w].obs_cnt, 0, sizeof(long long) * kNumObs, b->stream) != cudaSuccess)
+      r = fail(DQMC_ERR_CUDA, "clearing the accumulators");
+  }
+  for (int bin = 0; bin < nbins && r == DQMC_OK; ++bin) {
+    for (int s = 0; s < bin_size / 2 && r == DQMC_OK; ++s) {
+      r = dqmc_sweep_0_to_beta(b, 1);
+      if (r == DQMC_OK) r = dqmc_sweep_beta_to_0(b, 1);
+    }
+    if (r == DQMC_OK) launch_bin_close(b->dW, b->nw, d_bins, nbins, bin, b->stream);
+    for (int s = 0; s < sweeps_between / 2 && r == DQMC_OK; ++s) {
+      r = dqmc_sweep_0_to_beta(b, 0);
+      if (r == DQMC_OK) r = dqmc_sweep_beta_to_0(b, 0);
+    }
+  }
+  if (r == DQMC_OK) {
+    if (cudaMemcpyAsync(out, d_bins, sizeof(double) * n, cudaMemcpyDeviceToHost, b->stream) != cudaSuccess ||
+        cudaStreamSynchronize(b->stream) != cudaSuccess)
+      r = fail(DQMC_ERR_CUDA, "reading the bins");
+  } else {
+    cudaStreamSynchronize(b->stream);
+  }
+  cudaFree(d_bins);
+  return r;
 }
 
 int dqmc_clear_observables(dqmc_batch* b) {

@@ -1055,6 +1055,27 @@ __global__ void __launch_bounds__(kThreads) sign_kernel(const WalkerDev* __restr
 __global__ void bump_counter_kernel(unsigned long long* ctr) { *ctr += 1ULL; }
 void launch_bump(unsigned long long* ctr, cudaStream_t st) { bump_counter_kernel<<<1, 1, 0, st>>>(ctr); }
 
+// MeasureHandler::normalize_stats + write_stats_to_bins + clear_temporary
+// (src/measure/measure_handler.cpp:170-277) for every walker on the device:
+// bin = sum / (count <sign>), the sign bin |<sign>|, accumulators cleared.
+// bins: [walker][nbins][kNumObs].
+__global__ void bin_close_kernel(const WalkerDev* __restrict__ W, int nw, double* bins, int nbins, int bin) {
+  const int w = blockIdx.x * blockDim.x + threadIdx.x;
+  if (w >= nw) return;
+  const WalkerDev& h = W[w];
+  const double sign = h.obs[kNumObs - 1] / (double)h.obs_cnt[kNumObs - 1];
+  double* out = bins + ((long long)w * nbins + bin) * kNumObs;
+  for (int k = 0; k < kNumObs - 1; ++k) out[k] = h.obs[k] / ((double)h.obs_cnt[k] * sign);
+  out[kNumObs - 1] = fabs(sign);
+  for (int k = 0; k < kNumObs; ++k) {
+    h.obs[k] = 0.0;
+    h.obs_cnt[k] = 0;
+  }
+}
+void launch_bin_close(const WalkerDev* W, int nw, double* bins, int nbins, int bin, cudaStream_t st) {
+  bin_close_kernel<<<(nw + 127) / 128, 128, 0, st>>>(W, nw, bins, nbins, bin);
+}
+
 // --------------------------------------------------------------------------
 // FP64 FMA throughput probe: 8 independent register FMA chains per thread.
 // --------------------------------------------------------------------------

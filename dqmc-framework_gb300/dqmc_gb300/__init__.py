@@ -37,7 +37,7 @@ EXPORTS = [
     "dqmc_profile_enable", "dqmc_profile_read", "dqmc_microbench_fp64", "dqmc_get_observables_all",
     "dqmc_product_check", "dqmc_product_device_noalloc", "dqmc_launch_count", "dqmc_tuning",
     "dqmc_sweep_dynamic", "dqmc_get_dynamic", "dqmc_clear_dynamic", "dqmc_get_green_dynamic", "dqmc_get_dynamic_obs",
-    "dqmc_get_dynamic_r",
+    "dqmc_get_dynamic_r", "dqmc_measure_bins",
 ]
 KCLASSES = ["segment", "push", "greens", "measure", "product", "metropolis"]
 
@@ -97,6 +97,7 @@ def load() -> ctypes.CDLL:
         "dqmc_clear_dynamic": (c, [vp]), "dqmc_get_green_dynamic": (c, [vp, c, c, c, dp]),
         "dqmc_get_dynamic_obs": (c, [vp, c, dp, dp, dp]),
         "dqmc_get_dynamic_r": (c, [vp, c, dp]),
+        "dqmc_measure_bins": (c, [vp, c, c, c, dp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -234,6 +235,13 @@ class Batch:
         _check(load().dqmc_get_observables_all(self.h, s.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
                                                c.ctypes.data_as(ctypes.POINTER(ctypes.c_int64))))
         return s, c
+
+    def measure_bins(self, nbins: int, bin_size: int, sweeps_between: int = 0) -> np.ndarray:
+        """Dqmc::measure with device-side binning: [walker][bin][NUM_OBS] normalised bins."""
+        out = np.zeros((len(self.walkers), nbins, NUM_OBS))
+        _check(load().dqmc_measure_bins(self.h, nbins, bin_size, sweeps_between,
+                                        out.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
+        return out
 
     def clear_observables(self):
         _check(load().dqmc_clear_observables(self.h))

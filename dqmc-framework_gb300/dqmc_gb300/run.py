@@ -73,6 +73,11 @@ def run(cfg: dio.RunConfig, out_dir: str, walkers: int = 1, seed: int = 12345, f
         dyn_bins = {k: [[] for _ in range(walkers)] for k in ("greens", "dos", "dss", "rho", "sign")}
         ks = dio.kstars(L)
         klist = [ks[i] for i in dio.momentum_list_indices(L, cfg.momentum_list or "KstarsAll")]
+        if eqt and not dyn:  # equal-time only: bins normalised on the device, one copy out
+            binned = b.measure_bins(nbins, max(cfg.bin_size, 2), cfg.sweeps_between_bins)
+            for w in range(walkers):
+                eq_bins[w].extend(binned[w])
+            nbins = 0
         for _ in range(nbins):
             b.clear_observables()
             if dyn:

@@ -155,6 +155,13 @@ int dqmc_sweep_dynamic(dqmc_batch* b, const int* taus, int ntau);
 /* Sums of sign * G(k,tau) and their counts, in the order of the last tau list. */
 int dqmc_get_dynamic(dqmc_batch* b, int walker, double* sums, int64_t* counts);
 int dqmc_clear_dynamic(dqmc_batch* b);
+/* Dqmc::measure (src/dqmc.cpp:108-151) with the binning on the device: nbins bins of
+ * bin_size / 2 forth-and-back half-sweep pairs with equal-time measurements, each bin
+ * normalised and stored by a kernel (MeasureHandler::normalize_stats and
+ * write_stats_to_bins, src/measure/measure_handler.cpp:170-277), sweeps_between / 2
+ * unmeasured pairs between bins; one copy out at the end.  out: [walker][nbins][9] in
+ * the order of dqmc_get_observables, the last entry |<sign>|. */
+int dqmc_measure_bins(dqmc_batch* b, int nbins, int bin_size, int sweeps_between, double* out);
 /* Sums per listed tau of the other dynamic observables of the reference
  * (src/measure/measure_methods.cpp:315-461): the density of states D(tau)
  * (measure_density_of_states), the local dynamic spin susceptibility
