@@ -9,7 +9,9 @@ writes a compact fixture:
   * the final 160x64 Ising configuration of example/output/fields.out,
     packed 1 bit per site (t-major, bit set = +1),
   * the mean +/- error of every equal-time observable and the maximum wrap
-    error printed in example/log.out.
+    error printed in example/log.out,
+  * the mean +/- error of the dynamic observables of example/output/dos.out,
+    dss.out and greens.out at a few tau (and k stars).
 
 Usage: python tests/golden/make_example_fixture.py <reference-checkout>
 """
@@ -56,6 +58,26 @@ def main(ref: str) -> None:
                 if m:
                     observables[key] = [float(m.group(1)), float(m.group(2))]
 
+    def table(name, ncols):
+        rows = {}
+        with open(os.path.join(ref, "example", "output", name)) as f:
+            f.readline()
+            for line in f:
+                p = line.split()
+                if len(p) == ncols:
+                    rows[tuple(int(x) for x in p[:ncols - 3])] = [float(p[-3]), float(p[-2])]
+        return rows
+
+    taus = [0, 1, 5, 20, 80, 140, 159]
+    dos, dss, greens = table("dos.out", 4), table("dss.out", 4), table("greens.out", 5)
+    dynamic = {
+        "taus": taus,
+        "density_of_states": [dos[(t,)] for t in taus],
+        "dynamic_spin_susceptibility": [dss[(t,)] for t in taus],
+        "greens_kstars": [0, 7, 14],
+        "greens_functions": [[greens[(k, t)] for t in taus] for k in (0, 7, 14)],
+    }
+
     fixture = {
         "source": "reference example run: example/config.toml, example/log.out:42-55, example/output/fields.out",
         "model": "attractive", "L": 8, "hopping_t": 1.0, "onsite_u": 4.0, "mu": 0.0,
@@ -64,6 +86,7 @@ def main(ref: str) -> None:
         "fields_packed_hex": packed,
         "max_wrap_error": wrap,
         "observables": observables,
+        "dynamic": dynamic,
     }
     out = os.path.join(os.path.dirname(os.path.abspath(__file__)), "example_8x8.json")
     with open(out, "w") as f:

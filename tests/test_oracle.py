@@ -426,3 +426,77 @@ def test_dynamic_displacement_sums_give_g_of_every_k(oracle_mod):
     for (kx, ky), row in zip(ks, G):
         e = -2.0 * (np.cos(kx) + np.cos(ky)) + mu
         np.testing.assert_allclose(row, np.exp(-np.array(taus) * beta / Lt * e) / (1 + np.exp(-beta * e)), atol=1e-12)
+
+
+def _pin_chain_dynamic(args):
+    import os
+    import sys
+
+    root = args[0]
+    sys.path.insert(0, os.path.join(root, "oracle"))
+    import oracle as O
+
+    O.use_scipy_lapack(True)
+    seed, fields, warm, nbins, binsize, taus, kstars = args[1:]
+    w = O.Walker(model=O.ATTRACTIVE, L=8, U=4.0, beta=8.0, Lt=160, pace=10)
+    w.seed(seed)
+    w.set_fields(fields)
+    w.init()
+    for _ in range(warm):
+        w.sweep_0_to_beta()
+        w.sweep_beta_to_0()
+    alltau = list(range(160))
+    r = np.arange(64)
+    rx, ry = r % 8, r // 8
+    ff = np.array([[np.cos(-(rx * kx + ry * ky))] for kx, ky in kstars])[:, 0, :]  # [k][r]
+    prev = None
+    out = {"dos": [], "dss": [], "greens": []}
+    for _ in range(nbins):
+        sg = 0.0
+        for _ in range(binsize):
+            w.sweep_dynamic(alltau)
+            sg += w.sign
+            w.sweep_beta_to_0()
+        d, c, _ = w.dynamic_obs()
+        S = w.dynamic_r()
+        cur = (d.copy(), c.copy(), S.copy())
+        if prev is not None:
+            d, c, S = d - prev[0], c - prev[1], S - prev[2]
+        prev = cur
+        norm = binsize * (sg / binsize)  # MeasureHandler::normalize_stats with the dynamic sign
+        out["dos"].append(d[taus] / norm)
+        out["dss"].append(c[taus] / norm)
+        out["greens"].append((ff @ S.T)[:, taus] / norm)
+    return {k: np.array(v) for k, v in out.items()}
+
+
+@pytest.mark.slow
+def test_statistical_pin_dynamic_against_reference_example(oracle_mod, example_fixture):
+    """Oracle dynamic observables vs the reference's example/output/dos.out, dss.out and
+    greens.out (attractive 8x8, beta = 8, warm-started from fields.out)."""
+    import os
+
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    dyn = example_fixture["dynamic"]
+    taus = dyn["taus"]
+    L = 8
+    ks_all = [(i / L * 2 * np.pi - np.pi, j / L * 2 * np.pi - np.pi)
+              for i in range(L // 2, L + 1) for j in range(L // 2, i + 1)]
+    kstars = [ks_all[k] for k in dyn["greens_kstars"]]
+    jobs = [(root, 900 + k, example_fixture["fields"], 4, 3, 8, taus, kstars) for k in range(8)]
+    with mp.get_context("spawn").Pool(8) as pool:
+        res = pool.map(_pin_chain_dynamic, jobs)
+
+    def check(name, bins, ref):
+        bins = np.concatenate(bins)
+        mean = bins.mean(axis=0)
+        err = np.sqrt(np.maximum((bins ** 2).mean(axis=0) - mean ** 2, 0)) / np.sqrt(len(bins) - 1)
+        ref = np.array(ref)
+        sigma = np.hypot(err, ref[..., 1])
+        # bins of one chain are autocorrelated: allow 5 combined sigma
+        bad = np.abs(mean - ref[..., 0]) > 5 * sigma
+        assert not bad.any(), (name, mean[bad], err[bad], ref[..., 0][bad], ref[..., 1][bad])
+
+    check("density_of_states", [r["dos"] for r in res], dyn["density_of_states"])
+    check("dynamic_spin_susceptibility", [r["dss"] for r in res], dyn["dynamic_spin_susceptibility"])
+    check("greens_functions", [r["greens"] for r in res], dyn["greens_functions"])
