@@ -11,7 +11,9 @@ observables the forward half-sweep is sweep_for_dynamic_greens and the equal-tim
 measurement is taken on the backward one), the normalisation of
 MeasureHandler::normalize_stats, and sweeps_between_bins / 2 unmeasured sweeps
 between bins; the bins of all walkers are pooled (the reference's MPI gather) and
-analysed as Observable::analyse.  Output: the terminal summary of the scalar
+analysed as Observable::analyse.  Under torchrun every process runs W walkers on its
+own GPU and rank 0 gathers the bins, analyses and writes (the reference's MPI
+layout, include/utils/mpi.hpp:29-104).  Output: the terminal summary of the scalar
 observables and fields.out, kstars.out, tgrids.out, swave(.bins).out,
 dos(.bins).out, greens(.bins).out, dss(.bins).out in the reference's formats.
 G(k, tau) covers the configured `momentum_list` (rows of greens.out in the
@@ -27,6 +29,7 @@ import sys
 import numpy as np
 
 from . import io as dio
+from . import parallel
 
 DESCRIPTIONS = {
     "filling_number": "Filling number", "double_occupancy": "Double occupation", "kinetic_energy": "Kinetic energy",
@@ -39,15 +42,21 @@ DESCRIPTIONS = {
 
 def run(cfg: dio.RunConfig, out_dir: str, walkers: int = 1, seed: int = 12345, fields_file: str | None = None,
         precision: str = "fp64", rng: str = "minstd", log=sys.stdout) -> dict:
-    """Run the configuration; returns {name: (mean, error)} and writes the output files."""
+    """Run the configuration; returns {name: (mean, error)} and writes the output files
+    (rank 0 of a torchrun launch; the other ranks return {})."""
     import dqmc_gb300 as dq
 
+    rank, size = parallel.init()
+    if size > 1:
+        import torch
+
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
     L, lt = cfg.L, cfg.time_size
     kidx = dio.momentum_index(L, cfg.momentum) if cfg.momentum else -1
     model = dq.ATTRACTIVE if cfg.model == "AttractiveHubbard" else dq.REPULSIVE
     descs = [dq.WalkerDesc(model=model, L=L, t=cfg.hopping_t, U=cfg.onsite_u, mu=cfg.chemical_potential,
                            beta=cfg.beta, Lt=lt, pace=cfg.stabilization_pace, checkerboard=cfg.checkerboard,
-                           momentum_index=kidx, seed=seed + w) for w in range(walkers)]
+                           momentum_index=kidx, seed=seed + rank * walkers + w) for w in range(walkers)]
     # the dynamic half-sweep runs on the HBM path, which walkers with N <= 64 take only when asked
     b = dq.Batch(descs, rng=dq.RNG_PHILOX if rng == "philox" else dq.RNG_MINSTD,
                  precision=dq.MIXED if precision == "mixed" else dq.FP64, hbm=bool(cfg.dynamic))
@@ -68,7 +77,7 @@ def run(cfg: dio.RunConfig, out_dir: str, walkers: int = 1, seed: int = 12345, f
             b.sweep_beta_to_0()
         eqt, dyn = bool(cfg.equaltime), bool(cfg.dynamic)
         taus = list(range(lt))
-        nbins = math.ceil(cfg.bin_num / walkers) if (eqt or dyn) else 0
+        nbins = math.ceil(cfg.bin_num / (walkers * size)) if (eqt or dyn) else 0
         eq_bins = [[] for _ in range(walkers)]
         dyn_bins = {k: [[] for _ in range(walkers)] for k in ("greens", "dos", "dss", "rho", "sign")}
         ks = dio.kstars(L)
@@ -113,6 +122,12 @@ def run(cfg: dio.RunConfig, out_dir: str, walkers: int = 1, seed: int = 12345, f
     finally:
         b.close()
 
+    eq_local = np.array([bb for wb in eq_bins for bb in wb])
+    dyn_local = {k: np.array([x for wb in v for x in wb]) for k, v in dyn_bins.items()}
+    eq_all = parallel.gather_bins(eq_local) if eqt else None
+    dyn_all = {k: parallel.gather_bins(v) for k, v in dyn_local.items()} if dyn else None
+    if rank != 0:
+        return {}
     os.makedirs(out_dir, exist_ok=True)
     results = {}
 
@@ -121,7 +136,7 @@ def run(cfg: dio.RunConfig, out_dir: str, walkers: int = 1, seed: int = 12345, f
             f.write(text)
 
     if eqt:
-        pooled = np.array([bb for wb in eq_bins for bb in wb])
+        pooled = eq_all
         mean, err = dio.analyse_bins(pooled)
         for i, name in enumerate(dq.OBS_NAMES):
             if name == "equaltime_sign" or name in cfg.equaltime:
@@ -131,7 +146,7 @@ def run(cfg: dio.RunConfig, out_dir: str, walkers: int = 1, seed: int = 12345, f
             write("swave.out", dio.format_scalar(mean[i], err[i]))
             write("swave.bins.out", dio.format_bins_scalar(pooled[:, i]))
     if dyn:
-        pool = {k: np.array([x for wb in v for x in wb]) for k, v in dyn_bins.items()}
+        pool = dyn_all
         results["dynamic_sign"] = tuple(float(x) for x in dio.analyse_bins(pool["sign"]))
         for name, key, fname in (("density_of_states", "dos", "dos"), ("dynamic_spin_susceptibility", "dss", "dss")):
             if name in cfg.dynamic:
