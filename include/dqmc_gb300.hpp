@@ -140,6 +140,19 @@ class DqmcWalker {
     if (counts) *counts = c;
     return s;
   }
+  // per-displacement sums [tau][r] of the time-displaced Green's function: G(k,tau) of
+  // measure_greens_functions for any momentum list is sum_r FourierFactor(r, k) S[tau][r]
+  std::vector<double> DynamicGreensR(int w, int ntau) const {
+    std::vector<double> s((size_t)ntau * N_);
+    check(dqmc_get_dynamic_r(b_, w, s.data()));
+    return s;
+  }
+  // Dqmc::measure with the bins normalised on the device: [walker][bin][9]
+  std::vector<double> MeasureBins(int nbins, int bin_size, int sweeps_between) {
+    std::vector<double> out((size_t)n_ * nbins * 9);
+    check(dqmc_measure_bins(b_, nbins, bin_size, sweeps_between, out.data()));
+    return out;
+  }
   // measure_density_of_states, measure_dynamic_spin_susceptibility and the per-tau terms of
   // measure_superfluid_stiffness (src/measure/measure_methods.cpp:315-461), sums per listed tau
   struct DynamicObservables { std::vector<double> density_of_states, spin_susceptibility, stiffness_terms; };
