@@ -992,17 +992,12 @@ __global__ void __launch_bounds__(kThreads) sign_kernel(const WalkerDev* __restr
   extern __shared__ double smem[];
   const int N = w.N, ld = N + 1;
   double* M = smem;
-  double* Y = M + (long long)N * ld;  // unused right-hand side (1 column used)
-  double* red = Y + (long long)N * ld;
   __shared__ int s_neg;
   if (threadIdx.x == 0) s_neg = 0;
   int total_neg = 0;
   for (int sp = 0; sp < 2; ++sp) {
     const double* Gg = w.G + (long long)sp * N * N;
-    for (int e = threadIdx.x; e < N * N; e += kThreads) {
-      at(M, ld, e % N, e / N) = Gg[e];
-      at(Y, ld, e % N, e / N) = 0.0;
-    }
+    for (int e = threadIdx.x; e < N * N; e += kThreads) at(M, ld, e % N, e / N) = Gg[e];
     __syncthreads();
     // LU with partial pivoting, counting swaps and negative pivots
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -1047,7 +1042,6 @@ __global__ void __launch_bounds__(kThreads) sign_kernel(const WalkerDev* __restr
     }
     total_neg = s_neg;
   }
-  (void)red;
   if (threadIdx.x == 0) *w.sign = (total_neg % 2 == 0) ? 1.0 : -1.0;
 }
 
