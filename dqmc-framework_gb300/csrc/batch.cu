@@ -1124,6 +1124,17 @@ int dqmc_get_green(dqmc_batch* b, int w, int spin, double* out) {
   return DQMC_OK;
 }
 
+int dqmc_set_green(dqmc_batch* b, int w, int spin, const double* g) {
+  if (int r = check_walker(b, w)) return r;
+  if (spin < 0 || spin > 1 || !g) return fail(DQMC_ERR_ARG, "bad spin or null input");
+  if (!b->initialised) return fail(DQMC_ERR_STATE, "dqmc_set_green before dqmc_init_greens");
+  const int N = b->hw[w].N;
+  CUDA_TRY(cudaMemcpyAsync(b->hw[w].G + (size_t)spin * N * N, g, sizeof(double) * N * N, cudaMemcpyHostToDevice,
+                           b->stream));
+  CUDA_TRY(cudaStreamSynchronize(b->stream));
+  return DQMC_OK;
+}
+
 static int read_scal_bytes(dqmc_batch* b, int w, const void* dptr, void* out, size_t bytes) {
   if (int r = check_walker(b, w)) return r;
   if (!out) return fail(DQMC_ERR_ARG, "null output");

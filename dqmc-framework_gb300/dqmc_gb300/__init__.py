@@ -37,7 +37,7 @@ EXPORTS = [
     "dqmc_profile_enable", "dqmc_profile_read", "dqmc_microbench_fp64", "dqmc_get_observables_all",
     "dqmc_product_check", "dqmc_product_device_noalloc", "dqmc_launch_count", "dqmc_tuning",
     "dqmc_sweep_dynamic", "dqmc_get_dynamic", "dqmc_clear_dynamic", "dqmc_get_green_dynamic", "dqmc_get_dynamic_obs",
-    "dqmc_get_dynamic_r", "dqmc_measure_bins",
+    "dqmc_get_dynamic_r", "dqmc_measure_bins", "dqmc_set_green",
 ]
 KCLASSES = ["segment", "push", "greens", "measure", "product", "metropolis"]
 
@@ -98,6 +98,7 @@ def load() -> ctypes.CDLL:
         "dqmc_get_dynamic_obs": (c, [vp, c, dp, dp, dp]),
         "dqmc_get_dynamic_r": (c, [vp, c, dp]),
         "dqmc_measure_bins": (c, [vp, c, c, c, dp]),
+        "dqmc_set_green": (c, [vp, c, c, dp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -200,6 +201,11 @@ class Batch:
         g = np.zeros((N, N), order="F")
         _check(load().dqmc_get_green(self.h, w, spin, g.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
         return g
+
+    def set_green(self, w: int, spin: int, g):
+        """Overwrite walker w's equal-time G of one spin (restart and test hook)."""
+        g = np.asfortranarray(g, dtype=np.float64)
+        _check(load().dqmc_set_green(self.h, w, spin, g.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
 
     def config_sign(self, w: int) -> float:
         v = ctypes.c_double()

@@ -181,6 +181,11 @@ int dqmc_get_green_dynamic(dqmc_batch* b, int walker, int which, int spin, doubl
 /* Accessors: DqmcWalker::GreenttUp/GreenttDn, ConfigSign, WrapError
  * (include/dqmc_walker.h:150-184). spin 0 = up, 1 = down. */
 int dqmc_get_green(dqmc_batch* b, int walker, int spin, double* out);
+/* Overwrite the equal-time G of one walker and spin (column-major N x N; the
+ * attractive model's walkers use spin 0).  The reference's walker owns G and has no
+ * setter: this is a restart and test hook (the tests inject a non-finite entry this
+ * way and check that only that walker's status word reports it). */
+int dqmc_set_green(dqmc_batch* b, int walker, int spin, const double* g);
 int dqmc_get_config_sign(dqmc_batch* b, int walker, double* out);
 int dqmc_get_wrap_error(dqmc_batch* b, int walker, double* out);
 int dqmc_get_accept_count(dqmc_batch* b, int walker, int64_t* out);
