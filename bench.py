@@ -372,7 +372,7 @@ def run_gpu(args, wl, rank, world):
                                "the reference's rank-1 update flops, 2 N^2 per accepted flip and spin")
     else:
         for k in ("segment", "push", "greens"):
-            model[k] = ("fp64", fm[k] * units, fp64_peak / 1e3, "FP64 flops of the class (see DESIGN.md)")
+            model[k] = ("fp64", fm[k] * units, fp64_peak / 1e3, "FP64 flops of the class (flops_model: wraps, chain products, Green's assembly)")
     dom = max((k for k in model if prof.get(k, (0, 0))[1] > 0), key=lambda k: prof[k][0])
     bound, flops, peak, what = model[dom]
     dom_ms, dom_n = prof[dom]
