@@ -30,7 +30,7 @@ class RunConfig:
     hopping_t: float = 1.0
     onsite_u: float = 4.0
     chemical_potential: float = 0.0
-    lattice: str = "Square"
+    lattice: str = "Square"   # "Square" or "Cubic"
     cell: tuple = (4, 4)
     momentum: str = ""
     momentum_list: str = ""
@@ -47,6 +47,10 @@ class RunConfig:
     @property
     def L(self) -> int:
         return self.cell[0]
+
+    @property
+    def dim(self) -> int:
+        return len(self.cell)
 
     @property
     def equaltime(self) -> list:
@@ -71,17 +75,21 @@ def parse_config(text: str) -> RunConfig:
     cfg.onsite_u = float(p.get("onsite_u", 4.0))
     cfg.chemical_potential = float(p.get("chemical_potential", 0.0))
     cfg.lattice = lat.get("type", "Square")
-    if cfg.lattice != "Square":
-        raise ValueError(f"lattice type '{cfg.lattice}' is not supported (the square lattice is)")
+    dims = {"Square": (2, "2d square", "two"), "Cubic": (3, "3d cubic", "three")}
+    if cfg.lattice not in dims:  # Honeycomb: left unimplemented by the reference
+        raise ValueError(f"undefined lattice type '{cfg.lattice}'")
+    dim, what, count = dims[cfg.lattice]
     cell = lat.get("cell")
-    if not isinstance(cell, list) or len(cell) != 2 or any((not isinstance(v, int)) or v < 1 for v in cell):
-        raise ValueError("the input cell of 2d square lattice should be a vector containing two positive integers")
-    if cell[0] != cell[1]:
-        raise ValueError("the square lattice must have equal sides")
-    cfg.cell = (cell[0], cell[1])
+    if not isinstance(cell, list) or len(cell) != dim or any((not isinstance(v, int)) or v < 1 for v in cell):
+        raise ValueError(f"the input cell of {what} lattice should be a vector containing {count} positive integers")
+    if len(set(cell)) != 1:  # Square/Cubic::set_lattice_params assert equal sides
+        raise ValueError(f"the {what} lattice must have equal sides")
+    cfg.cell = tuple(cell)
     cfg.momentum = lat.get("momentum", "")
     cfg.momentum_list = lat.get("momentum_list", "")
     cfg.checkerboard = bool(c.get("CheckerBoard", {}).get("whether_or_not", False))
+    if cfg.checkerboard and cfg.lattice != "Square":
+        raise ValueError("the checkerboard method is currently only implemented for 2d square lattice")
     cfg.beta = float(mc.get("beta", 4.0))
     cfg.time_size = int(mc.get("time_size", 80))
     cfg.stabilization_pace = int(mc.get("stabilization_pace", 10))
@@ -99,6 +107,8 @@ def parse_config(text: str) -> RunConfig:
     for o in obs:
         if o not in ALL_OBSERVABLES:
             raise ValueError(f"unsupported observable '{o}'")
+    if cfg.lattice != "Square":  # a square-lattice observable (dqmc_initializer.cpp:233-237)
+        obs = [o for o in obs if o != "superfluid_stiffness"]
     cfg.observables = obs
     return cfg
 
@@ -108,44 +118,64 @@ def load_config(path: str) -> RunConfig:
         return parse_config(f.read())
 
 
-# ---- lattice tables (src/lattice/square.cpp:42-145) ------------------------------
-def kstars(L: int) -> list:
-    """The inequivalent momenta (k stars) of the L x L square lattice, in the reference's order."""
-    out = []
-    for i in range(math.ceil(L / 2), L + 1):
-        for j in range(math.ceil(L / 2), i + 1):
-            out.append((i / L * 2 * math.pi - math.pi, j / L * 2 * math.pi - math.pi))
-    return out
+# ---- lattice tables (src/lattice/square.cpp:42-145, src/lattice/cubic.cpp:47-183) ----
+def kstars(L: int, dim: int = 2) -> list:
+    """The inequivalent momenta (k stars) of the L x L square or L x L x L cubic lattice, in
+    the reference's order (the cubic ones fill the tetrahedron (0,0,0), (pi,0,0), (pi,pi,0),
+    (pi,pi,pi) with kz outermost)."""
+    m = lambda i: i / L * 2 * math.pi - math.pi
+    lo = math.ceil(L / 2)
+    if dim == 2:
+        return [(m(i), m(j)) for i in range(lo, L + 1) for j in range(lo, i + 1)]
+    return [(m(i), m(j), m(k)) for k in range(lo, L + 1) for i in range(k, L + 1) for j in range(k, i + 1)]
 
 
-def momentum_index(L: int, name: str) -> int:
-    """Index of a high-symmetry point among the k stars (Square::initial_symmetry_points)."""
-    nk = len(kstars(L))
-    table = {"GammaPoint": 0, "XPoint": nk - L // 2 - 1, "MPoint": nk - 1}
-    if name not in table:
-        raise ValueError(f"unsupported momentum '{name}' (GammaPoint, XPoint, MPoint)")
-    return table[name]
-
-
-def momentum_list_indices(L: int, name: str) -> list:
-    """k-star indices of a momentum list (Square::initial_symmetry_points and the
-    initializer's momentum_list options): KstarsAll, DeltaLine, ZLine, SigmaLine,
-    Gamma2X2M2GammaLoop, or a single point."""
-    nk = len(kstars(L))
+def _points(L: int, dim: int) -> dict:
+    """Square/Cubic::initial_symmetry_points: indices of the high-symmetry points."""
     h = L // 2
-    xp = nk - h - 1
-    if name == "KstarsAll":
-        return list(range(nk))
-    if name == "DeltaLine":
-        return [i * (i + 1) // 2 for i in range(h + 1)]
-    if name == "ZLine":
-        return [xp + i for i in range(h + 1)]
-    if name == "SigmaLine":
-        return [i * (i + 3) // 2 for i in range(h + 1)]
-    if name == "Gamma2X2M2GammaLoop":
-        return ([i * (i + 1) // 2 for i in range(h)] + [xp + i for i in range(h)] +
-                [i * (i + 3) // 2 for i in range(h, 0, -1)])
-    return [momentum_index(L, name)]
+    m_point = (h + 1) * (h + 2) // 2 - 1  # the last k star of the kz = 0 plane
+    pts = {"GammaPoint": 0, "XPoint": m_point - h, "MPoint": m_point}
+    if dim == 3:
+        pts["RPoint"] = len(kstars(L, 3)) - 1
+    return pts
+
+
+def momentum_index(L: int, name: str, dim: int = 2) -> int:
+    """Index of a high-symmetry point among the k stars: GammaPoint, XPoint, MPoint, and on
+    the cubic lattice RPoint."""
+    pts = _points(L, dim)
+    if name not in pts:
+        raise ValueError(f"undefined momentum '{name}' for the {'2d square' if dim == 2 else '3d cubic'} lattice "
+                         f"({', '.join(pts)})")
+    return pts[name]
+
+
+def momentum_list_indices(L: int, name: str, dim: int = 2) -> list:
+    """k-star indices of a momentum list (Square/Cubic::initial_symmetry_points and the
+    initializer's momentum_list options): KstarsAll, DeltaLine, ZLine, SigmaLine, and
+    Gamma2X2M2GammaLoop (square) or LambdaLine, SLine, TLine (cubic); a single point name
+    gives that point."""
+    nk = len(kstars(L, dim))
+    h = L // 2
+    pts = _points(L, dim)
+    xp, mp = pts["XPoint"], pts["MPoint"]
+    lines = {"KstarsAll": list(range(nk)), "DeltaLine": [i * (i + 1) // 2 for i in range(h + 1)],
+             "ZLine": [xp + i for i in range(h + 1)], "SigmaLine": [i * (i + 3) // 2 for i in range(h + 1)]}
+    if dim == 2:
+        lines["Gamma2X2M2GammaLoop"] = ([i * (i + 1) // 2 for i in range(h)] + [xp + i for i in range(h)] +
+                                        [i * (i + 3) // 2 for i in range(h, 0, -1)])
+    else:  # cubic.cpp:160-182: each step skips one kz plane of the tetrahedron
+        lam, sl, tl = [0], [xp], [mp]
+        for i in range(1, h + 1):
+            lam.append(lam[-1] + (h + 2 - i) * (h + 3 - i) // 2)
+            sl.append(sl[-1] + (h + 1 - i) * (h + 2 - i) // 2 + 1)
+            tl.append(tl[-1] + (h + 1 - i) * (h + 2 - i) // 2)
+        lines.update(LambdaLine=lam, SLine=sl, TLine=tl)
+    if name in lines:
+        return lines[name]
+    if name in pts:
+        return [pts[name]]
+    raise ValueError(f"undefined momentum list '{name}' ({', '.join(list(lines) + list(pts))})")
 
 
 # ---- text formats (boost::format "%| 20.10f|" etc. of include/dqmc_io.h) ------------
@@ -200,9 +230,10 @@ def format_bins_matrix(bins) -> str:
     return "".join(out)
 
 
-def format_kstars(L: int) -> str:
-    ks = kstars(L)
-    return _d(len(ks)) + "\n" + "".join(_d(i) + _f(kx) + _f(ky) + "\n" for i, (kx, ky) in enumerate(ks))
+def format_kstars(L: int, dim: int = 2) -> str:
+    """DqmcIO::output_k_stars: the count, then 'index kx ky (kz)' per k star."""
+    ks = kstars(L, dim)
+    return _d(len(ks)) + "\n" + "".join(_d(i) + "".join(_f(c) for c in k) + "\n" for i, k in enumerate(ks))
 
 
 def format_tgrids(beta: float, time_size: int) -> str:

@@ -46,6 +46,8 @@ def run(cfg: dio.RunConfig, out_dir: str, walkers: int = 1, seed: int = 12345, f
     (rank 0 of a torchrun launch; the other ranks return {})."""
     import dqmc_gb300 as dq
 
+    if cfg.lattice != "Square":
+        raise NotImplementedError(f"the GPU sweep runs the square lattice; '{cfg.lattice}' is not built on the device")
     rank, size = parallel.init()
     if size > 1:
         import torch

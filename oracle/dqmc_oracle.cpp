@@ -11,7 +11,8 @@
  *   src/svd_stack.cpp:34-87                 UDV stack
  *   include/utils/numerical_stable.hpp:34-239  stable (1 + L R^T)^-1
  *   include/utils/linear_algebra.hpp:41-80  dgesvd semantics (U, S desc, V)
- *   src/lattice/square.cpp:31-177           lattice tables (hopping matrix zeroed)
+ *   src/lattice/square.cpp:31-178           square lattice tables (hopping matrix zeroed)
+ *   src/lattice/cubic.cpp:35-219            cubic lattice tables (dense K only)
  *   src/measure/measure_methods.cpp:22-255  equal-time observables
  *   src/measure/measure_handler.cpp:170-240 bin normalisation
  * Third-party arithmetic replaced here: Eigen 3.4 GEMM / PartialPivLU /
@@ -572,49 +573,74 @@ Vec equaltime_greens(int n, const Stack& left, const Stack& right) {
 }
 
 // ----------------------------------------------------------------------------
-// Square lattice tables (src/lattice/square.cpp:31-177)
+// Square and cubic lattice tables (src/lattice/square.cpp:31-178,
+// src/lattice/cubic.cpp:35-219).  Site i has coordinates x = i % L,
+// y = (i / L) % L, z = i / L^2; a displacement is stored as the site index of
+// its vector, each component taken mod L.
 // ----------------------------------------------------------------------------
 struct Lattice {
-  int L = 0, N = 0, nk = 0, m_point = 0;
-  std::vector<int> nn;  // [i][4]
+  int L = 0, dim = 2, N = 0, nk = 0, m_point = 0;  // m_point: the last k star, (pi, ..., pi)
+  std::vector<int> nn;  // [i][2 dim]: +x, +y (, +z), then -x, -y (, -z) (square.cpp:69-85, cubic.cpp:84-109)
   Vec hop;              // N x N
-  std::vector<double> kx, ky;
+  std::vector<double> kx, ky, kz;
+  int coord(int i, int a) const { return a == 0 ? i % L : a == 1 ? (i / L) % L : i / (L * L); }
+  // displacement from site i to site j (square.cpp:88-105, cubic.cpp:112-132)
   int disp(int i, int j) const {
-    const int xi = i % L, yi = i / L, xj = j % L, yj = j / L;
-    return (xj - xi + L) % L + ((yj - yi + L) % L) * L;
+    int d = 0, w = 1;
+    for (int a = 0; a < dim; ++a, w *= L) d += ((coord(j, a) - coord(i, a) + L) % L) * w;
+    return d;
   }
+  // the site at displacement d from site i (disp(i, shift(i, d)) == d)
+  int shift(int i, int d) const {
+    int j = 0, w = 1;
+    for (int a = 0; a < dim; ++a, w *= L) j += ((coord(i, a) + coord(d, a)) % L) * w;
+    return j;
+  }
+  // Re exp(-i k.r) (square.cpp:148-161, cubic.cpp:186-200)
   double fourier(int d, int k) const {
-    const int x = d % L, y = d / L;
-    return std::cos(-x * kx[k] - y * ky[k]);
+    if (dim == 2) return std::cos(-coord(d, 0) * kx[k] - coord(d, 1) * ky[k]);
+    return std::cos(-coord(d, 0) * kx[k] - coord(d, 1) * ky[k] - coord(d, 2) * kz[k]);
   }
-  void init(int L_) {
+  void init(int L_, int dim_) {
     L = L_;
-    N = L * L;
-    nn.assign((size_t)N * 4, 0);
-    for (int i = 0; i < N; ++i) {
-      const int x = i % L, y = i / L;
-      nn[i * 4 + 0] = (x + 1) % L + L * y;
-      nn[i * 4 + 2] = (x - 1 + L) % L + L * y;
-      nn[i * 4 + 1] = x + L * ((y + 1) % L);
-      nn[i * 4 + 3] = x + L * ((y - 1 + L) % L);
-    }
+    dim = dim_;
+    N = dim == 2 ? L * L : L * L * L;
+    const int nd = 2 * dim;
+    nn.assign((size_t)N * nd, 0);
+    for (int i = 0; i < N; ++i)
+      for (int a = 0, w = 1; a < dim; ++a, w *= L) {
+        const int c = coord(i, a);
+        nn[i * nd + a] = i + ((c + 1) % L - c) * w;
+        nn[i * nd + dim + a] = i + ((c - 1 + L) % L - c) * w;
+      }
     hop.assign((size_t)N * N, 0.0);  // zeroed: the reference resizes without init (square.cpp:166)
-    for (int i = 0; i < N; ++i) {
-      const int a = nn[i * 4 + 0], b = nn[i * 4 + 1];
-      at(hop, N, i, a) += 1.0;
-      at(hop, N, a, i) += 1.0;
-      at(hop, N, i, b) += 1.0;
-      at(hop, N, b, i) += 1.0;
-    }
-    const int h = L / 2;  // floor(L/2)
-    nk = (h + 1) * (h + 2) / 2;
+    for (int i = 0; i < N; ++i)
+      for (int a = 0; a < dim; ++a) {
+        const int j = nn[i * nd + a];
+        at(hop, N, i, j) += 1.0;
+        at(hop, N, j, i) += 1.0;
+      }
     kx.clear();
     ky.clear();
-    for (int i = (L + 1) / 2; i <= L; ++i)
-      for (int j = (L + 1) / 2; j <= i; ++j) {
-        kx.push_back((double)i / L * 2 * M_PI - M_PI);
-        ky.push_back((double)j / L * 2 * M_PI - M_PI);
-      }
+    kz.clear();
+    const auto mom = [&](int i) { return (double)i / L * 2 * M_PI - M_PI; };
+    const int lo = (L + 1) / 2;  // ceil(L/2)
+    if (dim == 2) {
+      for (int i = lo; i <= L; ++i)
+        for (int j = lo; j <= i; ++j) {
+          kx.push_back(mom(i));
+          ky.push_back(mom(j));
+        }
+    } else {  // the tetrahedron (0,0,0), (pi,0,0), (pi,pi,0), (pi,pi,pi); z outermost (cubic.cpp:47-81)
+      for (int k = lo; k <= L; ++k)
+        for (int i = k; i <= L; ++i)
+          for (int j = k; j <= i; ++j) {
+            kx.push_back(mom(i));
+            ky.push_back(mom(j));
+            kz.push_back(mom(k));
+          }
+    }
+    nk = (int)kx.size();
     m_point = nk - 1;
   }
 };
@@ -663,7 +689,11 @@ struct Oracle {
 
   void setup(const orc_params& pp) {
     p = pp;
-    lat.init(p.L);
+    if (p.L < 1 || (p.lattice != ORC_SQUARE && p.lattice != ORC_CUBIC))
+      throw std::invalid_argument("lattice: unknown type or side < 1");
+    if (p.lattice == ORC_CUBIC && p.checkerboard)  // dqmc_initializer.cpp:169-182
+      throw std::invalid_argument("the checkerboard method is only implemented for the square lattice");
+    lat.init(p.L, p.lattice == ORC_CUBIC ? 3 : 2);
     N = lat.N;
     Lt = p.Lt;
     pace = p.pace;
@@ -1089,10 +1119,9 @@ struct Oracle {
     dyn_sum[slot] += sum;
     dyn_cnt[slot] += 1;
     for (int r = 0; r < N; ++r) {
-      const int rx = r % lat.L, ry = r / lat.L;
       double sr = 0.0;
       for (int i = 0; i < N; ++i) {
-        const int j = (i % lat.L + rx) % lat.L + lat.L * ((i / lat.L + ry) % lat.L);  // disp(i, j) = r
+        const int j = lat.shift(i, r);  // disp(i, j) = r
         sr += sign * 0.5 * (at(gu, N, j, i) + at(gd, N, j, i)) / N;
       }
       dyn_r[(size_t)slot * N + r] += sr;
@@ -1107,7 +1136,7 @@ struct Oracle {
   //   superfluid stiffness (345-416): 0.25 t^2 sign / N^2 sum_ij (cos kx rx - cos kx ry) (uncorrelated
   //     and correlated current terms), one contribution per tau (the reference sums them over all tau).
   void measure_dynamic_obs(int ntau) {
-    const double s = sign, invN = 1.0 / N, kx1 = lat.kx[1];
+    const double s = sign, invN = 1.0 / N, kx1 = lat.nk > 1 ? lat.kx[1] : 0.0;
     const Vec& g00u = G[0];
     const Vec& g00d = G[1];
     for (int k = 0; k < ntau; ++k) {
@@ -1129,6 +1158,9 @@ struct Oracle {
                 at(g0td, N, i, i) * at(gt0d, N, i, i) - gcttu * gc00d - gc00u * gcttd);
       }
       dyn_chi[k] += chi;
+      // the superfluid stiffness is a square-lattice observable (dqmc_initializer.cpp:233-237
+      // drops it elsewhere; measure_methods.cpp:350 asserts the square lattice)
+      if (lat.dim != 2) continue;
       double rho = 0.0;
       for (int i = 0; i < N; ++i) {
         const int ipx = lat.nn[i * 4 + 0];
@@ -1228,8 +1260,8 @@ struct Oracle {
         tr += a + b;
         dbl += (1 - a) * (1 - b);
         loc += sg * (a + b - 2 * a * b);
-        for (int dir = 0; dir < 2; ++dir) {
-          const int j = lat.nn[i * 4 + dir];
+        for (int dir = 0; dir < lat.dim; ++dir) {  // +x, +y (, +z): measure_methods.cpp:87-95
+          const int j = lat.nn[i * 2 * lat.dim + dir];
           kin += at(gu, N, i, j) + at(gd, N, i, j);
         }
       }
@@ -1284,7 +1316,12 @@ void orc_set_lapack(orc_dgemm_t gemm_fn, orc_dgesvd_t gesvd_fn) {
 
 void* orc_create(const orc_params* p) {
   auto* o = new Oracle();
-  o->setup(*p);
+  try {
+    o->setup(*p);
+  } catch (const std::exception&) {
+    delete o;
+    return nullptr;
+  }
   return o;
 }
 void orc_destroy(void* h) { delete O(h); }
@@ -1410,5 +1447,14 @@ void orc_greens_from_udv(int n, const double* u, const double* d, const double* 
 int orc_num_k_stars(void* h) { return O(h)->lat.nk; }
 int orc_m_point_index(void* h) { return O(h)->lat.m_point; }
 double orc_fourier_factor(void* h, int disp, int k) { return O(h)->lat.fourier(disp, k); }
+int orc_space_dim(void* h) { return O(h)->lat.dim; }
+int orc_nearest_neighbour(void* h, int i, int dir) { return O(h)->lat.nn[(size_t)i * 2 * O(h)->lat.dim + dir]; }
+int orc_displacement(void* h, int i, int j) { return O(h)->lat.disp(i, j); }
+void orc_k_star(void* h, int k, double* out) {
+  const Lattice& l = O(h)->lat;
+  out[0] = l.kx[k];
+  out[1] = l.ky[k];
+  if (l.dim == 3) out[2] = l.kz[k];
+}
 
 }  // extern "C"

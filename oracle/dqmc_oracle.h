@@ -23,6 +23,7 @@ extern "C" {
 
 enum { ORC_REPULSIVE = 0, ORC_ATTRACTIVE = 1 };
 enum { ORC_STACK_SVD = 0, ORC_STACK_QRP = 1 };
+enum { ORC_SQUARE = 0, ORC_CUBIC = 1 };
 
 /* Observable slots (equal-time); order fixed for the C interface. */
 enum {
@@ -40,17 +41,19 @@ enum {
 
 typedef struct orc_params {
   int model;          /* ORC_REPULSIVE / ORC_ATTRACTIVE */
-  int L;              /* square lattice side, N = L*L */
+  int L;              /* lattice side, N = L*L (square) or L*L*L (cubic) */
   double hopping_t;
   double onsite_u;    /* |U| (attractive takes |U|, reference asserts U >= 0) */
   double mu;
   double beta;
   int Lt;             /* time slices, dtau = beta / Lt */
   int pace;           /* stabilization pace */
-  int checkerboard;   /* 0 dense exp(-dtau K), 1 checkerboard break-up */
+  int checkerboard;   /* 0 dense exp(-dtau K), 1 checkerboard break-up (square lattice only) */
   int stack_kind;     /* ORC_STACK_SVD (reference) / ORC_STACK_QRP (device algorithm) */
-  int momentum_index; /* k-star index for SDW/CDW/n(k); -1 -> M point */
+  int momentum_index; /* k-star index for SDW/CDW/n(k); -1 -> the last k star, (pi, ..., pi):
+                         the M point of the square lattice, the R point of the cubic one */
   int record_greens;  /* 1: keep the Lt-slice G series and measure from it */
+  int lattice;        /* ORC_SQUARE (src/lattice/square.cpp) / ORC_CUBIC (src/lattice/cubic.cpp) */
 } orc_params;
 
 /* BLAS/LAPACK hooks (Fortran calling convention).  When unset the oracle
@@ -64,6 +67,7 @@ typedef void (*orc_dgesvd_t)(const char*, const char*, const int*, const int*, d
                              int*);
 void orc_set_lapack(orc_dgemm_t gemm, orc_dgesvd_t gesvd);
 
+/* NULL when the parameters are rejected (checkerboard on the cubic lattice, L < 1, ...). */
 void* orc_create(const orc_params* p);
 void orc_destroy(void* h);
 int orc_space_size(void* h);
@@ -134,10 +138,14 @@ void orc_svd(int n, const double* a, double* u, double* s, double* v);
 void orc_qrp_udt(int n, const double* a, double* u, double* d, double* t);
 void orc_greens_from_udv(int n, const double* u, const double* d, const double* f, double* g);
 
-/* Lattice tables (src/lattice/square.cpp). */
+/* Lattice tables (src/lattice/square.cpp, src/lattice/cubic.cpp). */
 int orc_num_k_stars(void* h);
-int orc_m_point_index(void* h);
+int orc_m_point_index(void* h);                     /* the last k star, (pi, ..., pi) */
 double orc_fourier_factor(void* h, int disp, int k);
+int orc_space_dim(void* h);
+int orc_nearest_neighbour(void* h, int i, int dir); /* dir < 2 dim: +x, +y (, +z), -x, -y (, -z) */
+int orc_displacement(void* h, int i, int j);        /* index of the displacement from site i to j */
+void orc_k_star(void* h, int k, double* out);       /* momentum of k star k, SpaceDim components */
 
 #ifdef __cplusplus
 }

@@ -23,6 +23,7 @@ SOURCES = [os.path.join(HERE, "dqmc_oracle.cpp")]
 
 REPULSIVE, ATTRACTIVE = 0, 1
 STACK_SVD, STACK_QRP = 0, 1
+SQUARE, CUBIC = 0, 1
 OBS_NAMES = [
     "filling_number", "double_occupancy", "kinetic_energy", "momentum_distribution",
     "local_spin_corr", "spin_density_structure_factor", "charge_density_structure_factor",
@@ -49,7 +50,7 @@ class Params(ctypes.Structure):
         ("onsite_u", ctypes.c_double), ("mu", ctypes.c_double), ("beta", ctypes.c_double),
         ("Lt", ctypes.c_int), ("pace", ctypes.c_int), ("checkerboard", ctypes.c_int),
         ("stack_kind", ctypes.c_int), ("momentum_index", ctypes.c_int),
-        ("record_greens", ctypes.c_int),
+        ("record_greens", ctypes.c_int), ("lattice", ctypes.c_int),
     ]
 
 
@@ -105,6 +106,10 @@ def lib() -> ctypes.CDLL:
         "orc_greens_from_udv": (None, [ctypes.c_int, dp, dp, dp, dp]),
         "orc_num_k_stars": (ctypes.c_int, [vp]), "orc_m_point_index": (ctypes.c_int, [vp]),
         "orc_fourier_factor": (ctypes.c_double, [vp, ctypes.c_int, ctypes.c_int]),
+        "orc_space_dim": (ctypes.c_int, [vp]),
+        "orc_nearest_neighbour": (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_int]),
+        "orc_displacement": (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_int]),
+        "orc_k_star": (None, [vp, ctypes.c_int, dp]),
         "orc_set_lapack": (None, [vp, vp]),
     }
     for name, (res, args) in sig.items():
@@ -142,11 +147,13 @@ class Walker:
     """One reference walker (model + lattice + DqmcWalker + equal-time measure)."""
 
     def __init__(self, model=REPULSIVE, L=4, t=1.0, U=4.0, mu=0.0, beta=4.0, Lt=80, pace=10,
-                 checkerboard=False, stack=STACK_SVD, momentum_index=-1, record=True):
+                 checkerboard=False, stack=STACK_SVD, momentum_index=-1, record=True, lattice=SQUARE):
         self.p = Params(model, L, t, abs(U), mu, beta, Lt, pace, int(checkerboard), stack,
-                        momentum_index, int(record))
+                        momentum_index, int(record), lattice)
         self.h = lib().orc_create(ctypes.byref(self.p))
-        self.N = L * L
+        if not self.h:
+            raise ValueError("oracle: parameters rejected (lattice type, side, or checkerboard off the square lattice)")
+        self.N = L ** (3 if lattice == CUBIC else 2)
         self.Lt = Lt
         self._u = None
 
@@ -315,6 +322,27 @@ class Walker:
 
     def fourier(self, disp: int, k: int) -> float:
         return lib().orc_fourier_factor(self.h, disp, k)
+
+    def space_dim(self) -> int:
+        return lib().orc_space_dim(self.h)
+
+    def nearest_neighbour(self, i: int, direction: int) -> int:
+        """LatticeBase::NearestNeighbour: direction < 2 dim, +x, +y (, +z), -x, -y (, -z)."""
+        if not 0 <= direction < 2 * self.space_dim() or not 0 <= i < self.N:
+            raise IndexError("site or direction out of range")
+        return lib().orc_nearest_neighbour(self.h, i, direction)
+
+    def displacement(self, i: int, j: int) -> int:
+        if not (0 <= i < self.N and 0 <= j < self.N):
+            raise IndexError("site out of range")
+        return lib().orc_displacement(self.h, i, j)
+
+    def k_star(self, k: int) -> np.ndarray:
+        if not 0 <= k < self.num_k_stars():
+            raise IndexError("k star out of range")
+        out = np.zeros(3)
+        lib().orc_k_star(self.h, k, _dp(out))
+        return out[: self.space_dim()]
 
 
 def svd(a):

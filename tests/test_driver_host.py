@@ -156,3 +156,13 @@ def test_dynamic_run(fake, tmp_path):
     assert res["superfluid_stiffness"][0] == pytest.approx(0.06)  # 6 tau x 0.01
     assert res["dynamic_sign"][0] == pytest.approx(0.5)
     assert open(tmp_path / "greens.bins.out").read().splitlines()[0] == dio._d(6) + dio._d(3) + dio._d(6)
+
+
+def test_cubic_configuration_is_refused_before_any_device_work(fake, tmp_path):
+    """The cubic lattice parses (its tables live in dqmc_gb300.io and the oracle) but the
+    device sweep is built for the square lattice: the driver refuses it loudly."""
+    cfg = dio.parse_config('[Lattice]\ntype = "Cubic"\ncell = [4, 4, 4]\nmomentum = "RPoint"\n'
+                           '[Measure]\nobservables = ["filling_number"]\n')
+    with pytest.raises(NotImplementedError):
+        drv.run(cfg, str(tmp_path), walkers=1, log=open(os.devnull, "w"))
+    assert not fake.created

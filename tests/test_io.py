@@ -138,3 +138,88 @@ def test_parse_config_keys_defaults_and_keywords():
 def test_parse_config_rejects_what_the_reference_rejects(bad):
     with pytest.raises(ValueError):
         dio.parse_config(bad)
+
+
+CUBIC = """
+[Model]
+    type = "RepulsiveHubbard"
+[Lattice]
+    type = "Cubic"
+    cell = [4, 4, 4]
+    momentum = "RPoint"
+    momentum_list = "LambdaLine"
+[Measure]
+    observables = [ "all" ]
+"""
+
+
+def test_parse_cubic_config():
+    """Cubic tables of DqmcInitializer::parse_toml_config (dqmc_initializer.cpp:118-150,
+    233-237, 293-327): three equal sides, R point, cubic lines, no superfluid stiffness."""
+    c = dio.parse_config(CUBIC)
+    assert (c.lattice, c.cell, c.L, c.dim) == ("Cubic", (4, 4, 4), 4, 3)
+    assert "superfluid_stiffness" not in c.observables
+    assert c.observables == [o for o in dio.ALL_OBSERVABLES if o != "superfluid_stiffness"]
+    assert dio.momentum_index(4, c.momentum, 3) == len(dio.kstars(4, 3)) - 1
+    with pytest.raises(ValueError):
+        dio.momentum_index(4, "RPoint")  # not a square-lattice point
+    with pytest.raises(ValueError):
+        dio.momentum_list_indices(4, "Gamma2X2M2GammaLoop", 3)  # not a cubic-lattice list
+
+
+@pytest.mark.parametrize("bad", [
+    '[Lattice]\ntype = "Cubic"\ncell = [4, 4]\n[Measure]\nobservables = ["all"]\n',
+    '[Lattice]\ntype = "Cubic"\ncell = [4, 4, 3]\n[Measure]\nobservables = ["all"]\n',
+    '[Lattice]\ntype = "Cubic"\ncell = [4, 4, 4]\n[CheckerBoard]\nwhether_or_not = true\n[Measure]\nobservables = ["all"]\n',
+    '[Lattice]\ntype = "Square"\ncell = [4, 4, 4]\n[Measure]\nobservables = ["all"]\n',
+])
+def test_parse_cubic_rejects_what_the_reference_rejects(bad):
+    with pytest.raises(ValueError):
+        dio.parse_config(bad)
+
+
+@pytest.mark.parametrize("L", [2, 3, 4, 5, 6, 7, 8])
+def test_cubic_kstars_points_and_lines(L):
+    """Cubic::initial_index2momentum_table and initial_symmetry_points (cubic.cpp:47-183):
+    the count's closed form, the points X, M, R and the six lines lying where they should."""
+    ks = np.array(dio.kstars(L, 3))
+    h = L // 2 + 1
+    assert len(ks) == round(h * (h + 1) * (2 * h + 1) / 12 + h * (h + 1) / 4)
+    pi = np.pi
+    first = ks[0, 0]  # 0 for even L; the reference's grid is offset by pi for odd L
+    pts = {n: ks[dio.momentum_index(L, n, 3)] for n in ("GammaPoint", "XPoint", "MPoint", "RPoint")}
+    np.testing.assert_allclose(pts["GammaPoint"], [first] * 3, atol=1e-12)
+    np.testing.assert_allclose(pts["XPoint"], [pi, first, first], atol=1e-12)
+    np.testing.assert_allclose(pts["MPoint"], [pi, pi, first], atol=1e-12)
+    np.testing.assert_allclose(pts["RPoint"], [pi, pi, pi], atol=1e-12)
+    line = lambda n: ks[dio.momentum_list_indices(L, n, 3)]
+    d, z, s = line("DeltaLine"), line("ZLine"), line("SigmaLine")
+    lam, sl, tl = line("LambdaLine"), line("SLine"), line("TLine")
+    for pts_, fixed in ((d, [1, 2]), (z, [2]), (s, [2]), (sl, []), (tl, [])):
+        for a in fixed:
+            np.testing.assert_allclose(pts_[:, a], first, atol=1e-12)
+    np.testing.assert_allclose(d[:, 0], np.sort(d[:, 0]))                       # Gamma -> X
+    np.testing.assert_allclose(z[:, 0], pi, atol=1e-12)                         # X -> M
+    np.testing.assert_allclose(s[:, 0], s[:, 1])                                # Gamma -> M
+    np.testing.assert_allclose(lam[:, 0], lam[:, 1]); np.testing.assert_allclose(lam[:, 1], lam[:, 2])  # Gamma -> R
+    np.testing.assert_allclose(sl[:, 0], pi, atol=1e-12); np.testing.assert_allclose(sl[:, 1], sl[:, 2])  # X -> R
+    np.testing.assert_allclose(tl[:, :2], pi, atol=1e-12)                       # M -> R
+    for seq in (d[:, 0], z[:, 1], s[:, 0], lam[:, 0], sl[:, 1], tl[:, 2]):
+        assert len(seq) == L // 2 + 1 and (np.diff(seq) > 0).all()
+
+
+def test_cubic_kstars_file_layout():
+    """DqmcIO::output_k_stars writes SpaceDim components per k star."""
+    text = dio.format_kstars(4, 3)
+    lines = text.splitlines()
+    assert int(lines[0]) == len(dio.kstars(4, 3)) == 10
+    assert all(len(l) == 80 for l in lines[1:])  # index + kx + ky + kz, 20 columns each
+    assert dio.format_kstars(4) == dio.format_kstars(4, 2)
+
+
+def test_cubic_kstars_agree_with_the_oracle(oracle_mod):
+    w = oracle_mod.Walker(L=5, Lt=4, pace=2, lattice=oracle_mod.CUBIC)
+    ks = dio.kstars(5, 3)
+    assert len(ks) == w.num_k_stars()
+    for k, v in enumerate(ks):
+        np.testing.assert_array_equal(w.k_star(k), v)
