@@ -431,8 +431,7 @@ int dqmc_batch_create(const dqmc_walker_desc* descs, int n, const dqmc_batch_opt
   if (e == cudaSuccess) e = configure_submatrix_kernel();
   if (e == cudaSuccess) e = configure_stab_oz_kernels(kMaxOzN);
   if (e != cudaSuccess) {
-    cudaFree(b->arena);
-    delete b;
+    dqmc_batch_destroy(b);  // frees the arena and the stream, if it was created
     return fail(DQMC_ERR_CUDA, "stream/kernel set-up: %s", cudaGetErrorString(e));
   }
   b->stream = b->own;
@@ -460,7 +459,13 @@ int dqmc_batch_create(const dqmc_walker_desc* descs, int n, const dqmc_batch_opt
   b->dW = reinterpret_cast<WalkerDev*>(base + desc_off);
   if (o.rng == DQMC_RNG_MINSTD) {
     b->d_uni = reinterpret_cast<double*>(base + uni_off);
-    cudaMallocHost(&b->h_uni, sizeof(double) * b->uni_stride * n);
+    e = cudaMallocHost(&b->h_uni, sizeof(double) * b->uni_stride * n);
+    if (e != cudaSuccess) {
+      b->h_uni = nullptr;
+      dqmc_batch_destroy(b);
+      return fail(DQMC_ERR_CUDA, "cudaMallocHost(%zu bytes): %s", sizeof(double) * b->uni_stride * n,
+                  cudaGetErrorString(e));
+    }
   }
   // upload dense matrices and Fourier tables
   for (size_t i = 0; i < dense.size(); ++i) {
