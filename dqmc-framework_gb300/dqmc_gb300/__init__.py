@@ -174,12 +174,21 @@ class Batch:
         """Model::set_bosonic_fields_to_random with the walker's own engine."""
         _check(load().dqmc_fields_random(self.h, w))
 
+    def _walker(self, w: int) -> "WalkerDesc":
+        if not 0 <= w < len(self.walkers):
+            raise IndexError(f"walker {w} outside the batch of {len(self.walkers)}")
+        return self.walkers[w]
+
     def set_fields(self, w: int, fields):
+        """Walker w's fields, [Lt][N] of +1/-1 (the library reads exactly Lt * N bytes)."""
+        d = self._walker(w)
         f = np.ascontiguousarray(fields, dtype=np.int8)
+        if f.size != d.Lt * d.N:
+            raise ValueError(f"fields of walker {w}: {f.size} values, expected Lt * N = {d.Lt * d.N}")
         _check(load().dqmc_set_fields(self.h, w, f.ctypes.data_as(ctypes.POINTER(ctypes.c_int8))))
 
     def fields(self, w: int) -> np.ndarray:
-        d = self.walkers[w]
+        d = self._walker(w)
         f = np.zeros((d.Lt, d.N), dtype=np.int8)
         _check(load().dqmc_get_fields(self.h, w, f.ctypes.data_as(ctypes.POINTER(ctypes.c_int8))))
         return f
@@ -197,14 +206,17 @@ class Batch:
 
     # --- accessors -------------------------------------------------------------
     def green(self, w: int, spin: int) -> np.ndarray:
-        N = self.walkers[w].N
+        N = self._walker(w).N
         g = np.zeros((N, N), order="F")
         _check(load().dqmc_get_green(self.h, w, spin, g.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
         return g
 
     def set_green(self, w: int, spin: int, g):
         """Overwrite walker w's equal-time G of one spin (restart and test hook)."""
+        N = self._walker(w).N
         g = np.asfortranarray(g, dtype=np.float64)
+        if g.shape != (N, N):
+            raise ValueError(f"G of walker {w}: shape {g.shape}, expected ({N}, {N})")
         _check(load().dqmc_set_green(self.h, w, spin, g.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
 
     def config_sign(self, w: int) -> float:
@@ -255,7 +267,7 @@ class Batch:
     def trace(self, w: int) -> np.ndarray:
         n = ctypes.c_int()
         _check(load().dqmc_trace_count(self.h, ctypes.byref(n)))
-        N = self.walkers[w].N
+        N = self._walker(w).N
         out = np.zeros((n.value, 2, N, N))
         for k in range(n.value):
             for s in range(2):
@@ -305,14 +317,14 @@ class Batch:
     def dynamic_r(self, w: int) -> np.ndarray:
         """[tau][r] sums of sign * 0.5 sum_i (G_up + G_dn)(i + r, i) / N per displacement r."""
         n = len(getattr(self, "_taus", []))
-        out = np.zeros((max(n, 1), self.walkers[w].N))
+        out = np.zeros((max(n, 1), self._walker(w).N))
         _check(load().dqmc_get_dynamic_r(self.h, w, out.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
         return out[:n]
 
     def dynamic_greens_k(self, w: int, momenta) -> np.ndarray:
         """G(k,tau) sums [k][tau] for the momenta (kx, ky) (measure_greens_functions):
         sum_r cos(-(rx kx + ry ky)) S(r)."""
-        L = self.walkers[w].L
+        L = self._walker(w).L
         r = np.arange(L * L)
         rx, ry = r % L, r // L
         ff = np.array([np.cos(-(rx * kx + ry * ky)) for kx, ky in momenta])  # [k][r]
@@ -323,7 +335,7 @@ class Batch:
 
     def green_dynamic(self, w: int, which: int, spin: int) -> np.ndarray:
         """G(beta, 0) (which 0) or G(0, beta) (which 1) after the last dynamic half-sweep."""
-        N = self.walkers[w].N
+        N = self._walker(w).N
         g = np.zeros((N, N), order="F")
         _check(load().dqmc_get_green_dynamic(self.h, w, which, spin, g.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
         return g

@@ -10,6 +10,7 @@
 // failures throw dqmc_gb300::Error instead of calling exit(1).
 #pragma once
 
+#include <algorithm>
 #include <cmath>
 #include <stdexcept>
 #include <string>
@@ -124,42 +125,56 @@ class DqmcWalker {
     N_ = lat.SpaceSize();
   }
   void set_bosonic_fields_to_random() { for (int w = 0; w < n_; ++w) check(dqmc_fields_random(b_, w)); }
-  void set_bosonic_fields(int w, const std::vector<int8_t>& f) { check(dqmc_set_fields(b_, w, f.data())); }
+  // fields of walker w, [Lt][N] of +1/-1: the library reads exactly Lt * N bytes
+  void set_bosonic_fields(int w, const std::vector<int8_t>& f) {
+    if (f.size() != (size_t)lt_ * N_) throw Error(DQMC_ERR_ARG, "set_bosonic_fields: expected Lt * N values");
+    check(dqmc_set_fields(b_, w, f.data()));
+  }
   void initial_greens_functions() { check(dqmc_init_greens(b_)); }  // stacks + G(0) + sign
   void sweep_from_0_to_beta(bool measure = false) { check(dqmc_sweep_0_to_beta(b_, measure)); }
   void sweep_from_beta_to_0(bool measure = false) { check(dqmc_sweep_beta_to_0(b_, measure)); }
-  // sweep_for_dynamic_greens (include/dqmc_walker.h:131) + G(k,tau) at the listed tau
+  // sweep_for_dynamic_greens (include/dqmc_walker.h:131) + G(k,tau) at the listed tau; the
+  // accessors below return one entry per tau of the last list
   void sweep_for_dynamic_greens(const std::vector<int>& taus) {
     check(dqmc_sweep_dynamic(b_, taus.data(), (int)taus.size()));
+    ntau_ = (int)taus.size();
   }
   // G(k,tau) accumulators of walker w in the order of the last tau list
-  std::vector<double> DynamicGreens(int w, std::vector<int64_t>* counts = nullptr, int ntau = 0) const {
-    std::vector<double> s(ntau);
-    std::vector<int64_t> c(ntau);
+  std::vector<double> DynamicGreens(int w, std::vector<int64_t>* counts = nullptr) const {
+    std::vector<double> s(std::max(ntau_, 1));
+    std::vector<int64_t> c(std::max(ntau_, 1));
     check(dqmc_get_dynamic(b_, w, s.data(), c.data()));
+    s.resize(ntau_);
+    c.resize(ntau_);
     if (counts) *counts = c;
     return s;
   }
   // per-displacement sums [tau][r] of the time-displaced Green's function: G(k,tau) of
   // measure_greens_functions for any momentum list is sum_r FourierFactor(r, k) S[tau][r]
-  std::vector<double> DynamicGreensR(int w, int ntau) const {
-    std::vector<double> s((size_t)ntau * N_);
+  std::vector<double> DynamicGreensR(int w) const {
+    std::vector<double> s((size_t)std::max(ntau_, 1) * N_);
     check(dqmc_get_dynamic_r(b_, w, s.data()));
+    s.resize((size_t)ntau_ * N_);
     return s;
   }
   // Dqmc::measure with the bins normalised on the device: [walker][bin][9]
   std::vector<double> MeasureBins(int nbins, int bin_size, int sweeps_between) {
-    std::vector<double> out((size_t)n_ * nbins * 9);
+    std::vector<double> out((size_t)n_ * std::max(nbins, 1) * DQMC_NUM_OBS);
     check(dqmc_measure_bins(b_, nbins, bin_size, sweeps_between, out.data()));
+    out.resize((size_t)n_ * std::max(nbins, 0) * DQMC_NUM_OBS);
     return out;
   }
   // measure_density_of_states, measure_dynamic_spin_susceptibility and the per-tau terms of
   // measure_superfluid_stiffness (src/measure/measure_methods.cpp:315-461), sums per listed tau
   struct DynamicObservables { std::vector<double> density_of_states, spin_susceptibility, stiffness_terms; };
-  DynamicObservables DynamicObs(int w, int ntau) const {
-    DynamicObservables o{std::vector<double>(ntau), std::vector<double>(ntau), std::vector<double>(ntau)};
+  DynamicObservables DynamicObs(int w) const {
+    const size_t n = std::max(ntau_, 1);
+    DynamicObservables o{std::vector<double>(n), std::vector<double>(n), std::vector<double>(n)};
     check(dqmc_get_dynamic_obs(b_, w, o.density_of_states.data(), o.spin_susceptibility.data(),
                                o.stiffness_terms.data()));
+    o.density_of_states.resize(ntau_);
+    o.spin_susceptibility.resize(ntau_);
+    o.stiffness_terms.resize(ntau_);
     return o;
   }
   std::vector<double> Greent0Up(int w) const { return green_dyn(w, 0, 0); }  // G(beta,0) after the last dynamic half-sweep
@@ -189,6 +204,7 @@ class DqmcWalker {
   }
   dqmc_batch* b_ = nullptr;
   int n_ = 0, N_ = 0, lt_ = 80, pace_ = 10;
+  int ntau_ = 0;  // length of the last dynamic tau list
   double beta_ = 4.0;
 };
 

@@ -73,3 +73,21 @@ def test_no_cpu_fallback_without_gpu(dq):
     with pytest.raises(dq.DqmcError) as e:
         dq.Batch([dq.WalkerDesc()])
     assert "status 2" in str(e.value)
+
+
+def test_python_setters_check_sizes_before_the_library_reads(dq):
+    """set_fields / set_green hand a raw pointer to the library, which reads Lt * N bytes or
+    N * N doubles: the binding refuses arrays of another size and walkers outside the batch."""
+    import numpy as np
+
+    b = dq.Batch.__new__(dq.Batch)  # no device: only the host-side checks run
+    b.h = None
+    b.walkers = [dq.WalkerDesc(L=4, Lt=8)]
+    with pytest.raises(ValueError):
+        b.set_fields(0, np.ones((8, 15), dtype=np.int8))
+    with pytest.raises(ValueError):
+        b.set_green(0, 0, np.eye(15))
+    with pytest.raises(IndexError):
+        b.set_fields(1, np.ones((8, 16), dtype=np.int8))
+    with pytest.raises(IndexError):
+        b.green(-1, 0)
