@@ -64,6 +64,49 @@ DEFAULT_WORKLOAD = "mixed_batch_16x16_attractive"
 METRIC = "HS-field updates/s (walkers*N*Lt / half-sweep time)"
 
 
+# DRAM traffic per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the dominant
+# kernel of a class on the tensor-core path, from one ncu --set full capture each of an
+# 8-walker launch of the 16x16, beta = 10 configuration.  ncu replays a kernel with L2
+# flushed, and each walker's G, chain and slices are its own, so this cold-cache traffic
+# grows in proportion to the walkers a launch covers.
+NCU_TRAFFIC_8_WALKERS = {
+    "metropolis": ("metropolis_sub_kernel", 4436480 + 256),
+    "product": ("oz_prod_tc_kernel<3,7>", 8307200 + 0),
+}
+
+
+def ncu_traffic(workload: dict, cls: str, walkers_per_launch: int):
+    """(bytes per launch, kernel, how it was obtained) of a class's dominant kernel, scaled
+    from the 8-walker capture, or (None, None, reason) where no capture covers the class."""
+    if workload.get("precision") != "mixed" or workload["L"] != 16 or cls not in NCU_TRAFFIC_8_WALKERS:
+        return None, None, "no ncu capture of this class for this workload"
+    kern, b8 = NCU_TRAFFIC_8_WALKERS[cls]
+    return b8 * walkers_per_launch / 8, kern, (
+        f"ncu --set full capture of {kern} on an 8-walker launch (L2 flushed), scaled to the "
+        f"{walkers_per_launch} walkers of one profiled launch")
+
+
+L2_BYTES = 129 * 2 ** 20
+
+
+def working_set_bytes(wl: dict) -> int:
+    """Device bytes one timed step touches per GPU, a lower bound: each walker's G (both
+    spins), B-chain and the two UDT stacks (U, F and D per level and spin)."""
+    N, S = wl["L"] ** 2, (1 if wl["model"] == 1 else 2)
+    ns = -(-wl["Lt"] // wl["pace"])
+    per = 8 * (2 * N * N + S * N * N + 2 * S * ns * (2 * N * N + N))
+    return wl["walkers"] * per
+
+
+def l2_note(wl: dict) -> str:
+    ws = working_set_bytes(wl)
+    if ws > L2_BYTES:
+        return (f"no flush: the per-GPU working set (G, chains, UDT stacks, >= {ws / 2 ** 30:.2f} GiB) "
+                f"is larger than the 129 MB L2")
+    return (f"no flush, working set {ws / 2 ** 20:.1f} MiB fits in L2: a latency case, "
+            f"not a bandwidth measurement")
+
+
 def _descs(dq, wl, seed0=1000):
     return [dq.WalkerDesc(model=wl["model"], L=wl["L"], U=wl["U"], mu=wl["mu"], beta=wl["beta"], Lt=wl["Lt"],
                           pace=wl["pace"], checkerboard=wl["checkerboard"], seed=seed0 + w)
@@ -377,8 +420,11 @@ def run_gpu(args, wl, rank, world):
     bound, flops, peak, what = model[dom]
     dom_ms, dom_n = prof[dom]
     achieved = flops / (dom_ms * 1e-3) / 1e12
+    # the profiled replay runs one branch, so each of its launches covers every walker
+    traffic, traffic_kernel, traffic_src = ncu_traffic(wl, dom, len(descs))
     roofline = {"bound": bound, "kernel": f"{dom} kernel class", "achieved": achieved, "peak": peak,
-                "unit": "TFLOP/s", "frac": achieved / peak, "traffic": None,
+                "unit": "TFLOP/s", "frac": achieved / peak, "traffic": traffic,
+                "traffic_kernel": traffic_kernel, "traffic_source": traffic_src,
                 "peak_source": bf16_src if bound == "tensor" else fp64_src, "counted": what,
                 "avg_launch_ms": dom_ms / max(dom_n, 1),
                 "kernel_share": {k: prof[k][0] / prof_total for k in prof if prof[k][1] > 0},
@@ -441,7 +487,7 @@ def main():
               "pace": wl["pace"], "expK": "checkerboard" if wl["checkerboard"] else "dense",
               "precision": wl.get("precision", "fp64"),
               "measure": "equal-time, fused", "parallelism": f"replicas x{args.gpus}",
-              "l2": "no flush: per-GPU working set (G, chains, UDT stacks) > 1 GB, larger than L2"}
+              "l2": l2_note(wl)}
 
     if args.impl == "reference":
         if rank != 0:

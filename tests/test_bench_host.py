@@ -1,0 +1,85 @@
+"""bench.py's host logic, without a GPU: the flop model of the roofline (the per-walker
+work of a half-sweep, dqmc_walker.cpp:246-412 counted as the reference executes it), the
+ncu traffic attached to the dominant class, and the reference arm's JSON line (the CPU
+restatement of the reference, timed on this machine's cores for a few seconds)."""
+import json
+import os
+import subprocess
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="module")
+def bench():
+    sys.path.insert(0, ROOT)
+    import bench as b
+
+    return b
+
+
+def test_flop_model_counts_the_reference_work(bench):
+    wl = dict(bench.WORKLOADS["fp64_single_4x4_dense"])  # N = 16, Lt = 80, pace 10, repulsive
+    N, Lt, S = 16, 80, 2
+    A = 300.0  # accepted flips per half-sweep
+    fm = bench.flops_model(wl, A)
+    W, C = 4 * N ** 3 + 2 * N * N, 2 * N ** 3 + N * N  # dense wrap and B-chain step
+    assert fm["segment"] == S * Lt * (W + C) + S * A * 2 * N * N
+    ns = Lt // 10
+    assert fm["push"] == pytest.approx(S * ns * (8 / 3 + 1) * N ** 3)
+    assert fm["nominal_F"] == S * Lt * (W + C) + S * A * 2 * N * N + S * ns * 33 * N ** 3
+    cb = bench.flops_model(dict(bench.WORKLOADS["fp64_batch_8x8_checkerboard"]), 0.0)
+    assert cb["segment"] == 2 * 160 * (34 + 17) * 64 * 64  # checkerboard passes, no flips
+
+
+def test_blocked_qr_products_flops(bench):
+    """Each panel of the blocked QR costs its trailing update and the Q formation; the counts
+    grow like N^3 and exceed the plain 2N^3 products they include."""
+    p1, g1 = bench.stab_tensor_flops(128)
+    p2, g2 = bench.stab_tensor_flops(256)
+    assert p1 > 2 * 128 ** 3 and g1 > 6 * 128 ** 3
+    assert 6 < p2 / p1 < 10 and 6 < g2 / g1 < 10
+
+
+def test_traffic_of_the_dominant_class(bench):
+    wl = dict(bench.WORKLOADS["mixed_batch_16x16_attractive"])
+    t, kern, src = bench.ncu_traffic(wl, "metropolis", 128)
+    assert kern == "metropolis_sub_kernel" and t == (4436480 + 256) * 16
+    assert "8-walker" in src and "128 walkers" in src
+    assert bench.ncu_traffic(wl, "product", 8)[0] == 8307200
+    for w, cls in ((bench.WORKLOADS["fp64_batch_8x8_checkerboard"], "segment"), (wl, "greens")):
+        t, kern, src = bench.ncu_traffic(dict(w), cls, 64)
+        assert t is None and kern is None and src
+
+
+@pytest.mark.timeout(600)
+def test_reference_arm_prints_the_contract_line():
+    """--impl reference: one JSON line with impl, cpu_baseline (kind, cores, sample, value equal
+    to the line's) and e2e with zero copies, on the metric and unit of the GPU arm."""
+    env = dict(os.environ, CUDA_VISIBLE_DEVICES="")
+    out = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference",
+                          "--workload", "fp64_single_4x4_dense", "--steps", "1", "--warmup", "0",
+                          "--cpu-budget", "2"], capture_output=True, text=True, timeout=600, env=env, cwd=ROOT)
+    assert out.returncode == 0, out.stderr[-2000:]
+    lines = [l for l in out.stdout.splitlines() if l.startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference" and d["unit"] == "updates/s" and d["higher_is_better"] is True
+    assert d["metric"].startswith("HS-field updates/s")
+    cb = d["cpu_baseline"]
+    assert cb["value"] == d["value"] > 0 and cb["kind"] == "port" and cb["cores"] >= 1 and cb["sample"]
+    assert d["e2e"] == {"value": d["value"], "unit": "updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+    assert d["config"]["workload"] == "fp64_single_4x4_dense"
+
+
+def test_l2_note_follows_the_working_set(bench):
+    """The batches' working sets exceed L2 (no flush needed); the single 4x4 walker fits and
+    says so."""
+    big = bench.WORKLOADS["mixed_batch_16x16_attractive"]
+    # per walker: G 2N^2, chain N^2, stacks 2 x 13 levels x (2N^2 + N) doubles (N = 256, S = 1)
+    assert bench.working_set_bytes(big) == 128 * 8 * (2 * 65536 + 65536 + 2 * 13 * (2 * 65536 + 256))
+    assert bench.l2_note(big).startswith("no flush: the per-GPU working set")
+    assert bench.working_set_bytes(bench.WORKLOADS["fp64_batch_8x8_checkerboard"]) > bench.L2_BYTES
+    assert "fits in L2" in bench.l2_note(bench.WORKLOADS["fp64_single_4x4_dense"])
