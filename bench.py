@@ -21,8 +21,10 @@ Legs printed on one JSON line:
                host draws each walker's minstd_rand0 uniforms, copies them in
                (pinned -> HBM), runs the half-sweep and reads every walker's
                observable accumulators back, all inside the timed region
-  roofline     the dominant kernel class, timed with CUDA events in the timed
-               region, against the FP64 FMA rate measured on this device
+  roofline     the dominant kernel class: its algorithmic flops over its CUDA-event
+               time in profiled replays of the same half-sweeps, against the FP64
+               FMA rate measured on this device (FP64 classes) or the measured bf16
+               rate (tensor-core classes); DRAM traffic per launch from ncu
   cpu_baseline the CPU oracle (reference algorithm restated, scipy LAPACK),
                one walker per host core, on a bounded sample
 
