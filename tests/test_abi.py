@@ -91,3 +91,26 @@ def test_python_setters_check_sizes_before_the_library_reads(dq):
         b.set_fields(1, np.ones((8, 16), dtype=np.int8))
     with pytest.raises(IndexError):
         b.green(-1, 0)
+
+
+def test_header_is_plain_c_and_links(dq, tmp_path):
+    """include/dqmc_gb300.h is what an FFI binding (cgo, ctypes, JNI) includes: it must compile as
+    strict C99 and a C program must link against the library with it."""
+    import shutil
+    import subprocess
+
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    src = tmp_path / "abi.c"
+    src.write_text('#include "dqmc_gb300.h"\n'
+                   "int main(void) { dqmc_batch_options o = {0}; (void)o;\n"
+                   "  return dqmc_abi_version() == DQMC_ABI_VERSION ? 0 : 1; }\n")
+    inc = os.path.join(ROOT, "include")
+    libdir = os.path.dirname(dq.LIB_PATH)
+    subprocess.run([cc, "-std=c99", "-Wall", "-Wextra", "-pedantic", "-Werror", "-fsyntax-only", "-I", inc, str(src)],
+                   check=True)
+    exe = tmp_path / "abi"
+    subprocess.run([cc, "-std=c99", "-I", inc, str(src), "-L", libdir, "-ldqmc_gb300", "-Wl,-rpath," + libdir,
+                    "-o", str(exe)], check=True)
+    assert subprocess.run([str(exe)]).returncode == 0  # dqmc_abi_version needs no device
