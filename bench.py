@@ -254,6 +254,24 @@ def stab_tensor_flops(N, TB=32):
     return push, greens
 
 
+def observable_deviation(mixed, fp64, names, write_bin):
+    """Each equal-time observable of the mixed path against the FP64 path run on the same
+    fields and uniforms: |mean over walkers (mixed) - mean (FP64)| in units of the standard
+    error of the FP64 walkers' mean.  mixed, fp64: (sums, counts) per walker as
+    observables_all returns them; write_bin normalises one walker's bin."""
+    import numpy as np
+
+    vm = np.array([write_bin(s, c) for s, c in zip(*mixed)])
+    vf = np.array([write_bin(s, c) for s, c in zip(*fp64)])
+    n = len(vf)
+    out = {}
+    for k, name in enumerate(names):
+        d = float(abs(vm[:, k].mean() - vf[:, k].mean()))
+        se = float(vf[:, k].std(ddof=1) / np.sqrt(n)) if n > 1 else 0.0
+        out[name] = {"abs_diff": d, "fp64_stderr": se, "in_stderr": d / se if se > 0 else None}
+    return out
+
+
 def fp64_comparison(args, dq, wl, stream, sample=8):
     """The FP64 path on the same configuration (throughput), the plain
     single-walker FP64 path, and max |dG| of the mixed path against FP64 at
@@ -284,7 +302,7 @@ def fp64_comparison(args, dq, wl, stream, sample=8):
     single_value, single_ms = timed_rate(descs[:1], 1)
     # accuracy gate on a sample of walkers: identical decisions, |dG| at every stabilization
     sub = descs[:sample]
-    traces, fields = [], []
+    traces, fields, obs = [], [], []
     for prec in (dq.MIXED, dq.FP64):
         b = dq.Batch(sub, rng=dq.RNG_PHILOX, precision=prec, trace=True)
         for w in range(len(sub)):
@@ -293,14 +311,21 @@ def fp64_comparison(args, dq, wl, stream, sample=8):
         b.sweep_0_to_beta(measure=True)
         traces.append([b.trace(w) for w in range(len(sub))])
         fields.append([b.fields(w) for w in range(len(sub))])
+        obs.append(b.observables_all())
         b.close()
     same = [bool((fields[0][w] == fields[1][w]).all()) for w in range(len(sub))]
     dg = max(float(abs(traces[0][w] - traces[1][w]).max()) for w in range(len(sub)) if same[w]) if any(same) else None
+    try:
+        dev = observable_deviation(obs[0], obs[1], dq.OBS_NAMES, dq.write_bin)
+        worst = max((v["in_stderr"] for v in dev.values() if v["in_stderr"] is not None), default=None)
+    except Exception as e:  # the throughput line must not depend on this report
+        dev, worst = {"unavailable": f"{type(e).__name__}: {e}"}, None
     return {"fp64_batch_value": fp64_value, "fp64_batch_ms_per_step": fp64_ms,
             "fp64_single_walker_value": single_value, "fp64_single_walker_ms_per_step": single_ms,
             "max_abs_dG": dg, "dG_sample": f"{len(sub)} walkers, every stabilization of one 0->beta half-sweep, "
                                             f"same fields and Philox uniforms",
-            "walkers_with_identical_decisions": int(sum(same))}
+            "walkers_with_identical_decisions": int(sum(same)),
+            "observables_vs_fp64": dev, "max_observable_dev_in_stderr": worst}
 
 
 def run_gpu(args, wl, rank, world):

@@ -83,3 +83,28 @@ def test_l2_note_follows_the_working_set(bench):
     assert bench.l2_note(big).startswith("no flush: the per-GPU working set")
     assert bench.working_set_bytes(bench.WORKLOADS["fp64_batch_8x8_checkerboard"]) > bench.L2_BYTES
     assert "fits in L2" in bench.l2_note(bench.WORKLOADS["fp64_single_4x4_dense"])
+
+
+def test_observable_deviation_in_units_of_the_stderr(bench):
+    """Each observable's mixed-vs-FP64 difference of walker means over the FP64 standard
+    error; an observable with no spread (the sign of a sign-free model) reports None."""
+    import numpy as np
+
+    sys.path.insert(0, os.path.join(ROOT, "dqmc-framework_gb300"))
+    import dqmc_gb300 as dq
+
+    rng = np.random.default_rng(3)
+    n, k = 8, dq.NUM_OBS
+    counts = np.full((n, k), 100, dtype=np.int64)
+    sums_f = rng.normal(1.0, 0.1, (n, k)) * 100
+    sums_f[:, -1] = 100.0  # sign = +1 in every walker
+    sums_m = sums_f.copy()
+    sums_m[:, 2] += 100 * 1e-3  # shift the kinetic energy of every walker by 1e-3
+    dev = bench.observable_deviation((sums_m, counts), (sums_f, counts), dq.OBS_NAMES, dq.write_bin)
+    vf = sums_f[:, 2] / 100
+    se = vf.std(ddof=1) / np.sqrt(n)
+    assert dev["kinetic_energy"]["abs_diff"] == pytest.approx(1e-3)
+    assert dev["kinetic_energy"]["in_stderr"] == pytest.approx(1e-3 / se)
+    assert dev["filling_number"]["abs_diff"] == 0.0 and dev["filling_number"]["in_stderr"] == 0.0
+    assert dev["equaltime_sign"]["in_stderr"] is None
+    json.dumps(dev)
