@@ -114,3 +114,18 @@ def test_header_is_plain_c_and_links(dq, tmp_path):
     subprocess.run([cc, "-std=c99", "-I", inc, str(src), "-L", libdir, "-ldqmc_gb300", "-Wl,-rpath," + libdir,
                     "-o", str(exe)], check=True)
     assert subprocess.run([str(exe)]).returncode == 0  # dqmc_abi_version needs no device
+
+
+def test_cpp_driver_fails_loudly_without_a_device(dq):
+    """The C++ driver built over include/dqmc_gb300.hpp exits non-zero with the library's
+    message when no GPU is visible (no CPU fallback), and rejects unknown arguments."""
+    import subprocess
+
+    exe = os.path.join(os.path.dirname(dq.LIB_PATH), "dqmc_run")
+    if not os.path.exists(exe):
+        pytest.skip("driver not built")
+    env = dict(os.environ, CUDA_VISIBLE_DEVICES="")
+    r = subprocess.run([exe, "L=4", "walkers=2"], capture_output=True, text=True, env=env, timeout=120)
+    assert r.returncode != 0 and "no CUDA device" in (r.stdout + r.stderr)
+    r = subprocess.run([exe, "bogus=1"], capture_output=True, text=True, env=env, timeout=120)
+    assert r.returncode != 0 and "unknown argument" in (r.stdout + r.stderr)
