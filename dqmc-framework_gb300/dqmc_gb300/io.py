@@ -272,6 +272,88 @@ def format_summary_line(description: str, mean: float, err: float) -> str:
     return f"{description:>30s}{'->':>7s}{mean:20.12f}  pm  {err:.12f}\n"
 
 
+# the terminal descriptions (observable_handler.cpp:140-277) and the order in which
+# dqmc_main prints the scalar results (src/dqmc_main.cpp:213-266)
+DESCRIPTIONS = {
+    "equaltime_sign": "Averaged sign (equal-time)", "dynamic_sign": "Averaged sign (dynamical)",
+    "filling_number": "Filling number", "double_occupancy": "Double occupation", "kinetic_energy": "Kinetic energy",
+    "local_spin_corr": "Local spin correlation", "momentum_distribution": "Momentum distribution",
+    "spin_density_structure_factor": "SDW order parameter", "charge_density_structure_factor": "CDW order parameter",
+    "s_wave_pairing_corr": "S-wave pairing correlation", "superfluid_stiffness": "Superfluid stiffness",
+}
+SUMMARY_SIGNS = ["equaltime_sign", "dynamic_sign"]
+SUMMARY_ORDER = ["filling_number", "double_occupancy", "kinetic_energy", "local_spin_corr", "momentum_distribution",
+                 "spin_density_structure_factor", "charge_density_structure_factor", "s_wave_pairing_corr",
+                 "superfluid_stiffness"]
+
+
+def format_summary(results: dict) -> str:
+    """The scalar results as dqmc_main prints them: the two signs, a blank line, then the
+    observables in the reference's fixed order (those measured)."""
+    out = [format_summary_line(DESCRIPTIONS[n], *results[n]) for n in SUMMARY_SIGNS if n in results]
+    out.append("\n")
+    out += [format_summary_line(DESCRIPTIONS[n], *results[n]) for n in SUMMARY_ORDER if n in results]
+    return "".join(out)
+
+
+def _param(name: str, value: str) -> str:
+    return f"{name:>30s}{'->':>7s}{value:>24s}\n"  # "%| 30s|%| 7s|%| 24s|\n"
+
+
+def format_init_info(cfg: RunConfig, world_size: int) -> str:
+    """DqmcIO::output_init_info (include/dqmc_io.h:101-236): model, lattice, checkerboard,
+    Monte Carlo and measuring parameters.  world_size is the number of chains (the
+    reference's MPI ranks); the bin count shown is bins per chain times chains."""
+    f3 = lambda v: f"{v:.3f}"
+    model = "Attractive Hubbard" if cfg.model == "AttractiveHubbard" else "Repulsive Hubbard"
+    out = [f"   Model: {model}\n", _param("Hopping constant 't'", f3(cfg.hopping_t)),
+           _param("Onsite interaction 'U'", f3(cfg.onsite_u)),
+           _param("Checimcal potential 'mu'", f3(cfg.chemical_potential)), "\n"]  # the reference's spelling
+    L, dim = cfg.L, cfg.dim
+    ks = kstars(L, dim)
+    k = ks[momentum_index(L, cfg.momentum, dim) if cfg.momentum else len(ks) - 1]
+    if dim == 2:
+        out += ["   Lattice: Square lattice\n", _param("Size of cell", f"{L} * {L}"),
+                _param("Momentum point", f"({k[0] / math.pi:.2f}, {k[1] / math.pi:.2f}) pi")]
+    else:
+        out += ["   Lattice: Cubic lattice\n", _param("Size of cell", f"{L} * {L} * {L}"),
+                _param("Momentum point", f"({k[0] / math.pi:.2f}, {k[1] / math.pi:.2f}, {k[2] / math.pi:.2f}) pi")]
+    tf = lambda b: "True" if b else "False"
+    out += [_param("Checkerboard breakups", tf(cfg.checkerboard)), "\n"]
+    out += ["   MonteCarlo Params:\n", _param("Inverse temperature", f3(cfg.beta)),
+            _param("Imaginary-time length", str(cfg.time_size)),
+            _param("Imaginary-time interval", f3(cfg.beta / cfg.time_size)),
+            _param("Stabilization pace", str(cfg.stabilization_pace)), "\n"]
+    out += ["   Measuring Params:\n", _param("Warm up", tf(cfg.sweeps_warmup != 0)),
+            _param("Equal-time measure", tf(bool(cfg.equaltime))), _param("Dynamical measure", tf(bool(cfg.dynamic))),
+            "\n"]
+    bins_per_chain = math.ceil(cfg.bin_num / world_size)
+    out += [_param("Sweeps for warmup", str(cfg.sweeps_warmup)),
+            _param("Number of bins", str(bins_per_chain * world_size)),
+            _param("Sweeps per bin", str(cfg.bin_size)), _param("Sweeps between bins", str(cfg.sweeps_between_bins)),
+            "\n"]
+    return "".join(out)
+
+
+def format_ending_info(seconds: float, wrap_error: float) -> str:
+    """DqmcIO::output_ending_info (include/dqmc_io.h:241-265): wall time and the maximum
+    wrapping error."""
+    ms = int(seconds * 1000)  # Dqmc::timer() counts milliseconds
+    day = ms // 86400000
+    hour = int((ms / 1000 - day * 86400) // 3600)
+    minute = int((ms / 1000 - day * 86400 - hour * 3600) // 60)
+    sec = ms / 1000 - 86400 * day - 3600 * hour - 60 * minute
+    if day:
+        t = f"{day} d {hour} h {minute} m {sec:.2f} s"
+    elif hour:
+        t = f"{hour} h {minute} m {sec:.2f} s"
+    elif minute:
+        t = f"{minute} m {sec:.2f} s"
+    else:
+        t = f"{sec:.2f} s"
+    return f"\n>> The simulation finished in {t}.\n\n>> Maximum of the wrapping error: {wrap_error:.5e}\n\n"
+
+
 def analyse_bins(bins):
     """Observable::analyse (include/measure/observable.h:169-211): mean over bins and
     sqrt(<x^2> - <x>^2) / sqrt(nbins - 1), elementwise for vectors and matrices."""

@@ -25,20 +25,12 @@ import argparse
 import math
 import os
 import sys
+import time
 
 import numpy as np
 
 from . import io as dio
 from . import parallel
-
-DESCRIPTIONS = {
-    "filling_number": "Filling number", "double_occupancy": "Double occupation", "kinetic_energy": "Kinetic energy",
-    "momentum_distribution": "Momentum distribution", "local_spin_corr": "Local spin correlation",
-    "spin_density_structure_factor": "SDW order parameter", "charge_density_structure_factor": "CDW order parameter",
-    "s_wave_pairing_corr": "S-wave pairing correlation", "superfluid_stiffness": "Superfluid stiffness",
-    "equaltime_sign": "Averaged sign (equal-time)", "dynamic_sign": "Averaged sign (dynamic)",
-}
-
 
 def run(cfg: dio.RunConfig, out_dir: str, walkers: int = 1, seed: int = 12345, fields_file: str | None = None,
         precision: str = "fp64", rng: str = "minstd", log=sys.stdout) -> dict:
@@ -49,6 +41,7 @@ def run(cfg: dio.RunConfig, out_dir: str, walkers: int = 1, seed: int = 12345, f
     if cfg.lattice != "Square":
         raise NotImplementedError(f"the GPU sweep runs the square lattice; '{cfg.lattice}' is not built on the device")
     rank, size = parallel.init()
+    t_start = time.perf_counter()
     if size > 1:
         import torch
 
@@ -62,6 +55,12 @@ def run(cfg: dio.RunConfig, out_dir: str, walkers: int = 1, seed: int = 12345, f
     # the dynamic half-sweep runs on the HBM path, which walkers with N <= 64 take only when asked
     b = dq.Batch(descs, rng=dq.RNG_PHILOX if rng == "philox" else dq.RNG_MINSTD,
                  precision=dq.MIXED if precision == "mixed" else dq.FP64, hbm=bool(cfg.dynamic))
+    if rank == 0:
+        log.write(">> Configurations of the bosonic fields "
+                  + ("read from the input config file.\n\n" if fields_file else "set to random.\n\n"))
+        log.write(">> Initialization finished. \n\n>> The simulation is going to get started with parameters "
+                  "shown below :\n\n")
+        log.write(dio.format_init_info(cfg, walkers * size))
     try:
         if fields_file:
             with open(fields_file, encoding="utf-8") as f:
@@ -121,6 +120,7 @@ def run(cfg: dio.RunConfig, out_dir: str, walkers: int = 1, seed: int = 12345, f
                 b.sweep_0_to_beta()
                 b.sweep_beta_to_0()
         fields0 = b.fields(0)
+        wrap = max(b.wrap_error(w) for w in range(walkers))
     finally:
         b.close()
 
@@ -128,8 +128,10 @@ def run(cfg: dio.RunConfig, out_dir: str, walkers: int = 1, seed: int = 12345, f
     dyn_local = {k: np.array([x for wb in v for x in wb]) for k, v in dyn_bins.items()}
     eq_all = parallel.gather_bins(eq_local) if eqt else None
     dyn_all = {k: parallel.gather_bins(v) for k, v in dyn_local.items()} if dyn else None
+    wrap_all = parallel.gather_bins(np.array([wrap]))
     if rank != 0:
         return {}
+    log.write(dio.format_ending_info(time.perf_counter() - t_start, float(np.max(wrap_all))))
     os.makedirs(out_dir, exist_ok=True)
     results = {}
 
@@ -165,9 +167,7 @@ def run(cfg: dio.RunConfig, out_dir: str, walkers: int = 1, seed: int = 12345, f
     write("fields.out", dio.format_fields(fields0))
     write("kstars.out", dio.format_kstars(L))
     write("tgrids.out", dio.format_tgrids(cfg.beta, lt))
-    for name in ["equaltime_sign"] + cfg.equaltime + ["dynamic_sign", "superfluid_stiffness"]:
-        if name in results:
-            log.write(dio.format_summary_line(DESCRIPTIONS[name], *results[name]))
+    log.write(dio.format_summary(results))
     return results
 
 

@@ -7,6 +7,10 @@ from the example's parameters and field configuration and compare digests, and
 re-format the recorded rows of the observable files field by field, so the
 writers' formats are pinned to the reference's own files.
 
+It also records three blocks of the example's terminal log (example/log.out): the
+parameter block of DqmcIO::output_init_info, the ending info and the scalar summary,
+which the tests rebuild from the example's configuration and logged numbers.
+
 Usage: python tests/golden/make_io_fixture.py <reference-checkout>
 """
 import hashlib
@@ -27,6 +31,17 @@ def main(ref: str) -> None:
         lines = data.decode().split("\n")
         out["files"][name] = {"sha256": hashlib.sha256(data).hexdigest(), "head": lines[:4],
                               "lines": len(lines)}
+    with open(os.path.join(ref, "example", "log.out"), encoding="utf-8") as f:
+        log = f.read().split("\n")
+    start = next(i for i, l in enumerate(log) if l.startswith("   Model:"))
+    stop = next(i for i, l in enumerate(log) if l.startswith(" Warming up"))
+    fin = next(i for i, l in enumerate(log) if l.startswith(">> The simulation finished"))
+    summ = next(i for i, l in enumerate(log) if "Averaged sign (equal-time)" in l)
+    end = max(i for i, l in enumerate(log) if " pm " in l)
+    out["log"] = {"source": "reference example run: example/log.out",
+                  "init_info": "\n".join(log[start:stop]),
+                  "ending_info": "\n".join(log[fin - 1:fin + 4]),
+                  "summary": "\n".join(log[summ:end + 1]) + "\n"}
     dst = os.path.join(os.path.dirname(os.path.abspath(__file__)), "io_formats.json")
     with open(dst, "w") as f:
         json.dump(out, f, indent=1)

@@ -37,6 +37,7 @@ class FakeBatch:
     def init_greens(self): pass
     def close(self): pass
     def config_sign(self, w): return SIGN
+    def wrap_error(self, w): return 1e-9 * (w + 1)
     def fields(self, w): return np.ones((self.lt, self.N), dtype=np.int8)
 
     def clear_observables(self):
@@ -136,7 +137,16 @@ def test_equaltime_run(fake, tmp_path):
     assert swave.startswith(dio._f(0.8 + 0.5))
     assert open(tmp_path / "swave.bins.out").read().splitlines()[0] == dio._d(6)
     assert not os.path.exists(tmp_path / "dos.out")
-    assert "Filling number" in open(tmp_path / "log").read()
+    text = open(tmp_path / "log").read()
+    assert "Filling number" in text
+    # dqmc_main's layout: start-up lines, the parameter block, the ending info with the
+    # largest wrap error over the walkers, the signs, a blank line, the observables
+    assert text.startswith(">> Configurations of the bosonic fields set to random.\n\n>> Initialization finished.")
+    assert "   Model: Repulsive Hubbard\n" in text and dio._param("Number of bins", "6") in text
+    assert ">> Maximum of the wrapping error: 2.00000e-09\n" in text
+    signs, rest = text.split(">> Maximum of the wrapping error: 2.00000e-09\n\n")[1].split("\n\n", 1)
+    assert signs.strip().startswith("Averaged sign (equal-time)")
+    assert rest.index("Filling number") < rest.index("S-wave pairing correlation")
 
 
 def test_dynamic_run(fake, tmp_path):

@@ -223,3 +223,60 @@ def test_cubic_kstars_agree_with_the_oracle(oracle_mod):
     assert len(ks) == w.num_k_stars()
     for k, v in enumerate(ks):
         np.testing.assert_array_equal(w.k_star(k), v)
+
+
+LOG = json.load(open(os.path.join(HERE, "golden", "io_formats.json")))["log"]
+EXAMPLE_CONFIG = """
+[Model]
+    type = "AttractiveHubbard"
+    [Model.Params]
+    hopping_t = 1.0
+    onsite_u = 4.0
+    chemical_potential = 0.0
+[Lattice]
+    type = "Square"
+    cell = [8, 8]
+    momentum = "MPoint"
+    momentum_list = "KstarsAll"
+[CheckerBoard]
+    whether_or_not = false
+[MonteCarlo]
+    beta = 8.0
+    time_size = 160
+    stabilization_pace = 10
+[Measure]
+    sweeps_warmup = 512
+    bin_num = 20
+    bin_size = 100
+    sweeps_between_bins = 20
+    observables = ["all"]
+"""
+
+
+def test_terminal_blocks_are_byte_identical_to_the_reference_log():
+    """DqmcIO::output_init_info, output_ending_info and dqmc_main's scalar summary rebuilt from
+    the example's parameters (10 MPI ranks) and logged numbers equal example/log.out."""
+    cfg = dio.parse_config(EXAMPLE_CONFIG)
+    assert dio.format_init_info(cfg, 10) == LOG["init_info"] + "\n"
+    assert dio.format_ending_info(102.03, 1.08516e-08) == LOG["ending_info"] + "\n"
+    names = {v: k for k, v in dio.DESCRIPTIONS.items()}
+    results = {}
+    for line in LOG["summary"].splitlines():
+        if "->" in line:
+            desc, rest = line.split("->")
+            mean, err = rest.split("pm")
+            results[names[desc.strip()]] = (float(mean), float(err))
+    assert len(results) == 11
+    assert dio.format_summary(results) == LOG["summary"]
+
+
+def test_ending_info_time_formats():
+    """d/h/m/s forms of DqmcIO::output_ending_info."""
+    assert ">> The simulation finished in 5.25 s." in dio.format_ending_info(5.25, 0.0)
+    assert ">> The simulation finished in 2 h 0 m 1.50 s." in dio.format_ending_info(7201.5, 0.0)
+    assert ">> The simulation finished in 1 d 1 h 1 m 1.00 s." in dio.format_ending_info(90061.0, 0.0)
+    cubic = dio.parse_config('[Lattice]\ntype = "Cubic"\ncell = [4, 4, 4]\nmomentum = "RPoint"\n'
+                             '[Measure]\nobservables = ["filling_number"]\n')
+    info = dio.format_init_info(cubic, 3)
+    assert "   Lattice: Cubic lattice\n" in info and "(1.00, 1.00, 1.00) pi" in info and "4 * 4 * 4" in info
+    assert dio._param("Number of bins", "21") in info and dio._param("Dynamical measure", "False") in info
