@@ -63,7 +63,10 @@ class RunConfig:
 
 def parse_config(text: str) -> RunConfig:
     """DqmcInitializer::parse_toml_config on a TOML string.  Raises ValueError where the
-    reference exits (unknown model or lattice, bad cell, missing observable list)."""
+    reference exits (unknown model or lattice, bad cell, checkerboard off the square lattice,
+    missing observable list, unknown momentum names when they are used).  The reference also
+    exits when `momentum` or `momentum_list` is absent; here they default to the last k star,
+    (pi, ..., pi), and to every k star."""
     c = tomllib.loads(text)
     m, lat = c.get("Model", {}), c.get("Lattice", {})
     p, mc, me = m.get("Params", {}), c.get("MonteCarlo", {}), c.get("Measure", {})
