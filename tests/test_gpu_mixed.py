@@ -1,9 +1,13 @@
-"""Mixed-precision path (DQMC_MIXED): wraps and B-chain products on the BF16
-tensor cores through exact integer slices (49-bit), FP64 everywhere else.
+"""Tensor-core path (DQMC_MIXED): wraps and B-chain products on the BF16 tensor
+cores through exact integer slices (49 bits), submatrix Metropolis with tensor-core
+block flushes, and for 128 <= N <= 768 the blocked Householder stabilization with
+56-bit products; FP64 for the panels, the decisions and the ratios.
 
 Bars: the product engine agrees with FP64 to 2^-38 of |A||B| (normwise) and is
-exact on integer inputs; the mixed sweep keeps max|dG| <= 1e-6 against the FP64
-path at every stabilization, on the same fields and uniforms.
+exact on integer inputs; the mixed sweep makes the FP64 path's accept/reject
+decisions and keeps max|dG| <= 1e-6 against it at every stabilization, on the same
+fields and uniforms; the autotuner's pick is one of its timed candidates; walker
+groups (graph branches) do not change any walker's result.
 """
 import numpy as np
 import pytest
