@@ -56,7 +56,10 @@ int main(int argc, char** argv) {
       std::vector<int8_t> f((size_t)lt * n, 1);
       int t, i;
       double s;
-      while (in >> t >> i >> s) f[(size_t)t * n + i] = s > 0 ? 1 : -1;
+      while (in >> t >> i >> s) {
+        if (t < 0 || t >= lt || i < 0 || i >= n) throw Error(DQMC_ERR_ARG, "fields file: site outside Lt x N");
+        f[(size_t)t * n + i] = s > 0 ? 1 : -1;
+      }
       for (int w = 0; w < nw; ++w) walker.set_bosonic_fields(w, f);
     }
     walker.initial_greens_functions();
