@@ -40,6 +40,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
@@ -178,8 +179,10 @@ class Clocks:
 
     def start(self):
         try:
-            os.makedirs(os.path.join(ROOT, "gpurun_out"), exist_ok=True)
-            self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+            # samples go to DQMC_BENCH_CLOCKS_DIR when set (to keep them), else a temporary file
+            d = os.environ.get("DQMC_BENCH_CLOCKS_DIR") or tempfile.gettempdir()
+            os.makedirs(d, exist_ok=True)
+            self.path = os.path.join(d, f"dqmc_bench_clocks_{os.getpid()}.csv")
             self.f = open(self.path, "w")
             self.p = subprocess.Popen(["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.Q}",
                                        "--format=csv,noheader,nounits", "-lms", "200"],
@@ -216,7 +219,7 @@ class Clocks:
 
 
 # ----------------------------------------------------------------------------
-# algorithmic work (per walker per half-sweep), the survey's figure F
+# algorithmic work per walker per half-sweep: the reference's sweep, counted as it executes
 # ----------------------------------------------------------------------------
 def flops_model(wl, accepts_per_walker_per_half):
     N, Lt, p = wl["L"] ** 2, wl["Lt"], wl["pace"]
