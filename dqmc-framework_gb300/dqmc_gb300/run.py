@@ -1,7 +1,10 @@
 """Run a reference configuration on the GPU and write the reference's output files.
 
-    python -m dqmc_gb300.run config.toml --out DIR [--walkers W] [--seed S]
-                            [--fields FILE] [--precision fp64|mixed] [--rng minstd|philox]
+    python -m dqmc_gb300.run -c config.toml -o DIR [-f FIELDS] [--walkers W] [--seed S]
+                             [--precision fp64|mixed] [--rng minstd|philox]
+
+(-c/--config, -o/--output and -f/--fields are dqmc_main's options, src/dqmc_main.cpp:53-62;
+the configuration may also be given as the first positional argument.)
 
 Follows the reference's driver (src/dqmc_main.cpp, src/dqmc.cpp:48-158): each walker
 is one of the reference's MPI ranks (one Markov chain); warm-up of
@@ -15,7 +18,10 @@ analysed as Observable::analyse.  Under torchrun every process runs W walkers on
 own GPU and rank 0 gathers the bins, analyses and writes (the reference's MPI
 layout, include/utils/mpi.hpp:29-104).  Output: the terminal summary of the scalar
 observables and fields.out, kstars.out, tgrids.out, swave(.bins).out,
-dos(.bins).out, greens(.bins).out, dss(.bins).out in the reference's formats.
+dos(.bins).out, greens(.bins).out, dss(.bins).out in the reference's formats.  As
+in dqmc_main (src/dqmc_main.cpp:280-283), the final fields of walker 0 go to the
+input fields file when one was given (so the next run resumes from them), else
+to fields.out in the output folder.
 G(k, tau) covers the configured `momentum_list` (rows of greens.out in the
 reference's k-star order).
 """
@@ -33,11 +39,12 @@ from . import io as dio
 from . import parallel
 
 def run(cfg: dio.RunConfig, out_dir: str, walkers: int = 1, seed: int = 12345, fields_file: str | None = None,
-        precision: str = "fp64", rng: str = "minstd", log=sys.stdout) -> dict:
+        precision: str = "fp64", rng: str = "minstd", log=None) -> dict:
     """Run the configuration; returns {name: (mean, error)} and writes the output files
     (rank 0 of a torchrun launch; the other ranks return {})."""
     import dqmc_gb300 as dq
 
+    log = log if log is not None else sys.stdout  # resolved per call, so redirections apply
     if cfg.lattice != "Square":
         raise NotImplementedError(f"the GPU sweep runs the square lattice; '{cfg.lattice}' is not built on the device")
     rank, size = parallel.init()
@@ -164,7 +171,11 @@ def run(cfg: dio.RunConfig, out_dir: str, walkers: int = 1, seed: int = 12345, f
         if "superfluid_stiffness" in cfg.dynamic:
             mean, err = dio.analyse_bins(pool["rho"])
             results["superfluid_stiffness"] = (float(mean), float(err))
-    write("fields.out", dio.format_fields(fields0))
+    if fields_file:  # dqmc_main writes the final fields back over the input file
+        with open(fields_file, "w", encoding="utf-8") as f:
+            f.write(dio.format_fields(fields0))
+    else:
+        write("fields.out", dio.format_fields(fields0))
     write("kstars.out", dio.format_kstars(L))
     write("tgrids.out", dio.format_tgrids(cfg.beta, lt))
     log.write(dio.format_summary(results))
@@ -173,15 +184,21 @@ def run(cfg: dio.RunConfig, out_dir: str, walkers: int = 1, seed: int = 12345, f
 
 def main(argv=None) -> int:
     ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
-    ap.add_argument("config")
-    ap.add_argument("--out", default="output")
+    ap.add_argument("config_file", nargs="?", help="configuration file (same as -c)")
+    ap.add_argument("-c", "--config", default=None, help="path of the TOML configuration file")
+    ap.add_argument("-o", "--output", "--out", dest="out", default="output",
+                    help="folder for the measured results (created if missing)")
+    ap.add_argument("-f", "--fields", default=None,
+                    help="fields file to start from (the reference's format); the final fields are written back to it")
     ap.add_argument("--walkers", type=int, default=1)
     ap.add_argument("--seed", type=int, default=12345)
-    ap.add_argument("--fields", default=None)
     ap.add_argument("--precision", choices=["fp64", "mixed"], default="fp64")
     ap.add_argument("--rng", choices=["minstd", "philox"], default="minstd")
     a = ap.parse_args(argv)
-    cfg = dio.load_config(a.config)
+    config = a.config or a.config_file
+    if not config:
+        ap.error("a configuration file is required (-c/--config)")
+    cfg = dio.load_config(config)
     run(cfg, a.out, walkers=a.walkers, seed=a.seed, fields_file=a.fields, precision=a.precision, rng=a.rng)
     return 0
 

@@ -176,3 +176,31 @@ def test_cubic_configuration_is_refused_before_any_device_work(fake, tmp_path):
     with pytest.raises(NotImplementedError):
         drv.run(cfg, str(tmp_path), walkers=1, log=open(os.devnull, "w"))
     assert not fake.created
+
+
+def test_reference_command_line_and_fields_resume(fake, tmp_path):
+    """dqmc_main's options (-c/--config, -o/--output, -f/--fields, src/dqmc_main.cpp:53-62): the
+    run starts from the fields file and writes the final fields back over it
+    (src/dqmc_main.cpp:280-283), and the output folder is created."""
+    cfg_path = tmp_path / "config.toml"
+    cfg_path.write_text(CONFIG % '"filling_number"')
+    start = [[-1] * 16 for _ in range(6)]
+    fpath = tmp_path / "fields.in"
+    fpath.write_text(dio.format_fields(start))
+    out = tmp_path / "out" / "run1"
+    import contextlib
+    import io as sio
+
+    with contextlib.redirect_stdout(sio.StringIO()) as buf:
+        assert drv.main(["--config", str(cfg_path), "--output", str(out), "--fields", str(fpath), "--walkers", "2"]) == 0
+    b = fake.created[0]
+    assert (b.f == -1).all()  # started from the file
+    lt, n, f = dio.parse_fields(fpath.read_text())
+    assert (lt, n) == (6, 16) and all(v == 1 for row in f for v in row)  # FakeBatch's final fields
+    assert not (out / "fields.out").exists() and (out / "kstars.out").exists()
+    assert "read from the input config file" in buf.getvalue()
+    with contextlib.redirect_stdout(sio.StringIO()):
+        assert drv.main(["-c", str(cfg_path), "-o", str(tmp_path / "o2")]) == 0
+    assert (tmp_path / "o2" / "fields.out").exists()
+    with pytest.raises(SystemExit):
+        drv.main(["-o", str(tmp_path / "o3")])  # no configuration
