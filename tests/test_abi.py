@@ -129,3 +129,37 @@ def test_cpp_driver_fails_loudly_without_a_device(dq):
     assert r.returncode != 0 and "no CUDA device" in (r.stdout + r.stderr)
     r = subprocess.run([exe, "bogus=1"], capture_output=True, text=True, env=env, timeout=120)
     assert r.returncode != 0 and "unknown argument" in (r.stdout + r.stderr)
+
+
+def test_cpp_mirror_analysis_matches_python(tmp_path):
+    """MeasureHandler::analyse_stats of include/dqmc_gb300.hpp and dqmc_gb300.io.analyse_bins
+    (both Observable::analyse, include/measure/observable.h:169-211) agree on the same bins."""
+    import shutil
+    import subprocess
+
+    import numpy as np
+
+    cxx = shutil.which("g++") or shutil.which("c++")
+    if cxx is None:
+        pytest.skip("no C++ compiler")
+    rng = np.random.default_rng(11)
+    bins = rng.normal(0.5, 0.2, (7, 9))
+    src = tmp_path / "analyse.cpp"
+    rows = ",\n".join("{" + ", ".join(repr(float(v)) for v in b) + "}" for b in bins)
+    src.write_text('#include <cstdio>\n#include "dqmc_gb300.hpp"\n'
+                   "int main() {\n  dqmc_gb300::MeasureHandler m;\n"
+                   f"  m.bins = {{{rows}}};\n  m.analyse_stats();\n"
+                   '  for (int k = 0; k < DQMC_NUM_OBS; ++k) std::printf("%.17g %.17g\\n", m.mean[k], m.error[k]);\n}\n')
+    exe = tmp_path / "analyse"
+    subprocess.run([cxx, "-std=c++17", "-O1", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)],
+                   check=True, timeout=120)
+    out = np.array([[float(x) for x in l.split()] for l in subprocess.run([str(exe)], capture_output=True, text=True,
+                                                                           check=True).stdout.splitlines()])
+    import sys
+
+    sys.path.insert(0, os.path.join(ROOT, "dqmc-framework_gb300"))
+    from dqmc_gb300 import io as dio
+
+    mean, err = dio.analyse_bins(bins)
+    np.testing.assert_allclose(out[:, 0], mean, rtol=1e-14)
+    np.testing.assert_allclose(out[:, 1], err, rtol=1e-12)
