@@ -109,15 +109,17 @@ class DqmcWalker {
     if (pace < 1) throw Error(DQMC_ERR_ARG, "set_stabilization_pace: pace >= 1");
     pace_ = pace;
   }
-  // one walker per seed; rng = DQMC_RNG_MINSTD reproduces the reference stream
+  // one walker per seed; rng = DQMC_RNG_MINSTD reproduces the reference stream; precision
+  // DQMC_MIXED selects the tensor-core path; hbm puts every walker on the HBM path (the
+  // dynamic half-sweep needs it for N <= 64)
   void initial(const Square& lat, const Model& model, const std::vector<uint64_t>& seeds,
-               int rng = DQMC_RNG_MINSTD) {
+               int rng = DQMC_RNG_MINSTD, int precision = DQMC_FP64, bool hbm = false) {
     std::vector<dqmc_walker_desc> d(seeds.size());
     for (size_t w = 0; w < seeds.size(); ++w) {
       d[w] = dqmc_walker_desc{model.type, lat.side, model.hopping_t, model.onsite_u, model.chemical_potential,
                               beta_, lt_, pace_, model.checkerboard ? 1 : 0, lat.momentum_index, seeds[w]};
     }
-    dqmc_batch_options o{rng, DQMC_FP64, 0, 1, 0};
+    dqmc_batch_options o{rng, precision, 0, 1, hbm ? 1 : 0};
     if (b_) dqmc_batch_destroy(b_);
     b_ = nullptr;
     check(dqmc_batch_create(d.data(), (int)d.size(), &o, &b_));
