@@ -1394,6 +1394,7 @@ void orc_set_green(void* h, int spin, const double* in) {
 }
 double orc_wrap_error(void* h) { return O(h)->wrap_err; }
 double orc_config_sign(void* h) { return O(h)->sign; }
+void orc_set_config_sign(void* h, double s) { O(h)->sign = (s >= 0) ? 1.0 : -1.0; }
 int64_t orc_accept_count(void* h) { return O(h)->accepts; }
 int orc_trace_count(void* h) { return (int)O(h)->trace.size() / 2; }
 void orc_trace_get(void* h, int k, int spin, double* out) {

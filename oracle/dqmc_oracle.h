@@ -116,6 +116,10 @@ void orc_get_green(void* h, int spin, double* out);    /* spin 0 up, 1 down */
 void orc_set_green(void* h, int spin, const double* in);
 double orc_wrap_error(void* h);
 double orc_config_sign(void* h);
+/* Test hook: overwrite the configuration sign (the reference's initial sign,
+ * sgn(det G_up det G_dn) of src/dqmc_walker.cpp:162, is not fixed by FP64 once
+ * G has eigenvalues below its rounding; a test may adopt the device's value). */
+void orc_set_config_sign(void* h, double s);
 int64_t orc_accept_count(void* h);
 /* G after every stabilization of the last half-sweep(s) since the last clear. */
 int orc_trace_count(void* h);

@@ -93,6 +93,7 @@ def lib() -> ctypes.CDLL:
         "orc_get_green": (None, [vp, ctypes.c_int, dp]),
         "orc_set_green": (None, [vp, ctypes.c_int, dp]),
         "orc_wrap_error": (ctypes.c_double, [vp]), "orc_config_sign": (ctypes.c_double, [vp]),
+        "orc_set_config_sign": (None, [vp, ctypes.c_double]),
         "orc_accept_count": (ctypes.c_int64, [vp]), "orc_trace_count": (ctypes.c_int, [vp]),
         "orc_trace_get": (None, [vp, ctypes.c_int, ctypes.c_int, dp]),
         "orc_trace_clear": (None, [vp]), "orc_trace_enable": (None, [vp, ctypes.c_int]),
@@ -267,6 +268,10 @@ class Walker:
     @property
     def sign(self) -> float:
         return lib().orc_config_sign(self.h)
+
+    @sign.setter
+    def sign(self, s: float):
+        lib().orc_set_config_sign(self.h, float(s))
 
     @property
     def accepts(self) -> int:

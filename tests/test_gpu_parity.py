@@ -30,13 +30,25 @@ def _oracle(O, d, stack):
     return w
 
 
+def _rel_err(a, b):
+    return float(abs(a - b).max()) / max(1.0, float(abs(b).max()))
+
+
 def _close(a, b, rel=REL):
-    scale = max(1.0, abs(b).max())
-    return abs(a - b).max() <= rel * scale
+    return _rel_err(a, b) <= rel
 
 
-def _run_pair(dq, O, descs, sweeps=1, stack=None, fields=None, measure=True):
-    O.use_scipy_lapack(False)
+def _run_pair(dq, O, descs, sweeps=1, stack=None, fields=None, measure=True, rel=REL, lapack=False, errs=None,
+              wrap_ratio=True, adopted=None):
+    """Both sides from the same seed (or fields) through `sweeps` forth-and-back pairs:
+    identical fields after every pair, G within `rel` (relative to max(1, |G|)) at every
+    stabilization and after every half-sweep, equal signs and accept counts, observable
+    sums within `rel`.  errs (a list) receives the relative G error of every
+    stabilization; wrap_ratio asks the two wrap errors to agree within a factor 10.
+    adopted (a list): where the initial signs differ, the oracle takes the device's and
+    the walker index is appended (for stacks whose G has eigenvalues below FP64
+    rounding, where sgn det G is not determined; see the callers); else they must agree."""
+    O.use_scipy_lapack(lapack)
     stack = O.STACK_QRP if stack is None else stack
     batch = dq.Batch(descs, rng=dq.RNG_MINSTD, trace=True)
     refs = [_oracle(O, d, stack) for d in descs]
@@ -52,7 +64,10 @@ def _run_pair(dq, O, descs, sweeps=1, stack=None, fields=None, measure=True):
     batch.init_greens()
     for k, r in enumerate(refs):
         for s in (0, 1):
-            assert _close(batch.green(k, s), r.green(s)), f"walker {k} initial G spin {s}"
+            assert _close(batch.green(k, s), r.green(s), rel), f"walker {k} initial G spin {s}"
+        if adopted is not None and batch.config_sign(k) != r.sign:
+            adopted.append(k)
+            r.sign = batch.config_sign(k)
         assert batch.config_sign(k) == r.sign
     for _ in range(sweeps):
         batch.trace_clear()
@@ -75,10 +90,12 @@ def _run_pair(dq, O, descs, sweeps=1, stack=None, fields=None, measure=True):
             tg = np.concatenate([tg_all[h * ns_max:h * ns_max + ns] for h in range(2)])
             assert tg.shape == tr.shape
             for i in range(tr.shape[0]):
-                for s in (0, 1):
-                    assert _close(tg[i, s], tr[i, s]), (k, i, s, abs(tg[i, s] - tr[i, s]).max())
+                e = max(_rel_err(tg[i, s], tr[i, s]) for s in (0, 1))
+                if errs is not None:
+                    errs.append(e)
+                assert e <= rel, (k, i, e)
             for s in (0, 1):
-                assert _close(batch.green(k, s), r.green(s))
+                assert _close(batch.green(k, s), r.green(s), rel)
             assert batch.config_sign(k) == r.sign
             assert batch.accept_count(k) == r.accepts
             assert batch.status(k) == 0
@@ -87,12 +104,13 @@ def _run_pair(dq, O, descs, sweeps=1, stack=None, fields=None, measure=True):
             sums, counts = batch.observables(k)
             rs, rc = r.accumulators()
             np.testing.assert_array_equal(counts, rc)
-            np.testing.assert_allclose(sums, rs, rtol=REL, atol=REL)
+            np.testing.assert_allclose(sums, rs, rtol=rel, atol=rel)
         # the wrap error is rounding noise amplified by the B chain: same
         # order of magnitude on both sides, not the same digits
         we, wr = batch.wrap_error(k), r.wrap_error
         assert we < 1e-6 and wr < 1e-6
-        assert we <= 10 * wr + 1e-13 and wr <= 10 * we + 1e-13, (we, wr)
+        if wrap_ratio:
+            assert we <= 10 * wr + 1e-13 and wr <= 10 * we + 1e-13, (we, wr)
     return batch, refs
 
 
