@@ -72,6 +72,69 @@ def test_reference_arm_prints_the_contract_line():
     assert cb["value"] == d["value"] > 0 and cb["kind"] == "port" and cb["cores"] >= 1 and cb["sample"]
     assert d["e2e"] == {"value": d["value"], "unit": "updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
     assert d["config"]["workload"] == "fp64_single_4x4_dense"
+    # the line states what it timed: steps per core and one core's time per step, which fit the run
+    assert d["steps"] == 1 and d["config"]["timed_walkers"] == cb["cores"]
+    assert 0 < d["steps"] * d["ms_per_step"] < 600e3
+
+
+def test_slice_pair_counts(bench):
+    """Wraps and B-chain: 7 slices (28 pairs) up to N = 256, 8 slices (36 pairs) above, the
+    configurations of ozaki::cfg_for_k."""
+    assert bench.wrap_slices(256) == 7 and bench.wrap_slices(257) == 8
+    assert bench.slice_pairs(7) == 28 and bench.slice_pairs(8) == 36 and bench.slice_pairs(6) == 21
+
+
+def test_metropolis_work_by_update_kind(bench):
+    """The Metropolis class is counted by the work it executes: the submatrix flush's bf16
+    slice products (21 pairs of 2 N^2 per accept plus the m^2 terms of T), its small FP64 part,
+    and the FP64 flush of the delayed kernel."""
+    sys.path.insert(0, os.path.join(ROOT, "dqmc-framework_gb300"))
+    import dqmc_gb300 as dq
+
+    d = dq.WalkerDesc(model=1, L=16, U=4.0, mu=-0.5, beta=10.0, Lt=100, pace=8)
+    N, A = 256, 0.6 * 256 * 100
+    bf, fp, what = bench.metropolis_work(d, A, 2, 32)
+    assert bf >= 21 * 2 * N * N * A and bf < 1.2 * 21 * 2 * N * N * A
+    assert 0 < fp < 0.05 * 2 * N * N * A and "submatrix" in what
+    bf0, fp0, _ = bench.metropolis_work(d, A, 0, 16)
+    assert bf0 == 0 and fp0 >= 2 * N * N * A
+    bf1, _, _ = bench.metropolis_work(d, A, 1, 32)
+    assert bf1 == 21 * 2 * N * N * A
+
+
+def test_uneven_workload_walkers(bench):
+    """The uneven batch: 64 walkers of each side 6, 8, 10, 12, Lt from beta in {4, 6, 8} at
+    dtau = 0.05, |U| in [2, 6); its per-side CPU samples cover every side."""
+    sys.path.insert(0, os.path.join(ROOT, "dqmc-framework_gb300"))
+    import dqmc_gb300 as dq
+
+    wl = bench.WORKLOADS["mixed_uneven_6_to_12"]
+    descs = bench._descs(dq, wl)
+    assert len(descs) == 256
+    assert {L: sum(1 for d in descs if d.L == L) for L in (6, 8, 10, 12)} == {6: 64, 8: 64, 10: 64, 12: 64}
+    assert {d.Lt for d in descs} == {80, 120, 160} and all(2 <= d.U < 6 for d in descs)
+    assert all(d.Lt == round(d.beta / 0.05) and d.pace == 10 for d in descs)
+    samples, _ = bench._cpu_samples(wl, 16)
+    assert sorted({p["L"] for p, _ in samples}) == [6, 8, 10, 12]
+    assert bench.working_set_bytes(wl) > bench.L2_BYTES
+
+
+def test_dg_series_per_stabilization(bench):
+    """max |dG| over the sampled walkers at each stabilization, in order; walkers whose
+    decisions differ are left out."""
+    import numpy as np
+
+    sys.path.insert(0, os.path.join(ROOT, "dqmc-framework_gb300"))
+    import dqmc_gb300 as dq
+
+    descs = [dq.WalkerDesc(L=4, Lt=20, pace=10), dq.WalkerDesc(L=4, Lt=30, pace=10)]
+    z = [np.zeros((3, 2, 16, 16)), np.zeros((3, 2, 16, 16))]
+    m = [a.copy() for a in z]
+    m[0][0] += 1e-9
+    m[1][2] += 3e-8
+    m[1][1] += 2e-9
+    assert bench.dg_series(m, z, descs, [True, True]) == pytest.approx([1e-9, 2e-9, 3e-8])
+    assert bench.dg_series(m, z, descs, [True, False]) == pytest.approx([1e-9, 0.0])
 
 
 def test_l2_note_follows_the_working_set(bench):
