@@ -55,7 +55,8 @@ void launch_metropolis_sub(const WalkerDev* W, int nw, int mode, int j, int q, i
 int delayed_pick_kd(int N, int S);
 void general_chain_init(int mode, const WalkerDev* W, int nw, int j, cudaStream_t st);
 void general_push(int mode, const WalkerDev* W, int nw, int j, int maxN, cudaStream_t st);
-void general_dynamic_slice(const WalkerDev* W, int nw, int j, int q, int maxN, bool mixed, cudaStream_t st);
+void general_dynamic_slice(const WalkerDev* W, int nw, int j, int q, int maxN, bool mixed, bool any_dense,
+                           bool any_cb, cudaStream_t st);
 void general_dynamic_stab(const WalkerDev* W, int nw, int j, int maxN, cudaStream_t st);
 void general_dynamic_begin(const WalkerDev* W, int nw, cudaStream_t st);
 void general_dynamic_end(const WalkerDev* W, int nw, int maxN, cudaStream_t st);
@@ -212,6 +213,10 @@ struct dqmc_batch {
   std::vector<WalkerDev> hw;        // host copies of the descriptors
   // dynamic half-sweep: buffers allocated on first use, the listed tau, stack position
   char* dyn_arena = nullptr;
+  // shared-memory walkers (N <= 64) take the HBM path's kernels in the dynamic half-sweep:
+  // their ping-pong chain, product temporary and stabilization scratch, per walker
+  struct DynGen { double* chain = nullptr; double* work = nullptr; double* scr = nullptr; };
+  std::vector<DynGen> dyn_gen;
   int* d_taus = nullptr;
   std::vector<int> taus;
   bool at_zero = false;  // stacks of t = 0 (after set-up or a backward half-sweep)
@@ -577,6 +582,7 @@ int dqmc_batch_create(const dqmc_walker_desc* descs, int n, const dqmc_batch_opt
     h.uni = b->d_uni ? b->d_uni + b->uni_stride * w : nullptr;
     h.seed = d.seed;
     h.widx = w;
+    h.wait_limit = kDefaultWaitLimit;
     h.sweep_ctr = b->d_sweep;
     h.trace = b->trace_cap ? reinterpret_cast<double*>(base + off[w].trace) : nullptr;
     h.trace_cap = b->trace_cap;
@@ -860,6 +866,14 @@ static void issue_half_sweep(dqmc_batch* b, int mode, int measure) {
     for (int g = 0; g < ng; ++g) cudaStreamWaitEvent(b->stream, b->ev_join[g], 0);
 }
 
+// owns a captured graph until the end of its scope, error returns included
+struct GraphGuard {
+  cudaGraph_t g = nullptr;
+  ~GraphGuard() {
+    if (g) cudaGraphDestroy(g);
+  }
+};
+
 static int half_sweep(dqmc_batch* b, int mode, int measure) {
   if (!b) return fail(DQMC_ERR_ARG, "null batch");
   if (!b->initialised) return fail(DQMC_ERR_STATE, "sweep before dqmc_init_greens");
@@ -877,17 +891,16 @@ static int half_sweep(dqmc_batch* b, int mode, int measure) {
   if (use_graph && b->prof) {
     // profiled replay: event nodes around each kernel class, read after the replay
     if (!b->pexec[mode][ms]) {
-      cudaGraph_t g = nullptr;
+      GraphGuard g;
       const size_t m0 = b->marks.size();
       CUDA_TRY(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
       b->capturing = true;
       issue_half_sweep(b, mode, measure);
       b->capturing = false;
-      CUDA_TRY(cudaStreamEndCapture(b->stream, &g));
+      CUDA_TRY(cudaStreamEndCapture(b->stream, &g.g));
       b->pmarks[mode][ms].assign(b->marks.begin() + m0, b->marks.end());
       b->marks.resize(m0);
-      CUDA_TRY(cudaGraphInstantiate(&b->pexec[mode][ms], g, 0));
-      cudaGraphDestroy(g);
+      CUDA_TRY(cudaGraphInstantiate(&b->pexec[mode][ms], g.g, 0));
     }
     CUDA_TRY(cudaGraphLaunch(b->pexec[mode][ms], b->stream));
     for (auto& m : b->pmarks[mode][ms]) {
@@ -900,17 +913,17 @@ static int half_sweep(dqmc_batch* b, int mode, int measure) {
   }
   if (b->nodes[mode][ms] < 0 || (use_graph && !b->prof && !b->gexec[mode][ms])) {
     // capture the half-sweep: its kernel nodes give the launch count; replayed when graphs are on
-    cudaGraph_t g = nullptr;
+    GraphGuard g;
     const bool prof = b->prof;
     b->prof = false;
     CUDA_TRY(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
     issue_half_sweep(b, mode, measure);
     b->prof = prof;
-    CUDA_TRY(cudaStreamEndCapture(b->stream, &g));
+    CUDA_TRY(cudaStreamEndCapture(b->stream, &g.g));
     size_t nn = 0;
-    CUDA_TRY(cudaGraphGetNodes(g, nullptr, &nn));
+    CUDA_TRY(cudaGraphGetNodes(g.g, nullptr, &nn));
     std::vector<cudaGraphNode_t> nodes(nn);
-    CUDA_TRY(cudaGraphGetNodes(g, nodes.data(), &nn));
+    CUDA_TRY(cudaGraphGetNodes(g.g, nodes.data(), &nn));
     int64_t k = 0;
     for (auto nd : nodes) {
       cudaGraphNodeType ty;
@@ -918,8 +931,7 @@ static int half_sweep(dqmc_batch* b, int mode, int measure) {
       if (ty == cudaGraphNodeTypeKernel) ++k;
     }
     b->nodes[mode][ms] = k;
-    if (use_graph && !b->prof) CUDA_TRY(cudaGraphInstantiate(&b->gexec[mode][ms], g, 0));
-    cudaGraphDestroy(g);
+    if (use_graph && !b->prof) CUDA_TRY(cudaGraphInstantiate(&b->gexec[mode][ms], g.g, 0));
   }
   if (use_graph && !b->prof) CUDA_TRY(cudaGraphLaunch(b->gexec[mode][ms], b->stream));
   else if (!use_graph) issue_half_sweep(b, mode, measure);
@@ -930,6 +942,14 @@ static int half_sweep(dqmc_batch* b, int mode, int measure) {
     CUDA_TRY(cudaStreamSynchronize(b->stream));
   }
   return launch_check("half-sweep kernels");
+}
+
+int dqmc_set_wait_limit(dqmc_batch* b, int limit) {
+  if (!b) return fail(DQMC_ERR_ARG, "null batch");
+  for (auto& h : b->hw) h.wait_limit = (limit < 0) ? kDefaultWaitLimit : limit;
+  CUDA_TRY(cudaMemcpyAsync(b->dW, b->hw.data(), sizeof(WalkerDev) * b->nw, cudaMemcpyHostToDevice, b->stream));
+  CUDA_TRY(cudaStreamSynchronize(b->stream));
+  return DQMC_OK;
 }
 
 int dqmc_tuning(dqmc_batch* b, int* kd, int* tc_flush, int* n_candidates, int* cand_kd, int* cand_tc,
@@ -971,7 +991,7 @@ static int dyn_alloc(dqmc_batch* b) {
   size_t cur = 0;
   auto take = [&](size_t bytes) { const size_t o = cur; cur = align256(cur + bytes); return o; };
   const size_t taus_off = take(sizeof(int) * kMaxTau);
-  constexpr int kOff = 10;
+  constexpr int kOff = 13;
   std::vector<size_t> off(b->nw * kOff);
   for (int w = 0; w < b->nw; ++w) {
     const WalkerDev& h = b->hw[w];
@@ -986,6 +1006,11 @@ static int dyn_alloc(dqmc_batch* b) {
     off[kOff * w + 7] = take(sizeof(double) * 2 * kMaxTau * h.N);     // parts awaiting G(beta,beta)
     off[kOff * w + 8] = take(sizeof(double) * 2 * kMaxTau);
     off[kOff * w + 9] = take(sizeof(double) * kMaxTau * h.N);        // per-displacement G sums
+    if (h.path == 0) {  // HBM-path buffers of a shared-memory walker
+      off[kOff * w + 10] = take(sizeof(double) * 2 * h.S * NN);  // chain (ping-pong)
+      off[kOff * w + 11] = take(sizeof(double) * h.S * NN);      // work
+      off[kOff * w + 12] = take(sizeof(double) * 2 * h.S * NN);  // scr
+    }
   }
   cudaError_t e = cudaMalloc(&b->dyn_arena, cur);
   if (e != cudaSuccess) {
@@ -1006,6 +1031,12 @@ static int dyn_alloc(dqmc_batch* b) {
     h.dyn_vec = reinterpret_cast<double*>(b->dyn_arena + off[kOff * w + 7]);
     h.dyn_part = reinterpret_cast<double*>(b->dyn_arena + off[kOff * w + 8]);
     h.dyn_r = reinterpret_cast<double*>(b->dyn_arena + off[kOff * w + 9]);
+    b->dyn_gen.resize(b->nw);
+    if (h.path == 0) {
+      b->dyn_gen[w].chain = reinterpret_cast<double*>(b->dyn_arena + off[kOff * w + 10]);
+      b->dyn_gen[w].work = reinterpret_cast<double*>(b->dyn_arena + off[kOff * w + 11]);
+      b->dyn_gen[w].scr = reinterpret_cast<double*>(b->dyn_arena + off[kOff * w + 12]);
+    }
     h.dyn_taus = b->d_taus;
     h.dyn_ntau = 0;
   }
@@ -1031,9 +1062,6 @@ int dqmc_sweep_dynamic(dqmc_batch* b, const int* taus, int ntau) {
   if (!b->initialised) return fail(DQMC_ERR_STATE, "dynamic sweep before dqmc_init_greens");
   if (!b->at_zero)
     return fail(DQMC_ERR_STATE, "dynamic sweep needs the stacks of t = 0 (after set-up or a backward half-sweep)");
-  if (b->any_small)
-    return fail(DQMC_ERR_ARG, "dynamic sweep needs every walker on the HBM path (N > 64 or DQMC_MIXED)");
-  if (b->any_general_cb) return fail(DQMC_ERR_ARG, "dynamic sweep: checkerboard walkers are not supported");
   if (ntau < 0 || ntau > kMaxTau || (ntau > 0 && !taus)) return fail(DQMC_ERR_ARG, "ntau must be in [0, 256]");
   for (int k = 0; k < ntau; ++k)
     for (int w = 0; w < b->nw; ++w)
@@ -1047,20 +1075,36 @@ int dqmc_sweep_dynamic(dqmc_batch* b, const int* taus, int ntau) {
     for (auto& h : b->hw) h.dyn_ntau = ntau;
     if (int r = dqmc_clear_dynamic(b)) return r;
   }
-  // the dynamic half-sweep stabilizes every walker with the FP64 kernels
+  // the dynamic half-sweep stabilizes every walker with the FP64 kernels; shared-memory
+  // walkers run it on the HBM path's kernels with their own buffers (the stacks, G and the
+  // fields are laid out alike on both paths)
   std::vector<WalkerDev> hv = b->hw;
-  for (auto& h : hv) h.ozstab = 0;
+  int maxN = 0, maxPace = 0;
+  bool any_dense = false, any_cb = false;
+  for (int w = 0; w < b->nw; ++w) {
+    WalkerDev& h = hv[w];
+    h.ozstab = 0;
+    if (h.path == 0) {
+      h.path = 1;
+      h.chain = b->dyn_gen[w].chain;
+      h.work = b->dyn_gen[w].work;
+      h.scr = b->dyn_gen[w].scr;
+    }
+    maxN = std::max(maxN, h.N);
+    maxPace = std::max(maxPace, h.pace);
+    if (h.cb) any_cb = true; else any_dense = true;
+  }
   CUDA_TRY(cudaMemcpyAsync(b->dW, hv.data(), sizeof(WalkerDev) * b->nw, cudaMemcpyHostToDevice, b->stream));
   general_dynamic_begin(b->dW, b->nw, b->stream);
   for (int j = 0; j < b->maxNs; ++j) {
     general_chain_init(MODE_FWD, b->dW, b->nw, j, b->stream);
-    for (int q = 0; q < b->maxPace_general; ++q)
-      general_dynamic_slice(b->dW, b->nw, j, q, b->maxN_general, b->mixed, b->stream);
-    general_push(MODE_FWD, b->dW, b->nw, j, b->maxN_general, b->stream);
-    general_greens(MODE_FWD, b->dW, b->nw, j, -1, b->maxN_general, b->stream);
-    general_dynamic_stab(b->dW, b->nw, j, b->maxN_general, b->stream);
+    for (int q = 0; q < maxPace; ++q)
+      general_dynamic_slice(b->dW, b->nw, j, q, maxN, b->mixed, any_dense, any_cb, b->stream);
+    general_push(MODE_FWD, b->dW, b->nw, j, maxN, b->stream);
+    general_greens(MODE_FWD, b->dW, b->nw, j, -1, maxN, b->stream);
+    general_dynamic_stab(b->dW, b->nw, j, maxN, b->stream);
   }
-  general_dynamic_end(b->dW, b->nw, b->maxN_general, b->stream);
+  general_dynamic_end(b->dW, b->nw, maxN, b->stream);
   CUDA_TRY(cudaMemcpyAsync(b->dW, b->hw.data(), sizeof(WalkerDev) * b->nw, cudaMemcpyHostToDevice, b->stream));
   CUDA_TRY(cudaStreamSynchronize(b->stream));
   if (int r = launch_check("dynamic sweep")) return r;

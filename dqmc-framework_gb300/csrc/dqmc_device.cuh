@@ -98,7 +98,12 @@ struct WalkerDev {
   int trace_cap;
   int ozstab;                // 1: stabilization by the tensor-core blocked QR (kernels_stab_oz.cu)
   int widx;                  // index of the walker in its batch (Philox counter word)
+  // iteration limit of the wraps' and B-chain products' waits for their operands to land
+  // (oz_prod_tc_kernel); kDefaultWaitLimit unless a test lowers it (dqmc_set_wait_limit)
+  int wait_limit;
 };
+
+constexpr int kDefaultWaitLimit = 1 << 24;
 
 // Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11): uniform double in [0,1)
 // keyed by the walker's seed, counter (site attempt, half-sweep, walker).
@@ -117,6 +122,38 @@ __device__ __forceinline__ double philox_uniform(unsigned long long seed, unsign
   }
   const unsigned long long m = ((unsigned long long)(c0 >> 5) << 26) | (unsigned long long)(c1 >> 6);
   return (double)m * (1.0 / 9007199254740992.0);
+}
+
+// Metropolis ratio of flipping the field s of a site whose equal-time diagonals are
+// gu = G_up(i,i), gd = G_dn(i,i) (si = 0 for s = +1, 1 for s = -1):
+//   repulsive   r = (1 + (1 - gu)(e^{-2as} - 1)) (1 + (1 - gd)(e^{+2as} - 1))
+//   attractive  r = e^{2as} (1 + (1 - gu)(e^{-2as} - 1)) (1 + (1 - gd)(e^{-2as} - 1))
+// (get_update_ratio, src/model/repulsive_hubbard.cpp:112-124 and
+// src/model/attractive_hubbard.cpp:112-125), each operation rounded on its own in the
+// reference's order, never contracted into an FMA, so equal diagonals give bit-equal
+// ratios and decisions on every path.  Every Metropolis kernel evaluates it here.
+struct FlipRatio {
+  double r;       // the ratio
+  double ru, rd;  // its spin factors 1 + (1 - G_ii) Delta
+  double cu, cd;  // Delta_up, Delta_dn (e^{-+2as} - 1)
+};
+
+__device__ __forceinline__ FlipRatio flip_ratio(const WalkerDev& w, int si, double gu, double gd) {
+  FlipRatio q;
+  q.cu = w.cm[si];
+  q.cd = (w.model == 0) ? w.cp[si] : w.cm[si];
+  q.ru = __dadd_rn(1.0, __dmul_rn(__dsub_rn(1.0, gu), q.cu));
+  q.rd = __dadd_rn(1.0, __dmul_rn(__dsub_rn(1.0, gd), q.cd));
+  q.r = (w.model == 0) ? __dmul_rn(q.ru, q.rd) : __dmul_rn(__dmul_rn(w.ex2[si], q.ru), q.rd);
+  return q;
+}
+
+// The factors f_sigma = Delta_sigma / (1 + (1 - G_ii) Delta_sigma) of the accepted flip's
+// rank-1 update (update_greens_function, src/model/repulsive_hubbard.cpp:127-155; the
+// attractive model's factor_dn equals factor_up, src/model/attractive_hubbard.cpp:149).
+__device__ __forceinline__ void flip_factors(const WalkerDev& w, const FlipRatio& q, double* f) {
+  f[0] = __ddiv_rn(q.cu, q.ru);
+  f[1] = (w.model == 0) ? __ddiv_rn(q.cd, q.rd) : f[0];
 }
 
 __host__ __device__ inline double* stack_level(const WalkerDev& w, int side, int spin, int level) {

@@ -438,20 +438,15 @@ __global__ void __launch_bounds__(kThreads) segment_kernel(const WalkerDev* __re
             gu = at(Gs[0], ld, i, i);
             gd = at(Gs[1], ld, i, i);
           }
-          const double cu = w.cm[si];
-          const double cd = (w.model == 0) ? w.cp[si] : w.cm[si];
-          // same operation order as the reference, no contraction
-          const double ru = __dadd_rn(1.0, __dmul_rn(__dsub_rn(1.0, gu), cu));
-          const double rd = __dadd_rn(1.0, __dmul_rn(__dsub_rn(1.0, gd), cd));
-          const double r = (w.model == 0) ? __dmul_rn(ru, rd) : __dmul_rn(__dmul_rn(w.ex2[si], ru), rd);
+          const FlipRatio q = flip_ratio(w, si, gu, gd);  // reference operation order
+          const double r = q.r;
           const int attempt = (MODE == MODE_FWD) ? (eff * N + i) : ((Lt - t) * N + i);
           const double u = (w.rng == 0) ? w.uni[attempt]
                                         : philox_uniform(w.seed, (unsigned)w.widx, sweep, (unsigned)(eff * N + i));
           const double prob = fmin(1.0, fabs(r));
           if (!isfinite(r)) atomicOr(w.status, ST_NONFINITE_RATIO);
           if (u < prob) {
-            s_f[0] = __ddiv_rn(cu, ru);
-            s_f[1] = (w.model == 0) ? __ddiv_rn(cd, rd) : s_f[0];
+            flip_factors(w, q, s_f);
             s_field[i] = (int8_t)(-s);
             sign = (r >= 0) ? sign : -sign;
             ++acc_count;

@@ -286,6 +286,9 @@ __global__ void __launch_bounds__(256) gemm_op_kernel(const WalkerDev* __restric
 //   kind 1: wrap bwd  G <- G diag(e^+) P_A P_B ; G <- P_B^-1 P_A^-1 diag(e^-) G
 //   kind 2: chain fwd C <- diag(e^+) P_A P_B C
 //   kind 3: chain bwd C <- P_B P_A diag(e^+) C
+//   kind 4: time-displaced steps of the dynamic half-sweep (mult_B_from_left and
+//           mult_invB_from_right, src/dqmc_walker.cpp:455-466):
+//           G(t,0) <- diag(e^+) P_A P_B G(t-1,0),  G(0,t) <- G(0,t-1) P_B^-1 P_A^-1 diag(e^-)
 // --------------------------------------------------------------------------
 __device__ void cbg_pass(double* M, int N, int L, int parity, const double* P, bool left, const double* pre,
                          const double* post) {
@@ -349,6 +352,25 @@ __global__ void __launch_bounds__(256) cb_general_kernel(const WalkerDev* __rest
       cbg_pass(C, N, L, 0, w.cbP, true, dpos, nullptr); __syncthreads();
       cbg_pass(C, N, L, 1, w.cbP, true, nullptr, nullptr); __syncthreads();
       break;
+    case 4: {
+      if (!w.gt0) return;
+      // ping-pong slots [parity][S][N*N]: read slice t - 1's, write slice t's, then in place
+      const long long NN = (long long)N * N;
+      const double* a0 = w.gt0 + ((long long)((t - 1) & 1) * w.S + sp) * NN;
+      double* a1 = w.gt0 + ((long long)(t & 1) * w.S + sp) * NN;
+      const double* b0 = w.g0t + ((long long)((t - 1) & 1) * w.S + sp) * NN;
+      double* b1 = w.g0t + ((long long)(t & 1) * w.S + sp) * NN;
+      for (long long e = threadIdx.x; e < NN; e += blockDim.x) {
+        a1[e] = a0[e];
+        b1[e] = b0[e];
+      }
+      __syncthreads();
+      cbg_pass(a1, N, L, 1, w.cbP, true, nullptr, nullptr); __syncthreads();
+      cbg_pass(a1, N, L, 0, w.cbP, true, nullptr, dpos); __syncthreads();
+      cbg_pass(b1, N, L, 1, w.cbI, false, nullptr, nullptr); __syncthreads();
+      cbg_pass(b1, N, L, 0, w.cbI, false, nullptr, dneg); __syncthreads();
+      break;
+    }
   }
 }
 
@@ -411,19 +433,15 @@ __global__ void __launch_bounds__(kMetroThreads) metropolis_general_kernel(const
         gu = Gs[0][(long long)i * N + i];
         gd = Gs[1][(long long)i * N + i];
       }
-      const double cu = w.cm[si];
-      const double cd = (w.model == 0) ? w.cp[si] : w.cm[si];
-      const double ru = __dadd_rn(1.0, __dmul_rn(__dsub_rn(1.0, gu), cu));
-      const double rd = __dadd_rn(1.0, __dmul_rn(__dsub_rn(1.0, gd), cd));
-      const double r = (w.model == 0) ? __dmul_rn(ru, rd) : __dmul_rn(__dmul_rn(w.ex2[si], ru), rd);
+      const FlipRatio q = flip_ratio(w, si, gu, gd);  // reference operation order
+      const double r = q.r;
       const int attempt = (mode == MODE_FWD) ? (eff * N + i) : ((Lt - t) * N + i);
       const double u = (w.rng == 0) ? w.uni[attempt]
                                     : philox_uniform(w.seed, (unsigned)w.widx, sweep, (unsigned)(eff * N + i));
       const double prob = fmin(1.0, fabs(r));
       if (!isfinite(r)) atomicOr(w.status, ST_NONFINITE_RATIO);
       if (u < prob) {
-        s_f[0] = __ddiv_rn(cu, ru);
-        s_f[1] = (w.model == 0) ? __ddiv_rn(cd, rd) : s_f[0];
+        flip_factors(w, q, s_f);
         s_field[i] = (int8_t)(-s);
         sign = (r >= 0) ? sign : -sign;
         ++acc_count;
@@ -1299,20 +1317,33 @@ void general_slice_post(int mode, const WalkerDev* W, int nw, int j, int q, int 
   }
 }
 
-// one slice of the dynamic half-sweep: wrap, G(t,0) and G(0,t) steps, B-chain, G(k,tau)
-void general_dynamic_slice(const WalkerDev* W, int nw, int j, int q, int maxN, bool mixed, cudaStream_t st) {
+// one slice of the dynamic half-sweep: wrap, G(t,0) and G(0,t) steps, B-chain, G(k,tau);
+// dense walkers through the products (tensor-core wraps and chain on the mixed path),
+// checkerboard walkers through the plaquette passes
+void general_dynamic_slice(const WalkerDev* W, int nw, int j, int q, int maxN, bool mixed, bool any_dense,
+                           bool any_cb, cudaStream_t st) {
   const dim3 g = gemm_grid(maxN, nw);
-  if (mixed) {
-    mixed_wrap_fwd(W, nw, maxN, j, q, st);
-  } else {
-    gemm_op_kernel<OP_WL_FWD><<<g, 256, 0, st>>>(W, MODE_FWD, j, q, -1);
-    gemm_op_kernel<OP_WR_FWD><<<g, 256, 0, st>>>(W, MODE_FWD, j, q, -1);
+  const size_t cb_sm = sizeof(double) * 2 * maxN;
+  if (any_dense) {
+    if (mixed) {
+      mixed_wrap_fwd(W, nw, maxN, j, q, st);
+    } else {
+      gemm_op_kernel<OP_WL_FWD><<<g, 256, 0, st>>>(W, MODE_FWD, j, q, -1);
+      gemm_op_kernel<OP_WR_FWD><<<g, 256, 0, st>>>(W, MODE_FWD, j, q, -1);
+    }
+    gemm_op_kernel<OP_DT0><<<g, 256, 0, st>>>(W, MODE_FWD, j, q, -1);
+    gemm_op_kernel<OP_D0T><<<g, 256, 0, st>>>(W, MODE_FWD, j, q, -1);
   }
-  gemm_op_kernel<OP_DT0><<<g, 256, 0, st>>>(W, MODE_FWD, j, q, -1);
-  gemm_op_kernel<OP_D0T><<<g, 256, 0, st>>>(W, MODE_FWD, j, q, -1);
+  if (any_cb) {
+    cb_general_kernel<<<2 * nw, 256, cb_sm, st>>>(W, MODE_FWD, j, q, 0);
+    cb_general_kernel<<<2 * nw, 256, cb_sm, st>>>(W, MODE_FWD, j, q, 4);
+  }
   dyn_measure_kernel<<<nw, 256, sizeof(double) * 32, st>>>(W, j, q, 0);
-  if (mixed) mixed_chain(W, nw, maxN, MODE_FWD, j, q, st);
-  else gemm_op_kernel<OP_CH_FWD><<<g, 256, 0, st>>>(W, MODE_FWD, j, q, -1);
+  if (any_dense) {
+    if (mixed) mixed_chain(W, nw, maxN, MODE_FWD, j, q, st);
+    else gemm_op_kernel<OP_CH_FWD><<<g, 256, 0, st>>>(W, MODE_FWD, j, q, -1);
+  }
+  if (any_cb) cb_general_kernel<<<2 * nw, 256, cb_sm, st>>>(W, MODE_FWD, j, q, 2);
 }
 
 // stabilization of the dynamic pieces after general_greens of forward step j

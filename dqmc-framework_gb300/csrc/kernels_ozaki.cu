@@ -374,7 +374,8 @@ __global__ void __launch_bounds__(256, oz_tc_minb(S)) oz_prod_tc_kernel(const Wa
     const long long cstep = (long long)(ozaki::tc_lines(N) / 8) * 128;
     bool ok;
     s_last = oztc::mainloop<S, MT, NT, NS>(tsm, full, done, taddr, job.A + (long long)(r0 / 8) * 128,
-                                            job.B + (long long)(c0 / 8) * 128, sstride, cstep, ldk / 16, ok);
+                                            job.B + (long long)(c0 / 8) * 128, sstride, cstep, ldk / 16, ok,
+                                            w.wait_limit);
     s_fail = ok ? 0 : 1;
   }
   __syncthreads();

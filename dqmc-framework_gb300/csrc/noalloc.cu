@@ -2,10 +2,9 @@
 // allocate device memory.
 //
 // Some callers of this library cannot call cudaMalloc at the point where
-// they need a product: a CUDA-graph or stream capture in progress, a host
-// application whose device memory is owned by its own pool or framework (an
-// embedding that forbids allocation inside its time loop), or a plugin whose
-// host grants it no allocation rights.  dqmc_product_device_noalloc serves
+// they need a product: a host application whose device memory is owned by its
+// own pool or framework (an embedding that forbids allocation inside its time
+// loop), or a plugin whose host grants it no allocation rights.  dqmc_product_device_noalloc serves
 // them: the caller passes device buffers for A, B and C, and the BF16 slice
 // scratch lives in the file-scope array below, a fixed 1.75 MB reserved in
 // every GPU that loads the library until the process exits.
@@ -21,6 +20,7 @@
 
 #include "../../include/dqmc_gb300.h"
 #include "dqmc_device.cuh"
+#include "ozaki.cuh"
 
 namespace dqmc {
 cudaError_t configure_ozaki_kernels();
@@ -33,6 +33,11 @@ namespace {
 
 constexpr int kNoAllocMaxN = 256;                        // 7-bit x 7 slices, ldk = N
 constexpr size_t kSliceElems = 7ull * kNoAllocMaxN * kNoAllocMaxN;
+// the slicing kernel writes cfg_for_k(n).slices slices of n x ldk(n) elements per
+// operand; both grow with n, so the largest n bounds every call
+static_assert((size_t)dqmc::ozaki::cfg_for_k(kNoAllocMaxN).slices * kNoAllocMaxN * ((kNoAllocMaxN + 15) / 16 * 16) <=
+                  kSliceElems,
+              "no-alloc scratch too small for the slice configuration of its largest n");
 constexpr size_t kScratchBytes = 2 * kSliceElems * sizeof(unsigned short)  // A and B slices
                                  + 2 * kNoAllocMaxN * sizeof(int);          // row / column exponents
 
@@ -51,8 +56,15 @@ extern "C" int dqmc_product_device_noalloc(int n, const double* a, const double*
     return dqmc::set_last_error(DQMC_ERR_ARG,
                                 "dqmc_product_device_noalloc: n must be in [1, 256] (fixed 1.75 MB scratch)");
   if (!a || !b || !c) return dqmc::set_last_error(DQMC_ERR_ARG, "dqmc_product_device_noalloc: null pointer");
+  // an error left pending by the caller's own earlier work is theirs, not this call's:
+  // report it as such and launch nothing
+  cudaError_t e = cudaPeekAtLastError();
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return dqmc::set_last_error(DQMC_ERR_CUDA, "dqmc_product_device_noalloc: a CUDA error was pending before the call");
+  }
   int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
+  e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return dqmc::set_last_error(DQMC_ERR_CUDA, cudaGetErrorString(e));
   if (dev < 0 || dev >= kMaxDevices) return dqmc::set_last_error(DQMC_ERR_CUDA, "device ordinal out of range");
   void* base = nullptr;

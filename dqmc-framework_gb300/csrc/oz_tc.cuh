@@ -27,11 +27,13 @@ __host__ __device__ constexpr int stage_bytes(int S, int MT, int NT) { return S 
 // chunk 0; consecutive slices sstride elements apart, consecutive chunks cstep.
 // Returns the last chunk whose MMAs were committed (-1: none); ok = false on a
 // timeout.  The MMAs of chunk `ret` completing (done[ret % NS], parity
-// (ret / NS) & 1) means all of them have.
+// (ret / NS) & 1) means all of them have.  land_limit bounds the waits for a
+// chunk's operands to land; the waits that drain copies in flight after a
+// timeout keep the full limit, so no copy is outstanding when the loop returns.
 template <int S, int MT, int NT, int NS>
 __device__ int mainloop(unsigned char* tsm, unsigned long long* full, unsigned long long* done, unsigned taddr,
                         const unsigned short* a0, const unsigned short* b0, long long sstride, long long cstep,
-                        int nch, bool& ok) {
+                        int nch, bool& ok, int land_limit = 1 << 24) {
   constexpr int A_SL = MT * 32, B_SL = NT * 32, STAGE = stage_bytes(S, MT, NT);
   constexpr uint32_t idesc = tc::idesc_bf16(MT, NT);
   auto produce = [&](int c, int st) {
@@ -49,7 +51,7 @@ __device__ int mainloop(unsigned char* tsm, unsigned long long* full, unsigned l
   for (; produced < min(NS, nch); ++produced) produce(produced, produced);
   for (int c = 0; c < nch; ++c) {
     const int st = c % NS;
-    if (!tc::mbar_wait(&full[st], (c / NS) & 1)) { ok = false; break; }
+    if (!tc::mbar_wait(&full[st], (c / NS) & 1, land_limit)) { ok = false; break; }
     landed = c + 1;
     tc::fence_after();
     const unsigned sa = tc::su32(tsm + st * STAGE), sb = sa + S * A_SL;

@@ -28,7 +28,7 @@ constexpr int kMaxSlices = 8;
 struct SliceCfg {
   int bits, slices;
 };
-__host__ __device__ inline SliceCfg cfg_for_k(int K) { return K <= 256 ? SliceCfg{7, 7} : SliceCfg{6, 8}; }
+__host__ __device__ constexpr SliceCfg cfg_for_k(int K) { return K <= 256 ? SliceCfg{7, 7} : SliceCfg{6, 8}; }
 
 // The tensor-core image of a slice (the sweep's operands): k in chunks of 16,
 // 8-line blocks of 256 bytes in core-matrix order ((k / 8) * 128 + (line % 8) * 16

@@ -29,10 +29,10 @@ __device__ __forceinline__ void mbar_init(unsigned long long* mbar) {
 }
 __device__ __forceinline__ void mbar_fence_init() { asm volatile("fence.mbarrier_init.release.cluster;"); }
 
-// waits for completion of the mbarrier phase with this parity; false after the iteration limit
-__device__ __forceinline__ bool mbar_wait(unsigned long long* mbar, unsigned parity) {
+// waits for completion of the mbarrier phase with this parity; false after `limit` tries
+__device__ __forceinline__ bool mbar_wait(unsigned long long* mbar, unsigned parity, int limit = 1 << 24) {
   unsigned done = 0;
-  for (int it = 0; it < (1 << 24) && !done; ++it)
+  for (int it = 0; it < limit && !done; ++it)
     asm volatile(
         "{\n .reg .pred q;\n mbarrier.try_wait.parity.shared::cta.b64 q, [%1], %2;\n selp.u32 %0, 1, 0, q;\n}\n"
         : "=r"(done)

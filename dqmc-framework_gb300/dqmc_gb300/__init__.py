@@ -37,7 +37,7 @@ EXPORTS = [
     "dqmc_profile_enable", "dqmc_profile_read", "dqmc_microbench_fp64", "dqmc_get_observables_all",
     "dqmc_product_check", "dqmc_product_device_noalloc", "dqmc_launch_count", "dqmc_tuning",
     "dqmc_sweep_dynamic", "dqmc_get_dynamic", "dqmc_clear_dynamic", "dqmc_get_green_dynamic", "dqmc_get_dynamic_obs",
-    "dqmc_get_dynamic_r", "dqmc_measure_bins", "dqmc_set_green",
+    "dqmc_get_dynamic_r", "dqmc_measure_bins", "dqmc_set_green", "dqmc_set_wait_limit",
 ]
 KCLASSES = ["segment", "push", "greens", "measure", "product", "metropolis"]
 
@@ -99,6 +99,7 @@ def load() -> ctypes.CDLL:
         "dqmc_get_dynamic_r": (c, [vp, c, dp]),
         "dqmc_measure_bins": (c, [vp, c, c, c, dp]),
         "dqmc_set_green": (c, [vp, c, c, dp]),
+        "dqmc_set_wait_limit": (c, [vp, c]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -278,6 +279,10 @@ class Batch:
 
     def trace_clear(self):
         _check(load().dqmc_trace_clear(self.h))
+
+    def set_wait_limit(self, limit: int):
+        """Test hook: iteration limit of the tensor-core products' operand waits (-1: default)."""
+        _check(load().dqmc_set_wait_limit(self.h, int(limit)))
 
     def profile_enable(self, on: bool = True):
         _check(load().dqmc_profile_enable(self.h, int(on)))

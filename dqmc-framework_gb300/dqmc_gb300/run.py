@@ -59,9 +59,8 @@ def run(cfg: dio.RunConfig, out_dir: str, walkers: int = 1, seed: int = 12345, f
     descs = [dq.WalkerDesc(model=model, L=L, t=cfg.hopping_t, U=cfg.onsite_u, mu=cfg.chemical_potential,
                            beta=cfg.beta, Lt=lt, pace=cfg.stabilization_pace, checkerboard=cfg.checkerboard,
                            momentum_index=kidx, seed=seed + rank * walkers + w) for w in range(walkers)]
-    # the dynamic half-sweep runs on the HBM path, which walkers with N <= 64 take only when asked
     b = dq.Batch(descs, rng=dq.RNG_PHILOX if rng == "philox" else dq.RNG_MINSTD,
-                 precision=dq.MIXED if precision == "mixed" else dq.FP64, hbm=bool(cfg.dynamic))
+                 precision=dq.MIXED if precision == "mixed" else dq.FP64)
     if rank == 0:
         log.write(">> Configurations of the bosonic fields "
                   + ("read from the input config file.\n\n" if fields_file else "set to random.\n\n"))

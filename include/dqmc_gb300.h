@@ -99,7 +99,7 @@ typedef struct dqmc_batch_options {
   int graphs;          /* 1: capture each kind of half-sweep once into a CUDA graph and replay
                           it (ignored while tracing or profiling) */
   int hbm;             /* 1: every walker on the HBM path, whatever its size (N <= 64 walkers
-                          otherwise live in shared memory; dqmc_sweep_dynamic needs this) */
+                          otherwise live in shared memory) */
 } dqmc_batch_options;
 
 typedef struct dqmc_batch dqmc_batch;
@@ -147,10 +147,11 @@ int dqmc_sweep_beta_to_0(dqmc_batch* b, int measure);
  * includes the equal-time G), and G(k,tau) = sign/N sum_ij FF(r_j - r_i)
  * (G_up(tau,0)(j,i) + G_dn(tau,0)(j,i))/2 is accumulated for the walker's
  * momentum at each listed tau in [0, Lt) (tau = 0 from G(beta,beta)).  Needs
- * the stacks of t = 0 (after dqmc_init_greens or dqmc_sweep_beta_to_0) and
- * every walker on the HBM path (N > 64 or DQMC_MIXED), dense exp(-dtau K);
- * stabilizes with the FP64 kernels.  A new tau list (at most 256 entries)
- * restarts the accumulators. */
+ * the stacks of t = 0 (after dqmc_init_greens or dqmc_sweep_beta_to_0).  Any
+ * walker: dense or checkerboard exp(-dtau K), shared-memory walkers (N <= 64)
+ * included (they run this half-sweep on the HBM path's kernels); stabilizes
+ * with the FP64 kernels.  A new tau list (at most 256 entries) restarts the
+ * accumulators. */
 int dqmc_sweep_dynamic(dqmc_batch* b, const int* taus, int ntau);
 /* Sums of sign * G(k,tau) and their counts, in the order of the last tau list. */
 int dqmc_get_dynamic(dqmc_batch* b, int walker, double* sums, int64_t* counts);
@@ -231,6 +232,12 @@ enum { DQMC_KCLASS_SEGMENT = 0, DQMC_KCLASS_PUSH = 1, DQMC_KCLASS_GREENS = 2, DQ
        DQMC_KCLASS_METROPOLIS = 5,  /* HBM walkers: Metropolis updates of a slice (+ fused measurement) */
        DQMC_NUM_KCLASS = 6 };
 int dqmc_profile_enable(dqmc_batch* b, int on);
+/* Test hook of the failure detection (no reference counterpart): the iteration limit of
+ * the waits in which the tensor-core wrap and B-chain products wait for their operands to
+ * land (default 2^24; 0 gives up at once).  A product whose wait runs out drains the copies
+ * it issued, skips its output and sets status bit 8 of its walker; the batch's other work
+ * and other batches are unaffected.  limit < 0 restores the default. */
+int dqmc_set_wait_limit(dqmc_batch* b, int limit);
 int dqmc_profile_read(dqmc_batch* b, int kclass, double* total_ms, int64_t* launches);
 
 /* The mixed-precision product engine on host matrices: C = A B for column-major
@@ -238,14 +245,16 @@ int dqmc_profile_read(dqmc_batch* b, int kclass, double* total_ms, int64_t* laun
  * (no reference counterpart: it exposes the engine for validation). */
 int dqmc_product_check(int n, const double* a, const double* b, double* c);
 
-/* The same product for callers that cannot allocate device memory (inside a
- * CUDA-graph capture, or under a host framework that owns all device memory):
- * a, b, c are the caller's device buffers (column-major n x n doubles) and the
- * BF16 slice scratch is a fixed 1.75 MB array in the library's device image, so
- * the call allocates nothing.  Limit: n <= 256 (larger n is rejected with
- * DQMC_ERR_ARG).  All calls on a device share that scratch: calls that overlap
- * on the GPU race, so the caller serialises them.  The first call on a device
- * resolves the scratch address and must come before any stream capture.
+/* The same product for callers that cannot allocate device memory: a host
+ * framework that owns every device buffer through its own pool, or a time loop
+ * that forbids allocation once it runs.  a, b, c are the caller's device buffers
+ * (column-major n x n doubles) and the BF16 slice scratch is a fixed 1.75 MB
+ * array in the library's device image, so the call allocates nothing.  Limit:
+ * n <= 256 (larger n is rejected with DQMC_ERR_ARG).  All calls on a device share
+ * that scratch: calls that overlap on the GPU race, so the caller serialises them.
+ * The first call on a device resolves the scratch address; make it before any
+ * stream capture.  A CUDA error already pending from the caller's own work is
+ * reported (DQMC_ERR_CUDA) before anything is launched.
  * No counterpart in the reference (it has no device code). */
 int dqmc_product_device_noalloc(int n, const double* a, const double* b, double* c, void* cuda_stream);
 

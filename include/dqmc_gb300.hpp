@@ -110,8 +110,7 @@ class DqmcWalker {
     pace_ = pace;
   }
   // one walker per seed; rng = DQMC_RNG_MINSTD reproduces the reference stream; precision
-  // DQMC_MIXED selects the tensor-core path; hbm puts every walker on the HBM path (the
-  // dynamic half-sweep needs it for N <= 64)
+  // DQMC_MIXED selects the tensor-core path; hbm puts every walker on the HBM path
   void initial(const Square& lat, const Model& model, const std::vector<uint64_t>& seeds,
                int rng = DQMC_RNG_MINSTD, int precision = DQMC_FP64, bool hbm = false) {
     std::vector<dqmc_walker_desc> d(seeds.size());

@@ -153,7 +153,7 @@ def test_dynamic_run(fake, tmp_path):
     cfg = dio.parse_config(CONFIG % '"all"')
     res = drv.run(cfg, str(tmp_path), walkers=3, log=open(os.devnull, "w"))
     b = fake.created[0]
-    assert b.hbm  # the dynamic half-sweep needs the HBM path at N = 16
+    assert not b.hbm  # shared-memory walkers run the dynamic half-sweep too
     # ceil(5 / 3) = 2 bins of 2 dynamic + backward pairs; forward half-sweeps only in warm-up and between
     assert b.half["dyn"] == 2 * 2 and b.half["fwd"] == 2 + 2 * 1 and b.half["bwd"] == 2 + 2 * 2 + 2 * 1
     dos = open(tmp_path / "dos.out").read().splitlines()

@@ -30,16 +30,23 @@ def _close(a, b, rel=REL):
     return abs(np.asarray(a) - np.asarray(b)).max() <= rel * scale
 
 
-@pytest.mark.parametrize("model,L,mu,Lt,pace", [
-    (0, 9, 0.0, 20, 5),     # repulsive, odd side, N = 81
-    (1, 10, -0.5, 24, 8),   # attractive, N = 100
+@pytest.mark.parametrize("model,L,mu,Lt,pace,cb", [
+    (0, 9, 0.0, 20, 5, False),     # repulsive, odd side, N = 81
+    (1, 10, -0.5, 24, 8, False),   # attractive, N = 100
+    (0, 8, 0.0, 20, 5, True),      # checkerboard break-up, shared-memory walker (N = 64)
+    (0, 10, 0.0, 20, 5, True),     # checkerboard, HBM walker (N = 100)
+    (1, 6, -0.3, 16, 4, False),    # shared-memory walker (N = 36)
 ])
-def test_dynamic_sweep_against_oracle(dq, oracle_mod, model, L, mu, Lt, pace):
+def test_dynamic_sweep_against_oracle(dq, oracle_mod, model, L, mu, Lt, pace, cb):
+    """Shared-memory walkers (N <= 64) run the dynamic half-sweep on the HBM path's kernels
+    and return to their own path for the backward half-sweep; checkerboard walkers take
+    G(t,0) and G(0,t) through the plaquette passes (mult_B_from_left / mult_invB_from_right
+    of the model's checkerboard link, src/dqmc_walker.cpp:455-466)."""
     O = oracle_mod
     O.use_scipy_lapack(False)
-    d = dq.WalkerDesc(model=model, L=L, U=4.0, mu=mu, beta=2.0, Lt=Lt, pace=pace, seed=61)
+    d = dq.WalkerDesc(model=model, L=L, U=4.0, mu=mu, beta=2.0, Lt=Lt, pace=pace, checkerboard=cb, seed=61)
     b = dq.Batch([d], rng=dq.RNG_MINSTD)
-    r = O.Walker(model=model, L=L, U=4.0, mu=mu, beta=2.0, Lt=Lt, pace=pace, stack=O.STACK_QRP)
+    r = O.Walker(model=model, L=L, U=4.0, mu=mu, beta=2.0, Lt=Lt, pace=pace, checkerboard=cb, stack=O.STACK_QRP)
     r.seed(61)
     b.fields_random(0)
     r.fields_random()
@@ -124,11 +131,8 @@ def test_dynamic_sweep_state_and_arguments(dq):
         b.sweep_dynamic([0])          # stacks at beta
     b.sweep_beta_to_0()
     b.sweep_dynamic([0, 4])
-    small = dq.Batch([dq.WalkerDesc(model=0, L=4, U=4.0, beta=1.0, Lt=10, pace=5, seed=2)], rng=dq.RNG_PHILOX)
-    small.fields_random(0)
-    small.init_greens()
     with pytest.raises(dq.DqmcError):
-        small.sweep_dynamic([0])      # shared-memory walkers
+        b.sweep_dynamic([0])          # stacks at beta again
 
 
 @pytest.mark.parametrize("model,L,mu,Lt,pace", [

@@ -1,8 +1,8 @@
 """The zero-allocation product entry point (dqmc_product_device_noalloc).
 
-Callers that cannot allocate device memory at the point of the call (a stream
-or graph capture in progress, or a host framework that owns every device
-buffer) pass their own device buffers for A, B and C; the slice scratch is a
+Callers that cannot allocate device memory at the point of the call (a host
+framework that owns every device buffer through its own pool, or a time loop
+that forbids allocation once it runs) pass their own device buffers for A, B and C; the slice scratch is a
 fixed array inside the library.  This checks, through the C-ABI, that two
 calls in a row give the same products as the allocating entry point
 dqmc_product_check, within the product engine's accuracy bound (2^-38 of
