@@ -413,7 +413,10 @@ def observable_deviation(mixed, fp64, names, write_bin):
     for k, name in enumerate(names):
         d = float(abs(vm[:, k].mean() - vf[:, k].mean()))
         se = float(vf[:, k].std(ddof=1) / np.sqrt(n)) if n > 1 else 0.0
-        out[name] = {"abs_diff": d, "fp64_stderr": se, "in_stderr": d / se if se > 0 else None}
+        # an observable the walkers share to rounding (the filling at half filling, the sign of a
+        # sign-free model) has no statistical error to compare against
+        spread = se > 1e-12 * max(1.0, float(abs(vf[:, k]).max()))
+        out[name] = {"abs_diff": d, "fp64_stderr": se, "in_stderr": d / se if spread else None}
     return out
 
 
@@ -654,15 +657,18 @@ def run_gpu(args, wl, rank, world):
     model = {}  # class -> (bound, algorithmic flops in the profiled steps, peak TFLOP/s, what is counted)
     extra = {}
     if mixed:
-        prod = push = greens = bf_met = fp_met = ref_rank1 = 0.0
+        prod = push = greens = bf_met = fp_met = ref_rank1 = dynp = 0.0
         met_what = ""
         for d, a in zip(descs, acc_w):
             N, S = d.L ** 2, (1 if d.model == 1 else 2)
             ns = -(-d.Lt // d.pace)
             pairs = slice_pairs(wrap_slices(N))
-            # forward: 2 wraps + chain; backward: chain + 2 wraps: 3 products per slice of an
-            # updating half-sweep (the profiled replays cover the graph-captured half-sweeps)
-            prod += steps * S * d.Lt * 3 * pairs * 2 * N ** 3
+            # forward: 2 wraps + chain; backward: chain + 2 wraps: 3 products per slice of a
+            # half-sweep; a step of the dynamic workload is two half-sweeps, whose dynamic one
+            # adds the G(t,0) and G(0,t) steps (2 products per slice, class "dynamic")
+            prod += steps * S * d.Lt * 3 * pairs * 2 * N ** 3 * (2 if dyn else 1)
+            if dyn:
+                dynp += steps * S * d.Lt * 2 * pairs * 2 * N ** 3
             if N >= 128:
                 pf, gf = stab_tensor_flops(N)
                 sp = slice_pairs(8 if N <= 256 else 9)
@@ -675,8 +681,15 @@ def run_gpu(args, wl, rank, world):
         model["product"] = ("tensor", prod, bf16_peak,
                             "BF16 flops of the exact-slice wrap and B-chain products: 3 per slice x slice pairs "
                             "(28 for N <= 256, 36 above) x 2N^3")
+        if dyn:
+            model["dynamic"] = ("tensor", dynp, bf16_peak,
+                                "BF16 flops of the G(t,0), G(0,t) steps of the dynamic half-sweep (2 products "
+                                "per slice x slice pairs x 2N^3); its G(k,tau) measurement runs in the same class")
         if push > 0:
-            model["push"] = ("tensor", push, bf16_peak,
+            # the dynamic half-sweep's push and equal-time assembly run in the same classes
+            # (its assembly for tensor-core walkers is timed under dynamic_stab): counted as
+            # many blocked-QR products again in push, not in greens
+            model["push"] = ("tensor", push * (2 if dyn else 1), bf16_peak,
                              "BF16 flops of the blocked-QR products (36 slice pairs, 45 for N > 256)")
             model["greens"] = ("tensor", greens, bf16_peak,
                                "BF16 flops of the Green's-assembly products (36 slice pairs, 45 for N > 256)")

@@ -55,13 +55,19 @@ void launch_metropolis_sub(const WalkerDev* W, int nw, int mode, int j, int q, i
 int delayed_pick_kd(int N, int S);
 void general_chain_init(int mode, const WalkerDev* W, int nw, int j, cudaStream_t st);
 void general_push(int mode, const WalkerDev* W, int nw, int j, int maxN, cudaStream_t st);
-void general_dynamic_slice(const WalkerDev* W, int nw, int j, int q, int maxN, bool mixed, bool any_dense,
+void general_dynamic_wrap(const WalkerDev* W, int nw, int j, int q, int maxN, bool mixed, bool any_dense,
+                          bool any_cb, cudaStream_t st);
+void general_dynamic_prop(const WalkerDev* W, int nw, int j, int q, int maxN, bool mixed, bool any_dense,
+                          bool any_cb, cudaStream_t st);
+void general_dynamic_chain(const WalkerDev* W, int nw, int j, int q, int maxN, bool mixed, bool any_dense,
                            bool any_cb, cudaStream_t st);
 void general_dynamic_stab(const WalkerDev* W, int nw, int j, int maxN, cudaStream_t st);
+void general_dynamic_stab_measure(const WalkerDev* W, int nw, int j, cudaStream_t st);
 void general_dynamic_begin(const WalkerDev* W, int nw, cudaStream_t st);
 void general_dynamic_end(const WalkerDev* W, int nw, int maxN, cudaStream_t st);
 void oz_push(int mode, const WalkerDev* W, int nw, int j, int maxN, cudaStream_t st);
-void oz_greens(int mode, const WalkerDev* W, int nw, int j, int trace_slot, int maxN, cudaStream_t st);
+void oz_greens(int mode, const WalkerDev* W, int nw, int j, int trace_slot, int maxN, cudaStream_t st,
+               bool dyn = false);
 cudaError_t configure_stab_oz_kernels(int maxN);
 void general_greens(int mode, const WalkerDev* W, int nw, int j, int trace_slot, int maxN, cudaStream_t st);
 void general_measure_after(int mode, const WalkerDev* W, int nw, int j, int maxN, cudaStream_t st);
@@ -1075,15 +1081,15 @@ int dqmc_sweep_dynamic(dqmc_batch* b, const int* taus, int ntau) {
     for (auto& h : b->hw) h.dyn_ntau = ntau;
     if (int r = dqmc_clear_dynamic(b)) return r;
   }
-  // the dynamic half-sweep stabilizes every walker with the FP64 kernels; shared-memory
-  // walkers run it on the HBM path's kernels with their own buffers (the stacks, G and the
-  // fields are laid out alike on both paths)
+  // walkers of the tensor-core path with 128 <= N <= 768 stabilize with the blocked QR
+  // (oz_push, oz_greens with the second right-hand side), the others with the FP64 kernels;
+  // shared-memory walkers run this half-sweep on the HBM path's kernels with their own
+  // buffers (the stacks, G and the fields are laid out alike on both paths)
   std::vector<WalkerDev> hv = b->hw;
   int maxN = 0, maxPace = 0;
   bool any_dense = false, any_cb = false;
   for (int w = 0; w < b->nw; ++w) {
     WalkerDev& h = hv[w];
-    h.ozstab = 0;
     if (h.path == 0) {
       h.path = 1;
       h.chain = b->dyn_gen[w].chain;
@@ -1095,16 +1101,34 @@ int dqmc_sweep_dynamic(dqmc_batch* b, const int* taus, int ntau) {
     if (h.cb) any_cb = true; else any_dense = true;
   }
   CUDA_TRY(cudaMemcpyAsync(b->dW, hv.data(), sizeof(WalkerDev) * b->nw, cudaMemcpyHostToDevice, b->stream));
-  general_dynamic_begin(b->dW, b->nw, b->stream);
+  const cudaStream_t st = b->stream;
+  const WalkerDev* W = b->dW;
+  const int nw = b->nw;
+  b->timed(DQMC_KCLASS_DYNAMIC, [&] { general_dynamic_begin(W, nw, st); });
   for (int j = 0; j < b->maxNs; ++j) {
-    general_chain_init(MODE_FWD, b->dW, b->nw, j, b->stream);
-    for (int q = 0; q < maxPace; ++q)
-      general_dynamic_slice(b->dW, b->nw, j, q, maxN, b->mixed, any_dense, any_cb, b->stream);
-    general_push(MODE_FWD, b->dW, b->nw, j, maxN, b->stream);
-    general_greens(MODE_FWD, b->dW, b->nw, j, -1, maxN, b->stream);
-    general_dynamic_stab(b->dW, b->nw, j, maxN, b->stream);
+    b->timed(DQMC_KCLASS_SEGMENT, [&] { general_chain_init(MODE_FWD, W, nw, j, st); });
+    for (int q = 0; q < maxPace; ++q) {
+      b->timed(DQMC_KCLASS_PRODUCT,
+               [&] { general_dynamic_wrap(W, nw, j, q, maxN, b->mixed, any_dense, any_cb, st); });
+      b->timed(DQMC_KCLASS_DYNAMIC,
+               [&] { general_dynamic_prop(W, nw, j, q, maxN, b->mixed, any_dense, any_cb, st); });
+      b->timed(DQMC_KCLASS_PRODUCT,
+               [&] { general_dynamic_chain(W, nw, j, q, maxN, b->mixed, any_dense, any_cb, st); });
+    }
+    b->timed(DQMC_KCLASS_PUSH, [&] {
+      general_push(MODE_FWD, W, nw, j, maxN, st);
+      if (b->any_ozstab) oz_push(MODE_FWD, W, nw, j, b->maxN_oz, st);
+    });
+    b->timed(DQMC_KCLASS_GREENS, [&] { general_greens(MODE_FWD, W, nw, j, -1, maxN, st); });
+    // the tensor-core walkers' equal-time assembly and their G(t,0), G(0,t) come from one
+    // oz_greens (one factorization of M), timed in this class
+    b->timed(DQMC_KCLASS_DYN_STAB, [&] {
+      general_dynamic_stab(W, nw, j, maxN, st);
+      if (b->any_ozstab) oz_greens(MODE_FWD, W, nw, j, -1, b->maxN_oz, st, true);
+      general_dynamic_stab_measure(W, nw, j, st);
+    });
   }
-  general_dynamic_end(b->dW, b->nw, maxN, b->stream);
+  b->timed(DQMC_KCLASS_DYNAMIC, [&] { general_dynamic_end(W, nw, maxN, st); });
   CUDA_TRY(cudaMemcpyAsync(b->dW, b->hw.data(), sizeof(WalkerDev) * b->nw, cudaMemcpyHostToDevice, b->stream));
   CUDA_TRY(cudaStreamSynchronize(b->stream));
   if (int r = launch_check("dynamic sweep")) return r;

@@ -96,7 +96,7 @@ __global__ void __launch_bounds__(256) gemm_op_kernel(const WalkerDev* __restric
   const bool slice_op = OP <= OP_CH_BWD || dyn_prop;
   if ((dyn_prop || dyn_out) && !w.gt0) return;
   if (slice_op && w.cb) return;  // checkerboard walkers take cb_general_kernel (expK is null for them)
-  if (slice_op && !dyn_prop && w.path == 2) return;  // mixed walkers take the tensor-core products
+  if (slice_op && w.path == 2) return;  // mixed walkers take the tensor-core products
   if (slice_op && !slice_of(w, mode, j, q, t, nsl, t_hi)) return;
   if (!slice_op && j >= w.nstack) return;
   if (!slice_op && w.ozstab) return;  // stabilized by kernels_stab_oz.cu
@@ -1036,7 +1036,7 @@ __global__ void __launch_bounds__(256) dyn_init_kernel(const WalkerDev* __restri
 __global__ void __launch_bounds__(1024) dyn_resolve_kernel(const WalkerDev* __restrict__ W, int j) {
   const int wi = blockIdx.x >> 1, sp = blockIdx.x & 1;
   const WalkerDev& w = W[wi];
-  if (!w.gt0 || sp >= w.S || j >= w.nstack) return;
+  if (!w.gt0 || w.ozstab || sp >= w.S || j >= w.nstack) return;  // tensor-core walkers: oz_greens
   const int N = w.N;
   const long long NN = (long long)N * N;
   const int nl = j + 1;  // forward step j: left stack holds j + 1 levels
@@ -1074,7 +1074,7 @@ __global__ void __launch_bounds__(1024) dyn_resolve_kernel(const WalkerDev* __re
 __global__ void __launch_bounds__(256) dyn_boundary_kernel(const WalkerDev* __restrict__ W, int j) {
   const int wi = blockIdx.y >> 1, sp = blockIdx.y & 1;
   const WalkerDev& w = W[wi];
-  if (!w.gt0 || sp >= w.S || j != w.nstack - 1) return;
+  if (!w.gt0 || w.ozstab || sp >= w.S || j != w.nstack - 1) return;
   const int N = w.N;
   const long long NN = (long long)N * N;
   const int par = w.Lt & 1;
@@ -1262,6 +1262,7 @@ static dim3 gemm_grid(int maxN, int nw) {
 void mixed_wrap_fwd(const WalkerDev* W, int nw, int maxN, int j, int q, cudaStream_t st);
 void mixed_wrap_bwd(const WalkerDev* W, int nw, int maxN, int j, int q, cudaStream_t st);
 void mixed_chain(const WalkerDev* W, int nw, int maxN, int mode, int j, int q, cudaStream_t st);
+void mixed_dynamic_prop(const WalkerDev* W, int nw, int maxN, int j, int q, cudaStream_t st);
 
 void launch_metropolis_delayed(bool mixed, const WalkerDev* W, int nw, int mode, int j, int q, int maxN, int S_max,
                                int KD, int tc_flush, cudaStream_t st);
@@ -1317,13 +1318,13 @@ void general_slice_post(int mode, const WalkerDev* W, int nw, int j, int q, int 
   }
 }
 
-// one slice of the dynamic half-sweep: wrap, G(t,0) and G(0,t) steps, B-chain, G(k,tau);
-// dense walkers through the products (tensor-core wraps and chain on the mixed path),
-// checkerboard walkers through the plaquette passes
-void general_dynamic_slice(const WalkerDev* W, int nw, int j, int q, int maxN, bool mixed, bool any_dense,
-                           bool any_cb, cudaStream_t st) {
+// One slice of the dynamic half-sweep in three launch groups (timed apart by the host):
+// the wrap; the G(t,0) and G(0,t) steps with the G(k,tau) measurement; the B-chain step.
+// Dense walkers through the products (on the tensor cores for mixed walkers),
+// checkerboard walkers through the plaquette passes.
+void general_dynamic_wrap(const WalkerDev* W, int nw, int j, int q, int maxN, bool mixed, bool any_dense,
+                          bool any_cb, cudaStream_t st) {
   const dim3 g = gemm_grid(maxN, nw);
-  const size_t cb_sm = sizeof(double) * 2 * maxN;
   if (any_dense) {
     if (mixed) {
       mixed_wrap_fwd(W, nw, maxN, j, q, st);
@@ -1331,22 +1332,37 @@ void general_dynamic_slice(const WalkerDev* W, int nw, int j, int q, int maxN, b
       gemm_op_kernel<OP_WL_FWD><<<g, 256, 0, st>>>(W, MODE_FWD, j, q, -1);
       gemm_op_kernel<OP_WR_FWD><<<g, 256, 0, st>>>(W, MODE_FWD, j, q, -1);
     }
-    gemm_op_kernel<OP_DT0><<<g, 256, 0, st>>>(W, MODE_FWD, j, q, -1);
-    gemm_op_kernel<OP_D0T><<<g, 256, 0, st>>>(W, MODE_FWD, j, q, -1);
   }
-  if (any_cb) {
-    cb_general_kernel<<<2 * nw, 256, cb_sm, st>>>(W, MODE_FWD, j, q, 0);
-    cb_general_kernel<<<2 * nw, 256, cb_sm, st>>>(W, MODE_FWD, j, q, 4);
+  if (any_cb) cb_general_kernel<<<2 * nw, 256, sizeof(double) * 2 * maxN, st>>>(W, MODE_FWD, j, q, 0);
+}
+
+void general_dynamic_prop(const WalkerDev* W, int nw, int j, int q, int maxN, bool mixed, bool any_dense,
+                          bool any_cb, cudaStream_t st) {
+  const dim3 g = gemm_grid(maxN, nw);
+  if (any_dense) {
+    if (mixed) {
+      mixed_dynamic_prop(W, nw, maxN, j, q, st);
+    } else {
+      gemm_op_kernel<OP_DT0><<<g, 256, 0, st>>>(W, MODE_FWD, j, q, -1);
+      gemm_op_kernel<OP_D0T><<<g, 256, 0, st>>>(W, MODE_FWD, j, q, -1);
+    }
   }
+  if (any_cb) cb_general_kernel<<<2 * nw, 256, sizeof(double) * 2 * maxN, st>>>(W, MODE_FWD, j, q, 4);
   dyn_measure_kernel<<<nw, 256, sizeof(double) * 32, st>>>(W, j, q, 0);
+}
+
+void general_dynamic_chain(const WalkerDev* W, int nw, int j, int q, int maxN, bool mixed, bool any_dense,
+                           bool any_cb, cudaStream_t st) {
+  const dim3 g = gemm_grid(maxN, nw);
   if (any_dense) {
     if (mixed) mixed_chain(W, nw, maxN, MODE_FWD, j, q, st);
     else gemm_op_kernel<OP_CH_FWD><<<g, 256, 0, st>>>(W, MODE_FWD, j, q, -1);
   }
-  if (any_cb) cb_general_kernel<<<2 * nw, 256, cb_sm, st>>>(W, MODE_FWD, j, q, 2);
+  if (any_cb) cb_general_kernel<<<2 * nw, 256, sizeof(double) * 2 * maxN, st>>>(W, MODE_FWD, j, q, 2);
 }
 
-// stabilization of the dynamic pieces after general_greens of forward step j
+// stabilization of the dynamic pieces after general_greens of forward step j (walkers
+// stabilized by the tensor-core blocked QR get theirs from oz_greens)
 void general_dynamic_stab(const WalkerDev* W, int nw, int j, int maxN, cudaStream_t st) {
   const dim3 g = gemm_grid(maxN, nw);
   const int threads = std::min(1024, ((maxN + 31) / 32) * 32);
@@ -1354,6 +1370,9 @@ void general_dynamic_stab(const WalkerDev* W, int nw, int j, int maxN, cudaStrea
   gemm_op_kernel<OP_DT0_OUT><<<g, 256, 0, st>>>(W, MODE_FWD, j, 0, -1);
   gemm_op_kernel<OP_D0T_OUT><<<g, 256, 0, st>>>(W, MODE_FWD, j, 0, -1);
   dyn_boundary_kernel<<<dim3(64, 2 * nw), 256, 0, st>>>(W, j);
+}
+// G(k,tau) measurement at the stabilization slice of forward step j (after both paths)
+void general_dynamic_stab_measure(const WalkerDev* W, int nw, int j, cudaStream_t st) {
   dyn_measure_kernel<<<nw, 256, sizeof(double) * 32, st>>>(W, j, 0, 1);
 }
 

@@ -270,7 +270,17 @@ __device__ __forceinline__ double* oz_chain(const WalkerDev& w, int spin, int wh
 //   OZ_CH_BWD  chain' = expK^T diag(e+) chain    (A: expK^T = expK as B-slices, B: diag(e+) chain)
 //   OZ_WR_BWD  work   = G diag(e+) expK          (A: G diag(e+), B: expK const)
 //   OZ_WL_BWD  G      = expK^-1 diag(e-) work    (A: invK const, B: diag(e-) work)
-enum OzOp { OZ_WL_FWD = 0, OZ_WR_FWD = 1, OZ_CH_FWD = 2, OZ_CH_BWD = 3, OZ_WR_BWD = 4, OZ_WL_BWD = 5 };
+// and the time-displaced steps of the dynamic half-sweep (the reference's
+// mult_B_from_left and mult_invB_from_right, src/dqmc_walker.cpp:455-466), on the
+// ping-pong slots [parity][S][N*N] of G(t,0) and G(0,t):
+//   OZ_DT0     G(t,0) = diag(e+) expK G(t-1,0)   (A: expK const, B: G(t-1,0))
+//   OZ_D0T     G(0,t) = G(0,t-1) expK^-1 diag(e-) (A: G(0,t-1),   B: invK const)
+enum OzOp { OZ_WL_FWD = 0, OZ_WR_FWD = 1, OZ_CH_FWD = 2, OZ_CH_BWD = 3, OZ_WR_BWD = 4, OZ_WL_BWD = 5,
+            OZ_DT0 = 6, OZ_D0T = 7 };
+
+__device__ __forceinline__ double* oz_dyn(double* base, const WalkerDev& w, int spin, int t) {
+  return base + ((long long)(t & 1) * w.S + spin) * w.N * w.N;
+}
 
 // slice the per-walker operand of op OP: grid (ceil(N/32), 2*nw), 256 threads
 template <int OP>
@@ -292,7 +302,10 @@ __global__ void __launch_bounds__(256) oz_slice_kernel(const WalkerDev* __restri
     case OZ_CH_BWD: X = oz_chain(w, sp, q & 1); role = 1; sgn = +1; break;
     case OZ_WR_BWD: X = w.G + sp * NN; role = 0; sgn = +1; break;
     case OZ_WL_BWD: X = w.work + sp * NN; role = 1; sgn = -1; break;
+    case OZ_DT0: X = w.gt0 ? oz_dyn(w.gt0, w, sp, t - 1) : nullptr; role = 1; break;
+    case OZ_D0T: X = w.g0t ? oz_dyn(w.g0t, w, sp, t - 1) : nullptr; role = 0; break;
   }
+  if (!X) return;
   if (sgn)
     for (int k = threadIdx.x; k < N; k += blockDim.x) s_pre[k] = oz_bscale(w, t, sp, sgn, k);
   __syncthreads();
@@ -340,7 +353,10 @@ __global__ void __launch_bounds__(256, oz_tc_minb(S)) oz_prod_tc_kernel(const Wa
     case OZ_CH_BWD: job = ProdJob{w.kB, ws, w.kBe, we}; out = oz_chain(w, sp, (q + 1) & 1); break;
     case OZ_WR_BWD: job = ProdJob{ws, w.kB, we, w.kBe}; out = w.work + sp * NN; break;
     case OZ_WL_BWD: job = ProdJob{w.iA, ws, w.iAe, we}; out = w.G + sp * NN; break;
+    case OZ_DT0: job = ProdJob{w.kA, ws, w.kAe, we}; out = w.gt0 ? oz_dyn(w.gt0, w, sp, t) : nullptr; break;
+    case OZ_D0T: job = ProdJob{ws, w.iB, we, w.iBe}; out = w.g0t ? oz_dyn(w.g0t, w, sp, t) : nullptr; break;
   }
+  if (!out) return;
   extern __shared__ __align__(1024) unsigned char tsm[];
   __shared__ int eA[MT], eB[NT];
   __shared__ double s_scale[MT];  // exp(+-alpha s) of the output rows (or columns)
@@ -350,9 +366,9 @@ __global__ void __launch_bounds__(256, oz_tc_minb(S)) oz_prod_tc_kernel(const Wa
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   if (tid < MT) eA[tid] = (r0 + tid < N) ? job.ea[r0 + tid] : -1100;
   if (tid < NT) eB[tid] = (c0 + tid < N) ? job.eb[c0 + tid] : -1100;
-  if (OP == OZ_WL_FWD || OP == OZ_CH_FWD) {
+  if (OP == OZ_WL_FWD || OP == OZ_CH_FWD || OP == OZ_DT0) {
     if (tid < MT) s_scale[tid] = (r0 + tid < N) ? oz_bscale(w, t, sp, +1, r0 + tid) : 0.0;
-  } else if (OP == OZ_WR_FWD) {
+  } else if (OP == OZ_WR_FWD || OP == OZ_D0T) {
     if (tid < NT) s_scale[tid] = (c0 + tid < N) ? oz_bscale(w, t, sp, -1, c0 + tid) : 0.0;
   }
   if (tid == 0) {
@@ -404,8 +420,8 @@ __global__ void __launch_bounds__(256, oz_tc_minb(S)) oz_prod_tc_kernel(const Wa
           for (int m = 4; m < S; ++m) lo = (lo << SB) + (long long)__float2int_rn(__uint_as_float(v[m][u]));
           const int e = eA[rl] + eB[cl];
           double val = ozaki::combine_hilo<S, (S <= 7 ? 7 : 6)>(hi, lo, e);
-          if (OP == OZ_WL_FWD || OP == OZ_CH_FWD) val *= s_scale[rl];
-          if (OP == OZ_WR_FWD) val *= s_scale[cl];
+          if (OP == OZ_WL_FWD || OP == OZ_CH_FWD || OP == OZ_DT0) val *= s_scale[rl];
+          if (OP == OZ_WR_FWD || OP == OZ_D0T) val *= s_scale[cl];
           out[(long long)col * N + r] = val;
         }
       }
@@ -447,6 +463,8 @@ cudaError_t configure_ozaki_kernels() {
   OZCFG(7, oz_prod_tc_kernel<OZ_CH_BWD, 7>); OZCFG(7, oz_prod_tc_kernel<OZ_WR_BWD, 7>); OZCFG(7, oz_prod_tc_kernel<OZ_WL_BWD, 7>);
   OZCFG(8, oz_prod_tc_kernel<OZ_WL_FWD, 8>); OZCFG(8, oz_prod_tc_kernel<OZ_WR_FWD, 8>); OZCFG(8, oz_prod_tc_kernel<OZ_CH_FWD, 8>);
   OZCFG(8, oz_prod_tc_kernel<OZ_CH_BWD, 8>); OZCFG(8, oz_prod_tc_kernel<OZ_WR_BWD, 8>); OZCFG(8, oz_prod_tc_kernel<OZ_WL_BWD, 8>);
+  OZCFG(7, oz_prod_tc_kernel<OZ_DT0, 7>); OZCFG(7, oz_prod_tc_kernel<OZ_D0T, 7>);
+  OZCFG(8, oz_prod_tc_kernel<OZ_DT0, 8>); OZCFG(8, oz_prod_tc_kernel<OZ_D0T, 8>);
 #undef OZCFG
   if ((e = cudaFuncSetAttribute(oz_selftest_prod_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)oz_prod_smem(8))))
@@ -473,6 +491,11 @@ void mixed_wrap_fwd(const WalkerDev* W, int nw, int maxN, int j, int q, cudaStre
 void mixed_chain(const WalkerDev* W, int nw, int maxN, int mode, int j, int q, cudaStream_t st) {
   if (mode == MODE_FWD) oz_op<OZ_CH_FWD>(W, nw, maxN, mode, j, q, st);
   else oz_op<OZ_CH_BWD>(W, nw, maxN, mode, j, q, st);
+}
+// the time-displaced steps of the dynamic half-sweep for mixed walkers
+void mixed_dynamic_prop(const WalkerDev* W, int nw, int maxN, int j, int q, cudaStream_t st) {
+  oz_op<OZ_DT0>(W, nw, maxN, MODE_FWD, j, q, st);
+  oz_op<OZ_D0T>(W, nw, maxN, MODE_FWD, j, q, st);
 }
 void mixed_wrap_bwd(const WalkerDev* W, int nw, int maxN, int j, int q, cudaStream_t st) {
   oz_op<OZ_WR_BWD>(W, nw, maxN, MODE_BWD, j, q, st);

@@ -17,6 +17,11 @@
 //           R^-1 Q^T Y by blocked reflector application and blocked back
 //           substitution (FP64 diagonal blocks); G = U_R Drmax^-1 X.  Boundary
 //           steps (one stack empty) form M = Y + Dmin F and G = X or X^T.
+//   dynamic half-sweep (compute_dynamic_greens, include/utils/numerical_stable.hpp:
+//           246-325): the same factorization of M also solves the second
+//           right-hand side Y2 = Dlmin F_L, X2 = M^-1 Y2; then G(t,0) = U_R
+//           Drmax^-1 X2 and G(0,t) = -F_R^T Drmin X (at t = beta, right stack
+//           empty: G(beta,0) = X2, G(0,beta) = -X).
 // Every product slices its two FP64 operands once (zslice_kernel, tensor-core
 // images) into 8 integer slices of 7 bits (56 significant bits, K <= 256) or 9
 // of 6 (54 bits, K <= 1024) and multiplies them on the BF16 tensor cores with
@@ -104,8 +109,14 @@ struct ZJob {
   int neg;             // 1: the product enters negated (an operand modifier, no FP64 multiply)
   const double* rs;    // row multiplier of the product, or null
   const double* cs;    // column multiplier, or null
-  int out;             // 1: Green's function output (wrap error, trace, spin copy)
+  int out;             // 1: Green's function output (wrap error, trace, spin copy);
+                       // 2: time-displaced output (wrap error against the propagated value)
 };
+
+// the ping-pong slot of G(t,0) or G(0,t) at slice t ([parity][S][N*N])
+__device__ __forceinline__ double* zdyn_slot(double* base, const WalkerDev& w, int sp, int t) {
+  return base + ((long long)(t & 1) * w.S + sp) * w.N * w.N;
+}
 
 __device__ __forceinline__ double zel(const ZOpnd& o, int i, int k, bool isB) {
   const int row = (o.tr != (int)isB) ? k : i;
@@ -134,6 +145,12 @@ enum ZOp {
   Z_AQ_UPD,      // Y(j0:, :) -= V_p Wb
   Z_TR_UPD,      // Y(j0:j0+pb, :) -= R(j0:j0+pb, j0+pb:) Y(j0+pb:, :)
   Z_GG,          // G = U_R Drmax^-1 X
+  // the dynamic half-sweep's second right-hand side Y2 (dynx) and outputs
+  Z_AQ2_W,       // Wb = (V_p T_p)^T Y2(j0:, :)
+  Z_AQ2_UPD,     // Y2(j0:, :) -= V_p Wb
+  Z_TR2_UPD,     // Y2(j0:j0+pb, :) -= R(j0:j0+pb, j0+pb:) Y2(j0+pb:, :)
+  Z_DT0_OUT,     // G(t,0) = U_R Drmax^-1 X2
+  Z_D0T_OUT,     // G(0,t) = -F_R^T Drmin X
 };
 
 __device__ bool zjob(const WalkerDev& w, int op, int mode, int j, int p, int sp, ZJob& jb) {
@@ -231,12 +248,50 @@ __device__ bool zjob(const WalkerDev& w, int op, int mode, int j, int p, int sp,
       }
       return true;
     }
-    case Z_TR_UPD: {
+    case Z_TR_UPD:
+    case Z_TR2_UPD: {
       if (j0 + pb >= N) return false;
+      if (op == Z_TR2_UPD && !w.dynx) return false;
+      double* Yr = (op == Z_TR_UPD) ? z.Y : w.dynx + sp * NN;
       jb.a = ZOpnd{z.X + (long long)(j0 + pb) * N + j0, N, 0, 0, nullptr, nullptr};
-      jb.b = ZOpnd{z.Y + j0 + pb, N, 0, 0, nullptr, nullptr};
-      jb.c = z.Y + j0; jb.ldc = N; jb.M = pb; jb.N = N; jb.K = N - j0 - pb;
+      jb.b = ZOpnd{Yr + j0 + pb, N, 0, 0, nullptr, nullptr};
+      jb.c = Yr + j0; jb.ldc = N; jb.M = pb; jb.N = N; jb.K = N - j0 - pb;
       jb.beta = 1; jb.neg = 1;
+      return true;
+    }
+    case Z_AQ2_W:
+    case Z_AQ2_UPD: {
+      if (!w.dynx) return false;
+      double* Y2 = w.dynx + sp * NN;
+      if (op == Z_AQ2_W) {
+        jb.a = VtT;
+        jb.b = ZOpnd{Y2 + j0, N, 0, 0, nullptr, nullptr};
+        jb.c = z.Wb; jb.ldc = TB; jb.M = pb; jb.N = N; jb.K = m;
+      } else {
+        jb.a = Vp;
+        jb.b = Wbo;
+        jb.c = Y2 + j0; jb.ldc = N; jb.M = m; jb.N = N; jb.K = pb;
+        jb.beta = 1; jb.neg = 1;
+      }
+      return true;
+    }
+    case Z_DT0_OUT:
+    case Z_D0T_OUT: {
+      // forward step j of the dynamic half-sweep, both stacks present
+      if (!w.gt0 || !w.dynx || mode != MODE_FWD || !(nl > 0 && nr > 0)) return false;
+      const int t_end = min((j + 1) * w.pace, w.Lt);
+      const double* UR = stack_level(w, 1, sp, nr - 1);
+      if (op == Z_DT0_OUT) {
+        jb.a = ZOpnd{UR, N, 0, 0, nullptr, z.drmaxi};
+        jb.b = ZOpnd{w.dynx + sp * NN, N, 0, 0, nullptr, nullptr};
+        jb.c = zdyn_slot(w.gt0, w, sp, t_end);
+      } else {
+        jb.a = ZOpnd{UR + NN, N, 1, 0, nullptr, z.drmin};  // F_R^T, times Drmin along k
+        jb.b = ZOpnd{z.Y, N, 0, 0, nullptr, nullptr};
+        jb.c = zdyn_slot(w.g0t, w, sp, t_end);
+        jb.neg = 1;
+      }
+      jb.ldc = N; jb.M = N; jb.N = N; jb.K = N; jb.out = 2;
       return true;
     }
   }
@@ -418,7 +473,7 @@ __global__ void __launch_bounds__(256, MINB) zgemm_tc_kernel(const WalkerDev* __
   bool finite = true;
   double* tr = (jb.out && w.trace && trace_slot >= 0 && trace_slot < w.trace_cap)
                    ? w.trace + ((long long)trace_slot * 2 + sp) * NN : nullptr;
-  const bool check = jb.out && !(mode == MODE_INIT || (mode == MODE_BWD && j == w.nstack - 1));
+  const bool check = (jb.out == 2) || (jb.out && !(mode == MODE_INIT || (mode == MODE_BWD && j == w.nstack - 1)));
   const int q4 = warp & 3, half = warp >> 2;
   const int rl = q4 * 32 + lane, r = r0 + rl;
   // K <= 32: every group sum is below 2^22 and converts with an FP32 add (the conversion
@@ -454,6 +509,11 @@ __global__ void __launch_bounds__(256, MINB) zgemm_tc_kernel(const WalkerDev* __
         if (!jb.out) {
           if (jb.neg) val = -val;
           jb.c[o] = jb.beta ? jb.c[o] + val : val;
+        } else if (jb.out == 2) {
+          if (jb.neg) val = -val;
+          err = fmax(err, fabs(val - jb.c[o]));
+          if (!isfinite(val)) finite = false;
+          jb.c[o] = val;
         } else {
           if (check) err = fmax(err, fabs(val - jb.c[o]));
           if (!isfinite(val)) finite = false;
@@ -714,11 +774,14 @@ __global__ void __launch_bounds__(256) zgreens_prep_kernel(const WalkerDev* __re
   }
 }
 
-// back substitution of the diagonal block p: R_pp X(j0:j0+pb, c) = Y(j0:j0+pb, c), thread per column
-__global__ void __launch_bounds__(128) ztrsm_diag_kernel(const WalkerDev* __restrict__ W, int mode, int j, int p) {
+// back substitution of the diagonal block p: R_pp X(j0:j0+pb, c) = Y(j0:j0+pb, c), thread per
+// column; rhs 0: Y, 1: the dynamic half-sweep's second right-hand side (dynx)
+__global__ void __launch_bounds__(128) ztrsm_diag_kernel(const WalkerDev* __restrict__ W, int mode, int j, int p,
+                                                         int rhs) {
   const int wi = blockIdx.y >> 1, sp = blockIdx.y & 1;
   const WalkerDev& w = W[wi];
   if (!w.ozstab || sp >= w.S || j >= w.nstack) return;
+  if (rhs && !w.dynx) return;
   const int N = w.N, j0 = p * TB;
   if (j0 >= N) return;
   const int pb = min(TB, N - j0);
@@ -738,7 +801,7 @@ __global__ void __launch_bounds__(128) ztrsm_diag_kernel(const WalkerDev* __rest
   __syncthreads();
   const int c = blockIdx.x * 128 + threadIdx.x;
   if (c >= N) return;
-  double* y = z.Y + (long long)c * N + j0;
+  double* y = (rhs ? w.dynx + (long long)sp * N * N : z.Y) + (long long)c * N + j0;
   double x[TB];
 #pragma unroll
   for (int i = 0; i < TB; ++i) x[i] = (i < pb) ? y[i] : 0.0;
@@ -792,6 +855,50 @@ __global__ void __launch_bounds__(256) zgreens_out_kernel(const WalkerDev* __res
   }
 }
 
+// dynamic half-sweep, forward step j: the second right-hand side Y2 = min(D_L, 1) F_L of the
+// left stack's top level, column-major into dynx
+__global__ void __launch_bounds__(256) zdyn_prep_kernel(const WalkerDev* __restrict__ W, int j) {
+  const int wi = blockIdx.y >> 1, sp = blockIdx.y & 1;
+  const WalkerDev& w = W[wi];
+  if (!w.ozstab || !w.dynx || sp >= w.S || j >= w.nstack) return;
+  const int N = w.N;
+  const long long NN = (long long)N * N;
+  const double* lv = stack_level(w, 0, sp, j);  // forward step j: left stack of j + 1 levels
+  const double* F = lv + NN;
+  const double* D = lv + 2 * NN;
+  double* Y2 = w.dynx + sp * NN;
+  for (long long e = blockIdx.x * 256LL + threadIdx.x; e < NN; e += (long long)gridDim.x * 256) {
+    const int r = (int)(e % N);
+    Y2[e] = fmin(D[r], 1.0) * F[e];
+  }
+}
+
+// dynamic half-sweep at t = beta (right stack empty): G(beta,0) = X2, G(0,beta) = -X, with
+// their wrap errors against the propagated values
+__global__ void __launch_bounds__(256) zdyn_boundary_kernel(const WalkerDev* __restrict__ W, int j) {
+  const int wi = blockIdx.y >> 1, sp = blockIdx.y & 1;
+  const WalkerDev& w = W[wi];
+  if (!w.ozstab || !w.gt0 || !w.dynx || sp >= w.S || j != w.nstack - 1) return;
+  const int N = w.N;
+  const long long NN = (long long)N * N;
+  const ZScr z = zscr(w, sp);
+  double* t0 = zdyn_slot(w.gt0, w, sp, w.Lt);
+  double* ot = zdyn_slot(w.g0t, w, sp, w.Lt);
+  const double* X2 = w.dynx + sp * NN;
+  double err = 0.0;
+  bool finite = true;
+  for (long long e = blockIdx.x * 256LL + threadIdx.x; e < NN; e += (long long)gridDim.x * 256) {
+    const double a = X2[e], b = -z.Y[e];
+    err = fmax(err, fmax(fabs(a - t0[e]), fabs(b - ot[e])));
+    if (!isfinite(a) || !isfinite(b)) finite = false;
+    t0[e] = a;
+    ot[e] = b;
+  }
+  if (!finite) atomicOr(w.status, ST_NONFINITE_G);
+  for (int o = 16; o > 0; o >>= 1) err = fmax(err, __shfl_xor_sync(0xffffffffu, err, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(w.wrap_bits, (unsigned long long)__double_as_longlong(err));
+}
+
 // --------------------------------------------------------------------------
 // host side
 // --------------------------------------------------------------------------
@@ -840,9 +947,12 @@ void oz_push(int mode, const WalkerDev* W, int nw, int j, int maxN, cudaStream_t
   }
 }
 
-void oz_greens(int mode, const WalkerDev* W, int nw, int j, int trace_slot, int maxN, cudaStream_t st) {
+// The Green's assembly; with dyn (forward steps of the dynamic half-sweep) the same
+// factorization of M also solves the second right-hand side and G(t,0), G(0,t) follow.
+void oz_greens(int mode, const WalkerDev* W, int nw, int j, int trace_slot, int maxN, cudaStream_t st, bool dyn) {
   const int np = (maxN + TB - 1) / TB;
   zgreens_prep_kernel<<<dim3(64, 2 * nw), 256, 0, st>>>(W, mode, j);
+  if (dyn) zdyn_prep_kernel<<<dim3(64, 2 * nw), 256, 0, st>>>(W, j);
   zgemm(W, nw, maxN, Z_GA, mode, j, 0, maxN, maxN, -1, st);
   zgemm(W, nw, maxN, Z_GB, mode, j, 0, maxN, maxN, -1, st);
   for (int p = 0; p < np; ++p) {
@@ -851,13 +961,26 @@ void oz_greens(int mode, const WalkerDev* W, int nw, int j, int trace_slot, int 
     zgemm(W, nw, maxN, Z_QR_UPD, mode, j, p, maxN, maxN, -1, st);
     zgemm(W, nw, maxN, Z_AQ_W, mode, j, p, TB, maxN, -1, st);
     zgemm(W, nw, maxN, Z_AQ_UPD, mode, j, p, maxN, maxN, -1, st);
+    if (dyn) {
+      zgemm(W, nw, maxN, Z_AQ2_W, mode, j, p, TB, maxN, -1, st);
+      zgemm(W, nw, maxN, Z_AQ2_UPD, mode, j, p, maxN, maxN, -1, st);
+    }
   }
   for (int p = np - 1; p >= 0; --p) {
     zgemm(W, nw, maxN, Z_TR_UPD, mode, j, p, TB, maxN, -1, st);
-    ztrsm_diag_kernel<<<dim3((maxN + 127) / 128, 2 * nw), 128, 0, st>>>(W, mode, j, p);
+    ztrsm_diag_kernel<<<dim3((maxN + 127) / 128, 2 * nw), 128, 0, st>>>(W, mode, j, p, 0);
+    if (dyn) {
+      zgemm(W, nw, maxN, Z_TR2_UPD, mode, j, p, TB, maxN, -1, st);
+      ztrsm_diag_kernel<<<dim3((maxN + 127) / 128, 2 * nw), 128, 0, st>>>(W, mode, j, p, 1);
+    }
   }
   zgemm(W, nw, maxN, Z_GG, mode, j, 0, maxN, maxN, trace_slot, st);
   zgreens_out_kernel<<<dim3(64, 2 * nw), 256, 0, st>>>(W, mode, j, trace_slot);
+  if (dyn) {
+    zgemm(W, nw, maxN, Z_DT0_OUT, mode, j, 0, maxN, maxN, -1, st);
+    zgemm(W, nw, maxN, Z_D0T_OUT, mode, j, 0, maxN, maxN, -1, st);
+    zdyn_boundary_kernel<<<dim3(64, 2 * nw), 256, 0, st>>>(W, j);
+  }
 }
 
 }  // namespace dqmc

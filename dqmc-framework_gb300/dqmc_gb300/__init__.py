@@ -39,7 +39,7 @@ EXPORTS = [
     "dqmc_sweep_dynamic", "dqmc_get_dynamic", "dqmc_clear_dynamic", "dqmc_get_green_dynamic", "dqmc_get_dynamic_obs",
     "dqmc_get_dynamic_r", "dqmc_measure_bins", "dqmc_set_green", "dqmc_set_wait_limit",
 ]
-KCLASSES = ["segment", "push", "greens", "measure", "product", "metropolis"]
+KCLASSES = ["segment", "push", "greens", "measure", "product", "metropolis", "dynamic", "dynamic_stab"]
 
 
 class DqmcError(RuntimeError):

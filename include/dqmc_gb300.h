@@ -149,9 +149,11 @@ int dqmc_sweep_beta_to_0(dqmc_batch* b, int measure);
  * momentum at each listed tau in [0, Lt) (tau = 0 from G(beta,beta)).  Needs
  * the stacks of t = 0 (after dqmc_init_greens or dqmc_sweep_beta_to_0).  Any
  * walker: dense or checkerboard exp(-dtau K), shared-memory walkers (N <= 64)
- * included (they run this half-sweep on the HBM path's kernels); stabilizes
- * with the FP64 kernels.  A new tau list (at most 256 entries) restarts the
- * accumulators. */
+ * included (they run this half-sweep on the HBM path's kernels).  On the
+ * DQMC_MIXED path the G(t,0), G(0,t) steps run on the tensor cores and walkers
+ * with 128 <= N <= 768 stabilize with the blocked Householder QR (one
+ * factorization of M for both right-hand sides); the others with the FP64
+ * kernels.  A new tau list (at most 256 entries) restarts the accumulators. */
 int dqmc_sweep_dynamic(dqmc_batch* b, const int* taus, int ntau);
 /* Sums of sign * G(k,tau) and their counts, in the order of the last tau list. */
 int dqmc_get_dynamic(dqmc_batch* b, int walker, double* sums, int64_t* counts);
@@ -230,7 +232,9 @@ int dqmc_launch_count(dqmc_batch* b, int64_t* launches);
 enum { DQMC_KCLASS_SEGMENT = 0, DQMC_KCLASS_PUSH = 1, DQMC_KCLASS_GREENS = 2, DQMC_KCLASS_MEASURE = 3,
        DQMC_KCLASS_PRODUCT = 4,     /* HBM walkers: dense products of a slice (wraps, B-chain step) */
        DQMC_KCLASS_METROPOLIS = 5,  /* HBM walkers: Metropolis updates of a slice (+ fused measurement) */
-       DQMC_NUM_KCLASS = 6 };
+       DQMC_KCLASS_DYNAMIC = 6,     /* dynamic half-sweep: the G(t,0), G(0,t) steps and G(k,tau) measurement */
+       DQMC_KCLASS_DYN_STAB = 7,    /* dynamic half-sweep: G(t,0), G(0,t) recomputed at a stabilization */
+       DQMC_NUM_KCLASS = 8 };
 int dqmc_profile_enable(dqmc_batch* b, int on);
 /* Test hook of the failure detection (no reference counterpart): the iteration limit of
  * the waits in which the tensor-core wrap and B-chain products wait for their operands to
