@@ -372,7 +372,7 @@ def block_accepts_sq(p_acc: float, kb: int = 32) -> float:
 def metropolis_work(d, accepts: float, tc_flush: int, kd: int):
     """Work one walker's Metropolis executes in a half-sweep with `accepts` accepted flips, by
     the kind the autotuner picked: (bf16 tensor flops, FP64 flops, what).
-      submatrix (tc_flush 2): per 32-site block with m accepts, Gamma's m x m products and the
+      submatrix (tc_flush 2, or 3 split per block): per 32-site block with m accepts, Gamma's m x m products and the
         rank-1 updates of the block in FP64, T = Gamma R_A (N x m x m) and the flush
         G -= G0(:, I_A) T (N x N x m) as 6 x 7-bit slice products (21 pairs);
       delayed (tc_flush 0 / 1): the corrected diagonal and the u, w vectors per accept in FP64
@@ -383,7 +383,7 @@ def metropolis_work(d, accepts: float, tc_flush: int, kd: int):
     p_acc = accepts / (N * Lt) if N * Lt else 0.0
     m2 = block_accepts_sq(p_acc) * nb * Lt  # sum over blocks of m^2 in the half-sweep
     m3 = (32 * p_acc) ** 3 * nb * Lt  # and of m^3 (mean-field)
-    if tc_flush == 2:
+    if tc_flush in (2, 3):
         bf16 = S * 21 * 2 * (N * N * accepts + N * m2)
         fp64 = S * (accepts * 2 * 32 * 32 / 3 + 2 * m2 * 32 + 2 * m3 / 3)
         what = ("submatrix updates: flush and T as 21 bf16 slice pairs of 2 N^2 m + 2 N m^2 per block; "

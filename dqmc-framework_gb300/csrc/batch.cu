@@ -52,6 +52,8 @@ cudaError_t configure_delayed_kernels();
 cudaError_t configure_submatrix_kernel();
 size_t submatrix_scratch_bytes(int N);
 void launch_metropolis_sub(const WalkerDev* W, int nw, int mode, int j, int q, int maxN, int S_max, cudaStream_t st);
+void launch_metropolis_sub_split(const WalkerDev* W, int nw, int mode, int j, int q, int maxN, int S_max,
+                                 cudaStream_t st);
 int delayed_pick_kd(int N, int S);
 void general_chain_init(int mode, const WalkerDev* W, int nw, int j, cudaStream_t st);
 void general_push(int mode, const WalkerDev* W, int nw, int j, int maxN, cudaStream_t st);
@@ -110,8 +112,9 @@ int fail(int code, const char* fmt, ...) {
     if (e_ != cudaSuccess) return fail(DQMC_ERR_CUDA, "%s: %s", #expr, cudaGetErrorString(e_)); \
   } while (0)
 
-// exp(x K) for symmetric K by cyclic Jacobi diagonalisation (host, once per batch).
-std::vector<double> sym_exp(int n, std::vector<double> a, double x) {
+// exp(x K) and exp(-x K) for symmetric K by one cyclic Jacobi diagonalisation (host, once
+// per lattice in a batch).
+std::pair<std::vector<double>, std::vector<double>> sym_exp_pair(int n, std::vector<double> a, double x) {
   auto A = [&](int r, int c) -> double& { return a[(size_t)c * n + r]; };
   std::vector<double> v((size_t)n * n, 0.0);
   auto V = [&](int r, int c) -> double& { return v[(size_t)c * n + r]; };
@@ -145,15 +148,18 @@ std::vector<double> sym_exp(int n, std::vector<double> a, double x) {
         }
       }
   }
-  std::vector<double> out((size_t)n * n, 0.0);
-  for (int m = 0; m < n; ++m) {
-    const double e = std::exp(x * A(m, m));
-    for (int c = 0; c < n; ++c) {
-      const double vc = V(c, m) * e;
-      for (int r = 0; r < n; ++r) out[(size_t)c * n + r] += V(r, m) * vc;
+  auto form = [&](double y) {
+    std::vector<double> out((size_t)n * n, 0.0);
+    for (int m = 0; m < n; ++m) {
+      const double e = std::exp(y * A(m, m));
+      for (int c = 0; c < n; ++c) {
+        const double vc = V(c, m) * e;
+        for (int r = 0; r < n; ++r) out[(size_t)c * n + r] += V(r, m) * vc;
+      }
     }
-  }
-  return out;
+    return out;
+  };
+  return {form(x), form(-x)};
 }
 
 // K = -t H + mu I on the periodic square lattice (src/lattice/square.cpp:164-177,
@@ -210,7 +216,8 @@ struct dqmc_batch {
   bool mixed = false;
   int kd = 0, smax = 1;  // delayed-update block size of the general walkers (0: rank-1 kernel)
   // Metropolis of HBM walkers: 0 delayed with FP64 flush, 1 delayed with tensor-core
-  // flush, 2 submatrix updates with tensor-core flush (mixed walkers)
+  // flush, 2 submatrix updates with tensor-core flush (mixed walkers, one CTA per walker),
+  // 3 the same split per 32-site block into a decision and a multi-CTA flush kernel
   int tc_flush = 1;
   bool tuned = false;
   std::vector<std::pair<std::pair<int, int>, float>> tune_log;  // ((kd, tc), ms) per candidate
@@ -404,7 +411,7 @@ int dqmc_batch_create(const dqmc_walker_desc* descs, int n, const dqmc_batch_opt
       if (it == dense_ids.end()) {
         const auto K = kinetic_matrix(d.L, d.hopping_t, d.mu);
         const double dt = d.beta / d.Lt;
-        dense.push_back({sym_exp(N, K, -dt), sym_exp(N, K, +dt)});
+        dense.push_back(sym_exp_pair(N, K, -dt));
         it = dense_ids.emplace(key, (int)dense.size() - 1).first;
       }
       off[w].dense_id = it->second;
@@ -703,16 +710,28 @@ static int launch_check(const char* what) {
 // for each candidate (block size k, update kind) on the batch's own state,
 // restoring G, the fields and the walker scalars after each trial, and keeps
 // the fastest.  Candidates: delayed updates with k in {32, 16, 8} that fit
-// shared memory; on the mixed path, submatrix updates (k = 32) and each
-// delayed k with the tensor-core flush and with the FP64 flush.
+// shared memory; on the mixed path, submatrix updates (k = 32) fused in one
+// kernel per walker and split per block (decision and multi-CTA flush kernels),
+// and each delayed k with the tensor-core flush and with the FP64 flush.
 static int autotune_delayed(dqmc_batch* b) {
   std::vector<std::pair<int, int>> cand;
   const int kmax = b->kd;
-  if (b->mixed) cand.push_back({32, 2});
+  if (b->mixed) {
+    cand.push_back({32, 2});
+    cand.push_back({32, 3});
+  }
   for (int kd : {32, 16, 8}) {
     if (kd > kmax) continue;
     if (b->mixed && kd >= 16) cand.push_back({kd, 1});
     cand.push_back({kd, 0});
+  }
+  // DQMC_METROPOLIS_KIND=0..3 keeps only the candidates of that update kind (tests)
+  if (const char* env = std::getenv("DQMC_METROPOLIS_KIND")) {
+    const int kind = std::atoi(env);
+    std::vector<std::pair<int, int>> keep;
+    for (auto c : cand)
+      if (c.second == kind) keep.push_back(c);
+    if (!keep.empty()) cand = keep;
   }
   // back up what one Metropolis slice changes: G (spins < S) into work, fields into scr
   std::vector<dqmc_batch::Scal> scal(b->nw);
@@ -735,6 +754,8 @@ static int autotune_delayed(dqmc_batch* b) {
       cudaEventRecord(e0, b->stream);
       if (c.second == 2)
         launch_metropolis_sub(b->dW, b->nw, MODE_FWD, 0, 0, b->maxN_general, b->smax, b->stream);
+      else if (c.second == 3)
+        launch_metropolis_sub_split(b->dW, b->nw, MODE_FWD, 0, 0, b->maxN_general, b->smax, b->stream);
       else
         launch_metropolis_delayed(b->mixed, b->dW, b->nw, MODE_FWD, 0, 0, b->maxN_general, b->smax, c.first,
                                   c.second, b->stream);

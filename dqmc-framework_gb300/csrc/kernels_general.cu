@@ -1267,6 +1267,8 @@ void mixed_dynamic_prop(const WalkerDev* W, int nw, int maxN, int j, int q, cuda
 void launch_metropolis_delayed(bool mixed, const WalkerDev* W, int nw, int mode, int j, int q, int maxN, int S_max,
                                int KD, int tc_flush, cudaStream_t st);
 void launch_metropolis_sub(const WalkerDev* W, int nw, int mode, int j, int q, int maxN, int S_max, cudaStream_t st);
+void launch_metropolis_sub_split(const WalkerDev* W, int nw, int mode, int j, int q, int maxN, int S_max,
+                                 cudaStream_t st);
 
 // One slice of general walkers in three launch groups (timed separately by the
 // host): the dense products before the updates (forward wrap), the Metropolis
@@ -1291,6 +1293,7 @@ void general_slice_metro(int mode, const WalkerDev* W, int nw, int j, int q, int
   if (mode == MODE_INIT) return;
   const size_t met_sm = sizeof(double) * 6 * maxN + maxN + 16;
   if (mixed && tc_flush == 2) launch_metropolis_sub(W, nw, mode, j, q, maxN, smax, st);
+  else if (mixed && tc_flush == 3) launch_metropolis_sub_split(W, nw, mode, j, q, maxN, smax, st);
   else if (kd > 0) launch_metropolis_delayed(mixed, W, nw, mode, j, q, maxN, smax, kd, tc_flush, st);
   else metropolis_general_kernel<<<nw, kMetroThreads, met_sm, st>>>(W, mode, j, q);
   if (measure) measure_general_kernel<<<nw, 256, sizeof(double) * 2 * maxN, st>>>(W, mode, j, q, 0);

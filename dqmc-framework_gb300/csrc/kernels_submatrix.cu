@@ -32,6 +32,7 @@
 // reference's unless a ratio lies within rounding of its uniform.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdint>
 
 #include "dqmc_device.cuh"
@@ -59,7 +60,7 @@ __host__ __device__ inline size_t al256(size_t x) { return (x + 255) & ~(size_t)
 // per-spin scratch in HBM (WalkerDev::msub): the operands' slices as tensor-core
 // images (ozaki::tc_index, k stride 32) and the line exponents
 struct SubOff {
-  size_t sGm, sG, sR, sT, eGm, eG, eR, eT, total;
+  size_t sGm, sG, sR, sT, eGm, eG, eR, eT, mc, total;
 };
 __host__ __device__ inline size_t sub_sst(int N) { return (size_t)ozaki::tc_lines(N) * KB; }
 __host__ __device__ inline SubOff sub_offsets(int N) {
@@ -73,7 +74,8 @@ __host__ __device__ inline SubOff sub_offsets(int N) {
   o.eG = o.eGm + al256(KB * sizeof(int));
   o.eR = o.eG + al256((size_t)N * sizeof(int));
   o.eT = o.eR + al256((size_t)N * sizeof(int));
-  o.total = o.eT + al256((size_t)N * sizeof(int));
+  o.mc = o.eT + al256((size_t)N * sizeof(int));  // accepts of the current block (split kernels, spin 0's)
+  o.total = o.mc + 256;
   return o;
 }
 
@@ -145,13 +147,14 @@ __device__ __forceinline__ long long group_sum(const uint32_t (&v)[OZS][8], int 
 }
 
 // The tile loop of one product, C = A B with A: nrb row blocks of 128 lines, B:
-// nct column tiles of 32 lines, K = 16 nk, both as tensor-core images in
-// global memory (slice stride a_sst / b_sst, a_nlb / b_nlb line blocks per k
-// chunk).  Tile u (global count across products) uses B buffer u % NBB and TMEM
-// accumulator u & 1; thread 0 copies the B tile of t+2 and issues the MMAs of
-// t+1 while every thread runs pre(row block, column tile) (loads that do not
-// need the product) and then epi(row block, column tile, TMEM address) on tile
-// t.  A is reloaded (after the MMAs of the previous tile) at each row block.
+// the column tiles cb0, cb0 + cbs, ... < nct of 32 lines, K = 16 nk, both as
+// tensor-core images in global memory (slice stride a_sst / b_sst, a_nlb / b_nlb
+// line blocks per k chunk).  Tile u (global count across products) uses B buffer
+// u % NBB and TMEM accumulator u & 1; thread 0 copies the B tile of t+2 and
+// issues the MMAs of t+1 while every thread runs pre(row block, column tile)
+// (loads that do not need the product) and then epi(row block, column tile, TMEM
+// address) on tile t.  A is reloaded (after the MMAs of the previous tile) at
+// each row block.
 struct SubTC {
   unsigned char* A;            // A_BYTES
   unsigned char* B;            // NBB x B_BYTES
@@ -165,13 +168,16 @@ struct SubTC {
 template <class Pre, class Epi>
 __device__ void sub_gemm(const SubTC& tc, unsigned& gt, unsigned& nA, const unsigned short* aG, long long a_sst,
                          int a_nlb, int nrb, const unsigned short* bG, long long b_sst, int b_nlb, int nct, int nk,
-                         Pre pre, Epi epi) {
+                         Pre pre, Epi epi, int cb0 = 0, int cbs = 1) {
   const int tid = threadIdx.x;
-  const int ntiles = nrb * nct;
+  const int ncl = (nct > cb0) ? (nct - cb0 + cbs - 1) / cbs : 0;  // column tiles of this CTA
+  const int ntiles = nrb * ncl;
+  if (ntiles == 0) return;
   constexpr uint32_t idesc = tc::idesc_bf16(TM, TN);
+  auto cb_of = [&](int t) { return cb0 + (t % ncl) * cbs; };
   auto load_b = [&](int t) {  // thread 0
     const unsigned u = gt + t;
-    const int cb = t % nct, bb = (int)(u % NBB);
+    const int cb = cb_of(t), bb = (int)(u % NBB);
     unsigned char* dst = tc.B + bb * B_BYTES;
     tc::mbar_expect_tx(&tc.ldB[bb], OZS * nk * TN * 32);
     for (int s2 = 0; s2 < OZS; ++s2)
@@ -181,9 +187,9 @@ __device__ void sub_gemm(const SubTC& tc, unsigned& gt, unsigned& nA, const unsi
   };
   auto issue = [&](int t) {  // thread 0: A if a new row block, then the MMAs of tile t
     const unsigned u = gt + t;
-    const int rb = t / nct, bb = (int)(u % NBB), acc = (int)(u & 1);
+    const int rb = t / ncl, bb = (int)(u % NBB), acc = (int)(u & 1);
     if (*tc.fail) return;
-    if (t % nct == 0) {
+    if (t % ncl == 0) {
       // the A buffer is free once the MMAs of the previous tile (all earlier ones) completed
       if (t > 0 && !tc::mbar_wait(&tc.mmab[(u - 1) & 1], ((u - 1) >> 1) & 1)) { *tc.fail = 1; return; }
       tc::mbar_expect_tx(tc.ldA, OZS * nk * TM * 32);
@@ -219,10 +225,10 @@ __device__ void sub_gemm(const SubTC& tc, unsigned& gt, unsigned& nA, const unsi
       if (t + 2 < ntiles) load_b(t + 2);  // its buffer held tile t - 1, whose epilogue is done
       if (t + 1 < ntiles) issue(t + 1);
     }
-    pre(t / nct, t % nct);
+    pre(t / ncl, cb_of(t));
     if (!*tc.fail && !tc::mbar_wait(&tc.mmab[u & 1], (u >> 1) & 1)) *tc.fail = 1;
     tc::fence_after();
-    epi(t / nct, t % nct, tc.tmem + (unsigned)((u & 1) * ACC_COLS), !*tc.fail);
+    epi(t / ncl, cb_of(t), tc.tmem + (unsigned)((u & 1) * ACC_COLS), !*tc.fail);
     tc::fence_before();
     __syncthreads();
   }
@@ -514,6 +520,333 @@ __global__ void __launch_bounds__(kSubThreads) metropolis_sub_kernel(const Walke
   }
 }
 
+// ---- the same updates split per 32-site block into two kernels ----------------
+// For walkers too few to fill the GPU (one CTA per walker leaves most SMs idle at
+// 32 walkers of N = 576), each block runs as a decision kernel (one CTA per walker:
+// the decisions, Gamma, the slices of Gamma, G0(:, I_A) and R_A, T^T on the tensor
+// cores) followed by a flush kernel whose CTAs share the walker's column tiles of G.
+// The arithmetic is the fused kernel's, element for element.  The autotuner times both.
+
+// dynamic shared memory of the decision kernel: the operand buffers, the FP64 block state,
+// the exponent scratch and the block's fields; of the flush kernel: the operand buffers
+size_t submatrix_block_smem_bytes(int S) {
+  return (size_t)A_BYTES + (size_t)NBB * B_BYTES + sizeof(double) * (KB + 6ull * S * KK) + 256 * sizeof(int) + KB;
+}
+size_t submatrix_flush_smem_bytes() { return (size_t)A_BYTES + (size_t)NBB * B_BYTES; }
+
+__global__ void __launch_bounds__(kSubThreads) metropolis_sub_block_kernel(const WalkerDev* __restrict__ W, int mode,
+                                                                           int j, int q, int blk) {
+  const WalkerDev& w = W[blockIdx.x];
+  if (w.path != 2) return;
+  int t;
+  if (!sub_slice_of(w, mode, j, q, t)) return;
+  const int N = w.N, S = w.S, Lt = w.Lt, tid = threadIdx.x;
+  const int i0 = blk * KB;
+  if (i0 >= N) return;
+  const int kb = min(KB, N - i0);
+  const long long NN = (long long)N * N;
+  extern __shared__ __align__(1024) unsigned char smem[];
+  double* sh = reinterpret_cast<double*>(smem + A_BYTES + NBB * B_BYTES);
+  double* uni = sh;                      // [KB] uniforms of the block's sites
+  double* Gb = uni + KB;                 // [S][KK] diagonal block, (r, c) at c * KB + r
+  double* Ac = Gb + S * KK;              // [S][q][x] a_q at compact index x
+  double* Bc = Ac + S * KK;              // [S][q][x] b_q
+  double* Ut = Bc + S * KK;              // [S][q][l] u~_q at block position l
+  double* Wt = Ut + S * KK;              // [S][q][l] w~_q
+  double* Gam = Wt + S * KK;             // [S][KK] Gamma(x, y) at y * KB + x
+  int* etmp = reinterpret_cast<int*>(Gam + S * KK);         // [256]
+  int8_t* s_field = reinterpret_cast<int8_t*>(etmp + 256);  // [KB]
+  __shared__ int s_next, s_pos[KB];
+  __shared__ double s_f[2];
+  __shared__ __align__(8) unsigned long long bar_ldA, bar_ldB[NBB], bar_mma[2];
+  __shared__ unsigned s_tmem;
+  __shared__ int s_tcfail;
+
+  const SubOff so = sub_offsets(N);
+  const double* G[2] = {w.G, (S == 2) ? w.G + NN : w.G};
+  const int eff = t - 1;
+  const unsigned long long sweep = (w.rng == 1) ? *w.sweep_ctr : 0ULL;
+  for (int l = tid; l < kb; l += kSubThreads) {
+    const int i = i0 + l;
+    s_field[l] = w.fields[(long long)eff * N + i];
+    const int attempt = (mode == MODE_FWD) ? (eff * N + i) : ((Lt - t) * N + i);
+    uni[l] = (w.rng == 0) ? w.uni[attempt] : philox_uniform(w.seed, (unsigned)w.widx, sweep, (unsigned)(eff * N + i));
+  }
+  for (int e = tid; e < S * KK; e += kSubThreads) {
+    const int sp = e / KK, c = (e % KK) / KB, r = e % KB;
+    Gb[e] = (r < kb && c < kb) ? G[sp][(long long)(i0 + c) * N + i0 + r] : 0.0;
+  }
+  double sign = 0.0;
+  long long acc_count = 0;
+  if (tid == 0) sign = *w.sign;
+  __syncthreads();
+
+  // ---- decisions, flip by flip, on the diagonal block
+  int m = 0, cur = 0;
+  while (true) {
+    if (tid == 0) {
+      int l = cur;
+      for (; l < kb; ++l) {
+        const int s = s_field[l];
+        const int si = s > 0 ? 0 : 1;
+        const double gu = Gb[l * KB + l];
+        const double gd = (S == 2) ? Gb[KK + l * KB + l] : gu;
+        const FlipRatio q = flip_ratio(w, si, gu, gd);  // reference operation order
+        const double r = q.r;
+        const double prob = fmin(1.0, fabs(r));
+        if (!isfinite(r)) atomicOr(w.status, ST_NONFINITE_RATIO);
+        if (uni[l] < prob) {
+          flip_factors(w, q, s_f);
+          s_field[l] = (int8_t)(-s);
+          sign = (r >= 0) ? sign : -sign;
+          ++acc_count;
+          break;
+        }
+      }
+      s_next = l;
+    }
+    __syncthreads();
+    const int l = s_next;
+    if (l >= kb) break;
+    for (int e = tid; e < S * 4 * KB; e += kSubThreads) {
+      const int sp = e / (4 * KB), role = (e / KB) & 3, x = e % KB;
+      const double f = s_f[sp];
+      const double* gb = Gb + sp * KK;
+      double* ut = Ut + sp * KK;
+      double* wt = Wt + sp * KK;
+      double* ac = Ac + sp * KK;
+      double* bc = Bc + sp * KK;
+      if (role == 0) {
+        ut[m * KB + x] = f * gb[l * KB + x];  // f G(x, l)
+      } else if (role == 1) {
+        wt[m * KB + x] = ((x == l) ? 1.0 : 0.0) - gb[x * KB + l];  // delta - G(l, x)
+      } else if (role == 2) {
+        double a = (x == m) ? 1.0 : 0.0;
+        for (int p = x; p < m; ++p) a = fma(-wt[p * KB + l], ac[p * KB + x], a);
+        ac[m * KB + x] = (x <= m) ? f * a : 0.0;
+      } else {
+        double b = (x == m) ? 1.0 : 0.0;
+        for (int p = x; p < m; ++p) b = fma(ut[p * KB + l], bc[p * KB + x], b);
+        bc[m * KB + x] = (x <= m) ? b : 0.0;
+      }
+    }
+    if (tid == 0) s_pos[m] = l;
+    __syncthreads();
+    for (int e = tid; e < S * KK; e += kSubThreads) {
+      const int sp = e / KK, c = (e % KK) / KB, r = e % KB;
+      if (r > l && c > l && r < kb && c < kb)
+        Gb[e] = fma(-Ut[sp * KK + m * KB + r], Wt[sp * KK + m * KB + c], Gb[e]);
+    }
+    ++m;
+    cur = l + 1;
+    __syncthreads();
+  }
+  int8_t* frw = w.fields + (long long)eff * N + i0;
+  for (int l = tid; l < kb; l += kSubThreads) frw[l] = s_field[l];
+  if (tid == 0) {
+    *w.sign = sign;
+    *w.accepts += acc_count;
+    if (mode == MODE_BWD && t == Lt && i0 + KB >= N) *w.sign_Lt = sign;
+    *reinterpret_cast<int*>(w.msub + so.mc) = m;
+  }
+  if (m == 0) return;
+
+  // ---- Gamma = sum_q a_q b_q^T
+  for (int e = tid; e < S * KK; e += kSubThreads) {
+    const int sp = e / KK, y = (e % KK) / KB, x = e % KB;
+    double gsum = 0.0;
+    if (x < m && y < m) {
+      const double* ac = Ac + sp * KK;
+      const double* bc = Bc + sp * KK;
+      for (int p = max(x, y); p < m; ++p) gsum = fma(ac[p * KB + x], bc[p * KB + y], gsum);
+    }
+    Gam[e] = gsum;
+  }
+  if (tid == 0) {
+    s_tcfail = 0;
+    tc::mbar_init(&bar_ldA);
+    for (int i = 0; i < NBB; ++i) tc::mbar_init(&bar_ldB[i]);
+    tc::mbar_init(&bar_mma[0]);
+    tc::mbar_init(&bar_mma[1]);
+    tc::mbar_fence_init();
+  }
+  if (tid < 32) tc::alloc(&s_tmem, TMEM_COLS);
+  tc::fence_before();
+  __syncthreads();
+  tc::fence_after();
+  const SubTC tcs{smem, smem + A_BYTES, &bar_ldA, bar_ldB, bar_mma, s_tmem, &s_tcfail};
+  unsigned gt = 0, nA = 0;
+  const int nlbN = ozaki::tc_lines(N) / 8;
+  const long long sstN = (long long)sub_sst(N), sstG = (long long)sub_sst(1);
+  const int nk = (m + 15) / 16;
+  for (int sp = 0; sp < S; ++sp) {
+    unsigned char* ms = w.msub + (size_t)sp * so.total;
+    unsigned short* sGm = reinterpret_cast<unsigned short*>(ms + so.sGm);
+    unsigned short* sG = reinterpret_cast<unsigned short*>(ms + so.sG);
+    unsigned short* sR = reinterpret_cast<unsigned short*>(ms + so.sR);
+    unsigned short* sT = reinterpret_cast<unsigned short*>(ms + so.sT);
+    int* eGm = reinterpret_cast<int*>(ms + so.eGm);
+    int* eG = reinterpret_cast<int*>(ms + so.eG);
+    int* eR = reinterpret_cast<int*>(ms + so.eR);
+    int* eT = reinterpret_cast<int*>(ms + so.eT);
+    const double* gam = Gam + sp * KK;
+    const double* Gs = G[sp];
+    slice_lines([&](int line, int k) { return gam[k * KB + line]; }, m, m, sGm, sstG, TM / 8, eGm, etmp);
+    slice_lines([&](int line, int k) { return Gs[(long long)(i0 + s_pos[k]) * N + line]; }, N, m, sG, sstN, nlbN,
+                eG, etmp);
+    slice_lines(
+        [&](int line, int k) {
+          const int i = i0 + s_pos[k];
+          return ((line == i) ? 1.0 : 0.0) - Gs[(long long)line * N + i];
+        },
+        N, m, sR, sstN, nlbN, eR, etmp);
+    asm volatile("fence.proxy.async.global;" ::: "memory");  // generic writes -> bulk-copy reads
+    __syncthreads();
+    // T^T = R_A^T Gamma^T, its epilogue slicing T into the flush's B image (as the fused kernel)
+    sub_gemm(tcs, gt, nA, sR, sstN, nlbN, (N + TM - 1) / TM, sGm, sstG, TM / 8, 1, nk, [&](int, int) {},
+             [&](int rb, int, unsigned tacc, bool ok) {
+               const int wq = (tid >> 5) & 3, xh = tid >> 7;
+               const int c = rb * TM + wq * 32 + (tid & 31);
+               const int ec = (c < N) ? eR[c] : 0;
+               double tv[16];
+               int e = -1100;
+               if (ok) {
+#pragma unroll
+                 for (int h = 0; h < 2; ++h) {
+                   uint32_t v[OZS][8];
+#pragma unroll
+                   for (int g = 0; g < OZS; ++g)
+                     tc::ld8(v[g], tacc + ((unsigned)(wq * 32) << 16) + (unsigned)(g * TN + xh * 16 + h * 8));
+                   tc::wait_ld();
+#pragma unroll
+                   for (int u = 0; u < 8; ++u) {
+                     const int x = xh * 16 + h * 8 + u;
+                     tv[h * 8 + u] = (x < m && c < N) ? ozaki::ldexp_i64(group_sum(v, u), ec + eGm[x] + kEOff) : 0.0;
+                     e = max(e, ozaki::exp_bound(tv[h * 8 + u]));
+                   }
+                 }
+               }
+               etmp[tid] = e;
+               __syncthreads();
+               e = max(e, etmp[tid ^ 128]);
+               if (ok && c < N) {
+                 if (xh == 0) eT[c] = e;
+                 unsigned pk[OZS][8];
+#pragma unroll
+                 for (int u = 0; u < 16; u += 2) {
+                   bool n0, n1;
+                   const unsigned long long q0 = ozaki::fixed42(tv[u], e, n0), q1 = ozaki::fixed42(tv[u + 1], e, n1);
+#pragma unroll
+                   for (int s2 = 0; s2 < OZS; ++s2)
+                     pk[s2][u >> 1] = (unsigned)ozaki::slice_bf16(q0, s2, OZB, n0) |
+                                      ((unsigned)ozaki::slice_bf16(q1, s2, OZB, n1) << 16);
+                 }
+                 unsigned short* o = sT + ozaki::tc_index(c, xh * 16, nlbN);
+#pragma unroll
+                 for (int s2 = 0; s2 < OZS; ++s2) {
+                   *reinterpret_cast<uint4*>(o + s2 * sstN) = make_uint4(pk[s2][0], pk[s2][1], pk[s2][2], pk[s2][3]);
+                   *reinterpret_cast<uint4*>(o + s2 * sstN + 64) =
+                       make_uint4(pk[s2][4], pk[s2][5], pk[s2][6], pk[s2][7]);
+                 }
+               }
+             });
+    __syncthreads();
+  }
+  asm volatile("fence.proxy.async.global;" ::: "memory");  // T's slices -> the flush's bulk copies
+  tc::fence_before();
+  __syncthreads();
+  if (tid < 32) tc::dealloc(s_tmem, TMEM_COLS);
+  if (tid == 0 && s_tcfail) {
+    atomicOr(w.status, ST_TIMEOUT);
+    *reinterpret_cast<int*>(w.msub + so.mc) = 0;  // no flush from a product that gave up
+  }
+}
+
+// The flush of block blk: G -= G0(:, I_A) T for both spins, the column tiles of G spread over
+// the gridDim.x CTAs of a walker (CTA p takes tiles p, p + gridDim.x, ...).
+__global__ void __launch_bounds__(kSubThreads) metropolis_sub_flush_kernel(const WalkerDev* __restrict__ W, int mode,
+                                                                           int j, int q, int blk) {
+  const WalkerDev& w = W[blockIdx.y];
+  if (w.path != 2) return;
+  int t;
+  if (!sub_slice_of(w, mode, j, q, t)) return;
+  const int N = w.N, S = w.S, tid = threadIdx.x;
+  if (blk * KB >= N) return;
+  const int nct = (N + TN - 1) / TN;
+  if ((int)blockIdx.x >= nct) return;
+  const SubOff so = sub_offsets(N);
+  const int m = *reinterpret_cast<const int*>(w.msub + so.mc);
+  if (m == 0) return;
+  const long long NN = (long long)N * N;
+  extern __shared__ __align__(1024) unsigned char smem[];
+  __shared__ __align__(8) unsigned long long bar_ldA, bar_ldB[NBB], bar_mma[2];
+  __shared__ unsigned s_tmem;
+  __shared__ int s_tcfail;
+  if (tid == 0) {
+    s_tcfail = 0;
+    tc::mbar_init(&bar_ldA);
+    for (int i = 0; i < NBB; ++i) tc::mbar_init(&bar_ldB[i]);
+    tc::mbar_init(&bar_mma[0]);
+    tc::mbar_init(&bar_mma[1]);
+    tc::mbar_fence_init();
+  }
+  if (tid < 32) tc::alloc(&s_tmem, TMEM_COLS);
+  tc::fence_before();
+  __syncthreads();
+  tc::fence_after();
+  const SubTC tcs{smem, smem + A_BYTES, &bar_ldA, bar_ldB, bar_mma, s_tmem, &s_tcfail};
+  unsigned gt = 0, nA = 0;
+  const int nlbN = ozaki::tc_lines(N) / 8;
+  const long long sstN = (long long)sub_sst(N);
+  const int nk = (m + 15) / 16;
+  for (int sp = 0; sp < S; ++sp) {
+    unsigned char* ms = w.msub + (size_t)sp * so.total;
+    const unsigned short* sG = reinterpret_cast<const unsigned short*>(ms + so.sG);
+    const unsigned short* sT = reinterpret_cast<const unsigned short*>(ms + so.sT);
+    const int* eG = reinterpret_cast<const int*>(ms + so.eG);
+    const int* eT = reinterpret_cast<const int*>(ms + so.eT);
+    double* Gs = w.G + sp * NN;
+    double gv[16];
+    int ecol[16];
+    const int wq = (tid >> 5) & 3, half = tid >> 7;
+    sub_gemm(tcs, gt, nA, sG, sstN, nlbN, (N + TM - 1) / TM, sT, sstN, nlbN, nct, nk,
+             [&](int rb, int cb) {
+               const int r = rb * TM + wq * 32 + (tid & 31), c0 = cb * TN + half * 16;
+#pragma unroll
+               for (int u = 0; u < 16; ++u) {
+                 const int c = c0 + u;
+                 gv[u] = (r < N && c < N) ? Gs[(long long)c * N + r] : 0.0;
+                 ecol[u] = (c < N) ? eT[c] : 0;
+               }
+             },
+             [&](int rb, int cb, unsigned tacc, bool ok) {
+               if (!ok) return;
+               const int r = rb * TM + wq * 32 + (tid & 31), c0 = cb * TN + half * 16;
+               const int er = (r < N) ? eG[r] : 0;
+               const unsigned ta = tacc + ((unsigned)(wq * 32) << 16);
+#pragma unroll
+               for (int h = 0; h < 2; ++h) {
+                 uint32_t v[OZS][8];
+#pragma unroll
+                 for (int g = 0; g < OZS; ++g) tc::ld8(v[g], ta + (unsigned)(g * TN + half * 16 + h * 8));
+                 tc::wait_ld();
+#pragma unroll
+                 for (int u = 0; u < 8; ++u) {
+                   const int c = c0 + h * 8 + u;
+                   const long long sv = group_sum(v, u);
+                   if (sv != 0 && r < N && c < N)
+                     Gs[(long long)c * N + r] = gv[h * 8 + u] - ozaki::ldexp_i64(sv, er + ecol[h * 8 + u] + kEOff);
+                 }
+               }
+             },
+             (int)blockIdx.x, (int)gridDim.x);
+  }
+  tc::fence_before();
+  __syncthreads();
+  if (tid < 32) tc::dealloc(s_tmem, TMEM_COLS);
+  if (tid == 0 && s_tcfail) atomicOr(w.status, ST_TIMEOUT);
+}
+
 static size_t g_sub_smem_limit = 0;  // dynamic shared memory the kernel may use
 
 cudaError_t configure_submatrix_kernel() {
@@ -527,11 +860,33 @@ cudaError_t configure_submatrix_kernel() {
     e = cudaFuncSetAttribute(metropolis_sub_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)g_sub_smem_limit);
   }
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(metropolis_sub_block_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)submatrix_block_smem_bytes(2));
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(metropolis_sub_flush_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)submatrix_flush_smem_bytes());
   return e;
 }
 
 void launch_metropolis_sub(const WalkerDev* W, int nw, int mode, int j, int q, int maxN, int S_max, cudaStream_t st) {
   metropolis_sub_kernel<<<nw, kSubThreads, submatrix_smem_bytes(maxN, S_max), st>>>(W, mode, j, q);
+}
+
+// CTAs per walker of the split flush: two column tiles of 32 each (at least one CTA)
+int submatrix_flush_ctas(int maxN) { return std::max(1, ((maxN + TN - 1) / TN + 1) / 2); }
+
+// One slice of Metropolis by the split kernels: for each 32-site block the decisions (one CTA
+// per walker) then the flush (submatrix_flush_ctas CTAs per walker); walkers whose N ends
+// earlier skip the blocks past it.
+void launch_metropolis_sub_split(const WalkerDev* W, int nw, int mode, int j, int q, int maxN, int S_max,
+                                 cudaStream_t st) {
+  const int nb = (maxN + KB - 1) / KB, P = submatrix_flush_ctas(maxN);
+  const size_t sm1 = submatrix_block_smem_bytes(S_max), sm2 = submatrix_flush_smem_bytes();
+  for (int blk = 0; blk < nb; ++blk) {
+    metropolis_sub_block_kernel<<<nw, kSubThreads, sm1, st>>>(W, mode, j, q, blk);
+    metropolis_sub_flush_kernel<<<dim3(P, nw), kSubThreads, sm2, st>>>(W, mode, j, q, blk);
+  }
 }
 
 }  // namespace dqmc

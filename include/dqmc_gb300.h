@@ -216,9 +216,12 @@ int dqmc_trace_clear(dqmc_batch* b);
 int dqmc_batch_info(dqmc_batch* b, int* n_walkers, int64_t* updates_per_half_sweep);
 
 /* The autotuner's choice for walkers whose G lives in HBM (N > 64 or the mixed
- * path): delayed-update block size k and whether its flush runs on the tensor
- * cores, with every candidate's time for one slice of the whole batch (arrays
- * sized 8).  dqmc_init_greens runs the tuner on the batch's own state. */
+ * path): delayed-update block size k and the update kind tc_flush (0 delayed
+ * updates with an FP64 flush, 1 with a tensor-core flush, 2 submatrix updates in
+ * one kernel per walker, 3 submatrix updates split per 32-site block into a
+ * decision kernel and a flush kernel of several CTAs per walker), with every
+ * candidate's time for one slice of the whole batch (arrays sized 8).
+ * dqmc_init_greens runs the tuner on the batch's own state. */
 int dqmc_tuning(dqmc_batch* b, int* kd, int* tc_flush, int* n_candidates, int* cand_kd, int* cand_tc,
                 float* cand_ms);
 

@@ -125,3 +125,34 @@ def test_walker_groups_give_identical_walkers(dq, monkeypatch):
         assert s1[w] == 0 and s4[w] == 0
     np.testing.assert_array_equal(o1[0], o4[0])
     np.testing.assert_array_equal(o1[1], o4[1])
+
+
+def test_split_submatrix_equals_fused(dq, monkeypatch):
+    """The submatrix updates split per 32-site block (a decision kernel, then a flush spread
+    over several CTAs per walker) do the fused kernel's arithmetic element for element:
+    with the tuner held to each kind (DQMC_METROPOLIS_KIND), fields, G and observables are
+    bitwise equal after two sweep pairs, for N = 144 (two spins) and N = 289 (partial tiles)."""
+    for L, model in ((12, 0), (17, 1)):
+        descs = [dq.WalkerDesc(model=model, L=L, U=4.0, mu=-0.3 * model, beta=1.0, Lt=10, pace=5, seed=400 + w)
+                 for w in range(3)]
+        res = []
+        for kind in ("2", "3"):
+            monkeypatch.setenv("DQMC_METROPOLIS_KIND", kind)
+            b = dq.Batch(descs, rng=dq.RNG_PHILOX, precision=dq.MIXED)
+            for w in range(3):
+                b.fields_random(w)
+            b.init_greens()
+            assert b.tuning()["tc_flush"] == int(kind)
+            for _ in range(2):
+                b.sweep_0_to_beta(measure=True)
+                b.sweep_beta_to_0(measure=True)
+            res.append(([b.fields(w) for w in range(3)], [b.green(w, s) for w in range(3) for s in (0, 1)],
+                        b.observables_all(), [b.status(w) for w in range(3)]))
+            b.close()
+        (f2, g2, o2, s2), (f3, g3, o3, s3) = res
+        assert s2 == [0, 0, 0] and s3 == [0, 0, 0]
+        for a, c in zip(f2, f3):
+            np.testing.assert_array_equal(a, c)
+        for a, c in zip(g2, g3):
+            np.testing.assert_array_equal(a, c)
+        np.testing.assert_array_equal(o2[0], o3[0])
