@@ -353,6 +353,21 @@ def stab_tensor_flops(N, TB=32):
     return push, greens
 
 
+def stab_rhs_flops(N, TB=32):
+    """FP64-equivalent flops of the products that carry one more right-hand side through the
+    Green's assembly's factorization (Q^T applied panel by panel, blocked back substitution),
+    per walker and spin: the second right-hand side of the dynamic half-sweep."""
+    f = 0
+    for p in range(-(-N // TB)):
+        j0 = p * TB
+        m = N - j0
+        pb = min(TB, m)
+        f += 2 * pb * N * m + 2 * pb * N * pb + 2 * m * N * pb
+        if j0 + pb < N:
+            f += 2 * pb * N * (N - j0 - pb)
+    return f
+
+
 def slice_pairs(n_slices: int) -> int:
     """Slice products of one exact-slice product: pairs (i, j) with i + j < S."""
     return n_slices * (n_slices + 1) // 2
@@ -657,7 +672,7 @@ def run_gpu(args, wl, rank, world):
     model = {}  # class -> (bound, algorithmic flops in the profiled steps, peak TFLOP/s, what is counted)
     extra = {}
     if mixed:
-        prod = push = greens = bf_met = fp_met = ref_rank1 = dynp = 0.0
+        prod = push = greens = bf_met = fp_met = ref_rank1 = dynp = dstab = 0.0
         met_what = ""
         for d, a in zip(descs, acc_w):
             N, S = d.L ** 2, (1 if d.model == 1 else 2)
@@ -674,6 +689,8 @@ def run_gpu(args, wl, rank, world):
                 sp = slice_pairs(8 if N <= 256 else 9)
                 push += steps * S * ns * pf * sp
                 greens += steps * S * ns * gf * sp
+                if dyn:  # the dynamic half-sweep's assembly with its second right-hand side and outputs
+                    dstab += steps * S * ns * (gf + stab_rhs_flops(N) + 2 * 2 * N ** 3) * sp
             b_, f_, met_what = metropolis_work(d, a, tuning["tc_flush"], tuning["kd"])
             bf_met += steps * b_
             fp_met += steps * f_
@@ -681,6 +698,11 @@ def run_gpu(args, wl, rank, world):
         model["product"] = ("tensor", prod, bf16_peak,
                             "BF16 flops of the exact-slice wrap and B-chain products: 3 per slice x slice pairs "
                             "(28 for N <= 256, 36 above) x 2N^3")
+        if dstab > 0:
+            model["dynamic_stab"] = ("tensor", dstab, bf16_peak,
+                                     "BF16 flops of the dynamic half-sweep's blocked-QR Green's assembly with the "
+                                     "second right-hand side and the G(t,0), G(0,t) products (45 slice pairs above "
+                                     "N = 256, 36 below)")
         if dyn:
             model["dynamic"] = ("tensor", dynp, bf16_peak,
                                 "BF16 flops of the G(t,0), G(0,t) steps of the dynamic half-sweep (2 products "

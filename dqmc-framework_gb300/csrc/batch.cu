@@ -18,6 +18,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <map>
+#include <mutex>
 #include <random>
 #include <string>
 #include <tuple>
@@ -199,6 +200,22 @@ std::vector<double> fourier_table(int L, int kidx) {
 }
 
 size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+// exp(-dtau K) and exp(+dtau K) of a lattice, kept for the life of the process: the Jacobi
+// diagonalisation costs seconds at N = 576 and every batch of the same lattice reuses it
+std::pair<std::vector<double>, std::vector<double>> dense_exponentials(int L, double t, double mu, double dtau) {
+  static std::mutex mu_cache;
+  static std::map<std::tuple<int, double, double, double>, std::pair<std::vector<double>, std::vector<double>>> cache;
+  const auto key = std::make_tuple(L, t, mu, dtau);
+  {
+    std::lock_guard<std::mutex> lock(mu_cache);
+    auto it = cache.find(key);
+    if (it != cache.end()) return it->second;
+  }
+  auto v = sym_exp_pair(L * L, kinetic_matrix(L, t, mu), -dtau);
+  std::lock_guard<std::mutex> lock(mu_cache);
+  return cache.emplace(key, std::move(v)).first->second;
+}
 
 }  // namespace
 
@@ -409,9 +426,7 @@ int dqmc_batch_create(const dqmc_walker_desc* descs, int n, const dqmc_batch_opt
       auto key = std::make_tuple(d.L, d.hopping_t, d.mu, d.beta / d.Lt);
       auto it = dense_ids.find(key);
       if (it == dense_ids.end()) {
-        const auto K = kinetic_matrix(d.L, d.hopping_t, d.mu);
-        const double dt = d.beta / d.Lt;
-        dense.push_back(sym_exp_pair(N, K, -dt));
+        dense.push_back(dense_exponentials(d.L, d.hopping_t, d.mu, d.beta / d.Lt));
         it = dense_ids.emplace(key, (int)dense.size() - 1).first;
       }
       off[w].dense_id = it->second;
