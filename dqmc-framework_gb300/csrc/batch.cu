@@ -82,6 +82,7 @@ void mixed_wrap_bwd(const WalkerDev* W, int nw, int maxN, int j, int q, cudaStre
 void mixed_chain(const WalkerDev* W, int nw, int maxN, int mode, int j, int q, cudaStream_t st);
 void oz_slice_const(const double* X, unsigned short* out, int* exps, int N, int ldk, int role, int bits, int slices,
                     int layout, cudaStream_t st);
+void oz_set_shape(int shape);
 void oz_selftest(const double* A, const double* B, double* C, unsigned short* sa, int* ea, unsigned short* sb, int* eb,
                  int N, cudaStream_t st);
 }  // namespace dqmc
@@ -238,6 +239,11 @@ struct dqmc_batch {
   int tc_flush = 1;
   bool tuned = false;
   std::vector<std::pair<std::pair<int, int>, float>> tune_log;  // ((kd, tc), ms) per candidate
+  // tile shape of the tensor-core wrap and chain products (oz_set_shape), tuned with the
+  // time of one slice's products of the whole batch per shape
+  int oz_shape = 0;
+  bool shape_tuned = false;
+  std::vector<std::pair<int, float>> shape_log;
   dqmc_batch_options opt{};
   std::vector<dqmc_walker_desc> desc;
   std::vector<WalkerDev> hw;        // host copies of the descriptors
@@ -802,8 +808,61 @@ static int autotune_delayed(dqmc_batch* b) {
   return DQMC_OK;
 }
 
+// Tile shape of the tensor-core wrap and chain products: one forward slice's wrap and chain
+// products of the whole batch timed with each shape (G backed up into the stabilization
+// scratch and restored after each trial; work and the chain are rebuilt before they are
+// read again), the faster kept.
+static int autotune_products(dqmc_batch* b) {
+  for (int w = 0; w < b->nw; ++w) {
+    const WalkerDev& h = b->hw[w];
+    if (h.path != 2) continue;
+    CUDA_TRY(cudaMemcpyAsync(h.scr, h.G, sizeof(double) * h.S * h.N * h.N, cudaMemcpyDeviceToDevice, b->stream));
+  }
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  float best = 1e30f;
+  int pick = 0;
+  b->shape_log.clear();
+  std::vector<int> shapes = {0, 1};
+  if (const char* env = std::getenv("DQMC_PRODUCT_TILE")) {  // holds the tuner to one shape (tests)
+    const int s = std::atoi(env);
+    if (s == 0 || s == 1) shapes = {s};
+  }
+  for (int shape : shapes) {
+    oz_set_shape(shape);
+    for (int rep = 0; rep < 2; ++rep) {  // first run warms caches and code
+      cudaEventRecord(e0, b->stream);
+      mixed_wrap_fwd(b->dW, b->nw, b->maxN_general, 0, 0, b->stream);
+      mixed_chain(b->dW, b->nw, b->maxN_general, MODE_FWD, 0, 0, b->stream);
+      cudaEventRecord(e1, b->stream);
+      CUDA_TRY(cudaEventSynchronize(e1));
+      float ms = 0;
+      cudaEventElapsedTime(&ms, e0, e1);
+      for (int w = 0; w < b->nw; ++w) {
+        const WalkerDev& h = b->hw[w];
+        if (h.path != 2) continue;
+        CUDA_TRY(cudaMemcpyAsync(h.G, h.scr, sizeof(double) * h.S * h.N * h.N, cudaMemcpyDeviceToDevice, b->stream));
+      }
+      if (rep == 1) {
+        b->shape_log.push_back({shape, ms});
+        if (ms < best) { best = ms; pick = shape; }
+      }
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  CUDA_TRY(cudaStreamSynchronize(b->stream));
+  if (int r = launch_check("product tile autotune")) return r;
+  b->oz_shape = pick;
+  oz_set_shape(pick);
+  b->shape_tuned = true;
+  return DQMC_OK;
+}
+
 int dqmc_init_greens(dqmc_batch* b) {
   if (!b) return fail(DQMC_ERR_ARG, "null batch");
+  oz_set_shape(b->oz_shape);
   for (int j = 0; j < b->maxNs; ++j) {
     if (b->any_small) {
       launch_segment(MODE_INIT, b->dW, b->nw, j, 0, b->maxN_small, b->stream);
@@ -838,6 +897,9 @@ int dqmc_init_greens(dqmc_batch* b) {
   b->trace_count = 0;
   if (b->any_general && (b->kd > 0 || b->mixed) && !b->tuned) {
     if (int r = autotune_delayed(b)) return r;
+  }
+  if (b->mixed && b->any_general_dense && !b->shape_tuned) {
+    if (int r = autotune_products(b)) return r;
   }
   return DQMC_OK;
 }
@@ -876,6 +938,7 @@ static int trace_slot(const dqmc_batch* b, int j) {
 // Profiled replays keep one branch (class events on one stream); otherwise the
 // general walkers run as b->ngroups forked branches.
 static void issue_half_sweep(dqmc_batch* b, int mode, int measure) {
+  oz_set_shape(b->oz_shape);
   if (b->opt.rng == DQMC_RNG_MINSTD)
     cudaMemcpyAsync(b->d_uni, b->h_uni, sizeof(double) * b->uni_stride * b->nw, cudaMemcpyHostToDevice, b->stream);
   else
@@ -1004,6 +1067,17 @@ int dqmc_tuning(dqmc_batch* b, int* kd, int* tc_flush, int* n_candidates, int* c
     if (cand_kd) cand_kd[k] = b->tune_log[k].first.first;
     if (cand_tc) cand_tc[k] = b->tune_log[k].first.second;
     if (cand_ms) cand_ms[k] = b->tune_log[k].second;
+  }
+  return DQMC_OK;
+}
+
+int dqmc_tuning_products(dqmc_batch* b, int* shape, int* n_candidates, int* cand_shape, float* cand_ms) {
+  if (!b) return fail(DQMC_ERR_ARG, "null batch");
+  if (shape) *shape = b->oz_shape;
+  if (n_candidates) *n_candidates = (int)b->shape_log.size();
+  for (size_t k = 0; k < b->shape_log.size(); ++k) {
+    if (cand_shape) cand_shape[k] = b->shape_log[k].first;
+    if (cand_ms) cand_ms[k] = b->shape_log[k].second;
   }
   return DQMC_OK;
 }
@@ -1140,6 +1214,7 @@ int dqmc_sweep_dynamic(dqmc_batch* b, const int* taus, int ntau) {
   const cudaStream_t st = b->stream;
   const WalkerDev* W = b->dW;
   const int nw = b->nw;
+  oz_set_shape(b->oz_shape);
   b->timed(DQMC_KCLASS_DYNAMIC, [&] { general_dynamic_begin(W, nw, st); });
   for (int j = 0; j < b->maxNs; ++j) {
     b->timed(DQMC_KCLASS_SEGMENT, [&] { general_chain_init(MODE_FWD, W, nw, j, st); });

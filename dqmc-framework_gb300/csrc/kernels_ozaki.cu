@@ -317,20 +317,27 @@ __global__ void __launch_bounds__(256) oz_slice_kernel(const WalkerDev* __restri
 // Product of op OP on the 5th-generation tensor cores: a 128 x NT output
 // tile per CTA with the S weight groups accumulated in TMEM (S x NT columns),
 // the operands streamed by oztc::mainloop (bulk copies through a ring of NS
-// stages of 16-deep k chunks).  The 49-bit configuration (7 slices) runs
-// 128 x 32 tiles with 3 stages so that two CTAs share an SM (256 TMEM columns,
-// 105 KB of shared memory, at most 128 registers each); the 48-bit one (8
-// slices, K > 256) 128 x 64 tiles with 4 stages, one CTA per SM.
-__host__ __device__ constexpr int oz_tc_nt(int S) { return S <= 7 ? 32 : 64; }
-__host__ __device__ constexpr int oz_tc_stages(int S) { return S <= 7 ? 3 : 4; }
-__host__ __device__ constexpr int oz_tc_minb(int S) { return S <= 7 ? 2 : 1; }
-__host__ __device__ constexpr int oz_tc_stage_bytes(int S) { return oztc::stage_bytes(S, 128, oz_tc_nt(S)); }
+// stages of 16-deep k chunks).  Two tile shapes per slice configuration, picked
+// per batch by the autotuner (dqmc_init_greens): 128 x 32 tiles, two CTAs per SM
+// (at most 256 TMEM columns, 105 KB (7 slices, 3 stages) or 80 KB (8 slices, 2
+// stages) of shared memory and 128 registers each), or 128 x 64 tiles, one CTA
+// per SM (512 TMEM columns, 3 or 4 stages).  Shape SH = 0 is 128 x 32 for the
+// 49-bit configuration (7 slices, K <= 256) and 128 x 64 for the 48-bit one (8
+// slices); SH = 1 swaps them.
+__host__ __device__ constexpr int oz_tc_nt(int S, int SH) { return ((S <= 7) == (SH == 0)) ? 32 : 64; }
+__host__ __device__ constexpr int oz_tc_stages(int S, int SH) {
+  return oz_tc_nt(S, SH) == 32 ? (S <= 7 ? 3 : 2) : (S <= 7 ? 3 : 4);
+}
+__host__ __device__ constexpr int oz_tc_minb(int S, int SH) { return oz_tc_nt(S, SH) == 32 ? 2 : 1; }
+__host__ __device__ constexpr int oz_tc_stage_bytes(int S, int SH) {
+  return oztc::stage_bytes(S, 128, oz_tc_nt(S, SH));
+}
 
-template <int OP, int S>
-__global__ void __launch_bounds__(256, oz_tc_minb(S)) oz_prod_tc_kernel(const WalkerDev* __restrict__ W, int mode,
-                                                                        int j, int q) {
-  constexpr int MT = 128, NT = oz_tc_nt(S), NS = oz_tc_stages(S);
-  constexpr int CW = (oz_tc_minb(S) > 1) ? 8 : 16;  // TMEM columns per load in the epilogue
+template <int OP, int S, int SH>
+__global__ void __launch_bounds__(256, oz_tc_minb(S, SH)) oz_prod_tc_kernel(const WalkerDev* __restrict__ W, int mode,
+                                                                            int j, int q) {
+  constexpr int MT = 128, NT = oz_tc_nt(S, SH), NS = oz_tc_stages(S, SH);
+  constexpr int CW = (oz_tc_minb(S, SH) > 1) ? 8 : 16;  // TMEM columns per load in the epilogue
   constexpr unsigned TCOLS = (S * NT <= 256) ? 256u : 512u;
   const int wi = blockIdx.z >> 1, sp = blockIdx.z & 1;
   const WalkerDev& w = W[wi];
@@ -453,18 +460,23 @@ __global__ void __launch_bounds__(256) oz_selftest_prod_kernel(const unsigned sh
   else ozaki_product_tile<8>(job, N, ldk, bits, r0, c0, ozsm, epi);
 }
 
-static size_t oz_tc_smem(int S) { return (size_t)oz_tc_stages(S) * oz_tc_stage_bytes(S); }
+static size_t oz_tc_smem(int S, int SH) { return (size_t)oz_tc_stages(S, SH) * oz_tc_stage_bytes(S, SH); }
 size_t oz_prod_smem(int S) { return sizeof(unsigned short) * 2 * 2 * S * 64 * kOzRow; }
 
 cudaError_t configure_ozaki_kernels() {
   cudaError_t e;
-#define OZCFG(S, ...) if ((e = cudaFuncSetAttribute(__VA_ARGS__, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)oz_tc_smem(S)))) return e
-  OZCFG(7, oz_prod_tc_kernel<OZ_WL_FWD, 7>); OZCFG(7, oz_prod_tc_kernel<OZ_WR_FWD, 7>); OZCFG(7, oz_prod_tc_kernel<OZ_CH_FWD, 7>);
-  OZCFG(7, oz_prod_tc_kernel<OZ_CH_BWD, 7>); OZCFG(7, oz_prod_tc_kernel<OZ_WR_BWD, 7>); OZCFG(7, oz_prod_tc_kernel<OZ_WL_BWD, 7>);
-  OZCFG(8, oz_prod_tc_kernel<OZ_WL_FWD, 8>); OZCFG(8, oz_prod_tc_kernel<OZ_WR_FWD, 8>); OZCFG(8, oz_prod_tc_kernel<OZ_CH_FWD, 8>);
-  OZCFG(8, oz_prod_tc_kernel<OZ_CH_BWD, 8>); OZCFG(8, oz_prod_tc_kernel<OZ_WR_BWD, 8>); OZCFG(8, oz_prod_tc_kernel<OZ_WL_BWD, 8>);
-  OZCFG(7, oz_prod_tc_kernel<OZ_DT0, 7>); OZCFG(7, oz_prod_tc_kernel<OZ_D0T, 7>);
-  OZCFG(8, oz_prod_tc_kernel<OZ_DT0, 8>); OZCFG(8, oz_prod_tc_kernel<OZ_D0T, 8>);
+#define OZCFG(OP)                                                                                         \
+  if ((e = cudaFuncSetAttribute(oz_prod_tc_kernel<OP, 7, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,  \
+                                (int)oz_tc_smem(7, 0))) ||                                                 \
+      (e = cudaFuncSetAttribute(oz_prod_tc_kernel<OP, 8, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,  \
+                                (int)oz_tc_smem(8, 0))) ||                                                 \
+      (e = cudaFuncSetAttribute(oz_prod_tc_kernel<OP, 7, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,  \
+                                (int)oz_tc_smem(7, 1))) ||                                                 \
+      (e = cudaFuncSetAttribute(oz_prod_tc_kernel<OP, 8, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,  \
+                                (int)oz_tc_smem(8, 1))))                                                   \
+  return e
+  OZCFG(OZ_WL_FWD); OZCFG(OZ_WR_FWD); OZCFG(OZ_CH_FWD); OZCFG(OZ_CH_BWD);
+  OZCFG(OZ_WR_BWD); OZCFG(OZ_WL_BWD); OZCFG(OZ_DT0); OZCFG(OZ_D0T);
 #undef OZCFG
   if ((e = cudaFuncSetAttribute(oz_selftest_prod_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)oz_prod_smem(8))))
@@ -472,15 +484,25 @@ cudaError_t configure_ozaki_kernels() {
   return cudaSuccess;
 }
 
+// tile shape of the products issued by this host thread (the issuing batch's tuned shape)
+static thread_local int g_oz_shape = 0;
+void oz_set_shape(int shape) { g_oz_shape = shape ? 1 : 0; }
+
+template <int OP, int SH>
+static void oz_op_shape(const WalkerDev* W, int nw, int maxN, int mode, int j, int q, cudaStream_t st) {
+  const dim3 g7((maxN + oz_tc_nt(7, SH) - 1) / oz_tc_nt(7, SH), (maxN + 127) / 128, 2 * nw);
+  oz_prod_tc_kernel<OP, 7, SH><<<g7, 256, oz_tc_smem(7, SH), st>>>(W, mode, j, q);
+  if (maxN > 256) {
+    const dim3 g8((maxN + oz_tc_nt(8, SH) - 1) / oz_tc_nt(8, SH), (maxN + 127) / 128, 2 * nw);
+    oz_prod_tc_kernel<OP, 8, SH><<<g8, 256, oz_tc_smem(8, SH), st>>>(W, mode, j, q);
+  }
+}
+
 template <int OP>
 static void oz_op(const WalkerDev* W, int nw, int maxN, int mode, int j, int q, cudaStream_t st) {
   oz_slice_kernel<OP><<<dim3((maxN + 31) / 32, 2 * nw), 256, 0, st>>>(W, mode, j, q);
-  const dim3 g7((maxN + oz_tc_nt(7) - 1) / oz_tc_nt(7), (maxN + 127) / 128, 2 * nw);
-  oz_prod_tc_kernel<OP, 7><<<g7, 256, oz_tc_smem(7), st>>>(W, mode, j, q);
-  if (maxN > 256) {
-    const dim3 g8((maxN + oz_tc_nt(8) - 1) / oz_tc_nt(8), (maxN + 127) / 128, 2 * nw);
-    oz_prod_tc_kernel<OP, 8><<<g8, 256, oz_tc_smem(8), st>>>(W, mode, j, q);
-  }
+  if (g_oz_shape) oz_op_shape<OP, 1>(W, nw, maxN, mode, j, q, st);
+  else oz_op_shape<OP, 0>(W, nw, maxN, mode, j, q, st);
 }
 
 // the slice work of mixed walkers (wraps and chain through the tensor cores)

@@ -37,7 +37,7 @@ EXPORTS = [
     "dqmc_profile_enable", "dqmc_profile_read", "dqmc_microbench_fp64", "dqmc_get_observables_all",
     "dqmc_product_check", "dqmc_product_device_noalloc", "dqmc_launch_count", "dqmc_tuning",
     "dqmc_sweep_dynamic", "dqmc_get_dynamic", "dqmc_clear_dynamic", "dqmc_get_green_dynamic", "dqmc_get_dynamic_obs",
-    "dqmc_get_dynamic_r", "dqmc_measure_bins", "dqmc_set_green", "dqmc_set_wait_limit",
+    "dqmc_get_dynamic_r", "dqmc_measure_bins", "dqmc_set_green", "dqmc_set_wait_limit", "dqmc_tuning_products",
 ]
 KCLASSES = ["segment", "push", "greens", "measure", "product", "metropolis", "dynamic", "dynamic_stab"]
 
@@ -100,6 +100,7 @@ def load() -> ctypes.CDLL:
         "dqmc_measure_bins": (c, [vp, c, c, c, dp]),
         "dqmc_set_green": (c, [vp, c, c, dp]),
         "dqmc_set_wait_limit": (c, [vp, c]),
+        "dqmc_tuning_products": (c, [vp, ip, ip, ip, ctypes.POINTER(ctypes.c_float)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -346,14 +347,22 @@ class Batch:
         return g
 
     def tuning(self) -> dict:
-        """The autotuner's pick (delayed block k, tensor-core flush) and every candidate's time."""
+        """The autotuner's picks and every candidate's time: the Metropolis update kind (delayed
+        block k, tc_flush 0-3) and the tensor-core products' tile shape (product_tile 0: 128 x 32
+        tiles up to N = 256 and 128 x 64 above, 1: the other way round)."""
         kd, tc, n = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
         ck = (ctypes.c_int * 8)()
         ct = (ctypes.c_int * 8)()
         cm = (ctypes.c_float * 8)()
         _check(load().dqmc_tuning(self.h, ctypes.byref(kd), ctypes.byref(tc), ctypes.byref(n), ck, ct, cm))
+        sh, ns = ctypes.c_int(), ctypes.c_int()
+        cs = (ctypes.c_int * 2)()
+        csm = (ctypes.c_float * 2)()
+        _check(load().dqmc_tuning_products(self.h, ctypes.byref(sh), ctypes.byref(ns), cs, csm))
         return {"kd": kd.value, "tc_flush": tc.value,
-                "candidates": [{"kd": ck[i], "tc_flush": ct[i], "ms_per_slice": cm[i]} for i in range(n.value)]}
+                "candidates": [{"kd": ck[i], "tc_flush": ct[i], "ms_per_slice": cm[i]} for i in range(n.value)],
+                "product_tile": sh.value,
+                "product_candidates": [{"tile": cs[i], "ms_per_slice": csm[i]} for i in range(ns.value)]}
 
     def launch_count(self) -> int:
         v = ctypes.c_int64()

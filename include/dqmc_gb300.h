@@ -224,6 +224,12 @@ int dqmc_batch_info(dqmc_batch* b, int* n_walkers, int64_t* updates_per_half_swe
  * dqmc_init_greens runs the tuner on the batch's own state. */
 int dqmc_tuning(dqmc_batch* b, int* kd, int* tc_flush, int* n_candidates, int* cand_kd, int* cand_tc,
                 float* cand_ms);
+/* The autotuner's tile shape for the tensor-core wrap and chain products of a DQMC_MIXED
+ * batch: 0 = 128 x 32 output tiles for N <= 256 (7 slices) and 128 x 64 above (8 slices),
+ * 1 = the other way round; with each candidate's time for one slice's products of the whole
+ * batch (arrays sized 2; no candidates for FP64 or checkerboard-only batches).  No reference
+ * counterpart: the reference's products are MKL calls. */
+int dqmc_tuning_products(dqmc_batch* b, int* shape, int* n_candidates, int* cand_shape, float* cand_ms);
 
 /* Kernels launched by this batch since creation (graph replays count every
  * kernel node of the replayed graph). */

@@ -159,6 +159,12 @@ int dqmc_batch_info(dqmc_batch* b, int* nw, int64_t* upd) {
 }
 int dqmc_profile_enable(dqmc_batch* b, int on) { (void)b, (void)on; return DQMC_ERR_STATE; }
 int dqmc_set_wait_limit(dqmc_batch* b, int limit) { (void)b, (void)limit; return DQMC_ERR_STATE; }
+int dqmc_tuning_products(dqmc_batch* b, int* shape, int* n, int* cs, float* cm) {
+  (void)b, (void)cs, (void)cm;
+  if (shape) *shape = 0;
+  if (n) *n = 0;
+  return DQMC_OK;
+}
 int dqmc_profile_read(dqmc_batch* b, int k, double* ms, int64_t* n) { (void)b, (void)k, (void)ms, (void)n; return DQMC_ERR_STATE; }
 int dqmc_microbench_fp64(double* t) { (void)t; return DQMC_ERR_STATE; }
 int dqmc_product_check(int n, const double* a, const double* b, double* c) { (void)n, (void)a, (void)b, (void)c; return DQMC_ERR_STATE; }

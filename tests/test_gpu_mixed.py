@@ -92,6 +92,10 @@ def test_autotuner_picks_a_timed_candidate(dq):
     best = min(cands, key=lambda c: c["ms_per_slice"])
     assert (t["kd"], t["tc_flush"]) == (best["kd"], best["tc_flush"])
     assert all(c["ms_per_slice"] > 0 for c in cands)
+    # the products' tile shape: both shapes timed, the faster kept
+    pc = t["product_candidates"]
+    assert sorted(c["tile"] for c in pc) == [0, 1] and all(c["ms_per_slice"] > 0 for c in pc)
+    assert t["product_tile"] == min(pc, key=lambda c: c["ms_per_slice"])["tile"]
     bf, of = _run(dq, descs, dq.FP64)
     assert {c["tc_flush"] for c in bf.tuning()["candidates"]} == {0}
     for w in range(len(descs)):
@@ -156,3 +160,28 @@ def test_split_submatrix_equals_fused(dq, monkeypatch):
         for a, c in zip(g2, g3):
             np.testing.assert_array_equal(a, c)
         np.testing.assert_array_equal(o2[0], o3[0])
+
+
+@pytest.mark.parametrize("model,L", [(1, 12), (0, 17)])  # 7-slice (N = 144) and 8-slice (N = 289) products
+def test_product_tile_shapes_agree(dq, monkeypatch, model, L):
+    """The wrap and chain products with 128 x 32 and with 128 x 64 output tiles (the tuner
+    held to each by DQMC_PRODUCT_TILE): the same decisions and G to 1e-10 after a sweep pair."""
+    descs = [dq.WalkerDesc(model=model, L=L, U=4.0, mu=-0.2 * model, beta=1.0, Lt=10, pace=5, seed=450 + w)
+             for w in range(2)]
+    res = []
+    for tile in ("0", "1"):
+        monkeypatch.setenv("DQMC_PRODUCT_TILE", tile)
+        b = dq.Batch(descs, rng=dq.RNG_MINSTD, precision=dq.MIXED)
+        for w in range(2):
+            b.fields_random(w)
+        b.init_greens()
+        assert b.tuning()["product_tile"] == int(tile)
+        b.sweep_0_to_beta(measure=True)
+        b.sweep_beta_to_0(measure=True)
+        res.append(([b.fields(w) for w in range(2)], [b.green(w, 0) for w in range(2)], [b.status(w) for w in range(2)]))
+        b.close()
+    (f0, g0, s0), (f1, g1, s1) = res
+    assert s0 == [0, 0] and s1 == [0, 0]
+    for w in range(2):
+        np.testing.assert_array_equal(f0[w], f1[w])
+        assert float(np.abs(g0[w] - g1[w]).max()) <= 1e-10
