@@ -253,6 +253,9 @@ struct dqmc_batch {
   // their ping-pong chain, product temporary and stabilization scratch, per walker
   struct DynGen { double* chain = nullptr; double* work = nullptr; double* scr = nullptr; };
   std::vector<DynGen> dyn_gen;
+  // the dynamic half-sweep captured once (walker-group branches) and its kernel nodes
+  cudaGraphExec_t dyn_exec = nullptr;
+  int64_t dyn_nodes = 0;
   int* d_taus = nullptr;
   std::vector<int> taus;
   bool at_zero = false;  // stacks of t = 0 (after set-up or a backward half-sweep)
@@ -650,6 +653,7 @@ int dqmc_batch_destroy(dqmc_batch* b) {
   for (auto& row : b->pexec)
     for (auto& g : row)
       if (g) cudaGraphExecDestroy(g);
+  if (b->dyn_exec) cudaGraphExecDestroy(b->dyn_exec);
   for (auto& row : b->pmarks)
     for (auto& v : row)
       for (auto& m : v) { cudaEventDestroy(m.a); cudaEventDestroy(m.b); }
@@ -1173,6 +1177,60 @@ int dqmc_clear_dynamic(dqmc_batch* b) {
   return DQMC_OK;
 }
 
+// The dynamic half-sweep's launch sequence: the walkers' largest N and pace, and which
+// kinds of exp(-dtau K) occur
+struct DynShape {
+  int maxN, maxPace;
+  bool any_dense, any_cb;
+};
+
+// Forward step j of the dynamic half-sweep for walkers W[0..nw) on stream st
+static void issue_dynamic_level(dqmc_batch* b, const DynShape& ds, int j, const WalkerDev* W, int nw,
+                                cudaStream_t st) {
+  const int maxN = ds.maxN;
+  b->timed(DQMC_KCLASS_SEGMENT, [&] { general_chain_init(MODE_FWD, W, nw, j, st); });
+  for (int q = 0; q < ds.maxPace; ++q) {
+    b->timed(DQMC_KCLASS_PRODUCT,
+             [&] { general_dynamic_wrap(W, nw, j, q, maxN, b->mixed, ds.any_dense, ds.any_cb, st); });
+    b->timed(DQMC_KCLASS_DYNAMIC,
+             [&] { general_dynamic_prop(W, nw, j, q, maxN, b->mixed, ds.any_dense, ds.any_cb, st); });
+    b->timed(DQMC_KCLASS_PRODUCT,
+             [&] { general_dynamic_chain(W, nw, j, q, maxN, b->mixed, ds.any_dense, ds.any_cb, st); });
+  }
+  b->timed(DQMC_KCLASS_PUSH, [&] {
+    general_push(MODE_FWD, W, nw, j, maxN, st);
+    if (b->any_ozstab) oz_push(MODE_FWD, W, nw, j, b->maxN_oz, st);
+  });
+  b->timed(DQMC_KCLASS_GREENS, [&] { general_greens(MODE_FWD, W, nw, j, -1, maxN, st); });
+  // the tensor-core walkers' equal-time assembly and their G(t,0), G(0,t) come from one
+  // oz_greens (one factorization of M), timed in this class
+  b->timed(DQMC_KCLASS_DYN_STAB, [&] {
+    general_dynamic_stab(W, nw, j, maxN, st);
+    if (b->any_ozstab) oz_greens(MODE_FWD, W, nw, j, -1, b->maxN_oz, st, true);
+    general_dynamic_stab_measure(W, nw, j, st);
+  });
+}
+
+// All device work of one dynamic half-sweep: as the updating half-sweeps, walker groups
+// run as forked branches (one branch when profiling)
+static void issue_dynamic(dqmc_batch* b, const DynShape& ds) {
+  const int ng = b->prof ? 1 : std::min(b->ngroups, b->nw);
+  b->timed(DQMC_KCLASS_DYNAMIC, [&] { general_dynamic_begin(b->dW, b->nw, b->stream); });
+  if (ng > 1) {
+    cudaEventRecord(b->ev_fork, b->stream);
+    for (int g = 0; g < ng; ++g) {
+      const int w0 = (int)((long long)b->nw * g / ng), w1 = (int)((long long)b->nw * (g + 1) / ng);
+      cudaStreamWaitEvent(b->gst[g], b->ev_fork, 0);
+      for (int j = 0; j < b->maxNs; ++j) issue_dynamic_level(b, ds, j, b->dW + w0, w1 - w0, b->gst[g]);
+      cudaEventRecord(b->ev_join[g], b->gst[g]);
+    }
+    for (int g = 0; g < ng; ++g) cudaStreamWaitEvent(b->stream, b->ev_join[g], 0);
+  } else {
+    for (int j = 0; j < b->maxNs; ++j) issue_dynamic_level(b, ds, j, b->dW, b->nw, b->stream);
+  }
+  b->timed(DQMC_KCLASS_DYNAMIC, [&] { general_dynamic_end(b->dW, b->nw, ds.maxN, b->stream); });
+}
+
 int dqmc_sweep_dynamic(dqmc_batch* b, const int* taus, int ntau) {
   if (!b) return fail(DQMC_ERR_ARG, "null batch");
   if (!b->initialised) return fail(DQMC_ERR_STATE, "dynamic sweep before dqmc_init_greens");
@@ -1211,35 +1269,33 @@ int dqmc_sweep_dynamic(dqmc_batch* b, const int* taus, int ntau) {
     if (h.cb) any_cb = true; else any_dense = true;
   }
   CUDA_TRY(cudaMemcpyAsync(b->dW, hv.data(), sizeof(WalkerDev) * b->nw, cudaMemcpyHostToDevice, b->stream));
-  const cudaStream_t st = b->stream;
-  const WalkerDev* W = b->dW;
-  const int nw = b->nw;
   oz_set_shape(b->oz_shape);
-  b->timed(DQMC_KCLASS_DYNAMIC, [&] { general_dynamic_begin(W, nw, st); });
-  for (int j = 0; j < b->maxNs; ++j) {
-    b->timed(DQMC_KCLASS_SEGMENT, [&] { general_chain_init(MODE_FWD, W, nw, j, st); });
-    for (int q = 0; q < maxPace; ++q) {
-      b->timed(DQMC_KCLASS_PRODUCT,
-               [&] { general_dynamic_wrap(W, nw, j, q, maxN, b->mixed, any_dense, any_cb, st); });
-      b->timed(DQMC_KCLASS_DYNAMIC,
-               [&] { general_dynamic_prop(W, nw, j, q, maxN, b->mixed, any_dense, any_cb, st); });
-      b->timed(DQMC_KCLASS_PRODUCT,
-               [&] { general_dynamic_chain(W, nw, j, q, maxN, b->mixed, any_dense, any_cb, st); });
+  const DynShape ds{maxN, maxPace, any_dense, any_cb};
+  if (b->opt.graphs && !b->prof) {
+    // captured once (the tau list and the per-walker descriptors are read on the device)
+    if (!b->dyn_exec) {
+      GraphGuard g;
+      CUDA_TRY(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+      issue_dynamic(b, ds);
+      CUDA_TRY(cudaStreamEndCapture(b->stream, &g.g));
+      size_t nn = 0;
+      CUDA_TRY(cudaGraphGetNodes(g.g, nullptr, &nn));
+      std::vector<cudaGraphNode_t> nodes(nn);
+      CUDA_TRY(cudaGraphGetNodes(g.g, nodes.data(), &nn));
+      int64_t k = 0;
+      for (auto nd : nodes) {
+        cudaGraphNodeType ty;
+        cudaGraphNodeGetType(nd, &ty);
+        if (ty == cudaGraphNodeTypeKernel) ++k;
+      }
+      b->dyn_nodes = k;
+      CUDA_TRY(cudaGraphInstantiate(&b->dyn_exec, g.g, 0));
     }
-    b->timed(DQMC_KCLASS_PUSH, [&] {
-      general_push(MODE_FWD, W, nw, j, maxN, st);
-      if (b->any_ozstab) oz_push(MODE_FWD, W, nw, j, b->maxN_oz, st);
-    });
-    b->timed(DQMC_KCLASS_GREENS, [&] { general_greens(MODE_FWD, W, nw, j, -1, maxN, st); });
-    // the tensor-core walkers' equal-time assembly and their G(t,0), G(0,t) come from one
-    // oz_greens (one factorization of M), timed in this class
-    b->timed(DQMC_KCLASS_DYN_STAB, [&] {
-      general_dynamic_stab(W, nw, j, maxN, st);
-      if (b->any_ozstab) oz_greens(MODE_FWD, W, nw, j, -1, b->maxN_oz, st, true);
-      general_dynamic_stab_measure(W, nw, j, st);
-    });
+    CUDA_TRY(cudaGraphLaunch(b->dyn_exec, b->stream));
+    b->launches += b->dyn_nodes;
+  } else {
+    issue_dynamic(b, ds);  // eager, one branch when profiling
   }
-  b->timed(DQMC_KCLASS_DYNAMIC, [&] { general_dynamic_end(W, nw, maxN, st); });
   CUDA_TRY(cudaMemcpyAsync(b->dW, b->hw.data(), sizeof(WalkerDev) * b->nw, cudaMemcpyHostToDevice, b->stream));
   CUDA_TRY(cudaStreamSynchronize(b->stream));
   if (int r = launch_check("dynamic sweep")) return r;
