@@ -145,6 +145,8 @@ enum ZOp {
   Z_AQ_UPD,      // Y(j0:, :) -= V_p Wb
   Z_TR_UPD,      // Y(j0:j0+pb, :) -= R(j0:j0+pb, j0+pb:) Y(j0+pb:, :)
   Z_GG,          // G = U_R Drmax^-1 X
+  Z_GRAM,        // Zg = V_p^T V_p (pb x pb, into Wb): the Gram matrix of the panel's reflectors
+  Z_VT,          // Vt = V_p T_p (m x pb, into W2), T_p from ztfac_kernel
   // the dynamic half-sweep's second right-hand side Y2 (dynx) and outputs
   Z_AQ2_W,       // Wb = (V_p T_p)^T Y2(j0:, :)
   Z_AQ2_UPD,     // Y2(j0:, :) -= V_p Wb
@@ -259,6 +261,16 @@ __device__ bool zjob(const WalkerDev& w, int op, int mode, int j, int p, int sp,
       jb.beta = 1; jb.neg = 1;
       return true;
     }
+    case Z_GRAM:
+      jb.a = ZOpnd{z.X + (long long)j0 * N + j0, N, 1, 1, nullptr, nullptr};  // V_p^T
+      jb.b = Vp;
+      jb.c = z.Wb; jb.ldc = TB; jb.M = pb; jb.N = pb; jb.K = m;
+      return true;
+    case Z_VT:
+      jb.a = Vp;
+      jb.b = ZOpnd{z.Tb + (long long)p * TB * TB, TB, 0, 2, nullptr, nullptr};  // T_p, upper with diagonal
+      jb.c = z.W2; jb.ldc = N; jb.M = m; jb.N = pb; jb.K = pb;
+      return true;
     case Z_AQ2_W:
     case Z_AQ2_UPD: {
       if (!w.dynx) return false;
@@ -602,8 +614,7 @@ __global__ void __launch_bounds__(256) zqr_panel_kernel(const WalkerDev* __restr
   const ZScr z = zscr(w, sp);
   extern __shared__ double psm[];
   double* P = psm;                // [TB][m], P[c * m + r]
-  double* T = P + TB * m;         // [TB][TB], T[c * TB + r]
-  double* Z = T + TB * TB;        // [TB][TB] Gram V^T V
+  double* T = P + TB * m;         // [TB][TB], T[c * TB + r] (tau on the diagonal)
   __shared__ double s_red[8];
   __shared__ double s_tau, s_scal;
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
@@ -647,38 +658,14 @@ __global__ void __launch_bounds__(256) zqr_panel_kernel(const WalkerDev* __restr
       }
     __syncthreads();
   }
-  // Gram Z(i, c) = v_i^T v_c for i < c (unit diagonal, zeros above)
-  for (int pr = wid; pr < pb * pb; pr += 8) {
-    const int i = pr / pb, c = pr % pb;
-    if (i >= c) continue;
-    double d = 0.0;
-    for (int r = c + 1 + lane; r < m; r += 32) d = fma(P[i * m + r], P[c * m + r], d);
-    d = zwarp_sum(d);
-    if (lane == 0) Z[c * TB + i] = d + P[i * m + c];
-  }
-  __syncthreads();
-  // T(0:c, c) = -tau_c T(0:c, 0:c) Z(0:c, c)
-  for (int c = 1; c < pb; ++c) {
-    if (tid < c) {
-      double s = 0.0;
-      for (int k = tid; k < c; ++k) s = fma(T[k * TB + tid], Z[c * TB + k], s);
-      T[c * TB + tid] = -T[c * TB + c] * s;
-    }
-    __syncthreads();
-  }
   for (int c = 0; c < pb; ++c)
     for (int r = tid; r < m; r += 256) z.X[(long long)(j0 + c) * N + j0 + r] = P[c * m + r];
-  // Vt = V_p T_p (m x pb, ld N) for the trailing updates: Vt(r, c) = sum_{q <= min(r, c)} V(r, q) T(q, c)
-  for (int e = tid; e < m * pb; e += 256) {
-    const int r = e % m, c = e / m;
-    double s = 0.0;
-    for (int q = 0; q <= min(r, c); ++q) s = fma((q == r) ? 1.0 : P[q * m + r], T[c * TB + q], s);
-    z.W2[(long long)c * N + r] = s;
-  }
+  // the Gram matrix V^T V, the T factor and Vt = V T follow on the tensor cores (Z_GRAM,
+  // ztfac_kernel, Z_VT); the panel leaves tau on the diagonal of its T slot
   double* Tg = z.Tb + (long long)p * TB * TB;
   for (int e = tid; e < TB * TB; e += 256) {
     const int r = e % TB, c = e / TB;
-    Tg[e] = (r <= c && c < pb) ? T[c * TB + r] : 0.0;
+    Tg[e] = (r == c && c < pb) ? T[c * TB + c] : 0.0;
   }
   if (push && tid < pb) {
     const int side = (mode == MODE_FWD) ? 0 : 1;
@@ -688,6 +675,36 @@ __global__ void __launch_bounds__(256) zqr_panel_kernel(const WalkerDev* __restr
     z.invd[j0 + tid] = (d != 0.0) ? 1.0 / d : 0.0;
     if (d == 0.0 || !isfinite(d)) atomicOr(w.status, ST_SINGULAR);
   }
+}
+
+// The T factor of panel p (LAPACK dlarft, forward, columnwise): T(c, c) = tau_c and
+// T(0:c, c) = -tau_c T(0:c, 0:c) Zg(0:c, c), Zg = V^T V from the Z_GRAM product (in Wb).
+// One warp per (walker, spin).
+__global__ void __launch_bounds__(32) ztfac_kernel(const WalkerDev* __restrict__ W, int mode, int j, int p) {
+  const int wi = blockIdx.x >> 1, sp = blockIdx.x & 1;
+  const WalkerDev& w = W[wi];
+  if (!w.ozstab || sp >= w.S || j >= w.nstack) return;
+  const int N = w.N, j0 = p * TB;
+  if (j0 >= N) return;
+  const int pb = min(TB, N - j0), tid = threadIdx.x;
+  const ZScr z = zscr(w, sp);
+  __shared__ double T[TB * TB], Zg[TB * TB];
+  double* Tg = z.Tb + (long long)p * TB * TB;
+  for (int e = tid; e < TB * TB; e += 32) {
+    T[e] = Tg[e];  // tau on the diagonal, zeros elsewhere
+    const int i = e % TB, c = e / TB;
+    Zg[e] = (i < pb && c < pb) ? z.Wb[(long long)c * TB + i] : 0.0;
+  }
+  __syncwarp();
+  for (int c = 1; c < pb; ++c) {
+    double s = 0.0;
+    if (tid < c)
+      for (int k = tid; k < c; ++k) s = fma(T[k * TB + tid], Zg[c * TB + k], s);
+    __syncwarp();
+    if (tid < c) T[c * TB + tid] = -T[c * TB + c] * s;
+    __syncwarp();
+  }
+  for (int e = tid; e < TB * TB; e += 32) Tg[e] = T[e];
 }
 
 // Vt = V_p T_p^T (m x pb, ld N) for forming Q: Vt(r, c) = sum_{c <= q <= r} V(r, q) T(c, q).
@@ -906,7 +923,7 @@ __global__ void __launch_bounds__(256) zdyn_boundary_kernel(const WalkerDev* __r
 #define ZGEMM56 zgemm_tc_kernel<8, 7, 32, 2, 2>
 #define ZGEMM54 zgemm_tc_kernel<9, 6, 32, 4, 1>
 static size_t ztc_smem(int S, int NT, int NS) { return (size_t)NS * oztc::stage_bytes(S, 128, NT); }
-static size_t zpanel_smem(int maxN) { return sizeof(double) * ((size_t)TB * maxN + 2 * TB * TB); }
+static size_t zpanel_smem(int maxN) { return sizeof(double) * ((size_t)TB * maxN + TB * TB); }
 
 cudaError_t configure_stab_oz_kernels(int maxN) {
   cudaError_t e;
@@ -930,11 +947,20 @@ static void zgemm(const WalkerDev* W, int nw, int maxN, int op, int mode, int j,
   if (maxN > 256) ZGEMM54<<<g, 256, ztc_smem(9, 32, 4), st>>>(W, op, mode, j, p, trace_slot);
 }
 
+// Householder panel p: the FP64 column factorization, then its Gram matrix, T factor and
+// Vt = V T (the block reflector in the form the trailing products apply)
+static void zpanel(const WalkerDev* W, int nw, int maxN, int mode, int j, int p, int push, cudaStream_t st) {
+  zqr_panel_kernel<<<2 * nw, 256, zpanel_smem(maxN), st>>>(W, mode, j, p, push);
+  zgemm(W, nw, maxN, Z_GRAM, mode, j, p, TB, TB, -1, st);
+  ztfac_kernel<<<2 * nw, 32, 0, st>>>(W, mode, j, p);
+  zgemm(W, nw, maxN, Z_VT, mode, j, p, maxN, TB, -1, st);
+}
+
 void oz_push(int mode, const WalkerDev* W, int nw, int j, int maxN, cudaStream_t st) {
   const int np = (maxN + TB - 1) / TB;
   zpush_prep_kernel<<<2 * nw, 256, sizeof(long long) * maxN, st>>>(W, mode, j);
   for (int p = 0; p < np; ++p) {
-    zqr_panel_kernel<<<2 * nw, 256, zpanel_smem(maxN), st>>>(W, mode, j, p, 1);
+    zpanel(W, nw, maxN, mode, j, p, 1, st);
     zgemm(W, nw, maxN, Z_QR_W, mode, j, p, TB, maxN, -1, st);
     zgemm(W, nw, maxN, Z_QR_UPD, mode, j, p, maxN, maxN, -1, st);
   }
@@ -956,7 +982,7 @@ void oz_greens(int mode, const WalkerDev* W, int nw, int j, int trace_slot, int 
   zgemm(W, nw, maxN, Z_GA, mode, j, 0, maxN, maxN, -1, st);
   zgemm(W, nw, maxN, Z_GB, mode, j, 0, maxN, maxN, -1, st);
   for (int p = 0; p < np; ++p) {
-    zqr_panel_kernel<<<2 * nw, 256, zpanel_smem(maxN), st>>>(W, mode, j, p, 0);
+    zpanel(W, nw, maxN, mode, j, p, 0, st);
     zgemm(W, nw, maxN, Z_QR_W, mode, j, p, TB, maxN, -1, st);
     zgemm(W, nw, maxN, Z_QR_UPD, mode, j, p, maxN, maxN, -1, st);
     zgemm(W, nw, maxN, Z_AQ_W, mode, j, p, TB, maxN, -1, st);
