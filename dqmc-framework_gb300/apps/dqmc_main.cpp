@@ -118,8 +118,6 @@ int main(int argc, char** argv) {
     const int N = dim == 2 ? L * L : L * L * L;
     const int kidx = cfg.momentum.empty() ? -1 : momentum_index(L, cfg.momentum, dim);
     const auto klist = momentum_list(L, cfg.momentum_list.empty() ? "KstarsAll" : cfg.momentum_list, dim);
-    if (!a.dry_run && cfg.lattice != "Square")
-      throw ConfigError("the GPU sweep runs the square lattice; '" + cfg.lattice + "' is not built on the device");
     std::filesystem::create_directories(a.output);
     std::vector<signed char> fields;
     if (!a.fields.empty()) fields = parse_fields(read_file(a.fields), lt, N);
@@ -143,8 +141,10 @@ int main(int argc, char** argv) {
     Model model = cfg.model == "AttractiveHubbard" ? (Model)AttractiveHubbard() : (Model)RepulsiveHubbard();
     model.set_model_params(cfg.hopping_t, cfg.onsite_u, cfg.chemical_potential);
     if (cfg.checkerboard) model.link_checkerboard(); else model.link();
-    Square lattice;
-    lattice.set_lattice_params({L, L});
+    Square square;
+    Cubic cubic;
+    if (dim == 2) square.set_lattice_params({L, L}); else cubic.set_lattice_params({L, L, L});
+    LatticeBase& lattice = dim == 2 ? (LatticeBase&)square : (LatticeBase&)cubic;
     lattice.momentum_index = kidx;
     DqmcWalker walker;
     walker.set_physical_params(cfg.beta, lt);
@@ -171,10 +171,14 @@ int main(int argc, char** argv) {
     std::vector<int> taus(lt);
     for (int t = 0; t < lt; ++t) taus[t] = t;
     const auto ks = kstars(L, dim);
-    // Fourier factors of the measured momenta, ff[q][r] = cos(-(rx kx + ry ky)) (square.cpp:148-161)
+    // Fourier factors of the measured momenta, ff[q][r] = cos(-r.k) (square.cpp:148-161, cubic.cpp:186-200)
     std::vector<std::vector<double>> ff(klist.size(), std::vector<double>(N));
     for (size_t q = 0; q < klist.size(); ++q)
-      for (int r = 0; r < N; ++r) ff[q][r] = std::cos(-((r % L) * ks[klist[q]][0] + (r / L) * ks[klist[q]][1]));
+      for (int r = 0; r < N; ++r) {
+        double rk = (r % L) * ks[klist[q]][0] + ((r / L) % L) * ks[klist[q]][1];
+        if (dim == 3) rk += (r / (L * L)) * ks[klist[q]][2];
+        ff[q][r] = std::cos(-rk);
+      }
     if (eqt && !dyn) {  // equal-time only: bins normalised on the device, one copy out
       const auto out = walker.MeasureBins(nbins, std::max(cfg.bin_size, 2), cfg.sweeps_between_bins);
       for (int w = 0; w < nw; ++w)

@@ -12,6 +12,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -164,15 +165,20 @@ std::pair<std::vector<double>, std::vector<double>> sym_exp_pair(int n, std::vec
   return {form(x), form(-x)};
 }
 
-// K = -t H + mu I on the periodic square lattice (src/lattice/square.cpp:164-177,
-// with the hopping matrix zero-initialised).
-std::vector<double> kinetic_matrix(int L, double t, double mu) {
-  const int N = L * L;
+int lattice_sites(int L, int dim) { return dim == 3 ? L * L * L : L * L; }
+int desc_sites(const dqmc_walker_desc& d) { return lattice_sites(d.L, d.lattice == DQMC_CUBIC ? 3 : 2); }
+
+// K = -t H + mu I on the periodic square lattice (src/lattice/square.cpp:164-177) or cubic
+// lattice (src/lattice/cubic.cpp:203-219): bonds to the +x, +y (, +z) neighbours, the hopping
+// matrix zero-initialised.
+std::vector<double> kinetic_matrix(int L, double t, double mu, int dim) {
+  const int N = lattice_sites(L, dim);
   std::vector<double> K((size_t)N * N, 0.0);
   for (int i = 0; i < N; ++i) {
-    const int x = i % L, y = i / L;
-    const int jx = (x + 1) % L + L * y, jy = x + L * ((y + 1) % L);
-    for (int j : {jx, jy}) {
+    const int x = i % L, y = (i / L) % L, z = i / (L * L);
+    const int jx = i - x + (x + 1) % L, jy = i + ((y + 1) % L - y) * L, jz = i + ((z + 1) % L - z) * L * L;
+    for (int a = 0; a < dim; ++a) {
+      const int j = a == 0 ? jx : a == 1 ? jy : jz;
       K[(size_t)j * N + i] += -t;
       K[(size_t)i * N + j] += -t;
     }
@@ -181,21 +187,35 @@ std::vector<double> kinetic_matrix(int L, double t, double mu) {
   return K;
 }
 
-// Fourier factors cos(-r.k) per displacement index for k-star kidx
-// (src/lattice/square.cpp:42-66, 148-161).
-std::vector<double> fourier_table(int L, int kidx) {
-  std::vector<double> kx, ky;
-  for (int i = (L + 1) / 2; i <= L; ++i)
-    for (int j = (L + 1) / 2; j <= i; ++j) {
-      kx.push_back((double)i / L * 2 * M_PI - M_PI);
-      ky.push_back((double)j / L * 2 * M_PI - M_PI);
-    }
-  const int nk = (int)kx.size();
-  if (kidx < 0) kidx = nk - 1;  // M point
-  std::vector<double> f((size_t)L * L);
-  for (int d = 0; d < L * L; ++d) {
-    const int x = d % L, y = d / L;
-    f[d] = std::cos(-x * kx[kidx] - y * ky[kidx]);
+// The k stars of the lattice (src/lattice/square.cpp:42-66: the triangle (0,0), (pi,0),
+// (pi,pi); src/lattice/cubic.cpp:47-81: the tetrahedron (0,0,0), (pi,0,0), (pi,pi,0),
+// (pi,pi,pi), z outermost), as (kx, ky, kz) triples.
+std::vector<std::array<double, 3>> k_stars(int L, int dim) {
+  std::vector<std::array<double, 3>> ks;
+  const auto mom = [&](int i) { return (double)i / L * 2 * M_PI - M_PI; };
+  const int lo = (L + 1) / 2;
+  if (dim == 2) {
+    for (int i = lo; i <= L; ++i)
+      for (int j = lo; j <= i; ++j) ks.push_back({mom(i), mom(j), 0.0});
+  } else {
+    for (int k = lo; k <= L; ++k)
+      for (int i = k; i <= L; ++i)
+        for (int j = k; j <= i; ++j) ks.push_back({mom(i), mom(j), mom(k)});
+  }
+  return ks;
+}
+
+// Fourier factors cos(-r.k) per displacement index (the site index of the displacement
+// vector) for k-star kidx (src/lattice/square.cpp:148-161, cubic.cpp:186-200).
+std::vector<double> fourier_table(int L, int kidx, int dim) {
+  const auto ks = k_stars(L, dim);
+  if (kidx < 0) kidx = (int)ks.size() - 1;  // (pi, pi) or (pi, pi, pi)
+  const int N = lattice_sites(L, dim);
+  std::vector<double> f((size_t)N);
+  for (int d = 0; d < N; ++d) {
+    const int x = d % L, y = (d / L) % L, z = d / (L * L);
+    f[d] = (dim == 2) ? std::cos(-x * ks[kidx][0] - y * ks[kidx][1])
+                      : std::cos(-x * ks[kidx][0] - y * ks[kidx][1] - z * ks[kidx][2]);
   }
   return f;
 }
@@ -204,16 +224,18 @@ size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
 // exp(-dtau K) and exp(+dtau K) of a lattice, kept for the life of the process: the Jacobi
 // diagonalisation costs seconds at N = 576 and every batch of the same lattice reuses it
-std::pair<std::vector<double>, std::vector<double>> dense_exponentials(int L, double t, double mu, double dtau) {
+std::pair<std::vector<double>, std::vector<double>> dense_exponentials(int L, int dim, double t, double mu,
+                                                                       double dtau) {
   static std::mutex mu_cache;
-  static std::map<std::tuple<int, double, double, double>, std::pair<std::vector<double>, std::vector<double>>> cache;
-  const auto key = std::make_tuple(L, t, mu, dtau);
+  static std::map<std::tuple<int, int, double, double, double>, std::pair<std::vector<double>, std::vector<double>>>
+      cache;
+  const auto key = std::make_tuple(L, dim, t, mu, dtau);
   {
     std::lock_guard<std::mutex> lock(mu_cache);
     auto it = cache.find(key);
     if (it != cache.end()) return it->second;
   }
-  auto v = sym_exp_pair(L * L, kinetic_matrix(L, t, mu), -dtau);
+  auto v = sym_exp_pair(lattice_sites(L, dim), kinetic_matrix(L, t, mu, dim), -dtau);
   std::lock_guard<std::mutex> lock(mu_cache);
   return cache.emplace(key, std::move(v)).first->second;
 }
@@ -353,13 +375,19 @@ int dqmc_batch_create(const dqmc_walker_desc* descs, int n, const dqmc_batch_opt
     const auto& d = descs[w];
     if (d.model != DQMC_REPULSIVE_HUBBARD && d.model != DQMC_ATTRACTIVE_HUBBARD)
       return fail(DQMC_ERR_ARG, "walker %d: unknown model %d", w, d.model);
+    if (d.lattice != DQMC_SQUARE && d.lattice != DQMC_CUBIC)
+      return fail(DQMC_ERR_ARG, "walker %d: unknown lattice %d", w, d.lattice);
     if (d.L < 2) return fail(DQMC_ERR_ARG, "walker %d: lattice side %d < 2", w, d.L);
-    if (d.L * d.L > kMaxN) return fail(DQMC_ERR_ARG, "walker %d: N = %d exceeds the supported %d", w, d.L * d.L, kMaxN);
+    if (d.L > kMaxN || desc_sites(d) > kMaxN)
+      return fail(DQMC_ERR_ARG, "walker %d: N = %lld exceeds the supported %d", w,
+                  (long long)d.L * d.L * (d.lattice == DQMC_CUBIC ? d.L : 1), kMaxN);
+    if (d.checkerboard && d.lattice == DQMC_CUBIC)  // dqmc_initializer.cpp:169-182
+      return fail(DQMC_ERR_ARG, "walker %d: the checkerboard break-up is built for the square lattice only", w);
     if (d.checkerboard && (d.L % 2)) return fail(DQMC_ERR_ARG, "walker %d: checkerboard needs an even side", w);
     if (d.Lt < 1 || d.pace < 1) return fail(DQMC_ERR_ARG, "walker %d: Lt and pace must be >= 1", w);
     if (!(d.beta > 0) || !(d.onsite_u >= 0) || !(d.hopping_t >= 0))
       return fail(DQMC_ERR_ARG, "walker %d: need beta > 0, U >= 0, t >= 0", w);
-    const int nk = (d.L / 2 + 1) * (d.L / 2 + 2) / 2;
+    const int nk = (int)k_stars(d.L, d.lattice == DQMC_CUBIC ? 3 : 2).size();
     if (d.momentum_index >= nk) return fail(DQMC_ERR_ARG, "walker %d: momentum index out of range", w);
   }
   int dev_count = 0;
@@ -371,7 +399,7 @@ int dqmc_batch_create(const dqmc_walker_desc* descs, int n, const dqmc_batch_opt
   b->opt = o;
   b->desc.assign(descs, descs + n);
   for (auto& d : b->desc) {
-    const int N = d.L * d.L;
+    const int N = desc_sites(d);
     if (N > kMaxSmemN || o.precision == DQMC_MIXED || o.hbm) {
       b->any_general = true;
       b->maxN_general = std::max(b->maxN_general, N);
@@ -385,7 +413,7 @@ int dqmc_batch_create(const dqmc_walker_desc* descs, int n, const dqmc_batch_opt
       b->any_small = true;
       b->maxN_small = std::max(b->maxN_small, N);
     }
-    b->maxN = std::max(b->maxN, d.L * d.L);
+    b->maxN = std::max(b->maxN, desc_sites(d));
     const int ns = (d.Lt % d.pace == 0) ? d.Lt / d.pace : d.Lt / d.pace + 1;
     b->maxNs = std::max(b->maxNs, ns);
     b->maxLt = std::max(b->maxLt, d.Lt);
@@ -400,9 +428,9 @@ int dqmc_batch_create(const dqmc_walker_desc* descs, int n, const dqmc_batch_opt
   // ---- arena layout ----
   struct Off { size_t G, chain, work, scr, sl, sle, stack, fields, ff, trace, msub, zsl; int dense_id; };
   std::vector<Off> off(n);
-  std::map<std::tuple<int, double, double, double>, int> dense_ids;  // (L, t, mu, dtau) -> id
+  std::map<std::tuple<int, int, double, double, double>, int> dense_ids;  // (L, dim, t, mu, dtau) -> id
   std::vector<std::pair<std::vector<double>, std::vector<double>>> dense;
-  std::map<std::pair<int, int>, size_t> ff_off;
+  std::map<std::tuple<int, int, int>, size_t> ff_off;  // (L, dim, k star) -> offset
   size_t cur = 0;
   auto take = [&](size_t bytes) { size_t o2 = cur; cur = align256(cur + bytes); return o2; };
   const size_t scal_off = take(sizeof(dqmc_batch::Scal) * n);
@@ -410,7 +438,7 @@ int dqmc_batch_create(const dqmc_walker_desc* descs, int n, const dqmc_batch_opt
   const size_t desc_off = take(sizeof(WalkerDev) * n);
   for (int w = 0; w < n; ++w) {
     const auto& d = b->desc[w];
-    const int N = d.L * d.L;
+    const int N = desc_sites(d);
     const int S = (d.model == DQMC_ATTRACTIVE_HUBBARD) ? 1 : 2;
     const int ns = (d.Lt % d.pace == 0) ? d.Lt / d.pace : d.Lt / d.pace + 1;
     const size_t lvl = (2 * (size_t)N * N + N + 31) & ~(size_t)31;
@@ -432,21 +460,22 @@ int dqmc_batch_create(const dqmc_walker_desc* descs, int n, const dqmc_batch_opt
                      : 0;
     off[w].dense_id = -1;
     if (!d.checkerboard) {
-      auto key = std::make_tuple(d.L, d.hopping_t, d.mu, d.beta / d.Lt);
+      const int dim = d.lattice == DQMC_CUBIC ? 3 : 2;
+      auto key = std::make_tuple(d.L, dim, d.hopping_t, d.mu, d.beta / d.Lt);
       auto it = dense_ids.find(key);
       if (it == dense_ids.end()) {
-        dense.push_back(dense_exponentials(d.L, d.hopping_t, d.mu, d.beta / d.Lt));
+        dense.push_back(dense_exponentials(d.L, dim, d.hopping_t, d.mu, d.beta / d.Lt));
         it = dense_ids.emplace(key, (int)dense.size() - 1).first;
       }
       off[w].dense_id = it->second;
     }
-    auto fk = std::make_pair(d.L, d.momentum_index < 0 ? -1 : d.momentum_index);
+    auto fk = std::make_tuple(d.L, d.lattice == DQMC_CUBIC ? 3 : 2, d.momentum_index < 0 ? -1 : d.momentum_index);
     if (!ff_off.count(fk)) ff_off[fk] = take(sizeof(double) * N);
     off[w].ff = ff_off[fk];
   }
   std::vector<size_t> dense_off(dense.size()), dense_sl(dense.size()), dense_sle(dense.size());
   std::vector<int> dense_n(dense.size());
-  for (auto& kv : dense_ids) dense_n[kv.second] = std::get<0>(kv.first) * std::get<0>(kv.first);
+  for (auto& kv : dense_ids) dense_n[kv.second] = lattice_sites(std::get<0>(kv.first), std::get<1>(kv.first));
   for (size_t i = 0; i < dense.size(); ++i) {
     const size_t nn = dense[i].first.size();
     dense_off[i] = take(sizeof(double) * 2 * nn);
@@ -532,7 +561,7 @@ int dqmc_batch_create(const dqmc_walker_desc* descs, int n, const dqmc_batch_opt
   }
   std::vector<std::vector<double>> fftabs;
   for (auto& kv : ff_off) {
-    fftabs.push_back(fourier_table(kv.first.first, kv.first.second));
+    fftabs.push_back(fourier_table(std::get<0>(kv.first), std::get<2>(kv.first), std::get<1>(kv.first)));
     cudaMemcpyAsync(base + kv.second, fftabs.back().data(), sizeof(double) * fftabs.back().size(),
                     cudaMemcpyHostToDevice, b->stream);
   }
@@ -544,9 +573,10 @@ int dqmc_batch_create(const dqmc_walker_desc* descs, int n, const dqmc_batch_opt
     const auto& d = b->desc[w];
     WalkerDev& h = b->hw[w];
     std::memset(&h, 0, sizeof h);
-    const int N = d.L * d.L;
+    const int N = desc_sites(d);
     h.N = N;
     h.L = d.L;
+    h.dim = (d.lattice == DQMC_CUBIC) ? 3 : 2;
     h.Lt = d.Lt;
     h.pace = d.pace;
     h.nstack = (d.Lt % d.pace == 0) ? d.Lt / d.pace : d.Lt / d.pace + 1;
@@ -692,7 +722,7 @@ static int check_walker(dqmc_batch* b, int w) {
 int dqmc_fields_random(dqmc_batch* b, int w) {
   if (int r = check_walker(b, w)) return r;
   const auto& d = b->desc[w];
-  const int N = d.L * d.L;
+  const int N = desc_sites(d);
   std::vector<int8_t> f((size_t)d.Lt * N);
   for (int t = 0; t < d.Lt; ++t)
     for (int i = 0; i < N; ++i)  // bernoulli(0.5): u < 0.5 -> +1 (repulsive_hubbard.cpp:92-97)
@@ -707,7 +737,7 @@ int dqmc_set_fields(dqmc_batch* b, int w, const int8_t* f) {
   if (int r = check_walker(b, w)) return r;
   if (!f) return fail(DQMC_ERR_ARG, "null fields");
   const auto& d = b->desc[w];
-  const size_t n = (size_t)d.Lt * d.L * d.L;
+  const size_t n = (size_t)d.Lt * desc_sites(d);
   for (size_t k = 0; k < n; ++k)
     if (f[k] != 1 && f[k] != -1) return fail(DQMC_ERR_ARG, "field value %d at %zu is not +/-1", (int)f[k], k);
   CUDA_TRY(cudaMemcpyAsync(b->hw[w].fields, f, n, cudaMemcpyHostToDevice, b->stream));
@@ -720,7 +750,7 @@ int dqmc_get_fields(dqmc_batch* b, int w, int8_t* f) {
   if (int r = check_walker(b, w)) return r;
   if (!f) return fail(DQMC_ERR_ARG, "null output");
   const auto& d = b->desc[w];
-  CUDA_TRY(cudaMemcpyAsync(f, b->hw[w].fields, (size_t)d.Lt * d.L * d.L, cudaMemcpyDeviceToHost, b->stream));
+  CUDA_TRY(cudaMemcpyAsync(f, b->hw[w].fields, (size_t)d.Lt * desc_sites(d), cudaMemcpyDeviceToHost, b->stream));
   CUDA_TRY(cudaStreamSynchronize(b->stream));
   return DQMC_OK;
 }
@@ -990,7 +1020,7 @@ static int half_sweep(dqmc_batch* b, int mode, int measure) {
     // one uniform per site attempt in sweep order, drawn as bernoulli_distribution does
     for (int w = 0; w < b->nw; ++w) {
       const auto& d = b->desc[w];
-      const size_t n = (size_t)d.Lt * d.L * d.L;
+      const size_t n = (size_t)d.Lt * desc_sites(d);
       double* u = b->h_uni + b->uni_stride * w;
       for (size_t k = 0; k < n; ++k) u[k] = std::generate_canonical<double, 53>(b->eng[w]);
     }
@@ -1566,7 +1596,7 @@ int dqmc_batch_info(dqmc_batch* b, int* nw, int64_t* upd) {
   if (nw) *nw = b->nw;
   if (upd) {
     int64_t s = 0;
-    for (auto& d : b->desc) s += (int64_t)d.L * d.L * d.Lt;
+    for (auto& d : b->desc) s += (int64_t)desc_sites(d) * d.Lt;
     *upd = s;
   }
   return DQMC_OK;

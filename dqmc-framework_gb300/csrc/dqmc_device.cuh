@@ -33,6 +33,7 @@ enum : int {
 
 struct WalkerDev {
   int N, L, Lt, pace, nstack, S, model, cb;  // model: 0 repulsive, 1 attractive
+  int dim;                                    // 2 square (N = L^2), 3 cubic (N = L^3)
   int rng;                                    // 0 host uniforms, 1 Philox
   int path;                                   // 0 SMEM FP64, 1 HBM FP64, 2 HBM mixed (tensor-core products)
   double hop_t;
@@ -154,6 +155,35 @@ __device__ __forceinline__ FlipRatio flip_ratio(const WalkerDev& w, int si, doub
 __device__ __forceinline__ void flip_factors(const WalkerDev& w, const FlipRatio& q, double* f) {
   f[0] = __ddiv_rn(q.cu, q.ru);
   f[1] = (w.model == 0) ? __ddiv_rn(q.cd, q.rd) : f[0];
+}
+
+// Site i of a walker's lattice is x + L y (+ L^2 z).  The displacement from site i to site j
+// as the site index of its vector, each component mod L (src/lattice/square.cpp:88-105,
+// src/lattice/cubic.cpp:112-132), and the neighbour of site i in direction +x, +y or +z.
+__device__ __forceinline__ int site_disp(int L, int dim, int i, int j) {
+  if (dim == 2) {
+    int dx = j % L - i % L, dy = j / L - i / L;
+    dx += (dx < 0) ? L : 0;
+    dy += (dy < 0) ? L : 0;
+    return dx + dy * L;
+  }
+  const int LL = L * L;
+  int dx = j % L - i % L, dy = (j / L) % L - (i / L) % L, dz = j / LL - i / LL;
+  dx += (dx < 0) ? L : 0;
+  dy += (dy < 0) ? L : 0;
+  dz += (dz < 0) ? L : 0;
+  return dx + dy * L + dz * LL;
+}
+__device__ __forceinline__ int site_nn(int L, int i, int a) {
+  const int w = (a == 0) ? 1 : (a == 1) ? L : L * L;
+  const int c = (i / w) % L;
+  return i + ((c + 1) % L - c) * w;
+}
+// the site at displacement r from site i
+__device__ __forceinline__ int site_shift(int L, int dim, int i, int r) {
+  int j = 0;
+  for (int a = 0, w = 1; a < dim; ++a, w *= L) j += (((i / w) % L + (r / w) % L) % L) * w;
+  return j;
 }
 
 __host__ __device__ inline double* stack_level(const WalkerDev& w, int side, int spin, int level) {

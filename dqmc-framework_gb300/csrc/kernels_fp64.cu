@@ -285,15 +285,16 @@ __device__ void mult_transB_left(const WalkerDev& w, double* M, int ld, const do
 // --------------------------------------------------------------------------
 __device__ void measure_slice(const WalkerDev& w, const double* gu, const double* gd, int ld, double sg,
                               double* scratch /* 2N */, double* red) {
-  const int N = w.N, L = w.L;
+  const int N = w.N, L = w.L, LL = L * L;
   double* du = scratch;
   double* dd = scratch + N;
-  __shared__ signed char s_x[kMaxSmemN], s_y[kMaxSmemN];
+  __shared__ signed char s_x[kMaxSmemN], s_y[kMaxSmemN], s_z[kMaxSmemN];
   for (int i = threadIdx.x; i < N; i += kThreads) {
     du[i] = 1.0 - at(gu, ld, i, i);
     dd[i] = 1.0 - at(gd, ld, i, i);
     s_x[i] = (signed char)(i % L);
-    s_y[i] = (signed char)(i / L);
+    s_y[i] = (signed char)((i / L) % L);
+    s_z[i] = (signed char)(i / LL);  // 0 on the square lattice
   }
   __syncthreads();
   // v: 0 trace, 1 double occ, 2 local spin, 3 kinetic, 4 n(k), 5 common, 6 cross, 7 s-wave
@@ -303,17 +304,23 @@ __device__ void measure_slice(const WalkerDev& w, const double* gu, const double
     v[0] += a + b;
     v[1] += du[i] * dd[i];
     v[2] += a + b - 2 * a * b;
-    const int x = i % L, y = i / L;
-    const int jx = (x + 1) % L + L * y, jy = x + L * ((y + 1) % L);
-    v[3] += at(gu, ld, i, jx) + at(gd, ld, i, jx) + at(gu, ld, i, jy) + at(gd, ld, i, jy);
+    // bonds to the +x, +y (, +z) neighbours (measure_methods.cpp:87-95)
+    const int jx = site_nn(L, i, 0), jy = site_nn(L, i, 1);
+    double kin = at(gu, ld, i, jx) + at(gd, ld, i, jx) + at(gu, ld, i, jy) + at(gd, ld, i, jy);
+    if (w.dim == 3) {
+      const int jz = site_nn(L, i, 2);
+      kin += at(gu, ld, i, jz) + at(gd, ld, i, jz);
+    }
+    v[3] += kin;
   }
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   for (int j = wid; j < N; j += kThreads / 32)
   for (int i = lane; i < N; i += 32) {
-    int dx = s_x[j] - s_x[i], dy = s_y[j] - s_y[i];
+    int dx = s_x[j] - s_x[i], dy = s_y[j] - s_y[i], dz = s_z[j] - s_z[i];
     dx += (dx < 0) ? L : 0;
     dy += (dy < 0) ? L : 0;
-    const double ff = w.ff[dx + dy * L];
+    dz += (dz < 0) ? L : 0;
+    const double ff = w.ff[dx + dy * L + dz * LL];
     const double gu_ij = at(gu, ld, i, j), gu_ji = at(gu, ld, j, i);
     const double gd_ij = at(gd, ld, i, j), gd_ji = at(gd, ld, j, i);
     const double dij = (i == j) ? 1.0 : 0.0;

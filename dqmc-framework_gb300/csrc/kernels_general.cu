@@ -536,23 +536,35 @@ __global__ void __launch_bounds__(256) measure_general_kernel(const WalkerDev* _
     v[0] += a + b;
     v[1] += du[i] * dd[i];
     v[2] += a + b - 2 * a * b;
-    const int x = i % L, y = i / L;
-    const int jx = (x + 1) % L + L * y, jy = x + L * ((y + 1) % L);
-    v[3] += gu[(long long)jx * N + i] + gd[(long long)jx * N + i] + gu[(long long)jy * N + i] + gd[(long long)jy * N + i];
+    // bonds to the +x, +y (, +z) neighbours (measure_methods.cpp:87-95)
+    const int jx = site_nn(L, i, 0), jy = site_nn(L, i, 1);
+    double kin = gu[(long long)jx * N + i] + gd[(long long)jx * N + i] + gu[(long long)jy * N + i] + gd[(long long)jy * N + i];
+    if (w.dim == 3) {
+      const int jz = site_nn(L, i, 2);
+      kin += gu[(long long)jz * N + i] + gd[(long long)jz * N + i];
+    }
+    v[3] += kin;
     // i = jj: the pair loop's off-diagonal forms give -ff0 (Gu_ii^2 + Gd_ii^2) and Gu_ii Gd_ii
     v[5] += ff0 * (a + b);
     v[7] += du[i] * dd[i] - a * b;
   }
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   double p4 = 0.0, p5 = 0.0;  // pair parts of v4 and v5 (one spin matrix: doubled below)
+  const int dim = w.dim;
   for (int jj = wid; jj < N; jj += blockDim.x >> 5) {
     const int xj = jj % L, yj = jj / L;
     double cu = 0.0, cd = 0.0;
     for (int i = lane; i < N; i += 32) {
-      int dx = xj - i % L, dy = yj - i / L;
-      dx += (dx < 0) ? L : 0;
-      dy += (dy < 0) ? L : 0;
-      const double ff = w.ff[dx + dy * L];
+      int r;
+      if (dim == 2) {
+        int dx = xj - i % L, dy = yj - i / L;
+        dx += (dx < 0) ? L : 0;
+        dy += (dy < 0) ? L : 0;
+        r = dx + dy * L;
+      } else {
+        r = site_disp(L, 3, i, jj);
+      }
+      const double ff = w.ff[r];
       const double gu_ij = gu[(long long)jj * N + i], gu_ji = gu[(long long)i * N + jj];
       cu = fma(ff, du[i], cu);
       if (one) {
@@ -1136,7 +1148,13 @@ __global__ void __launch_bounds__(256) dyn_measure_kernel(const WalkerDev* __res
     // G(k,tau) and the density of states read G(beta,beta) at tau = 0 (Greentt(Lt-1))
     const double* gk[2] = {phase == 2 ? gtt[0] : gt0[0], phase == 2 ? gtt[1] : gt0[1]};
     double v = 0.0, tr = 0.0, cpart = 0.0, rcor = 0.0;
-    for (int jj = wid; jj < N; jj += 8) {
+    // cubic lattice: G(k,tau) only; the stiffness is a square-lattice observable
+    // (dqmc_initializer.cpp:233-237, measure_methods.cpp:350)
+    if (w.dim == 3)
+      for (int jj = wid; jj < N; jj += 8)
+        for (int i = lane; i < N; i += 32)
+          v += w.ff[site_disp(L, 3, i, jj)] * (gk[0][(long long)i * N + jj] + gk[1][(long long)i * N + jj]);
+    for (int jj = wid; jj < N && w.dim == 2; jj += 8) {
       const int xj = jj % L, yj = jj / L;
       const int jpx = (xj + 1) % L + L * yj;
       for (int i = lane; i < N; i += 32) {
@@ -1163,7 +1181,7 @@ __global__ void __launch_bounds__(256) dyn_measure_kernel(const WalkerDev* __res
       const int rx = r % L, ry = r / L;
       double sr = 0.0;
       for (int i = lane; i < N; i += 32) {
-        const int jj = (i % L + rx) % L + L * ((i / L + ry) % L);
+        const int jj = (w.dim == 2) ? (i % L + rx) % L + L * ((i / L + ry) % L) : site_shift(L, 3, i, r);
         sr += gk[0][(long long)i * N + jj] + gk[1][(long long)i * N + jj];
       }
       sr = warp_sum_g(sr);
@@ -1171,7 +1189,7 @@ __global__ void __launch_bounds__(256) dyn_measure_kernel(const WalkerDev* __res
     }
     for (int i = threadIdx.x; i < N; i += blockDim.x) {
       const long long d = (long long)i * N + i;
-      const int xi = i % L, yi = i / L, ipx = (xi + 1) % L + L * yi;
+      const int ipx = site_nn(L, i, 0);
       tr += gk[0][d] + gk[1][d];
       cpart += g0t[0][d] * gt0[0][d] + g0t[1][d] * gt0[1][d];
       // parts that wait for G(beta,beta): d_i of the spin susceptibility, A_i of the stiffness
@@ -1210,7 +1228,7 @@ __global__ void __launch_bounds__(256) dyn_measure_kernel(const WalkerDev* __res
   double* B = e + N;
   for (int i = threadIdx.x; i < N; i += blockDim.x) {
     const long long d = (long long)i * N + i;
-    const int ipx = (i % L + 1) % L + L * (i / L);
+    const int ipx = site_nn(L, i, 0);
     const double* g0 = w.G;
     const double* g1 = w.G + (S == 2 ? NN : 0);
     e[i] = (1.0 - g0[d]) - (1.0 - g1[d]);
@@ -1221,7 +1239,7 @@ __global__ void __launch_bounds__(256) dyn_measure_kernel(const WalkerDev* __res
     const double* dv = w.dyn_vec + (long long)k * 2 * N;
     double ch = 0.0, un = 0.0;
     for (int i = threadIdx.x; i < N; i += blockDim.x) ch += dv[i] * e[i];
-    for (int jj = wid; jj < N; jj += 8) {
+    for (int jj = wid; jj < N && w.dim == 2; jj += 8) {
       const int xj = jj % L, yj = jj / L;
       for (int i = lane; i < N; i += 32) {
         int dx = xj - i % L, dy = yj - i / L;
@@ -1245,7 +1263,7 @@ __global__ void __launch_bounds__(256) dyn_measure_kernel(const WalkerDev* __res
       }
       const double n = (double)N;
       w.dyn_obs[k * 3 + 1] += 0.25 * sg / n * (c2 - w.dyn_part[k * 2 + 0]);
-      w.dyn_obs[k * 3 + 2] += 0.25 * w.hop_t * w.hop_t * sg * (w.dyn_part[k * 2 + 1] - u2) / (n * n);
+      if (w.dim == 2) w.dyn_obs[k * 3 + 2] += 0.25 * w.hop_t * w.hop_t * sg * (w.dyn_part[k * 2 + 1] - u2) / (n * n);
     }
     __syncthreads();
   }

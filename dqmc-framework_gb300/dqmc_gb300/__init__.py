@@ -18,6 +18,7 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(os.path.dirname(_HERE), "lib", "libdqmc_gb300.so")
 
 REPULSIVE, ATTRACTIVE = 0, 1
+SQUARE, CUBIC = 0, 1
 RNG_MINSTD, RNG_PHILOX = 0, 1
 FP64, MIXED = 0, 1
 OBS_NAMES = [
@@ -51,7 +52,7 @@ class _Desc(ctypes.Structure):
         ("model", ctypes.c_int), ("L", ctypes.c_int), ("hopping_t", ctypes.c_double),
         ("onsite_u", ctypes.c_double), ("mu", ctypes.c_double), ("beta", ctypes.c_double),
         ("Lt", ctypes.c_int), ("pace", ctypes.c_int), ("checkerboard", ctypes.c_int),
-        ("momentum_index", ctypes.c_int), ("seed", ctypes.c_uint64),
+        ("momentum_index", ctypes.c_int), ("seed", ctypes.c_uint64), ("lattice", ctypes.c_int),
     ]
 
 
@@ -129,14 +130,15 @@ class WalkerDesc:
     checkerboard: bool = False
     momentum_index: int = -1
     seed: int = 0
+    lattice: int = SQUARE
 
     @property
     def N(self) -> int:
-        return self.L * self.L
+        return self.L ** (3 if self.lattice == CUBIC else 2)
 
     def _c(self) -> _Desc:
         return _Desc(self.model, self.L, self.t, abs(self.U), self.mu, self.beta, self.Lt, self.pace,
-                     int(self.checkerboard), self.momentum_index, self.seed)
+                     int(self.checkerboard), self.momentum_index, self.seed, self.lattice)
 
 
 class Batch:
@@ -328,12 +330,13 @@ class Batch:
         return out[:n]
 
     def dynamic_greens_k(self, w: int, momenta) -> np.ndarray:
-        """G(k,tau) sums [k][tau] for the momenta (kx, ky) (measure_greens_functions):
-        sum_r cos(-(rx kx + ry ky)) S(r)."""
-        L = self._walker(w).L
-        r = np.arange(L * L)
-        rx, ry = r % L, r // L
-        ff = np.array([np.cos(-(rx * kx + ry * ky)) for kx, ky in momenta])  # [k][r]
+        """G(k,tau) sums [k][tau] for the momenta (kx, ky) or (kx, ky, kz) (measure_greens_functions):
+        sum_r cos(-k.r) S(r)."""
+        d = self._walker(w)
+        L = d.L
+        r = np.arange(d.N)
+        coords = [r % L, (r // L) % L, r // (L * L)]
+        ff = np.array([np.cos(-sum(c * k for c, k in zip(coords, kv))) for kv in momenta])  # [k][r]
         return ff @ self.dynamic_r(w).T
 
     def clear_dynamic(self):

@@ -45,20 +45,19 @@ def run(cfg: dio.RunConfig, out_dir: str, walkers: int = 1, seed: int = 12345, f
     import dqmc_gb300 as dq
 
     log = log if log is not None else sys.stdout  # resolved per call, so redirections apply
-    if cfg.lattice != "Square":
-        raise NotImplementedError(f"the GPU sweep runs the square lattice; '{cfg.lattice}' is not built on the device")
     rank, size = parallel.init()
     t_start = time.perf_counter()
     if size > 1:
         import torch
 
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
-    L, lt = cfg.L, cfg.time_size
-    kidx = dio.momentum_index(L, cfg.momentum) if cfg.momentum else -1
+    L, lt, dim = cfg.L, cfg.time_size, cfg.dim
+    kidx = dio.momentum_index(L, cfg.momentum, dim) if cfg.momentum else -1
     model = dq.ATTRACTIVE if cfg.model == "AttractiveHubbard" else dq.REPULSIVE
     descs = [dq.WalkerDesc(model=model, L=L, t=cfg.hopping_t, U=cfg.onsite_u, mu=cfg.chemical_potential,
                            beta=cfg.beta, Lt=lt, pace=cfg.stabilization_pace, checkerboard=cfg.checkerboard,
-                           momentum_index=kidx, seed=seed + rank * walkers + w) for w in range(walkers)]
+                           momentum_index=kidx, lattice=dq.CUBIC if dim == 3 else dq.SQUARE,
+                           seed=seed + rank * walkers + w) for w in range(walkers)]
     b = dq.Batch(descs, rng=dq.RNG_PHILOX if rng == "philox" else dq.RNG_MINSTD,
                  precision=dq.MIXED if precision == "mixed" else dq.FP64)
     if rank == 0:
@@ -71,7 +70,7 @@ def run(cfg: dio.RunConfig, out_dir: str, walkers: int = 1, seed: int = 12345, f
         if fields_file:
             with open(fields_file, encoding="utf-8") as f:
                 flt, fn, fields = dio.parse_fields(f.read())
-            if flt != lt or fn != L * L:
+            if flt != lt or fn != L ** dim:
                 raise ValueError("fields file size does not match the configuration")
             for w in range(walkers):
                 b.set_fields(w, np.array(fields, dtype=np.int8))
@@ -87,8 +86,8 @@ def run(cfg: dio.RunConfig, out_dir: str, walkers: int = 1, seed: int = 12345, f
         nbins = math.ceil(cfg.bin_num / (walkers * size)) if (eqt or dyn) else 0
         eq_bins = [[] for _ in range(walkers)]
         dyn_bins = {k: [[] for _ in range(walkers)] for k in ("greens", "dos", "dss", "rho", "sign")}
-        ks = dio.kstars(L)
-        klist = [ks[i] for i in dio.momentum_list_indices(L, cfg.momentum_list or "KstarsAll")]
+        ks = dio.kstars(L, dim)
+        klist = [ks[i] for i in dio.momentum_list_indices(L, cfg.momentum_list or "KstarsAll", dim)]
         if eqt and not dyn:  # equal-time only: bins normalised on the device, one copy out
             binned = b.measure_bins(nbins, max(cfg.bin_size, 2), cfg.sweeps_between_bins)
             for w in range(walkers):
@@ -175,7 +174,7 @@ def run(cfg: dio.RunConfig, out_dir: str, walkers: int = 1, seed: int = 12345, f
             f.write(dio.format_fields(fields0))
     else:
         write("fields.out", dio.format_fields(fields0))
-    write("kstars.out", dio.format_kstars(L))
+    write("kstars.out", dio.format_kstars(L, dim))
     write("tgrids.out", dio.format_tgrids(cfg.beta, lt))
     log.write(dio.format_summary(results))
     return results

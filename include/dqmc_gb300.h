@@ -27,7 +27,7 @@
 extern "C" {
 #endif
 
-#define DQMC_ABI_VERSION 2
+#define DQMC_ABI_VERSION 3
 
 enum dqmc_status {
   DQMC_OK = 0,
@@ -39,6 +39,10 @@ enum dqmc_status {
 };
 
 enum dqmc_model { DQMC_REPULSIVE_HUBBARD = 0, DQMC_ATTRACTIVE_HUBBARD = 1 };
+
+/* Lattice::Square (src/lattice/square.cpp) and Lattice::Cubic (src/lattice/cubic.cpp),
+ * periodic, side L: N = L^2 or L^3 sites, site index x + L y (+ L^2 z). */
+enum dqmc_lattice { DQMC_SQUARE = 0, DQMC_CUBIC = 1 };
 
 enum dqmc_rng {
   DQMC_RNG_MINSTD = 0,  /* parity mode: per-walker std::minstd_rand0 on the host,
@@ -73,22 +77,24 @@ enum dqmc_observable {
 
 /* One walker: the parameters the reference spreads over
  * Model::set_model_params (include/model/model_base.h:111-163),
- * Lattice::Square::set_lattice_params (src/lattice/square.cpp:16-28),
+ * Lattice::Square / Lattice::Cubic::set_lattice_params (src/lattice/square.cpp:16-28,
+ * src/lattice/cubic.cpp:17-32),
  * DqmcWalker::set_physical_params / set_stabilization_pace
  * (src/dqmc_walker.cpp:25-38) and the checkerboard link
  * (src/model/model_base.cpp:38-55). */
 typedef struct dqmc_walker_desc {
   int model;           /* enum dqmc_model */
-  int L;               /* square lattice side, N = L*L sites */
+  int L;               /* lattice side: N = L*L sites (square) or L*L*L (cubic) */
   double hopping_t;
   double onsite_u;     /* |U|; the attractive model takes |U| (attractive_hubbard.cpp:37) */
   double mu;
   double beta;
   int Lt;              /* imaginary-time slices, dtau = beta / Lt */
   int pace;            /* stabilization pace */
-  int checkerboard;    /* 0: dense exp(-dtau K); 1: checkerboard break-up (even L) */
-  int momentum_index;  /* k-star index for SDW/CDW/n(k); -1 = M point (pi, pi) */
+  int checkerboard;    /* 0: dense exp(-dtau K); 1: checkerboard break-up (even L, square only) */
+  int momentum_index;  /* k-star index for SDW/CDW/n(k); -1 = the last star, (pi, pi) or (pi, pi, pi) */
   uint64_t seed;       /* minstd seed (parity) or Philox key (throughput) */
+  int lattice;         /* enum dqmc_lattice (0 = square) */
 } dqmc_walker_desc;
 
 typedef struct dqmc_batch_options {

@@ -1,7 +1,7 @@
 // dqmc_gb300.hpp — C++ host interface over the C-ABI (include/dqmc_gb300.h),
 // mirroring the reference's operator interface (dqmc-framework):
 //   Model::RepulsiveHubbard / AttractiveHubbard   include/model/*.h
-//   Lattice::Square                                include/lattice/square.h
+//   Lattice::Square / Lattice::Cubic               include/lattice/square.h, cubic.h
 //   QuantumMonteCarlo::DqmcWalker                  include/dqmc_walker.h:107-184
 //   Measure::MeasureHandler                        include/measure/measure_handler.h
 //   QuantumMonteCarlo::Dqmc::thermalize / measure / analyse   src/dqmc.cpp:48-158
@@ -46,16 +46,29 @@ struct Model {
 struct RepulsiveHubbard : Model { RepulsiveHubbard() { type = DQMC_REPULSIVE_HUBBARD; } };
 struct AttractiveHubbard : Model { AttractiveHubbard() { type = DQMC_ATTRACTIVE_HUBBARD; } };
 
-// ---- Lattice::Square (src/lattice/square.cpp:16-28) ----------------------------
-struct Square {
+// ---- Lattice::Square (src/lattice/square.cpp:16-28), Lattice::Cubic (src/lattice/cubic.cpp:19-31)
+struct LatticeBase {
+  int type = DQMC_SQUARE;
   int side = 4;
-  int momentum_index = -1;  // -1 = MPoint
+  int momentum_index = -1;  // -1 = the last k star: MPoint (pi, pi) / RPoint (pi, pi, pi)
+  int SpaceDim() const { return type == DQMC_CUBIC ? 3 : 2; }
+  int SpaceSize() const { return type == DQMC_CUBIC ? side * side * side : side * side; }
+};
+struct Square : LatticeBase {
   void set_lattice_params(const std::vector<int>& side_length_vec) {
     if (side_length_vec.size() != 2 || side_length_vec[0] != side_length_vec[1] || side_length_vec[0] < 2)
       throw Error(DQMC_ERR_ARG, "Square: need two equal sides >= 2");
     side = side_length_vec[0];
   }
-  int SpaceSize() const { return side * side; }
+};
+struct Cubic : LatticeBase {
+  Cubic() { type = DQMC_CUBIC; }
+  void set_lattice_params(const std::vector<int>& side_length_vec) {
+    if (side_length_vec.size() != 3 || side_length_vec[0] != side_length_vec[1] ||
+        side_length_vec[0] != side_length_vec[2] || side_length_vec[0] < 2)
+      throw Error(DQMC_ERR_ARG, "Cubic: need three equal sides >= 2");
+    side = side_length_vec[0];
+  }
 };
 
 // ---- MeasureHandler (src/measure/measure_handler.cpp) ------------------------
@@ -111,12 +124,13 @@ class DqmcWalker {
   }
   // one walker per seed; rng = DQMC_RNG_MINSTD reproduces the reference stream; precision
   // DQMC_MIXED selects the tensor-core path; hbm puts every walker on the HBM path
-  void initial(const Square& lat, const Model& model, const std::vector<uint64_t>& seeds,
+  void initial(const LatticeBase& lat, const Model& model, const std::vector<uint64_t>& seeds,
                int rng = DQMC_RNG_MINSTD, int precision = DQMC_FP64, bool hbm = false) {
     std::vector<dqmc_walker_desc> d(seeds.size());
     for (size_t w = 0; w < seeds.size(); ++w) {
       d[w] = dqmc_walker_desc{model.type, lat.side, model.hopping_t, model.onsite_u, model.chemical_potential,
-                              beta_, lt_, pace_, model.checkerboard ? 1 : 0, lat.momentum_index, seeds[w]};
+                              beta_, lt_, pace_, model.checkerboard ? 1 : 0, lat.momentum_index, seeds[w],
+                              lat.type};
     }
     dqmc_batch_options o{rng, precision, 0, 1, hbm ? 1 : 0};
     if (b_) dqmc_batch_destroy(b_);

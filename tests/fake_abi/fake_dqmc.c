@@ -32,7 +32,7 @@ int dqmc_batch_create(const dqmc_walker_desc* d, int n, const dqmc_batch_options
   dqmc_batch* b = (dqmc_batch*)calloc(1, sizeof *b);
   b->n = n;
   b->lt = d[0].Lt;
-  b->N = d[0].L * d[0].L;
+  b->N = d[0].L * d[0].L * (d[0].lattice == DQMC_CUBIC ? d[0].L : 1);
   b->ecount = (int*)calloc(n, sizeof(int));
   b->dcount = (int*)calloc(n, sizeof(int));
   b->ebins = (int*)calloc(n, sizeof(int));

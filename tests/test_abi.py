@@ -36,7 +36,14 @@ def test_exports_every_declared_symbol(dq):
 
 
 def test_abi_version(dq):
-    assert dq.load().dqmc_abi_version() == 2
+    assert dq.load().dqmc_abi_version() == 3
+
+
+def test_walker_desc_layout_matches_header(dq):
+    """dqmc_walker_desc as the header lays it out: the lattice field last, after the seed."""
+    d = dq._Desc
+    assert d.lattice.offset == d.seed.offset + 8 and ctypes.sizeof(d) == d.lattice.offset + 8
+    assert dq.WalkerDesc(L=5, lattice=dq.CUBIC).N == 125 and dq.WalkerDesc(L=5).N == 25
 
 
 @pytest.mark.parametrize(
@@ -50,6 +57,10 @@ def test_abi_version(dq):
         (dict(beta=-1.0), "beta"),
         (dict(model=7), "model"),
         (dict(L=4, momentum_index=99), "momentum"),
+        (dict(L=4, lattice=2), "lattice"),
+        (dict(L=11, lattice=1), "exceeds"),  # 1331 sites
+        (dict(L=4, lattice=1, checkerboard=True), "square lattice only"),
+        (dict(L=4, lattice=1, momentum_index=10), "momentum"),  # 10 k stars of the 4^3 lattice
     ],
 )
 def test_bad_arguments_rejected_before_device(dq, kw, msg):

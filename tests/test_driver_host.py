@@ -168,14 +168,23 @@ def test_dynamic_run(fake, tmp_path):
     assert open(tmp_path / "greens.bins.out").read().splitlines()[0] == dio._d(6) + dio._d(3) + dio._d(6)
 
 
-def test_cubic_configuration_is_refused_before_any_device_work(fake, tmp_path):
-    """The cubic lattice parses (its tables live in dqmc_gb300.io and the oracle) but the
-    device sweep is built for the square lattice: the driver refuses it loudly."""
-    cfg = dio.parse_config('[Lattice]\ntype = "Cubic"\ncell = [4, 4, 4]\nmomentum = "RPoint"\n'
-                           '[Measure]\nobservables = ["filling_number"]\n')
-    with pytest.raises(NotImplementedError):
-        drv.run(cfg, str(tmp_path), walkers=1, log=open(os.devnull, "w"))
-    assert not fake.created
+def test_cubic_configuration_runs_cubic_walkers(fake, tmp_path):
+    """A cubic configuration (dqmc_initializer.cpp:118-150) gives walkers of the cubic
+    lattice with N = L^3, its measured momentum and momentum list from the cubic
+    tables, and no superfluid stiffness (dqmc_initializer.cpp:233-237)."""
+    cfg = dio.parse_config('[Lattice]\ntype = "Cubic"\ncell = [4, 4, 4]\nmomentum = "XPoint"\n'
+                           'momentum_list = "LambdaLine"\n[MonteCarlo]\nbeta = 1.0\ntime_size = 6\n'
+                           'stabilization_pace = 3\n[Measure]\nsweeps_warmup = 2\nbin_num = 2\nbin_size = 2\n'
+                           'sweeps_between_bins = 0\nobservables = ["all"]\n')
+    res = drv.run(cfg, str(tmp_path), walkers=1, log=open(os.devnull, "w"))
+    d = fake.created[0].descs[0]
+    assert d.lattice == dq.CUBIC and d.N == 64 and fake.created[0].N == 64
+    assert d.momentum_index == dio.momentum_index(4, "XPoint", 3)
+    assert "superfluid_stiffness" not in res and "filling_number" in res
+    greens = open(tmp_path / "greens.out").read().splitlines()
+    nline = len(dio.momentum_list_indices(4, "LambdaLine", 3))
+    assert greens[0] == dio._d(nline) + dio._d(6)
+    assert len(open(tmp_path / "kstars.out").read().splitlines()) == 1 + len(dio.kstars(4, 3))  # count line
 
 
 def test_reference_command_line_and_fields_resume(fake, tmp_path):

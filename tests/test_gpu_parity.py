@@ -25,7 +25,7 @@ def dq():
 
 def _oracle(O, d, stack):
     w = O.Walker(model=d.model, L=d.L, t=d.t, U=d.U, mu=d.mu, beta=d.beta, Lt=d.Lt, pace=d.pace,
-                 checkerboard=d.checkerboard, stack=stack, momentum_index=d.momentum_index)
+                 checkerboard=d.checkerboard, stack=stack, momentum_index=d.momentum_index, lattice=d.lattice)
     w.seed(d.seed)
     return w
 
