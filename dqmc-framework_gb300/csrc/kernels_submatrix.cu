@@ -151,10 +151,11 @@ __device__ __forceinline__ long long group_sum(const uint32_t (&v)[OZS][8], int 
 // tensor-core images in global memory (slice stride a_sst / b_sst, a_nlb / b_nlb
 // line blocks per k chunk).  Tile u (global count across products) uses B buffer
 // u % NBB and TMEM accumulator u & 1; thread 0 copies the B tile of t+2 and
-// issues the MMAs of t+1 while every thread runs pre(row block, column tile)
-// (loads that do not need the product) and then epi(row block, column tile, TMEM
-// address) on tile t.  A is reloaded (after the MMAs of the previous tile) at
-// each row block.
+// issues the MMAs of t+1 while every thread runs pre(row block, column tile, t+1)
+// (copies for the next tile's epilogue that do not need the product) and then
+// epi(row block, column tile, TMEM address, ok, t, t+1 < tiles) on tile t;
+// pre(.., 0) runs before the loop.  A is reloaded (after the MMAs of the
+// previous tile) at each row block.
 struct SubTC {
   unsigned char* A;            // A_BYTES
   unsigned char* B;            // NBB x B_BYTES
@@ -219,16 +220,18 @@ __device__ void sub_gemm(const SubTC& tc, unsigned& gt, unsigned& nA, const unsi
     if (ntiles > 1) load_b(1);
     issue(0);
   }
+  pre(0, cb_of(0), 0);
   for (int t = 0; t < ntiles; ++t) {
     const unsigned u = gt + t;
     if (tid == 0 && !*tc.fail) {
       if (t + 2 < ntiles) load_b(t + 2);  // its buffer held tile t - 1, whose epilogue is done
       if (t + 1 < ntiles) issue(t + 1);
     }
-    pre(t / ncl, cb_of(t));
+    const bool more = t + 1 < ntiles;
+    if (more) pre((t + 1) / ncl, cb_of(t + 1), t + 1);
     if (!*tc.fail && !tc::mbar_wait(&tc.mmab[u & 1], (u >> 1) & 1)) *tc.fail = 1;
     tc::fence_after();
-    epi(t / ncl, cb_of(t), tc.tmem + (unsigned)((u & 1) * ACC_COLS), !*tc.fail);
+    epi(t / ncl, cb_of(t), tc.tmem + (unsigned)((u & 1) * ACC_COLS), !*tc.fail, t, more);
     tc::fence_before();
     __syncthreads();
   }
@@ -237,36 +240,302 @@ __device__ void sub_gemm(const SubTC& tc, unsigned& gt, unsigned& nA, const unsi
 
 constexpr int kEOff = -OZB * (OZS + 1);
 
+// 8-byte asynchronous global -> shared copies (cp.async), one group per tile
+__device__ __forceinline__ void cp_async8(void* sdst, const void* gsrc) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(tc::su32(sdst)), "l"(gsrc) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait(bool one_pending) {
+  if (one_pending)
+    asm volatile("cp.async.wait_group 1;" ::: "memory");
+  else
+    asm volatile("cp.async.wait_group 0;" ::: "memory");
+}
+
+// The flush's G staging: two tiles of 16 elements per thread, [tile & 1][u][thread]
+constexpr int kStageBytes = 2 * 16 * kSubThreads * 8;
+
+// FP64 state of one block's decisions in shared memory, each [S][KK]: the diagonal block
+// G(I, I) ((r, c) at c * KB + r), the coefficients a_q, b_q ([q][x] at compact index x), u~_q,
+// w~_q ([q][l] at block position l) and Gamma ((x, y) at y * KB + x)
+struct SubState {
+  double *Gb, *Ac, *Bc, *Ut, *Wt, *Gam;
+};
+// bytes of Gb .. Wt (the part the fused kernel's flush overlays with its G staging)
+__host__ __device__ inline size_t sub_state_bytes(int S) {
+  const size_t b = 5ull * S * KK * sizeof(double);
+  return b > (size_t)kStageBytes ? b : (size_t)kStageBytes;
+}
+
+// Gb = G(I, I) of the block at sites i0 .. i0 + kb - 1, zero past kb
+__device__ __forceinline__ void sub_load_block(const SubState& st, const double* const* G, int S, int N, int i0, int kb) {
+  for (int e = threadIdx.x; e < S * KK; e += kSubThreads) {
+    const int sp = e / KK, c = (e % KK) / KB, r = e % KB;
+    st.Gb[e] = (r < kb && c < kb) ? G[sp][(long long)(i0 + c) * N + i0 + r] : 0.0;
+  }
+}
+
+// The decisions of one block, flip by flip, then Gamma = sum_q a_q b_q^T; returns m, the
+// accepts, with their block positions in s_pos.  uni and fld are the block's uniforms and
+// fields (position l).  The sites are visited in order: warp 0 evaluates the ratios of all
+// sites still to visit at once, on the diagonal as it stands, and the lowest accepted one is
+// the next accept of the sequential visit, since every site before it saw the same diagonal.
+// sign and acc_count are thread 0's.
+__device__ __forceinline__ int sub_decide(const WalkerDev& w, int S, int kb, const double* uni, int8_t* fld, const SubState& st,
+                          int* s_pos, int* s_next, double* s_f, double& sign, long long& acc_count) {
+  const int tid = threadIdx.x;
+  int m = 0, cur = 0;
+  while (true) {
+    if (tid < 32) {
+      const int l = cur + tid;
+      FlipRatio q{};
+      int s = 0;
+      bool acc = false;
+      if (l < kb) {
+        s = fld[l];
+        const int si = s > 0 ? 0 : 1;
+        const double gu = st.Gb[l * KB + l];
+        const double gd = (S == 2) ? st.Gb[KK + l * KB + l] : gu;
+        q = flip_ratio(w, si, gu, gd);  // reference operation order
+        acc = uni[l] < fmin(1.0, fabs(q.r));
+      }
+      const unsigned amask = __ballot_sync(0xffffffffu, acc);
+      const int first = amask ? __ffs(amask) - 1 : 32;
+      if (l < kb && tid <= first && !isfinite(q.r)) atomicOr(w.status, ST_NONFINITE_RATIO);
+      if (tid == first) {
+        flip_factors(w, q, s_f);
+        fld[l] = (int8_t)(-s);
+      }
+      const double rf = __shfl_sync(0xffffffffu, q.r, first & 31);
+      if (tid == 0) {
+        if (amask) {
+          sign = (rf >= 0) ? sign : -sign;
+          ++acc_count;
+        }
+        *s_next = amask ? cur + first : kb;
+      }
+    }
+    __syncthreads();
+    const int l = *s_next;
+    if (l >= kb) break;
+    // u~, w~ of accept m on the block, and its coefficients a_m, b_m
+    for (int e = tid; e < S * 4 * KB; e += kSubThreads) {
+      const int sp = e / (4 * KB), role = (e / KB) & 3, x = e % KB;
+      const double f = s_f[sp];
+      const double* gb = st.Gb + sp * KK;
+      double* ut = st.Ut + sp * KK;
+      double* wt = st.Wt + sp * KK;
+      double* ac = st.Ac + sp * KK;
+      double* bc = st.Bc + sp * KK;
+      if (role == 0) {
+        ut[m * KB + x] = f * gb[l * KB + x];  // f G(x, l)
+      } else if (role == 1) {
+        wt[m * KB + x] = ((x == l) ? 1.0 : 0.0) - gb[x * KB + l];  // delta - G(l, x)
+      } else if (role == 2) {
+        double a = (x == m) ? 1.0 : 0.0;
+        for (int p = x; p < m; ++p) a = fma(-wt[p * KB + l], ac[p * KB + x], a);
+        ac[m * KB + x] = (x <= m) ? f * a : 0.0;
+      } else {
+        double b = (x == m) ? 1.0 : 0.0;
+        for (int p = x; p < m; ++p) b = fma(ut[p * KB + l], bc[p * KB + x], b);
+        bc[m * KB + x] = (x <= m) ? b : 0.0;
+      }
+    }
+    if (tid == 0) s_pos[m] = l;
+    __syncthreads();
+    // rank-1 update of the part of the block later decisions read
+    for (int e = tid; e < S * KK; e += kSubThreads) {
+      const int sp = e / KK, c = (e % KK) / KB, r = e % KB;
+      if (r > l && c > l && r < kb && c < kb)
+        st.Gb[e] = fma(-st.Ut[sp * KK + m * KB + r], st.Wt[sp * KK + m * KB + c], st.Gb[e]);
+    }
+    ++m;
+    cur = l + 1;
+    __syncthreads();
+  }
+  if (m == 0) return 0;
+  for (int e = tid; e < S * KK; e += kSubThreads) {
+    const int sp = e / KK, y = (e % KK) / KB, x = e % KB;
+    double gsum = 0.0;
+    if (x < m && y < m) {
+      const double* ac = st.Ac + sp * KK;
+      const double* bc = st.Bc + sp * KK;
+      for (int p = max(x, y); p < m; ++p) gsum = fma(ac[p * KB + x], bc[p * KB + y], gsum);
+    }
+    st.Gam[e] = gsum;
+  }
+  __syncthreads();
+  return m;
+}
+
+// Spin sp of a block with m accepts at sites i0 + s_pos[q]: the slices of Gamma, G0(:, I_A) and
+// R_A = E_A^T - G0(I_A, :) (taken before G changes), then T^T = R_A^T Gamma^T on the tensor
+// cores: warp w and w + 4 share TMEM lanes 32 (w & 3).. (columns c) and take x in [0, 16) and
+// [16, 32); the column exponent max over x goes through etmp, and the epilogue slices T straight
+// into the B image of the flush (line c, k = x).  Line exponents: eGm [KB] of Gamma, eG [N] of
+// G0(:, I_A), eR [N] of R_A, eT [N] of T (shared or global memory).
+__device__ __forceinline__ void sub_prepare(const SubTC& tcs, unsigned& gt, unsigned& nA, const WalkerDev& w, int sp, int N, int m,
+                            int i0, const int* s_pos, const double* gam, const double* Gs, int* eGm, int* eG, int* eR,
+                            int* eT, int* etmp) {
+  const SubOff so = sub_offsets(N);
+  unsigned char* ms = w.msub + (size_t)sp * so.total;
+  unsigned short* sGm = reinterpret_cast<unsigned short*>(ms + so.sGm);
+  unsigned short* sG = reinterpret_cast<unsigned short*>(ms + so.sG);
+  unsigned short* sR = reinterpret_cast<unsigned short*>(ms + so.sR);
+  unsigned short* sT = reinterpret_cast<unsigned short*>(ms + so.sT);
+  const int tid = threadIdx.x;
+  const int nlbN = ozaki::tc_lines(N) / 8, nk = (m + 15) / 16;
+  const long long sstN = (long long)sub_sst(N), sstG = (long long)sub_sst(1);
+  slice_lines([&](int line, int k) { return gam[k * KB + line]; }, m, m, sGm, sstG, TM / 8, eGm, etmp);
+  slice_lines([&](int line, int k) { return Gs[(long long)(i0 + s_pos[k]) * N + line]; }, N, m, sG, sstN, nlbN, eG,
+              etmp);
+  slice_lines(
+      [&](int line, int k) {
+        const int i = i0 + s_pos[k];
+        return ((line == i) ? 1.0 : 0.0) - Gs[(long long)line * N + i];
+      },
+      N, m, sR, sstN, nlbN, eR, etmp);
+  asm volatile("fence.proxy.async.global;" ::: "memory");  // generic writes -> bulk-copy reads
+  __syncthreads();
+  sub_gemm(tcs, gt, nA, sR, sstN, nlbN, (N + TM - 1) / TM, sGm, sstG, TM / 8, 1, nk, [&](int, int, int) {},
+           [&](int rb, int, unsigned tacc, bool ok, int, bool) {
+             const int wq = (tid >> 5) & 3, xh = tid >> 7;
+             const int c = rb * TM + wq * 32 + (tid & 31);
+             const int ec = (c < N) ? eR[c] : 0;
+             double tv[16];
+             int e = -1100;
+             if (ok) {
+#pragma unroll
+               for (int h = 0; h < 2; ++h) {
+                 uint32_t v[OZS][8];
+#pragma unroll
+                 for (int g = 0; g < OZS; ++g)
+                   tc::ld8(v[g], tacc + ((unsigned)(wq * 32) << 16) + (unsigned)(g * TN + xh * 16 + h * 8));
+                 tc::wait_ld();
+#pragma unroll
+                 for (int u = 0; u < 8; ++u) {
+                   const int x = xh * 16 + h * 8 + u;
+                   tv[h * 8 + u] = (x < m && c < N) ? ozaki::ldexp_i64(group_sum(v, u), ec + eGm[x] + kEOff) : 0.0;
+                   e = max(e, ozaki::exp_bound(tv[h * 8 + u]));
+                 }
+               }
+             }
+             etmp[tid] = e;
+             __syncthreads();
+             e = max(e, etmp[tid ^ 128]);
+             if (ok && c < N) {
+               if (xh == 0) eT[c] = e;
+               unsigned pk[OZS][8];
+#pragma unroll
+               for (int u = 0; u < 16; u += 2) {
+                 bool n0, n1;
+                 const unsigned long long q0 = ozaki::fixed42(tv[u], e, n0), q1 = ozaki::fixed42(tv[u + 1], e, n1);
+#pragma unroll
+                 for (int s2 = 0; s2 < OZS; ++s2)
+                   pk[s2][u >> 1] = (unsigned)ozaki::slice_bf16(q0, s2, OZB, n0) |
+                                    ((unsigned)ozaki::slice_bf16(q1, s2, OZB, n1) << 16);
+               }
+               unsigned short* o = sT + ozaki::tc_index(c, xh * 16, nlbN);
+#pragma unroll
+               for (int s2 = 0; s2 < OZS; ++s2) {
+                 *reinterpret_cast<uint4*>(o + s2 * sstN) = make_uint4(pk[s2][0], pk[s2][1], pk[s2][2], pk[s2][3]);
+                 *reinterpret_cast<uint4*>(o + s2 * sstN + 64) =
+                     make_uint4(pk[s2][4], pk[s2][5], pk[s2][6], pk[s2][7]);
+               }
+             }
+           });
+  asm volatile("fence.proxy.async.global;" ::: "memory");  // T's slices -> the flush's bulk copies
+  __syncthreads();
+}
+
+// G -= G0(:, I_A) T for spin sp over the column tiles cb0, cb0 + cbs, ... of G: warp w reads
+// TMEM lanes 32 (w & 3) .. (rows), columns 16 (w >> 2) ..  Each thread's 16 elements of G of
+// the next tile are copied into stage (kStageBytes of shared memory) while the epilogue of the
+// current tile runs, so the epilogue reads G from shared memory; eG, eT: line exponents.
+__device__ __forceinline__ void sub_flush(const SubTC& tcs, unsigned& gt, unsigned& nA, const WalkerDev& w, int sp, int N, int m,
+                          double* Gs, const int* eG, const int* eT, double* stage, int cb0, int cbs) {
+  const SubOff so = sub_offsets(N);
+  const unsigned char* ms = w.msub + (size_t)sp * so.total;
+  const unsigned short* sG = reinterpret_cast<const unsigned short*>(ms + so.sG);
+  const unsigned short* sT = reinterpret_cast<const unsigned short*>(ms + so.sT);
+  const int tid = threadIdx.x, wq = (tid >> 5) & 3, half = tid >> 7;
+  const int nlbN = ozaki::tc_lines(N) / 8, nk = (m + 15) / 16, nct = (N + TN - 1) / TN;
+  const long long sstN = (long long)sub_sst(N);
+  sub_gemm(tcs, gt, nA, sG, sstN, nlbN, (N + TM - 1) / TM, sT, sstN, nlbN, nct, nk,
+           [&](int rb, int cb, int tl) {
+             const int r = rb * TM + wq * 32 + (tid & 31), c0 = cb * TN + half * 16;
+             double* dst = stage + (tl & 1) * 16 * kSubThreads + tid;
+             if (r < N) {
+#pragma unroll
+               for (int u = 0; u < 16; ++u)
+                 if (c0 + u < N) cp_async8(dst + u * kSubThreads, Gs + (long long)(c0 + u) * N + r);
+             }
+             cp_async_commit();
+           },
+           [&](int rb, int cb, unsigned tacc, bool ok, int tl, bool more) {
+             cp_async_wait(more);  // this tile's copies (the next tile's may be in flight)
+             if (!ok) return;
+             const int r = rb * TM + wq * 32 + (tid & 31), c0 = cb * TN + half * 16;
+             const double* gsv = stage + (tl & 1) * 16 * kSubThreads + tid;
+             const int er = (r < N) ? eG[r] : 0;
+             const unsigned ta = tacc + ((unsigned)(wq * 32) << 16);
+#pragma unroll
+             for (int h = 0; h < 2; ++h) {
+               uint32_t v[OZS][8];
+#pragma unroll
+               for (int g = 0; g < OZS; ++g) tc::ld8(v[g], ta + (unsigned)(g * TN + half * 16 + h * 8));
+               tc::wait_ld();
+#pragma unroll
+               for (int u = 0; u < 8; ++u) {
+                 const int c = c0 + h * 8 + u;
+                 const long long sv = group_sum(v, u);
+                 if (sv != 0 && r < N && c < N)
+                   Gs[(long long)c * N + r] =
+                       gsv[(h * 8 + u) * kSubThreads] - ozaki::ldexp_i64(sv, er + eT[c] + kEOff);
+               }
+             }
+           },
+           cb0, cbs);
+}
+
 }  // namespace
 
 size_t submatrix_scratch_bytes(int N) { return sub_offsets(N).total; }
 
-// dynamic shared memory: tensor-core operand buffers first (1024-byte aligned
-// base), then the FP64 block state, the exponent scratch and the fields
+// dynamic shared memory of the fused kernel: tensor-core operand buffers first (1024-byte
+// aligned base), then the slice's uniforms [N], Gamma [S][KK], the block state (overlaid by the
+// flush's G staging), the line exponents eG, eT, eR [N] and eGm [KB], the exponent scratch
+// [256] and the fields [N]
 size_t submatrix_smem_bytes(int N, int S) {
   const size_t Nu = (size_t)((N + 1) & ~1);
-  return (size_t)A_BYTES + (size_t)NBB * B_BYTES + sizeof(double) * (Nu + 6ull * S * KK) + 256 * sizeof(int) +
-         (size_t)N;
+  return (size_t)A_BYTES + (size_t)NBB * B_BYTES + sizeof(double) * (Nu + (size_t)S * KK) + sub_state_bytes(S) +
+         sizeof(int) * (3 * Nu + KB + 256) + (size_t)N;
 }
 
-__global__ void __launch_bounds__(kSubThreads) metropolis_sub_kernel(const WalkerDev* __restrict__ W, int mode, int j,
+__global__ void __launch_bounds__(kSubThreads, 1) metropolis_sub_kernel(const WalkerDev* __restrict__ W, int mode, int j,
                                                                      int q) {
   const WalkerDev& w = W[blockIdx.x];
   if (w.path != 2) return;
   int t;
   if (!sub_slice_of(w, mode, j, q, t)) return;
   const int N = w.N, S = w.S, Lt = w.Lt, tid = threadIdx.x;
+  const int Nu = (N + 1) & ~1;
   const long long NN = (long long)N * N;
   extern __shared__ __align__(1024) unsigned char smem[];
-  double* sh = reinterpret_cast<double*>(smem + A_BYTES + NBB * B_BYTES);
-  double* uni = sh;                      // [N] uniforms of the slice
-  double* Gb = uni + ((N + 1) & ~1);     // [S][KK] diagonal block, (r, c) at c * KB + r
-  double* Ac = Gb + S * KK;              // [S][q][x] a_q at compact index x
-  double* Bc = Ac + S * KK;              // [S][q][x] b_q
-  double* Ut = Bc + S * KK;              // [S][q][l] u~_q at block position l
-  double* Wt = Ut + S * KK;              // [S][q][l] w~_q
-  double* Gam = Wt + S * KK;             // [S][KK] Gamma(x, y) at y * KB + x
-  int* etmp = reinterpret_cast<int*>(Gam + S * KK);         // [256]
+  double* uni = reinterpret_cast<double*>(smem + A_BYTES + NBB * B_BYTES);  // [N] uniforms of the slice
+  SubState st;
+  st.Gam = uni + Nu;
+  st.Gb = st.Gam + S * KK;
+  st.Ac = st.Gb + S * KK;
+  st.Bc = st.Ac + S * KK;
+  st.Ut = st.Bc + S * KK;
+  st.Wt = st.Ut + S * KK;
+  double* stage = st.Gb;  // the flush's G tiles over the dead block state
+  int* s_eG = reinterpret_cast<int*>(reinterpret_cast<unsigned char*>(st.Gb) + sub_state_bytes(S));
+  int* s_eT = s_eG + Nu;
+  int* s_eR = s_eT + Nu;
+  int* s_eGm = s_eR + Nu;
+  int* etmp = s_eGm + KB;                                   // [256]
   int8_t* s_field = reinterpret_cast<int8_t*>(etmp + 256);  // [N]
   __shared__ int s_next, s_pos[KB];
   __shared__ double s_f[2];
@@ -274,7 +543,6 @@ __global__ void __launch_bounds__(kSubThreads) metropolis_sub_kernel(const Walke
   __shared__ unsigned s_tmem;
   __shared__ int s_tcfail;
 
-  const SubOff so = sub_offsets(N);
   double* G[2] = {w.G, (S == 2) ? w.G + NN : w.G};
   const int eff = t - 1;
   const unsigned long long sweep = (w.rng == 1) ? *w.sweep_ctr : 0ULL;
@@ -300,209 +568,16 @@ __global__ void __launch_bounds__(kSubThreads) metropolis_sub_kernel(const Walke
   tc::fence_after();
   const SubTC tcs{smem, smem + A_BYTES, &bar_ldA, bar_ldB, bar_mma, s_tmem, &s_tcfail};
   unsigned gt = 0, nA = 0;  // tiles and A loads so far (mbarrier phases)
-  const int nlbN = ozaki::tc_lines(N) / 8;
-  const long long sstN = (long long)sub_sst(N), sstG = (long long)sub_sst(1);
 
   for (int i0 = 0; i0 < N; i0 += KB) {
     const int kb = min(KB, N - i0);
-    for (int e = tid; e < S * KK; e += kSubThreads) {
-      const int sp = e / KK, c = (e % KK) / KB, r = e % KB;
-      Gb[e] = (r < kb && c < kb) ? G[sp][(long long)(i0 + c) * N + i0 + r] : 0.0;
-    }
+    sub_load_block(st, G, S, N, i0, kb);
     __syncthreads();
-
-    // ---- decisions, flip by flip, on the diagonal block
-    int m = 0, cur = 0;
-    while (true) {
-      if (tid == 0) {
-        int l = cur;
-        for (; l < kb; ++l) {
-          const int i = i0 + l;
-          const int s = s_field[i];
-          const int si = s > 0 ? 0 : 1;
-          const double gu = Gb[l * KB + l];
-          const double gd = (S == 2) ? Gb[KK + l * KB + l] : gu;
-          const FlipRatio q = flip_ratio(w, si, gu, gd);  // reference operation order
-          const double r = q.r;
-          const double prob = fmin(1.0, fabs(r));
-          if (!isfinite(r)) atomicOr(w.status, ST_NONFINITE_RATIO);
-          if (uni[i] < prob) {
-            flip_factors(w, q, s_f);
-            s_field[i] = (int8_t)(-s);
-            sign = (r >= 0) ? sign : -sign;
-            ++acc_count;
-            break;
-          }
-        }
-        s_next = l;
-      }
-      __syncthreads();
-      const int l = s_next;
-      if (l >= kb) break;
-      // u~, w~ of accept m on the block, and its coefficients a_m, b_m
-      for (int e = tid; e < S * 4 * KB; e += kSubThreads) {
-        const int sp = e / (4 * KB), role = (e / KB) & 3, x = e % KB;
-        const double f = s_f[sp];
-        const double* gb = Gb + sp * KK;
-        double* ut = Ut + sp * KK;
-        double* wt = Wt + sp * KK;
-        double* ac = Ac + sp * KK;
-        double* bc = Bc + sp * KK;
-        if (role == 0) {
-          ut[m * KB + x] = f * gb[l * KB + x];  // f G(x, l)
-        } else if (role == 1) {
-          wt[m * KB + x] = ((x == l) ? 1.0 : 0.0) - gb[x * KB + l];  // delta - G(l, x)
-        } else if (role == 2) {
-          double a = (x == m) ? 1.0 : 0.0;
-          for (int p = x; p < m; ++p) a = fma(-wt[p * KB + l], ac[p * KB + x], a);
-          ac[m * KB + x] = (x <= m) ? f * a : 0.0;
-        } else {
-          double b = (x == m) ? 1.0 : 0.0;
-          for (int p = x; p < m; ++p) b = fma(ut[p * KB + l], bc[p * KB + x], b);
-          bc[m * KB + x] = (x <= m) ? b : 0.0;
-        }
-      }
-      if (tid == 0) s_pos[m] = l;
-      __syncthreads();
-      // rank-1 update of the part of the block later decisions read
-      for (int e = tid; e < S * KK; e += kSubThreads) {
-        const int sp = e / KK, c = (e % KK) / KB, r = e % KB;
-        if (r > l && c > l && r < kb && c < kb)
-          Gb[e] = fma(-Ut[sp * KK + m * KB + r], Wt[sp * KK + m * KB + c], Gb[e]);
-      }
-      ++m;
-      cur = l + 1;
-      __syncthreads();
-    }
+    const int m = sub_decide(w, S, kb, uni + i0, s_field + i0, st, s_pos, &s_next, s_f, sign, acc_count);
     if (m == 0) continue;
-
-    // ---- Gamma = sum_q a_q b_q^T
-    for (int e = tid; e < S * KK; e += kSubThreads) {
-      const int sp = e / KK, y = (e % KK) / KB, x = e % KB;
-      double gsum = 0.0;
-      if (x < m && y < m) {
-        const double* ac = Ac + sp * KK;
-        const double* bc = Bc + sp * KK;
-        for (int p = max(x, y); p < m; ++p) gsum = fma(ac[p * KB + x], bc[p * KB + y], gsum);
-      }
-      Gam[e] = gsum;
-    }
-    __syncthreads();
-
-    const int nk = (m + 15) / 16;  // k chunks of 16 (slices are zero past m)
     for (int sp = 0; sp < S; ++sp) {
-      unsigned char* ms = w.msub + (size_t)sp * so.total;
-      unsigned short* sGm = reinterpret_cast<unsigned short*>(ms + so.sGm);
-      unsigned short* sG = reinterpret_cast<unsigned short*>(ms + so.sG);
-      unsigned short* sR = reinterpret_cast<unsigned short*>(ms + so.sR);
-      unsigned short* sT = reinterpret_cast<unsigned short*>(ms + so.sT);
-      int* eGm = reinterpret_cast<int*>(ms + so.eGm);
-      int* eG = reinterpret_cast<int*>(ms + so.eG);
-      int* eR = reinterpret_cast<int*>(ms + so.eR);
-      int* eT = reinterpret_cast<int*>(ms + so.eT);
-      const double* gam = Gam + sp * KK;
-      double* Gs = G[sp];
-      // Gamma (lines = rows x, k = y), G0(:, I_A) (lines = rows, k = accept) and
-      // R_A = E_A^T - G0(I_A, :) (lines = columns c, k = accept), taken before G changes
-      slice_lines([&](int line, int k) { return gam[k * KB + line]; }, m, m, sGm, sstG, TM / 8, eGm, etmp);
-      slice_lines([&](int line, int k) { return Gs[(long long)(i0 + s_pos[k]) * N + line]; }, N, m, sG, sstN, nlbN,
-                  eG, etmp);
-      slice_lines(
-          [&](int line, int k) {
-            const int i = i0 + s_pos[k];
-            return ((line == i) ? 1.0 : 0.0) - Gs[(long long)line * N + i];
-          },
-          N, m, sR, sstN, nlbN, eR, etmp);
-      asm volatile("fence.proxy.async.global;" ::: "memory");  // generic writes -> bulk-copy reads
-      __syncthreads();
-      // T^T = R_A^T Gamma^T (rows c, columns x): warp w and w + 4 share TMEM lanes 32 (w & 3)..
-      // (columns c) and take x in [0, 16) and [16, 32); the column exponent max over x goes
-      // through shared memory, and the epilogue slices T straight into the B image of the
-      // flush (line c, k = x)
-      sub_gemm(tcs, gt, nA, sR, sstN, nlbN, (N + TM - 1) / TM, sGm, sstG, TM / 8, 1, nk, [&](int, int) {},
-               [&](int rb, int, unsigned tacc, bool ok) {
-                 const int wq = (tid >> 5) & 3, xh = tid >> 7;
-                 const int c = rb * TM + wq * 32 + (tid & 31);
-                 const int ec = (c < N) ? eR[c] : 0;
-                 double tv[16];
-                 int e = -1100;
-                 if (ok) {
-#pragma unroll
-                   for (int h = 0; h < 2; ++h) {
-                     uint32_t v[OZS][8];
-#pragma unroll
-                     for (int g = 0; g < OZS; ++g)
-                       tc::ld8(v[g], tacc + ((unsigned)(wq * 32) << 16) + (unsigned)(g * TN + xh * 16 + h * 8));
-                     tc::wait_ld();
-#pragma unroll
-                     for (int u = 0; u < 8; ++u) {
-                       const int x = xh * 16 + h * 8 + u;
-                       tv[h * 8 + u] = (x < m && c < N) ? ozaki::ldexp_i64(group_sum(v, u), ec + eGm[x] + kEOff) : 0.0;
-                       e = max(e, ozaki::exp_bound(tv[h * 8 + u]));
-                     }
-                   }
-                 }
-                 etmp[tid] = e;
-                 __syncthreads();
-                 e = max(e, etmp[tid ^ 128]);
-                 if (ok && c < N) {
-                   if (xh == 0) eT[c] = e;
-                   unsigned pk[OZS][8];
-#pragma unroll
-                   for (int u = 0; u < 16; u += 2) {
-                     bool n0, n1;
-                     const unsigned long long q0 = ozaki::fixed42(tv[u], e, n0), q1 = ozaki::fixed42(tv[u + 1], e, n1);
-#pragma unroll
-                     for (int s2 = 0; s2 < OZS; ++s2)
-                       pk[s2][u >> 1] = (unsigned)ozaki::slice_bf16(q0, s2, OZB, n0) |
-                                        ((unsigned)ozaki::slice_bf16(q1, s2, OZB, n1) << 16);
-                   }
-                   unsigned short* o = sT + ozaki::tc_index(c, xh * 16, nlbN);
-#pragma unroll
-                   for (int s2 = 0; s2 < OZS; ++s2) {
-                     *reinterpret_cast<uint4*>(o + s2 * sstN) = make_uint4(pk[s2][0], pk[s2][1], pk[s2][2], pk[s2][3]);
-                     *reinterpret_cast<uint4*>(o + s2 * sstN + 64) =
-                         make_uint4(pk[s2][4], pk[s2][5], pk[s2][6], pk[s2][7]);
-                   }
-                 }
-               });
-      asm volatile("fence.proxy.async.global;" ::: "memory");
-      __syncthreads();
-      // G -= G0(:, I_A) T: warp w reads TMEM lanes 32 (w & 3) .. (rows), columns 16 (w >> 2) ..;
-      // the G values and column exponents of a tile are loaded before its MMAs are waited on
-      double gv[16];
-      int ecol[16];
-      const int wq = (tid >> 5) & 3, half = tid >> 7;
-      sub_gemm(tcs, gt, nA, sG, sstN, nlbN, (N + TM - 1) / TM, sT, sstN, nlbN, (N + TN - 1) / TN, nk,
-               [&](int rb, int cb) {
-                 const int r = rb * TM + wq * 32 + (tid & 31), c0 = cb * TN + half * 16;
-#pragma unroll
-                 for (int u = 0; u < 16; ++u) {
-                   const int c = c0 + u;
-                   gv[u] = (r < N && c < N) ? Gs[(long long)c * N + r] : 0.0;
-                   ecol[u] = (c < N) ? eT[c] : 0;
-                 }
-               },
-               [&](int rb, int cb, unsigned tacc, bool ok) {
-                 if (!ok) return;
-                 const int r = rb * TM + wq * 32 + (tid & 31), c0 = cb * TN + half * 16;
-                 const int er = (r < N) ? eG[r] : 0;
-                 const unsigned ta = tacc + ((unsigned)(wq * 32) << 16);
-#pragma unroll
-                 for (int h = 0; h < 2; ++h) {
-                   uint32_t v[OZS][8];
-#pragma unroll
-                   for (int g = 0; g < OZS; ++g) tc::ld8(v[g], ta + (unsigned)(g * TN + half * 16 + h * 8));
-                   tc::wait_ld();
-#pragma unroll
-                   for (int u = 0; u < 8; ++u) {
-                     const int c = c0 + h * 8 + u;
-                     const long long sv = group_sum(v, u);
-                     if (sv != 0 && r < N && c < N)
-                       Gs[(long long)c * N + r] = gv[h * 8 + u] - ozaki::ldexp_i64(sv, er + ecol[h * 8 + u] + kEOff);
-                   }
-                 }
-               });
+      sub_prepare(tcs, gt, nA, w, sp, N, m, i0, s_pos, st.Gam + sp * KK, G[sp], s_eGm, s_eG, s_eR, s_eT, etmp);
+      sub_flush(tcs, gt, nA, w, sp, N, m, G[sp], s_eG, s_eT, stage, 0, 1);
     }
   }
 
@@ -525,14 +600,18 @@ __global__ void __launch_bounds__(kSubThreads) metropolis_sub_kernel(const Walke
 // 32 walkers of N = 576), each block runs as a decision kernel (one CTA per walker:
 // the decisions, Gamma, the slices of Gamma, G0(:, I_A) and R_A, T^T on the tensor
 // cores) followed by a flush kernel whose CTAs share the walker's column tiles of G.
-// The arithmetic is the fused kernel's, element for element.  The autotuner times both.
+// The arithmetic is the fused kernel's (the same device functions).  The autotuner
+// times both.
 
-// dynamic shared memory of the decision kernel: the operand buffers, the FP64 block state,
-// the exponent scratch and the block's fields; of the flush kernel: the operand buffers
+// dynamic shared memory of the decision kernel: the operand buffers, the block's uniforms,
+// the FP64 block state, the exponent scratch and the block's fields; of the flush kernel: the
+// operand buffers, the G staging and the line exponents eG, eT [N]
 size_t submatrix_block_smem_bytes(int S) {
   return (size_t)A_BYTES + (size_t)NBB * B_BYTES + sizeof(double) * (KB + 6ull * S * KK) + 256 * sizeof(int) + KB;
 }
-size_t submatrix_flush_smem_bytes() { return (size_t)A_BYTES + (size_t)NBB * B_BYTES; }
+size_t submatrix_flush_smem_bytes(int N) {
+  return (size_t)A_BYTES + (size_t)NBB * B_BYTES + kStageBytes + 2 * sizeof(int) * (size_t)((N + 1) & ~1);
+}
 
 __global__ void __launch_bounds__(kSubThreads) metropolis_sub_block_kernel(const WalkerDev* __restrict__ W, int mode,
                                                                            int j, int q, int blk) {
@@ -546,15 +625,15 @@ __global__ void __launch_bounds__(kSubThreads) metropolis_sub_block_kernel(const
   const int kb = min(KB, N - i0);
   const long long NN = (long long)N * N;
   extern __shared__ __align__(1024) unsigned char smem[];
-  double* sh = reinterpret_cast<double*>(smem + A_BYTES + NBB * B_BYTES);
-  double* uni = sh;                      // [KB] uniforms of the block's sites
-  double* Gb = uni + KB;                 // [S][KK] diagonal block, (r, c) at c * KB + r
-  double* Ac = Gb + S * KK;              // [S][q][x] a_q at compact index x
-  double* Bc = Ac + S * KK;              // [S][q][x] b_q
-  double* Ut = Bc + S * KK;              // [S][q][l] u~_q at block position l
-  double* Wt = Ut + S * KK;              // [S][q][l] w~_q
-  double* Gam = Wt + S * KK;             // [S][KK] Gamma(x, y) at y * KB + x
-  int* etmp = reinterpret_cast<int*>(Gam + S * KK);         // [256]
+  double* uni = reinterpret_cast<double*>(smem + A_BYTES + NBB * B_BYTES);  // [KB] uniforms of the block
+  SubState st;
+  st.Gam = uni + KB;
+  st.Gb = st.Gam + S * KK;
+  st.Ac = st.Gb + S * KK;
+  st.Bc = st.Ac + S * KK;
+  st.Ut = st.Bc + S * KK;
+  st.Wt = st.Ut + S * KK;
+  int* etmp = reinterpret_cast<int*>(st.Wt + S * KK);       // [256]
   int8_t* s_field = reinterpret_cast<int8_t*>(etmp + 256);  // [KB]
   __shared__ int s_next, s_pos[KB];
   __shared__ double s_f[2];
@@ -572,75 +651,13 @@ __global__ void __launch_bounds__(kSubThreads) metropolis_sub_block_kernel(const
     const int attempt = (mode == MODE_FWD) ? (eff * N + i) : ((Lt - t) * N + i);
     uni[l] = (w.rng == 0) ? w.uni[attempt] : philox_uniform(w.seed, (unsigned)w.widx, sweep, (unsigned)(eff * N + i));
   }
-  for (int e = tid; e < S * KK; e += kSubThreads) {
-    const int sp = e / KK, c = (e % KK) / KB, r = e % KB;
-    Gb[e] = (r < kb && c < kb) ? G[sp][(long long)(i0 + c) * N + i0 + r] : 0.0;
-  }
+  sub_load_block(st, G, S, N, i0, kb);
   double sign = 0.0;
   long long acc_count = 0;
   if (tid == 0) sign = *w.sign;
   __syncthreads();
 
-  // ---- decisions, flip by flip, on the diagonal block
-  int m = 0, cur = 0;
-  while (true) {
-    if (tid == 0) {
-      int l = cur;
-      for (; l < kb; ++l) {
-        const int s = s_field[l];
-        const int si = s > 0 ? 0 : 1;
-        const double gu = Gb[l * KB + l];
-        const double gd = (S == 2) ? Gb[KK + l * KB + l] : gu;
-        const FlipRatio q = flip_ratio(w, si, gu, gd);  // reference operation order
-        const double r = q.r;
-        const double prob = fmin(1.0, fabs(r));
-        if (!isfinite(r)) atomicOr(w.status, ST_NONFINITE_RATIO);
-        if (uni[l] < prob) {
-          flip_factors(w, q, s_f);
-          s_field[l] = (int8_t)(-s);
-          sign = (r >= 0) ? sign : -sign;
-          ++acc_count;
-          break;
-        }
-      }
-      s_next = l;
-    }
-    __syncthreads();
-    const int l = s_next;
-    if (l >= kb) break;
-    for (int e = tid; e < S * 4 * KB; e += kSubThreads) {
-      const int sp = e / (4 * KB), role = (e / KB) & 3, x = e % KB;
-      const double f = s_f[sp];
-      const double* gb = Gb + sp * KK;
-      double* ut = Ut + sp * KK;
-      double* wt = Wt + sp * KK;
-      double* ac = Ac + sp * KK;
-      double* bc = Bc + sp * KK;
-      if (role == 0) {
-        ut[m * KB + x] = f * gb[l * KB + x];  // f G(x, l)
-      } else if (role == 1) {
-        wt[m * KB + x] = ((x == l) ? 1.0 : 0.0) - gb[x * KB + l];  // delta - G(l, x)
-      } else if (role == 2) {
-        double a = (x == m) ? 1.0 : 0.0;
-        for (int p = x; p < m; ++p) a = fma(-wt[p * KB + l], ac[p * KB + x], a);
-        ac[m * KB + x] = (x <= m) ? f * a : 0.0;
-      } else {
-        double b = (x == m) ? 1.0 : 0.0;
-        for (int p = x; p < m; ++p) b = fma(ut[p * KB + l], bc[p * KB + x], b);
-        bc[m * KB + x] = (x <= m) ? b : 0.0;
-      }
-    }
-    if (tid == 0) s_pos[m] = l;
-    __syncthreads();
-    for (int e = tid; e < S * KK; e += kSubThreads) {
-      const int sp = e / KK, c = (e % KK) / KB, r = e % KB;
-      if (r > l && c > l && r < kb && c < kb)
-        Gb[e] = fma(-Ut[sp * KK + m * KB + r], Wt[sp * KK + m * KB + c], Gb[e]);
-    }
-    ++m;
-    cur = l + 1;
-    __syncthreads();
-  }
+  const int m = sub_decide(w, S, kb, uni, s_field, st, s_pos, &s_next, s_f, sign, acc_count);
   int8_t* frw = w.fields + (long long)eff * N + i0;
   for (int l = tid; l < kb; l += kSubThreads) frw[l] = s_field[l];
   if (tid == 0) {
@@ -651,17 +668,6 @@ __global__ void __launch_bounds__(kSubThreads) metropolis_sub_block_kernel(const
   }
   if (m == 0) return;
 
-  // ---- Gamma = sum_q a_q b_q^T
-  for (int e = tid; e < S * KK; e += kSubThreads) {
-    const int sp = e / KK, y = (e % KK) / KB, x = e % KB;
-    double gsum = 0.0;
-    if (x < m && y < m) {
-      const double* ac = Ac + sp * KK;
-      const double* bc = Bc + sp * KK;
-      for (int p = max(x, y); p < m; ++p) gsum = fma(ac[p * KB + x], bc[p * KB + y], gsum);
-    }
-    Gam[e] = gsum;
-  }
   if (tid == 0) {
     s_tcfail = 0;
     tc::mbar_init(&bar_ldA);
@@ -676,83 +682,12 @@ __global__ void __launch_bounds__(kSubThreads) metropolis_sub_block_kernel(const
   tc::fence_after();
   const SubTC tcs{smem, smem + A_BYTES, &bar_ldA, bar_ldB, bar_mma, s_tmem, &s_tcfail};
   unsigned gt = 0, nA = 0;
-  const int nlbN = ozaki::tc_lines(N) / 8;
-  const long long sstN = (long long)sub_sst(N), sstG = (long long)sub_sst(1);
-  const int nk = (m + 15) / 16;
   for (int sp = 0; sp < S; ++sp) {
     unsigned char* ms = w.msub + (size_t)sp * so.total;
-    unsigned short* sGm = reinterpret_cast<unsigned short*>(ms + so.sGm);
-    unsigned short* sG = reinterpret_cast<unsigned short*>(ms + so.sG);
-    unsigned short* sR = reinterpret_cast<unsigned short*>(ms + so.sR);
-    unsigned short* sT = reinterpret_cast<unsigned short*>(ms + so.sT);
-    int* eGm = reinterpret_cast<int*>(ms + so.eGm);
-    int* eG = reinterpret_cast<int*>(ms + so.eG);
-    int* eR = reinterpret_cast<int*>(ms + so.eR);
-    int* eT = reinterpret_cast<int*>(ms + so.eT);
-    const double* gam = Gam + sp * KK;
-    const double* Gs = G[sp];
-    slice_lines([&](int line, int k) { return gam[k * KB + line]; }, m, m, sGm, sstG, TM / 8, eGm, etmp);
-    slice_lines([&](int line, int k) { return Gs[(long long)(i0 + s_pos[k]) * N + line]; }, N, m, sG, sstN, nlbN,
-                eG, etmp);
-    slice_lines(
-        [&](int line, int k) {
-          const int i = i0 + s_pos[k];
-          return ((line == i) ? 1.0 : 0.0) - Gs[(long long)line * N + i];
-        },
-        N, m, sR, sstN, nlbN, eR, etmp);
-    asm volatile("fence.proxy.async.global;" ::: "memory");  // generic writes -> bulk-copy reads
-    __syncthreads();
-    // T^T = R_A^T Gamma^T, its epilogue slicing T into the flush's B image (as the fused kernel)
-    sub_gemm(tcs, gt, nA, sR, sstN, nlbN, (N + TM - 1) / TM, sGm, sstG, TM / 8, 1, nk, [&](int, int) {},
-             [&](int rb, int, unsigned tacc, bool ok) {
-               const int wq = (tid >> 5) & 3, xh = tid >> 7;
-               const int c = rb * TM + wq * 32 + (tid & 31);
-               const int ec = (c < N) ? eR[c] : 0;
-               double tv[16];
-               int e = -1100;
-               if (ok) {
-#pragma unroll
-                 for (int h = 0; h < 2; ++h) {
-                   uint32_t v[OZS][8];
-#pragma unroll
-                   for (int g = 0; g < OZS; ++g)
-                     tc::ld8(v[g], tacc + ((unsigned)(wq * 32) << 16) + (unsigned)(g * TN + xh * 16 + h * 8));
-                   tc::wait_ld();
-#pragma unroll
-                   for (int u = 0; u < 8; ++u) {
-                     const int x = xh * 16 + h * 8 + u;
-                     tv[h * 8 + u] = (x < m && c < N) ? ozaki::ldexp_i64(group_sum(v, u), ec + eGm[x] + kEOff) : 0.0;
-                     e = max(e, ozaki::exp_bound(tv[h * 8 + u]));
-                   }
-                 }
-               }
-               etmp[tid] = e;
-               __syncthreads();
-               e = max(e, etmp[tid ^ 128]);
-               if (ok && c < N) {
-                 if (xh == 0) eT[c] = e;
-                 unsigned pk[OZS][8];
-#pragma unroll
-                 for (int u = 0; u < 16; u += 2) {
-                   bool n0, n1;
-                   const unsigned long long q0 = ozaki::fixed42(tv[u], e, n0), q1 = ozaki::fixed42(tv[u + 1], e, n1);
-#pragma unroll
-                   for (int s2 = 0; s2 < OZS; ++s2)
-                     pk[s2][u >> 1] = (unsigned)ozaki::slice_bf16(q0, s2, OZB, n0) |
-                                      ((unsigned)ozaki::slice_bf16(q1, s2, OZB, n1) << 16);
-                 }
-                 unsigned short* o = sT + ozaki::tc_index(c, xh * 16, nlbN);
-#pragma unroll
-                 for (int s2 = 0; s2 < OZS; ++s2) {
-                   *reinterpret_cast<uint4*>(o + s2 * sstN) = make_uint4(pk[s2][0], pk[s2][1], pk[s2][2], pk[s2][3]);
-                   *reinterpret_cast<uint4*>(o + s2 * sstN + 64) =
-                       make_uint4(pk[s2][4], pk[s2][5], pk[s2][6], pk[s2][7]);
-                 }
-               }
-             });
-    __syncthreads();
+    sub_prepare(tcs, gt, nA, w, sp, N, m, i0, s_pos, st.Gam + sp * KK, G[sp], reinterpret_cast<int*>(ms + so.eGm),
+                reinterpret_cast<int*>(ms + so.eG), reinterpret_cast<int*>(ms + so.eR),
+                reinterpret_cast<int*>(ms + so.eT), etmp);
   }
-  asm volatile("fence.proxy.async.global;" ::: "memory");  // T's slices -> the flush's bulk copies
   tc::fence_before();
   __syncthreads();
   if (tid < 32) tc::dealloc(s_tmem, TMEM_COLS);
@@ -777,8 +712,12 @@ __global__ void __launch_bounds__(kSubThreads) metropolis_sub_flush_kernel(const
   const SubOff so = sub_offsets(N);
   const int m = *reinterpret_cast<const int*>(w.msub + so.mc);
   if (m == 0) return;
+  const int Nu = (N + 1) & ~1;
   const long long NN = (long long)N * N;
   extern __shared__ __align__(1024) unsigned char smem[];
+  double* stage = reinterpret_cast<double*>(smem + A_BYTES + NBB * B_BYTES);
+  int* s_eG = reinterpret_cast<int*>(reinterpret_cast<unsigned char*>(stage) + kStageBytes);
+  int* s_eT = s_eG + Nu;
   __shared__ __align__(8) unsigned long long bar_ldA, bar_ldB[NBB], bar_mma[2];
   __shared__ unsigned s_tmem;
   __shared__ int s_tcfail;
@@ -796,50 +735,16 @@ __global__ void __launch_bounds__(kSubThreads) metropolis_sub_flush_kernel(const
   tc::fence_after();
   const SubTC tcs{smem, smem + A_BYTES, &bar_ldA, bar_ldB, bar_mma, s_tmem, &s_tcfail};
   unsigned gt = 0, nA = 0;
-  const int nlbN = ozaki::tc_lines(N) / 8;
-  const long long sstN = (long long)sub_sst(N);
-  const int nk = (m + 15) / 16;
   for (int sp = 0; sp < S; ++sp) {
-    unsigned char* ms = w.msub + (size_t)sp * so.total;
-    const unsigned short* sG = reinterpret_cast<const unsigned short*>(ms + so.sG);
-    const unsigned short* sT = reinterpret_cast<const unsigned short*>(ms + so.sT);
+    const unsigned char* ms = w.msub + (size_t)sp * so.total;
     const int* eG = reinterpret_cast<const int*>(ms + so.eG);
     const int* eT = reinterpret_cast<const int*>(ms + so.eT);
-    double* Gs = w.G + sp * NN;
-    double gv[16];
-    int ecol[16];
-    const int wq = (tid >> 5) & 3, half = tid >> 7;
-    sub_gemm(tcs, gt, nA, sG, sstN, nlbN, (N + TM - 1) / TM, sT, sstN, nlbN, nct, nk,
-             [&](int rb, int cb) {
-               const int r = rb * TM + wq * 32 + (tid & 31), c0 = cb * TN + half * 16;
-#pragma unroll
-               for (int u = 0; u < 16; ++u) {
-                 const int c = c0 + u;
-                 gv[u] = (r < N && c < N) ? Gs[(long long)c * N + r] : 0.0;
-                 ecol[u] = (c < N) ? eT[c] : 0;
-               }
-             },
-             [&](int rb, int cb, unsigned tacc, bool ok) {
-               if (!ok) return;
-               const int r = rb * TM + wq * 32 + (tid & 31), c0 = cb * TN + half * 16;
-               const int er = (r < N) ? eG[r] : 0;
-               const unsigned ta = tacc + ((unsigned)(wq * 32) << 16);
-#pragma unroll
-               for (int h = 0; h < 2; ++h) {
-                 uint32_t v[OZS][8];
-#pragma unroll
-                 for (int g = 0; g < OZS; ++g) tc::ld8(v[g], ta + (unsigned)(g * TN + half * 16 + h * 8));
-                 tc::wait_ld();
-#pragma unroll
-                 for (int u = 0; u < 8; ++u) {
-                   const int c = c0 + h * 8 + u;
-                   const long long sv = group_sum(v, u);
-                   if (sv != 0 && r < N && c < N)
-                     Gs[(long long)c * N + r] = gv[h * 8 + u] - ozaki::ldexp_i64(sv, er + ecol[h * 8 + u] + kEOff);
-                 }
-               }
-             },
-             (int)blockIdx.x, (int)gridDim.x);
+    for (int i = tid; i < N; i += kSubThreads) {
+      s_eG[i] = eG[i];
+      s_eT[i] = eT[i];
+    }
+    __syncthreads();
+    sub_flush(tcs, gt, nA, w, sp, N, m, w.G + sp * NN, s_eG, s_eT, stage, (int)blockIdx.x, (int)gridDim.x);
   }
   tc::fence_before();
   __syncthreads();
@@ -865,7 +770,7 @@ cudaError_t configure_submatrix_kernel() {
                              (int)submatrix_block_smem_bytes(2));
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(metropolis_sub_flush_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)submatrix_flush_smem_bytes());
+                             (int)submatrix_flush_smem_bytes(kMaxN));
   return e;
 }
 
@@ -882,7 +787,7 @@ int submatrix_flush_ctas(int maxN) { return std::max(1, ((maxN + TN - 1) / TN + 
 void launch_metropolis_sub_split(const WalkerDev* W, int nw, int mode, int j, int q, int maxN, int S_max,
                                  cudaStream_t st) {
   const int nb = (maxN + KB - 1) / KB, P = submatrix_flush_ctas(maxN);
-  const size_t sm1 = submatrix_block_smem_bytes(S_max), sm2 = submatrix_flush_smem_bytes();
+  const size_t sm1 = submatrix_block_smem_bytes(S_max), sm2 = submatrix_flush_smem_bytes(maxN);
   for (int blk = 0; blk < nb; ++blk) {
     metropolis_sub_block_kernel<<<nw, kSubThreads, sm1, st>>>(W, mode, j, q, blk);
     metropolis_sub_flush_kernel<<<dim3(P, nw), kSubThreads, sm2, st>>>(W, mode, j, q, blk);
