@@ -43,7 +43,8 @@ namespace dqmc {
 
 namespace {
 
-constexpr int kSubThreads = 256;
+constexpr int kSubThreads = 256;             // worker threads: decisions, slicing, epilogues
+constexpr int kSubCTA = kSubThreads + 32;     // + one producer warp (bulk copies and MMAs)
 constexpr int KB = 32;           // sites per block
 constexpr int KK = KB * KB;
 constexpr int OZS = 6, OZB = 7;  // 6 slices of 7 bits; group sums < 2^22 for K <= 32
@@ -56,6 +57,9 @@ constexpr int ACC_COLS = OZS * TN;          // TMEM columns of one accumulator (
 constexpr unsigned TMEM_COLS = 512;         // two accumulators
 
 __host__ __device__ inline size_t al256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+// barrier of the eight worker warps alone (named barrier 1); __syncthreads joins the producer
+__device__ __forceinline__ void wsync() { asm volatile("bar.sync 1, %0;" ::"n"(kSubThreads) : "memory"); }
 
 // per-spin scratch in HBM (WalkerDev::msub): the operands' slices as tensor-core
 // images (ozaki::tc_index, k stride 32) and the line exponents
@@ -88,45 +92,61 @@ __device__ __forceinline__ bool sub_slice_of(const WalkerDev& w, int mode, int j
   return true;
 }
 
-// Slices nlines lines x K (<= KB) of an operand into the tensor-core image
-// dst (slice stride sst, nlb 8-line blocks per k chunk; k past K written as
-// zeros) with one exponent per line (ex[line]); get(line, k) is the FP64
-// element.  All threads take part; 4 threads per line, 8 k each.
-template <class Get>
-__device__ void slice_lines(Get get, int nlines, int K, unsigned short* dst, long long sst, int nlb, int* ex,
-                            int* etmp) {
+// Slices nlines lines x K (<= KB) of NOP operands (1 or 2) into their tensor-core images
+// dst[o] (slice stride sst, nlb 8-line blocks per k chunk; k past K written as zeros) with one
+// exponent per line (ex[o][line]); get(o, line, k) is the FP64 element.  The worker threads
+// take part; 4 threads per line, 8 k each, both operands' loads in flight together.
+// etmp: [2][256] scratch.
+template <int NOP, class Get>
+__device__ void slice_lines(Get get, int nlines, int K, unsigned short* const* dst, long long sst, int nlb,
+                            int* const* ex, int* etmp) {
   const int tid = threadIdx.x, ll = tid & 63, part = tid >> 6;
   for (int l0 = 0; l0 < nlines; l0 += 64) {
     const int line = l0 + ll;
-    double v[8];
-    int e = -1100;
+    double v[NOP][8];
+    int e[NOP];
 #pragma unroll
-    for (int u = 0; u < 8; ++u) {
-      const int k = part * 8 + u;
-      v[u] = (line < nlines && k < K) ? get(line, k) : 0.0;
-      e = max(e, ozaki::exp_bound(v[u]));
+    for (int o = 0; o < NOP; ++o) {
+      e[o] = -1100;
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int k = part * 8 + u;
+        v[o][u] = (line < nlines && k < K) ? get(o, line, k) : 0.0;
+      }
     }
-    etmp[part * 64 + ll] = e;
-    __syncthreads();
-    e = max(max(etmp[ll], etmp[64 + ll]), max(etmp[128 + ll], etmp[192 + ll]));
-    if (line < nlines) {
-      if (part == 0) ex[line] = e;
-      unsigned pk[OZS][4];
 #pragma unroll
-      for (int u = 0; u < 8; u += 2) {
-        bool n0, n1;
-        const unsigned long long q0 = ozaki::fixed42(v[u], e, n0), q1 = ozaki::fixed42(v[u + 1], e, n1);
+    for (int o = 0; o < NOP; ++o) {
+#pragma unroll
+      for (int u = 0; u < 8; ++u) e[o] = max(e[o], ozaki::exp_bound(v[o][u]));
+      etmp[o * 256 + part * 64 + ll] = e[o];
+    }
+    wsync();
+#pragma unroll
+    for (int o = 0; o < NOP; ++o) {
+      const int* et = etmp + o * 256;
+      e[o] = max(max(et[ll], et[64 + ll]), max(et[128 + ll], et[192 + ll]));
+    }
+    if (line < nlines) {
+#pragma unroll
+      for (int o = 0; o < NOP; ++o) {
+        if (part == 0) ex[o][line] = e[o];
+        unsigned pk[OZS][4];
+#pragma unroll
+        for (int u = 0; u < 8; u += 2) {
+          bool n0, n1;
+          const unsigned long long q0 = ozaki::fixed42(v[o][u], e[o], n0), q1 = ozaki::fixed42(v[o][u + 1], e[o], n1);
+#pragma unroll
+          for (int s = 0; s < OZS; ++s)
+            pk[s][u >> 1] = (unsigned)ozaki::slice_bf16(q0, s, OZB, n0) |
+                            ((unsigned)ozaki::slice_bf16(q1, s, OZB, n1) << 16);
+        }
+        unsigned short* out = dst[o] + ozaki::tc_index(line, part * 8, nlb);
 #pragma unroll
         for (int s = 0; s < OZS; ++s)
-          pk[s][u >> 1] = (unsigned)ozaki::slice_bf16(q0, s, OZB, n0) |
-                          ((unsigned)ozaki::slice_bf16(q1, s, OZB, n1) << 16);
+          *reinterpret_cast<uint4*>(out + s * sst) = make_uint4(pk[s][0], pk[s][1], pk[s][2], pk[s][3]);
       }
-      unsigned short* o = dst + ozaki::tc_index(line, part * 8, nlb);
-#pragma unroll
-      for (int s = 0; s < OZS; ++s)
-        *reinterpret_cast<uint4*>(o + s * sst) = make_uint4(pk[s][0], pk[s][1], pk[s][2], pk[s][3]);
     }
-    __syncthreads();
+    wsync();
   }
 }
 
@@ -149,22 +169,42 @@ __device__ __forceinline__ long long group_sum(const uint32_t (&v)[OZS][8], int 
 // The tile loop of one product, C = A B with A: nrb row blocks of 128 lines, B:
 // the column tiles cb0, cb0 + cbs, ... < nct of 32 lines, K = 16 nk, both as
 // tensor-core images in global memory (slice stride a_sst / b_sst, a_nlb / b_nlb
-// line blocks per k chunk).  Tile u (global count across products) uses B buffer
-// u % NBB and TMEM accumulator u & 1; thread 0 copies the B tile of t+2 and
-// issues the MMAs of t+1 while every thread runs pre(row block, column tile, t+1)
-// (copies for the next tile's epilogue that do not need the product) and then
-// epi(row block, column tile, TMEM address, ok, t, t+1 < tiles) on tile t;
-// pre(.., 0) runs before the loop.  A is reloaded (after the MMAs of the
-// previous tile) at each row block.
+// line blocks per k chunk).  Called by all kSubCTA threads.  Tile u (global count
+// across products) uses B buffer u % NBB and TMEM accumulator u & 1.  The
+// producer (the first thread of the last warp) copies A at each row block and the
+// B tiles two ahead, waits until the epilogue of tile u - 2 has read its
+// accumulator, issues the MMAs of tile u and commits them to mmab[u & 1] and to the
+// B buffer's bfree.  The eight worker warps run pre(row block, column tile, t + 1)
+// (copies the next tile's epilogue needs that do not depend on the product), wait
+// for the MMAs of tile t, run epi(row block, column tile, TMEM address, ok, t,
+// t + 1 < tiles) and arrive on accfree[u & 1]; pre(.., 0) runs before the loop.
+// The workers and the producer meet only through the mbarriers, and at the end.
 struct SubTC {
   unsigned char* A;            // A_BYTES
   unsigned char* B;            // NBB x B_BYTES
   unsigned long long* ldA;     // [1]
   unsigned long long* ldB;     // [NBB]
-  unsigned long long* mmab;    // [2]
+  unsigned long long* mmab;    // [2] MMAs of the tile in accumulator a done
+  unsigned long long* bfree;   // [NBB] MMAs reading B buffer b done
+  unsigned long long* accfree; // [2] epilogue of the tile in accumulator a done (8 arrivals)
   unsigned tmem;
   volatile int* fail;          // shared flag: a bounded wait ran out
 };
+
+// the mbarriers of a SubTC, initialised by one thread
+__device__ __forceinline__ void sub_tc_init(unsigned long long* ldA, unsigned long long* ldB, unsigned long long* mmab,
+                                            unsigned long long* bfree, unsigned long long* accfree) {
+  tc::mbar_init(ldA);
+  for (int i = 0; i < NBB; ++i) {
+    tc::mbar_init(&ldB[i]);
+    tc::mbar_init(&bfree[i]);
+  }
+  for (int i = 0; i < 2; ++i) {
+    tc::mbar_init(&mmab[i]);
+    tc::mbar_init_n(&accfree[i], kSubThreads / 32);
+  }
+  tc::mbar_fence_init();
+}
 
 template <class Pre, class Epi>
 __device__ void sub_gemm(const SubTC& tc, unsigned& gt, unsigned& nA, const unsigned short* aG, long long a_sst,
@@ -174,67 +214,79 @@ __device__ void sub_gemm(const SubTC& tc, unsigned& gt, unsigned& nA, const unsi
   const int ncl = (nct > cb0) ? (nct - cb0 + cbs - 1) / cbs : 0;  // column tiles of this CTA
   const int ntiles = nrb * ncl;
   if (ntiles == 0) return;
-  constexpr uint32_t idesc = tc::idesc_bf16(TM, TN);
   auto cb_of = [&](int t) { return cb0 + (t % ncl) * cbs; };
-  auto load_b = [&](int t) {  // thread 0
-    const unsigned u = gt + t;
-    const int cb = cb_of(t), bb = (int)(u % NBB);
-    unsigned char* dst = tc.B + bb * B_BYTES;
-    tc::mbar_expect_tx(&tc.ldB[bb], OZS * nk * TN * 32);
-    for (int s2 = 0; s2 < OZS; ++s2)
-      for (int kk = 0; kk < nk; ++kk)
-        tc::bulk_g2s(dst + (s2 * 2 + kk) * TN * 32, bG + s2 * b_sst + ((long long)kk * b_nlb + cb * (TN / 8)) * 128,
-                     TN * 32, &tc.ldB[bb]);
-  };
-  auto issue = [&](int t) {  // thread 0: A if a new row block, then the MMAs of tile t
-    const unsigned u = gt + t;
-    const int rb = t / ncl, bb = (int)(u % NBB), acc = (int)(u & 1);
-    if (*tc.fail) return;
-    if (t % ncl == 0) {
-      // the A buffer is free once the MMAs of the previous tile (all earlier ones) completed
-      if (t > 0 && !tc::mbar_wait(&tc.mmab[(u - 1) & 1], ((u - 1) >> 1) & 1)) { *tc.fail = 1; return; }
-      tc::mbar_expect_tx(tc.ldA, OZS * nk * TM * 32);
-      for (int s2 = 0; s2 < OZS; ++s2)
+  if (tid >= kSubThreads) {
+    // ---- producer (one thread; its warp reconverges before the final barrier)
+    if (tid == kSubThreads) {
+      constexpr uint32_t idesc = tc::idesc_bf16(TM, TN);
+      auto load_b = [&](int t) {
+        const unsigned u = gt + t;
+        const int cb = cb_of(t), bb = (int)(u % NBB);
+        // the buffer's previous tile (u - NBB) has finished its MMAs
+        if (u >= NBB && !tc::mbar_wait(&tc.bfree[bb], ((u / NBB) - 1) & 1)) { *tc.fail = 1; return; }
+        unsigned char* dst = tc.B + bb * B_BYTES;
+        tc::mbar_expect_tx(&tc.ldB[bb], OZS * nk * TN * 32);
+        for (int s2 = 0; s2 < OZS; ++s2)
+          for (int kk = 0; kk < nk; ++kk)
+            tc::bulk_g2s(dst + (s2 * 2 + kk) * TN * 32,
+                         bG + s2 * b_sst + ((long long)kk * b_nlb + cb * (TN / 8)) * 128, TN * 32, &tc.ldB[bb]);
+      };
+      auto issue = [&](int t) {  // A if a new row block, then the MMAs of tile t
+        const unsigned u = gt + t;
+        const int rb = t / ncl, bb = (int)(u % NBB), acc = (int)(u & 1);
+        if (t % ncl == 0) {
+          // the A buffer is free once the MMAs of the previous tile (all earlier ones) completed
+          if (u > 0 && !tc::mbar_wait(&tc.mmab[(u - 1) & 1], ((u - 1) >> 1) & 1)) { *tc.fail = 1; return; }
+          tc::mbar_expect_tx(tc.ldA, OZS * nk * TM * 32);
+          for (int s2 = 0; s2 < OZS; ++s2)
+            for (int kk = 0; kk < nk; ++kk)
+              tc::bulk_g2s(tc.A + (s2 * 2 + kk) * TM * 32,
+                           aG + s2 * a_sst + ((long long)kk * a_nlb + rb * (TM / 8)) * 128, TM * 32, tc.ldA);
+          if (!tc::mbar_wait(tc.ldA, nA & 1)) { *tc.fail = 1; return; }
+          ++nA;
+        }
+        if (!tc::mbar_wait(&tc.ldB[bb], (u / NBB) & 1)) { *tc.fail = 1; return; }
+        // the epilogue of tile u - 2 has read this accumulator
+        if (u >= 2 && !tc::mbar_wait(&tc.accfree[acc], ((u >> 1) - 1) & 1)) { *tc.fail = 1; return; }
+        tc::fence_after();
+        const unsigned sa = tc::su32(tc.A), sb = tc::su32(tc.B + bb * B_BYTES);
         for (int kk = 0; kk < nk; ++kk)
-          tc::bulk_g2s(tc.A + (s2 * 2 + kk) * TM * 32, aG + s2 * a_sst + ((long long)kk * a_nlb + rb * (TM / 8)) * 128,
-                       TM * 32, tc.ldA);
-      if (!tc::mbar_wait(tc.ldA, nA & 1)) { *tc.fail = 1; return; }
-      ++nA;
-    }
-    if (!tc::mbar_wait(&tc.ldB[bb], (u / NBB) & 1)) { *tc.fail = 1; return; }
-    tc::fence_after();
-    const unsigned sa = tc::su32(tc.A), sb = tc::su32(tc.B + bb * B_BYTES);
-    for (int kk = 0; kk < nk; ++kk)
-#pragma unroll
-      for (int i = 0; i < OZS; ++i) {
-        const uint64_t ad = tc::desc(sa + (i * 2 + kk) * TM * 32, 128, 256);
-#pragma unroll
-        for (int jj = 0; jj < OZS - i; ++jj)
-          tc::mma(tc.tmem + (unsigned)(acc * ACC_COLS + (i + jj) * TN), ad,
-                  tc::desc(sb + (jj * 2 + kk) * TN * 32, 128, 256), idesc, kk > 0 || i > 0);
+  #pragma unroll
+          for (int i = 0; i < OZS; ++i) {
+            const uint64_t ad = tc::desc(sa + (i * 2 + kk) * TM * 32, 128, 256);
+  #pragma unroll
+            for (int jj = 0; jj < OZS - i; ++jj)
+              tc::mma(tc.tmem + (unsigned)(acc * ACC_COLS + (i + jj) * TN), ad,
+                      tc::desc(sb + (jj * 2 + kk) * TN * 32, 128, 256), idesc, kk > 0 || i > 0);
+          }
+        tc::commit(&tc.mmab[acc]);
+        tc::commit(&tc.bfree[bb]);
+      };
+      if (!*tc.fail) load_b(0);
+      if (ntiles > 1 && !*tc.fail) load_b(1);
+      for (int t = 0; t < ntiles && !*tc.fail; ++t) {
+        issue(t);
+        if (t + 2 < ntiles && !*tc.fail) load_b(t + 2);  // its buffer held tile t - 1
       }
-    tc::commit(&tc.mmab[acc]);
-  };
-  if (tid == 0 && !*tc.fail) {
-    load_b(0);
-    if (ntiles > 1) load_b(1);
-    issue(0);
-  }
-  pre(0, cb_of(0), 0);
-  for (int t = 0; t < ntiles; ++t) {
-    const unsigned u = gt + t;
-    if (tid == 0 && !*tc.fail) {
-      if (t + 2 < ntiles) load_b(t + 2);  // its buffer held tile t - 1, whose epilogue is done
-      if (t + 1 < ntiles) issue(t + 1);
     }
-    const bool more = t + 1 < ntiles;
-    if (more) pre((t + 1) / ncl, cb_of(t + 1), t + 1);
-    if (!*tc.fail && !tc::mbar_wait(&tc.mmab[u & 1], (u >> 1) & 1)) *tc.fail = 1;
-    tc::fence_after();
-    epi(t / ncl, cb_of(t), tc.tmem + (unsigned)((u & 1) * ACC_COLS), !*tc.fail, t, more);
-    tc::fence_before();
-    __syncthreads();
+    __syncwarp();
+  } else {
+    // ---- workers
+    pre(0, cb_of(0), 0);
+    for (int t = 0; t < ntiles; ++t) {
+      const unsigned u = gt + t;
+      const bool more = t + 1 < ntiles;
+      if (more) pre((t + 1) / ncl, cb_of(t + 1), t + 1);
+      if (!*tc.fail && !tc::mbar_wait(&tc.mmab[u & 1], (u >> 1) & 1)) *tc.fail = 1;
+      tc::fence_after();
+      const bool ok = __all_sync(0xffffffffu, !*tc.fail);  // warp-uniform: the epilogue's TMEM loads are .aligned
+      epi(t / ncl, cb_of(t), tc.tmem + (unsigned)((u & 1) * ACC_COLS), ok, t, more);
+      tc::fence_before();
+      __syncwarp();
+      if ((tid & 31) == 0) tc::mbar_arrive(&tc.accfree[u & 1]);
+    }
   }
+  __syncthreads();
   gt += ntiles;
 }
 
@@ -267,7 +319,7 @@ __host__ __device__ inline size_t sub_state_bytes(int S) {
   return b > (size_t)kStageBytes ? b : (size_t)kStageBytes;
 }
 
-// Gb = G(I, I) of the block at sites i0 .. i0 + kb - 1, zero past kb
+// Gb = G(I, I) of the block at sites i0 .. i0 + kb - 1, zero past kb (worker threads)
 __device__ __forceinline__ void sub_load_block(const SubState& st, const double* const* G, int S, int N, int i0, int kb) {
   for (int e = threadIdx.x; e < S * KK; e += kSubThreads) {
     const int sp = e / KK, c = (e % KK) / KB, r = e % KB;
@@ -275,47 +327,72 @@ __device__ __forceinline__ void sub_load_block(const SubState& st, const double*
   }
 }
 
-// The decisions of one block, flip by flip, then Gamma = sum_q a_q b_q^T; returns m, the
+// The decisions of one block, flip by flip, and Gamma = sum_q a_q b_q^T; returns m, the
 // accepts, with their block positions in s_pos.  uni and fld are the block's uniforms and
 // fields (position l).  The sites are visited in order: warp 0 evaluates the ratios of all
 // sites still to visit at once, on the diagonal as it stands, and the lowest accepted one is
 // the next accept of the sequential visit, since every site before it saw the same diagonal.
-// sign and acc_count are thread 0's.
-__device__ __forceinline__ int sub_decide(const WalkerDev& w, int S, int kb, const double* uni, int8_t* fld, const SubState& st,
-                          int* s_pos, int* s_next, double* s_f, double& sign, long long& acc_count) {
-  const int tid = threadIdx.x;
+// Each accept then takes two phases: (1) the coefficients u~, w~, a, b of the accept; (2)
+// its rank-1 update of the block, warp 0 updating the diagonal of the sites still to visit
+// before it scans them for the next accept, while warps 1-7 update the rest of the block and
+// add a b^T to Gamma (the fma sequence of the closed sum over accepts, so Gamma is the same
+// to the bit).  sign and acc_count are thread 0's.  Worker threads only.
+__device__ __forceinline__ int sub_decide(const WalkerDev& w, int S, int kb, const double* uni, int8_t* fld,
+                                          const SubState& st, int* s_pos, int* s_next, double* s_f, double& sign,
+                                          long long& acc_count) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  for (int e = tid; e < S * KK; e += kSubThreads) st.Gam[e] = 0.0;
   int m = 0, cur = 0;
   while (true) {
-    if (tid < 32) {
-      const int l = cur + tid;
+    if (warp == 0) {
+      const int l = cur + lane;
       FlipRatio q{};
+      double fq[2] = {0.0, 0.0};
       int s = 0;
       bool acc = false;
       if (l < kb) {
+        if (m > 0)  // the previous accept's update of this site's diagonal element
+          for (int sp = 0; sp < S; ++sp) {
+            double* gb = st.Gb + sp * KK;
+            gb[l * KB + l] = fma(-st.Ut[sp * KK + (m - 1) * KB + l], st.Wt[sp * KK + (m - 1) * KB + l], gb[l * KB + l]);
+          }
         s = fld[l];
         const int si = s > 0 ? 0 : 1;
         const double gu = st.Gb[l * KB + l];
         const double gd = (S == 2) ? st.Gb[KK + l * KB + l] : gu;
         q = flip_ratio(w, si, gu, gd);  // reference operation order
         acc = uni[l] < fmin(1.0, fabs(q.r));
+        flip_factors(w, q, fq);         // every lane: off the accepted lane's critical path
       }
       const unsigned amask = __ballot_sync(0xffffffffu, acc);
       const int first = amask ? __ffs(amask) - 1 : 32;
-      if (l < kb && tid <= first && !isfinite(q.r)) atomicOr(w.status, ST_NONFINITE_RATIO);
-      if (tid == first) {
-        flip_factors(w, q, s_f);
+      if (l < kb && lane <= first && !isfinite(q.r)) atomicOr(w.status, ST_NONFINITE_RATIO);
+      if (lane == first) {
+        s_f[0] = fq[0];
+        s_f[1] = fq[1];
         fld[l] = (int8_t)(-s);
       }
       const double rf = __shfl_sync(0xffffffffu, q.r, first & 31);
-      if (tid == 0) {
+      if (lane == 0) {
         if (amask) {
           sign = (rf >= 0) ? sign : -sign;
           ++acc_count;
         }
         *s_next = amask ? cur + first : kb;
       }
+    } else if (m > 0) {
+      // the previous accept (position cur - 1): rank-1 update off the diagonal, Gamma term
+      const int lp = cur - 1, q1 = m - 1;
+      for (int e = tid - 32; e < S * KK; e += kSubThreads - 32) {
+        const int sp = e / KK, c = (e % KK) / KB, r = e % KB;
+        if (r > lp && c > lp && r < kb && c < kb && r != c)
+          st.Gb[e] = fma(-st.Ut[sp * KK + q1 * KB + r], st.Wt[sp * KK + q1 * KB + c], st.Gb[e]);
+        const int y = c, x = r;
+        if (x <= q1 && y <= q1)
+          st.Gam[e] = fma(st.Ac[sp * KK + q1 * KB + x], st.Bc[sp * KK + q1 * KB + y], st.Gam[e]);
+      }
     }
-    __syncthreads();
+    wsync();
     const int l = *s_next;
     if (l >= kb) break;
     // u~, w~ of accept m on the block, and its coefficients a_m, b_m
@@ -342,29 +419,10 @@ __device__ __forceinline__ int sub_decide(const WalkerDev& w, int S, int kb, con
       }
     }
     if (tid == 0) s_pos[m] = l;
-    __syncthreads();
-    // rank-1 update of the part of the block later decisions read
-    for (int e = tid; e < S * KK; e += kSubThreads) {
-      const int sp = e / KK, c = (e % KK) / KB, r = e % KB;
-      if (r > l && c > l && r < kb && c < kb)
-        st.Gb[e] = fma(-st.Ut[sp * KK + m * KB + r], st.Wt[sp * KK + m * KB + c], st.Gb[e]);
-    }
+    wsync();
     ++m;
     cur = l + 1;
-    __syncthreads();
   }
-  if (m == 0) return 0;
-  for (int e = tid; e < S * KK; e += kSubThreads) {
-    const int sp = e / KK, y = (e % KK) / KB, x = e % KB;
-    double gsum = 0.0;
-    if (x < m && y < m) {
-      const double* ac = st.Ac + sp * KK;
-      const double* bc = st.Bc + sp * KK;
-      for (int p = max(x, y); p < m; ++p) gsum = fma(ac[p * KB + x], bc[p * KB + y], gsum);
-    }
-    st.Gam[e] = gsum;
-  }
-  __syncthreads();
   return m;
 }
 
@@ -373,7 +431,8 @@ __device__ __forceinline__ int sub_decide(const WalkerDev& w, int S, int kb, con
 // cores: warp w and w + 4 share TMEM lanes 32 (w & 3).. (columns c) and take x in [0, 16) and
 // [16, 32); the column exponent max over x goes through etmp, and the epilogue slices T straight
 // into the B image of the flush (line c, k = x).  Line exponents: eGm [KB] of Gamma, eG [N] of
-// G0(:, I_A), eR [N] of R_A, eT [N] of T (shared or global memory).
+// G0(:, I_A), eR [N] of R_A, eT [N] of T (shared or global memory); etmp: [2][256] scratch.
+// Called by all kSubCTA threads; the workers slice.
 __device__ __forceinline__ void sub_prepare(const SubTC& tcs, unsigned& gt, unsigned& nA, const WalkerDev& w, int sp, int N, int m,
                             int i0, const int* s_pos, const double* gam, const double* Gs, int* eGm, int* eG, int* eR,
                             int* eT, int* etmp) {
@@ -386,19 +445,24 @@ __device__ __forceinline__ void sub_prepare(const SubTC& tcs, unsigned& gt, unsi
   const int tid = threadIdx.x;
   const int nlbN = ozaki::tc_lines(N) / 8, nk = (m + 15) / 16;
   const long long sstN = (long long)sub_sst(N), sstG = (long long)sub_sst(1);
-  slice_lines([&](int line, int k) { return gam[k * KB + line]; }, m, m, sGm, sstG, TM / 8, eGm, etmp);
-  slice_lines([&](int line, int k) { return Gs[(long long)(i0 + s_pos[k]) * N + line]; }, N, m, sG, sstN, nlbN, eG,
-              etmp);
-  slice_lines(
-      [&](int line, int k) {
-        const int i = i0 + s_pos[k];
-        return ((line == i) ? 1.0 : 0.0) - Gs[(long long)line * N + i];
-      },
-      N, m, sR, sstN, nlbN, eR, etmp);
-  asm volatile("fence.proxy.async.global;" ::: "memory");  // generic writes -> bulk-copy reads
+  if (tid < kSubThreads) {
+    unsigned short* dGm[1] = {sGm};
+    int* xGm[1] = {eGm};
+    slice_lines<1>([&](int, int line, int k) { return gam[k * KB + line]; }, m, m, dGm, sstG, TM / 8, xGm, etmp);
+    // G0(:, I_A) (lines = rows) and R_A (lines = columns) in one pass
+    unsigned short* dGR[2] = {sG, sR};
+    int* xGR[2] = {eG, eR};
+    slice_lines<2>(
+        [&](int o, int line, int k) {
+          const int i = i0 + s_pos[k];
+          return o == 0 ? Gs[(long long)i * N + line] : ((line == i) ? 1.0 : 0.0) - Gs[(long long)line * N + i];
+        },
+        N, m, dGR, sstN, nlbN, xGR, etmp);
+    asm volatile("fence.proxy.async.global;" ::: "memory");  // generic writes -> bulk-copy reads
+  }
   __syncthreads();
   sub_gemm(tcs, gt, nA, sR, sstN, nlbN, (N + TM - 1) / TM, sGm, sstG, TM / 8, 1, nk, [&](int, int, int) {},
-           [&](int rb, int, unsigned tacc, bool ok, int, bool) {
+           [&](int rb, int, unsigned tacc, bool ok, int tl, bool) {
              const int wq = (tid >> 5) & 3, xh = tid >> 7;
              const int c = rb * TM + wq * 32 + (tid & 31);
              const int ec = (c < N) ? eR[c] : 0;
@@ -420,9 +484,10 @@ __device__ __forceinline__ void sub_prepare(const SubTC& tcs, unsigned& gt, unsi
                  }
                }
              }
-             etmp[tid] = e;
-             __syncthreads();
-             e = max(e, etmp[tid ^ 128]);
+             int* ex = etmp + (tl & 1) * kSubThreads;  // two tiles in flight between the halves
+             ex[tid] = e;
+             wsync();
+             e = max(e, ex[tid ^ 128]);
              if (ok && c < N) {
                if (xh == 0) eT[c] = e;
                unsigned pk[OZS][8];
@@ -443,12 +508,12 @@ __device__ __forceinline__ void sub_prepare(const SubTC& tcs, unsigned& gt, unsi
                      make_uint4(pk[s2][4], pk[s2][5], pk[s2][6], pk[s2][7]);
                }
              }
+             asm volatile("fence.proxy.async.global;" ::: "memory");  // T's slices -> the flush's bulk copies
            });
-  asm volatile("fence.proxy.async.global;" ::: "memory");  // T's slices -> the flush's bulk copies
-  __syncthreads();
 }
 
-// G -= G0(:, I_A) T for spin sp over the column tiles cb0, cb0 + cbs, ... of G: warp w reads
+// G -= G0(:, I_A) T for spin sp over the column tiles cb0, cb0 + cbs, ... of G (all kSubCTA
+// threads; the workers run the epilogue): worker warp w reads
 // TMEM lanes 32 (w & 3) .. (rows), columns 16 (w >> 2) ..  Each thread's 16 elements of G of
 // the next tile are copied into stage (kStageBytes of shared memory) while the epilogue of the
 // current tile runs, so the epilogue reads G from shared memory; eG, eT: line exponents.
@@ -505,20 +570,22 @@ size_t submatrix_scratch_bytes(int N) { return sub_offsets(N).total; }
 // dynamic shared memory of the fused kernel: tensor-core operand buffers first (1024-byte
 // aligned base), then the slice's uniforms [N], Gamma [S][KK], the block state (overlaid by the
 // flush's G staging), the line exponents eG, eT, eR [N] and eGm [KB], the exponent scratch
-// [256] and the fields [N]
+// [2][256] and the fields [N]
 size_t submatrix_smem_bytes(int N, int S) {
   const size_t Nu = (size_t)((N + 1) & ~1);
   return (size_t)A_BYTES + (size_t)NBB * B_BYTES + sizeof(double) * (Nu + (size_t)S * KK) + sub_state_bytes(S) +
-         sizeof(int) * (3 * Nu + KB + 256) + (size_t)N;
+         sizeof(int) * (3 * Nu + KB + 2 * kSubThreads) + (size_t)N;
 }
 
-__global__ void __launch_bounds__(kSubThreads, 1) metropolis_sub_kernel(const WalkerDev* __restrict__ W, int mode, int j,
-                                                                     int q) {
+// One slice for one walker per CTA: kSubCTA threads, the eight worker warps and the producer.
+__global__ void __launch_bounds__(kSubCTA, 1) metropolis_sub_kernel(const WalkerDev* __restrict__ W, int mode, int j,
+                                                                    int q) {
   const WalkerDev& w = W[blockIdx.x];
   if (w.path != 2) return;
   int t;
   if (!sub_slice_of(w, mode, j, q, t)) return;
   const int N = w.N, S = w.S, Lt = w.Lt, tid = threadIdx.x;
+  const bool worker = tid < kSubThreads;
   const int Nu = (N + 1) & ~1;
   const long long NN = (long long)N * N;
   extern __shared__ __align__(1024) unsigned char smem[];
@@ -535,45 +602,47 @@ __global__ void __launch_bounds__(kSubThreads, 1) metropolis_sub_kernel(const Wa
   int* s_eT = s_eG + Nu;
   int* s_eR = s_eT + Nu;
   int* s_eGm = s_eR + Nu;
-  int* etmp = s_eGm + KB;                                   // [256]
-  int8_t* s_field = reinterpret_cast<int8_t*>(etmp + 256);  // [N]
-  __shared__ int s_next, s_pos[KB];
+  int* etmp = s_eGm + KB;                                               // [2][256]
+  int8_t* s_field = reinterpret_cast<int8_t*>(etmp + 2 * kSubThreads);  // [N]
+  __shared__ int s_next, s_pos[KB], s_m;
   __shared__ double s_f[2];
-  __shared__ __align__(8) unsigned long long bar_ldA, bar_ldB[NBB], bar_mma[2];
+  __shared__ __align__(8) unsigned long long bar_ldA, bar_ldB[NBB], bar_mma[2], bar_bfree[NBB], bar_accfree[2];
   __shared__ unsigned s_tmem;
   __shared__ int s_tcfail;
 
   double* G[2] = {w.G, (S == 2) ? w.G + NN : w.G};
   const int eff = t - 1;
   const unsigned long long sweep = (w.rng == 1) ? *w.sweep_ctr : 0ULL;
-  for (int i = tid; i < N; i += kSubThreads) {
-    s_field[i] = w.fields[(long long)eff * N + i];
-    const int attempt = (mode == MODE_FWD) ? (eff * N + i) : ((Lt - t) * N + i);
-    uni[i] = (w.rng == 0) ? w.uni[attempt] : philox_uniform(w.seed, (unsigned)w.widx, sweep, (unsigned)(eff * N + i));
-  }
+  if (worker)
+    for (int i = tid; i < N; i += kSubThreads) {
+      s_field[i] = w.fields[(long long)eff * N + i];
+      const int attempt = (mode == MODE_FWD) ? (eff * N + i) : ((Lt - t) * N + i);
+      uni[i] = (w.rng == 0) ? w.uni[attempt] : philox_uniform(w.seed, (unsigned)w.widx, sweep, (unsigned)(eff * N + i));
+    }
   double sign = 0.0;
   long long acc_count = 0;
   if (tid == 0) {
     sign = *w.sign;
     s_tcfail = 0;
-    tc::mbar_init(&bar_ldA);
-    for (int i = 0; i < NBB; ++i) tc::mbar_init(&bar_ldB[i]);
-    tc::mbar_init(&bar_mma[0]);
-    tc::mbar_init(&bar_mma[1]);
-    tc::mbar_fence_init();
+    sub_tc_init(&bar_ldA, bar_ldB, bar_mma, bar_bfree, bar_accfree);
   }
   if (tid < 32) tc::alloc(&s_tmem, TMEM_COLS);
   tc::fence_before();
   __syncthreads();
   tc::fence_after();
-  const SubTC tcs{smem, smem + A_BYTES, &bar_ldA, bar_ldB, bar_mma, s_tmem, &s_tcfail};
+  const SubTC tcs{smem, smem + A_BYTES, &bar_ldA, bar_ldB, bar_mma, bar_bfree, bar_accfree, s_tmem, &s_tcfail};
   unsigned gt = 0, nA = 0;  // tiles and A loads so far (mbarrier phases)
 
   for (int i0 = 0; i0 < N; i0 += KB) {
     const int kb = min(KB, N - i0);
-    sub_load_block(st, G, S, N, i0, kb);
+    if (worker) {
+      sub_load_block(st, G, S, N, i0, kb);
+      wsync();
+      const int mm = sub_decide(w, S, kb, uni + i0, s_field + i0, st, s_pos, &s_next, s_f, sign, acc_count);
+      if (tid == 0) s_m = mm;
+    }
     __syncthreads();
-    const int m = sub_decide(w, S, kb, uni + i0, s_field + i0, st, s_pos, &s_next, s_f, sign, acc_count);
+    const int m = s_m;
     if (m == 0) continue;
     for (int sp = 0; sp < S; ++sp) {
       sub_prepare(tcs, gt, nA, w, sp, N, m, i0, s_pos, st.Gam + sp * KK, G[sp], s_eGm, s_eG, s_eR, s_eT, etmp);
@@ -582,7 +651,8 @@ __global__ void __launch_bounds__(kSubThreads, 1) metropolis_sub_kernel(const Wa
   }
 
   int8_t* frw = w.fields + (long long)eff * N;
-  for (int i = tid; i < N; i += kSubThreads) frw[i] = s_field[i];
+  if (worker)
+    for (int i = tid; i < N; i += kSubThreads) frw[i] = s_field[i];
   // TMEM back: every committed MMA has completed (each tile's commit was waited on)
   tc::fence_before();
   __syncthreads();
@@ -604,22 +674,24 @@ __global__ void __launch_bounds__(kSubThreads, 1) metropolis_sub_kernel(const Wa
 // times both.
 
 // dynamic shared memory of the decision kernel: the operand buffers, the block's uniforms,
-// the FP64 block state, the exponent scratch and the block's fields; of the flush kernel: the
-// operand buffers, the G staging and the line exponents eG, eT [N]
+// the FP64 block state, the exponent scratch [2][256] and the block's fields; of the flush
+// kernel: the operand buffers, the G staging and the line exponents eG, eT [N]
 size_t submatrix_block_smem_bytes(int S) {
-  return (size_t)A_BYTES + (size_t)NBB * B_BYTES + sizeof(double) * (KB + 6ull * S * KK) + 256 * sizeof(int) + KB;
+  return (size_t)A_BYTES + (size_t)NBB * B_BYTES + sizeof(double) * (KB + 6ull * S * KK) +
+         2 * kSubThreads * sizeof(int) + KB;
 }
 size_t submatrix_flush_smem_bytes(int N) {
   return (size_t)A_BYTES + (size_t)NBB * B_BYTES + kStageBytes + 2 * sizeof(int) * (size_t)((N + 1) & ~1);
 }
 
-__global__ void __launch_bounds__(kSubThreads) metropolis_sub_block_kernel(const WalkerDev* __restrict__ W, int mode,
-                                                                           int j, int q, int blk) {
+__global__ void __launch_bounds__(kSubCTA) metropolis_sub_block_kernel(const WalkerDev* __restrict__ W, int mode,
+                                                                       int j, int q, int blk) {
   const WalkerDev& w = W[blockIdx.x];
   if (w.path != 2) return;
   int t;
   if (!sub_slice_of(w, mode, j, q, t)) return;
   const int N = w.N, S = w.S, Lt = w.Lt, tid = threadIdx.x;
+  const bool worker = tid < kSubThreads;
   const int i0 = blk * KB;
   if (i0 >= N) return;
   const int kb = min(KB, N - i0);
@@ -633,11 +705,11 @@ __global__ void __launch_bounds__(kSubThreads) metropolis_sub_block_kernel(const
   st.Bc = st.Ac + S * KK;
   st.Ut = st.Bc + S * KK;
   st.Wt = st.Ut + S * KK;
-  int* etmp = reinterpret_cast<int*>(st.Wt + S * KK);       // [256]
-  int8_t* s_field = reinterpret_cast<int8_t*>(etmp + 256);  // [KB]
-  __shared__ int s_next, s_pos[KB];
+  int* etmp = reinterpret_cast<int*>(st.Wt + S * KK);                   // [2][256]
+  int8_t* s_field = reinterpret_cast<int8_t*>(etmp + 2 * kSubThreads);  // [KB]
+  __shared__ int s_next, s_pos[KB], s_m;
   __shared__ double s_f[2];
-  __shared__ __align__(8) unsigned long long bar_ldA, bar_ldB[NBB], bar_mma[2];
+  __shared__ __align__(8) unsigned long long bar_ldA, bar_ldB[NBB], bar_mma[2], bar_bfree[NBB], bar_accfree[2];
   __shared__ unsigned s_tmem;
   __shared__ int s_tcfail;
 
@@ -645,42 +717,39 @@ __global__ void __launch_bounds__(kSubThreads) metropolis_sub_block_kernel(const
   const double* G[2] = {w.G, (S == 2) ? w.G + NN : w.G};
   const int eff = t - 1;
   const unsigned long long sweep = (w.rng == 1) ? *w.sweep_ctr : 0ULL;
-  for (int l = tid; l < kb; l += kSubThreads) {
-    const int i = i0 + l;
-    s_field[l] = w.fields[(long long)eff * N + i];
-    const int attempt = (mode == MODE_FWD) ? (eff * N + i) : ((Lt - t) * N + i);
-    uni[l] = (w.rng == 0) ? w.uni[attempt] : philox_uniform(w.seed, (unsigned)w.widx, sweep, (unsigned)(eff * N + i));
+  if (worker) {
+    for (int l = tid; l < kb; l += kSubThreads) {
+      const int i = i0 + l;
+      s_field[l] = w.fields[(long long)eff * N + i];
+      const int attempt = (mode == MODE_FWD) ? (eff * N + i) : ((Lt - t) * N + i);
+      uni[l] = (w.rng == 0) ? w.uni[attempt] : philox_uniform(w.seed, (unsigned)w.widx, sweep, (unsigned)(eff * N + i));
+    }
+    sub_load_block(st, G, S, N, i0, kb);
+    double sign = (tid == 0) ? *w.sign : 0.0;
+    long long acc_count = 0;
+    wsync();
+    const int m = sub_decide(w, S, kb, uni, s_field, st, s_pos, &s_next, s_f, sign, acc_count);
+    int8_t* frw = w.fields + (long long)eff * N + i0;
+    for (int l = tid; l < kb; l += kSubThreads) frw[l] = s_field[l];
+    if (tid == 0) {
+      *w.sign = sign;
+      *w.accepts += acc_count;
+      if (mode == MODE_BWD && t == Lt && i0 + KB >= N) *w.sign_Lt = sign;
+      *reinterpret_cast<int*>(w.msub + so.mc) = m;
+      s_m = m;
+      s_tcfail = 0;
+      if (m > 0) sub_tc_init(&bar_ldA, bar_ldB, bar_mma, bar_bfree, bar_accfree);
+    }
   }
-  sub_load_block(st, G, S, N, i0, kb);
-  double sign = 0.0;
-  long long acc_count = 0;
-  if (tid == 0) sign = *w.sign;
   __syncthreads();
-
-  const int m = sub_decide(w, S, kb, uni, s_field, st, s_pos, &s_next, s_f, sign, acc_count);
-  int8_t* frw = w.fields + (long long)eff * N + i0;
-  for (int l = tid; l < kb; l += kSubThreads) frw[l] = s_field[l];
-  if (tid == 0) {
-    *w.sign = sign;
-    *w.accepts += acc_count;
-    if (mode == MODE_BWD && t == Lt && i0 + KB >= N) *w.sign_Lt = sign;
-    *reinterpret_cast<int*>(w.msub + so.mc) = m;
-  }
+  const int m = s_m;
   if (m == 0) return;
 
-  if (tid == 0) {
-    s_tcfail = 0;
-    tc::mbar_init(&bar_ldA);
-    for (int i = 0; i < NBB; ++i) tc::mbar_init(&bar_ldB[i]);
-    tc::mbar_init(&bar_mma[0]);
-    tc::mbar_init(&bar_mma[1]);
-    tc::mbar_fence_init();
-  }
   if (tid < 32) tc::alloc(&s_tmem, TMEM_COLS);
   tc::fence_before();
   __syncthreads();
   tc::fence_after();
-  const SubTC tcs{smem, smem + A_BYTES, &bar_ldA, bar_ldB, bar_mma, s_tmem, &s_tcfail};
+  const SubTC tcs{smem, smem + A_BYTES, &bar_ldA, bar_ldB, bar_mma, bar_bfree, bar_accfree, s_tmem, &s_tcfail};
   unsigned gt = 0, nA = 0;
   for (int sp = 0; sp < S; ++sp) {
     unsigned char* ms = w.msub + (size_t)sp * so.total;
@@ -699,8 +768,8 @@ __global__ void __launch_bounds__(kSubThreads) metropolis_sub_block_kernel(const
 
 // The flush of block blk: G -= G0(:, I_A) T for both spins, the column tiles of G spread over
 // the gridDim.x CTAs of a walker (CTA p takes tiles p, p + gridDim.x, ...).
-__global__ void __launch_bounds__(kSubThreads) metropolis_sub_flush_kernel(const WalkerDev* __restrict__ W, int mode,
-                                                                           int j, int q, int blk) {
+__global__ void __launch_bounds__(kSubCTA) metropolis_sub_flush_kernel(const WalkerDev* __restrict__ W, int mode,
+                                                                       int j, int q, int blk) {
   const WalkerDev& w = W[blockIdx.y];
   if (w.path != 2) return;
   int t;
@@ -718,31 +787,28 @@ __global__ void __launch_bounds__(kSubThreads) metropolis_sub_flush_kernel(const
   double* stage = reinterpret_cast<double*>(smem + A_BYTES + NBB * B_BYTES);
   int* s_eG = reinterpret_cast<int*>(reinterpret_cast<unsigned char*>(stage) + kStageBytes);
   int* s_eT = s_eG + Nu;
-  __shared__ __align__(8) unsigned long long bar_ldA, bar_ldB[NBB], bar_mma[2];
+  __shared__ __align__(8) unsigned long long bar_ldA, bar_ldB[NBB], bar_mma[2], bar_bfree[NBB], bar_accfree[2];
   __shared__ unsigned s_tmem;
   __shared__ int s_tcfail;
   if (tid == 0) {
     s_tcfail = 0;
-    tc::mbar_init(&bar_ldA);
-    for (int i = 0; i < NBB; ++i) tc::mbar_init(&bar_ldB[i]);
-    tc::mbar_init(&bar_mma[0]);
-    tc::mbar_init(&bar_mma[1]);
-    tc::mbar_fence_init();
+    sub_tc_init(&bar_ldA, bar_ldB, bar_mma, bar_bfree, bar_accfree);
   }
   if (tid < 32) tc::alloc(&s_tmem, TMEM_COLS);
   tc::fence_before();
   __syncthreads();
   tc::fence_after();
-  const SubTC tcs{smem, smem + A_BYTES, &bar_ldA, bar_ldB, bar_mma, s_tmem, &s_tcfail};
+  const SubTC tcs{smem, smem + A_BYTES, &bar_ldA, bar_ldB, bar_mma, bar_bfree, bar_accfree, s_tmem, &s_tcfail};
   unsigned gt = 0, nA = 0;
   for (int sp = 0; sp < S; ++sp) {
     const unsigned char* ms = w.msub + (size_t)sp * so.total;
     const int* eG = reinterpret_cast<const int*>(ms + so.eG);
     const int* eT = reinterpret_cast<const int*>(ms + so.eT);
-    for (int i = tid; i < N; i += kSubThreads) {
-      s_eG[i] = eG[i];
-      s_eT[i] = eT[i];
-    }
+    if (tid < kSubThreads)
+      for (int i = tid; i < N; i += kSubThreads) {
+        s_eG[i] = eG[i];
+        s_eT[i] = eT[i];
+      }
     __syncthreads();
     sub_flush(tcs, gt, nA, w, sp, N, m, w.G + sp * NN, s_eG, s_eT, stage, (int)blockIdx.x, (int)gridDim.x);
   }
@@ -775,7 +841,7 @@ cudaError_t configure_submatrix_kernel() {
 }
 
 void launch_metropolis_sub(const WalkerDev* W, int nw, int mode, int j, int q, int maxN, int S_max, cudaStream_t st) {
-  metropolis_sub_kernel<<<nw, kSubThreads, submatrix_smem_bytes(maxN, S_max), st>>>(W, mode, j, q);
+  metropolis_sub_kernel<<<nw, kSubCTA, submatrix_smem_bytes(maxN, S_max), st>>>(W, mode, j, q);
 }
 
 // CTAs per walker of the split flush: two column tiles of 32 each (at least one CTA)
@@ -789,8 +855,8 @@ void launch_metropolis_sub_split(const WalkerDev* W, int nw, int mode, int j, in
   const int nb = (maxN + KB - 1) / KB, P = submatrix_flush_ctas(maxN);
   const size_t sm1 = submatrix_block_smem_bytes(S_max), sm2 = submatrix_flush_smem_bytes(maxN);
   for (int blk = 0; blk < nb; ++blk) {
-    metropolis_sub_block_kernel<<<nw, kSubThreads, sm1, st>>>(W, mode, j, q, blk);
-    metropolis_sub_flush_kernel<<<dim3(P, nw), kSubThreads, sm2, st>>>(W, mode, j, q, blk);
+    metropolis_sub_block_kernel<<<nw, kSubCTA, sm1, st>>>(W, mode, j, q, blk);
+    metropolis_sub_flush_kernel<<<dim3(P, nw), kSubCTA, sm2, st>>>(W, mode, j, q, blk);
   }
 }
 

@@ -27,7 +27,15 @@ __host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
 __device__ __forceinline__ void mbar_init(unsigned long long* mbar) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(su32(mbar)));
 }
+// an mbarrier whose phase completes after `count` plain arrivals
+__device__ __forceinline__ void mbar_init_n(unsigned long long* mbar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(su32(mbar)), "r"(count));
+}
 __device__ __forceinline__ void mbar_fence_init() { asm volatile("fence.mbarrier_init.release.cluster;"); }
+// one arrival (release: this thread's earlier writes are visible to a thread that waits on the phase)
+__device__ __forceinline__ void mbar_arrive(unsigned long long* mbar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(su32(mbar)) : "memory");
+}
 
 // waits for completion of the mbarrier phase with this parity; false after `limit` tries
 __device__ __forceinline__ bool mbar_wait(unsigned long long* mbar, unsigned parity, int limit = 1 << 24) {
