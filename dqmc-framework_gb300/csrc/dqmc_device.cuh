@@ -152,12 +152,9 @@ __device__ __forceinline__ FlipRatio flip_ratio(const WalkerDev& w, int si, doub
 // The factors f_sigma = Delta_sigma / (1 + (1 - G_ii) Delta_sigma) of the accepted flip's
 // rank-1 update (update_greens_function, src/model/repulsive_hubbard.cpp:127-155; the
 // attractive model's factor_dn equals factor_up, src/model/attractive_hubbard.cpp:149).
-__device__ __forceinline__ double flip_factor(const WalkerDev& w, const FlipRatio& q, int spin) {
-  return (spin == 0 || w.model != 0) ? __ddiv_rn(q.cu, q.ru) : __ddiv_rn(q.cd, q.rd);
-}
 __device__ __forceinline__ void flip_factors(const WalkerDev& w, const FlipRatio& q, double* f) {
-  f[0] = flip_factor(w, q, 0);
-  f[1] = (w.model == 0) ? flip_factor(w, q, 1) : f[0];
+  f[0] = __ddiv_rn(q.cu, q.ru);
+  f[1] = (w.model == 0) ? __ddiv_rn(q.cd, q.rd) : f[0];
 }
 
 // Site i of a walker's lattice is x + L y (+ L^2 z).  The displacement from site i to site j

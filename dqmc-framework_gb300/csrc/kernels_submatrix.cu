@@ -332,17 +332,14 @@ __device__ __forceinline__ void sub_load_block(const SubState& st, const double*
 // fields (position l).  The sites are visited in order: warp 0 evaluates the ratios of all
 // sites still to visit at once, on the diagonal as it stands, and the lowest accepted one is
 // the next accept of the sequential visit, since every site before it saw the same diagonal.
-// Each accept then takes two phases: (2) the coefficients u~, w~, a, b of the accept, the
-// threads of u~ dividing out its factor f while the others run the a and b recursions (a
-// is stored unscaled, in araw); (1) its rank-1 update of the block, warp 0 updating the
-// diagonal of the sites still to visit before it scans them for the next accept, while warps
-// 1-7 update the rest of the block, store a = f araw and add a b^T to Gamma (the fma sequence
-// of the closed sum over accepts, so every value is the sequential form's to the bit).
-// s_fr: the accepted site's ratio terms; araw: [S][KB].  sign and acc_count are thread 0's.
-// Worker threads only.
+// Each accept then takes two phases: (1) the coefficients u~, w~, a, b of the accept; (2)
+// its rank-1 update of the block, warp 0 updating the diagonal of the sites still to visit
+// before it scans them for the next accept, while warps 1-7 update the rest of the block and
+// add a b^T to Gamma (the fma sequence of the closed sum over accepts, so Gamma is the same
+// to the bit).  sign and acc_count are thread 0's.  Worker threads only.
 __device__ __forceinline__ int sub_decide(const WalkerDev& w, int S, int kb, const double* uni, int8_t* fld,
-                                          const SubState& st, int* s_pos, int* s_next, double* s_f, FlipRatio* s_fr,
-                                          double* araw, double& sign, long long& acc_count) {
+                                          const SubState& st, int* s_pos, int* s_next, double* s_f, double& sign,
+                                          long long& acc_count) {
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   for (int e = tid; e < S * KK; e += kSubThreads) st.Gam[e] = 0.0;
   int m = 0, cur = 0;
@@ -350,6 +347,7 @@ __device__ __forceinline__ int sub_decide(const WalkerDev& w, int S, int kb, con
     if (warp == 0) {
       const int l = cur + lane;
       FlipRatio q{};
+      double fq[2] = {0.0, 0.0};
       int s = 0;
       bool acc = false;
       if (l < kb) {
@@ -364,12 +362,14 @@ __device__ __forceinline__ int sub_decide(const WalkerDev& w, int S, int kb, con
         const double gd = (S == 2) ? st.Gb[KK + l * KB + l] : gu;
         q = flip_ratio(w, si, gu, gd);  // reference operation order
         acc = uni[l] < fmin(1.0, fabs(q.r));
+        flip_factors(w, q, fq);         // every lane: off the accepted lane's critical path
       }
       const unsigned amask = __ballot_sync(0xffffffffu, acc);
       const int first = amask ? __ffs(amask) - 1 : 32;
       if (l < kb && lane <= first && !isfinite(q.r)) atomicOr(w.status, ST_NONFINITE_RATIO);
       if (lane == first) {
-        *s_fr = q;
+        s_f[0] = fq[0];
+        s_f[1] = fq[1];
         fld[l] = (int8_t)(-s);
       }
       const double rf = __shfl_sync(0xffffffffu, q.r, first & 31);
@@ -381,46 +381,37 @@ __device__ __forceinline__ int sub_decide(const WalkerDev& w, int S, int kb, con
         *s_next = amask ? cur + first : kb;
       }
     } else if (m > 0) {
-      // the previous accept q1 (position cur - 1): a = f araw, rank-1 update off the diagonal,
-      // Gamma term
+      // the previous accept (position cur - 1): rank-1 update off the diagonal, Gamma term
       const int lp = cur - 1, q1 = m - 1;
-      for (int e = tid - 32; e < S * KB; e += kSubThreads - 32) {
-        const int sp = e / KB, x = e % KB;
-        st.Ac[sp * KK + q1 * KB + x] = (x <= q1) ? s_f[sp] * araw[sp * KB + x] : 0.0;
-      }
       for (int e = tid - 32; e < S * KK; e += kSubThreads - 32) {
         const int sp = e / KK, c = (e % KK) / KB, r = e % KB;
         if (r > lp && c > lp && r < kb && c < kb && r != c)
           st.Gb[e] = fma(-st.Ut[sp * KK + q1 * KB + r], st.Wt[sp * KK + q1 * KB + c], st.Gb[e]);
         const int y = c, x = r;
-        if (x <= q1 && y <= q1) {
-          const double av = s_f[sp] * araw[sp * KB + x];  // a_q1(x), rounded as stored
-          st.Gam[e] = fma(av, st.Bc[sp * KK + q1 * KB + y], st.Gam[e]);
-        }
+        if (x <= q1 && y <= q1)
+          st.Gam[e] = fma(st.Ac[sp * KK + q1 * KB + x], st.Bc[sp * KK + q1 * KB + y], st.Gam[e]);
       }
     }
     wsync();
     const int l = *s_next;
     if (l >= kb) break;
-    // u~, w~ of accept m on the block, and its coefficients: role 0 u~ = f G(:, l) (with f),
-    // role 1 w~, role 2 the unscaled a recursion, role 3 b
+    // u~, w~ of accept m on the block, and its coefficients a_m, b_m
     for (int e = tid; e < S * 4 * KB; e += kSubThreads) {
       const int sp = e / (4 * KB), role = (e / KB) & 3, x = e % KB;
+      const double f = s_f[sp];
       const double* gb = st.Gb + sp * KK;
       double* ut = st.Ut + sp * KK;
       double* wt = st.Wt + sp * KK;
       double* ac = st.Ac + sp * KK;
       double* bc = st.Bc + sp * KK;
       if (role == 0) {
-        const double f = flip_factor(w, *s_fr, sp);
         ut[m * KB + x] = f * gb[l * KB + x];  // f G(x, l)
-        if (x == 0) s_f[sp] = f;
       } else if (role == 1) {
         wt[m * KB + x] = ((x == l) ? 1.0 : 0.0) - gb[x * KB + l];  // delta - G(l, x)
       } else if (role == 2) {
         double a = (x == m) ? 1.0 : 0.0;
         for (int p = x; p < m; ++p) a = fma(-wt[p * KB + l], ac[p * KB + x], a);
-        araw[sp * KB + x] = a;
+        ac[m * KB + x] = (x <= m) ? f * a : 0.0;
       } else {
         double b = (x == m) ? 1.0 : 0.0;
         for (int p = x; p < m; ++p) b = fma(ut[p * KB + l], bc[p * KB + x], b);
@@ -614,8 +605,7 @@ __global__ void __launch_bounds__(kSubCTA, 1) metropolis_sub_kernel(const Walker
   int* etmp = s_eGm + KB;                                               // [2][256]
   int8_t* s_field = reinterpret_cast<int8_t*>(etmp + 2 * kSubThreads);  // [N]
   __shared__ int s_next, s_pos[KB], s_m;
-  __shared__ double s_f[2], s_araw[2 * KB];
-  __shared__ FlipRatio s_fr;
+  __shared__ double s_f[2];
   __shared__ __align__(8) unsigned long long bar_ldA, bar_ldB[NBB], bar_mma[2], bar_bfree[NBB], bar_accfree[2];
   __shared__ unsigned s_tmem;
   __shared__ int s_tcfail;
@@ -648,8 +638,7 @@ __global__ void __launch_bounds__(kSubCTA, 1) metropolis_sub_kernel(const Walker
     if (worker) {
       sub_load_block(st, G, S, N, i0, kb);
       wsync();
-      const int mm = sub_decide(w, S, kb, uni + i0, s_field + i0, st, s_pos, &s_next, s_f, &s_fr, s_araw, sign,
-                                 acc_count);
+      const int mm = sub_decide(w, S, kb, uni + i0, s_field + i0, st, s_pos, &s_next, s_f, sign, acc_count);
       if (tid == 0) s_m = mm;
     }
     __syncthreads();
@@ -719,8 +708,7 @@ __global__ void __launch_bounds__(kSubCTA) metropolis_sub_block_kernel(const Wal
   int* etmp = reinterpret_cast<int*>(st.Wt + S * KK);                   // [2][256]
   int8_t* s_field = reinterpret_cast<int8_t*>(etmp + 2 * kSubThreads);  // [KB]
   __shared__ int s_next, s_pos[KB], s_m;
-  __shared__ double s_f[2], s_araw[2 * KB];
-  __shared__ FlipRatio s_fr;
+  __shared__ double s_f[2];
   __shared__ __align__(8) unsigned long long bar_ldA, bar_ldB[NBB], bar_mma[2], bar_bfree[NBB], bar_accfree[2];
   __shared__ unsigned s_tmem;
   __shared__ int s_tcfail;
@@ -740,7 +728,7 @@ __global__ void __launch_bounds__(kSubCTA) metropolis_sub_block_kernel(const Wal
     double sign = (tid == 0) ? *w.sign : 0.0;
     long long acc_count = 0;
     wsync();
-    const int m = sub_decide(w, S, kb, uni, s_field, st, s_pos, &s_next, s_f, &s_fr, s_araw, sign, acc_count);
+    const int m = sub_decide(w, S, kb, uni, s_field, st, s_pos, &s_next, s_f, sign, acc_count);
     int8_t* frw = w.fields + (long long)eff * N + i0;
     for (int l = tid; l < kb; l += kSubThreads) frw[l] = s_field[l];
     if (tid == 0) {
