@@ -469,20 +469,22 @@ __device__ __forceinline__ void sub_prepare(const SubTC& tcs, unsigned& gt, unsi
              double tv[16];
              int e = -1100;
              if (ok) {
+               uint32_t v[2][OZS][8];  // both halves' loads in flight before one wait
 #pragma unroll
-               for (int h = 0; h < 2; ++h) {
-                 uint32_t v[OZS][8];
+               for (int h = 0; h < 2; ++h)
 #pragma unroll
                  for (int g = 0; g < OZS; ++g)
-                   tc::ld8(v[g], tacc + ((unsigned)(wq * 32) << 16) + (unsigned)(g * TN + xh * 16 + h * 8));
-                 tc::wait_ld();
+                   tc::ld8(v[h][g], tacc + ((unsigned)(wq * 32) << 16) + (unsigned)(g * TN + xh * 16 + h * 8));
+               tc::wait_ld();
+#pragma unroll
+               for (int h = 0; h < 2; ++h)
 #pragma unroll
                  for (int u = 0; u < 8; ++u) {
                    const int x = xh * 16 + h * 8 + u;
-                   tv[h * 8 + u] = (x < m && c < N) ? ozaki::ldexp_i64(group_sum(v, u), ec + eGm[x] + kEOff) : 0.0;
+                   tv[h * 8 + u] =
+                       (x < m && c < N) ? ozaki::ldexp_i64(group_sum(v[h], u), ec + eGm[x] + kEOff) : 0.0;
                    e = max(e, ozaki::exp_bound(tv[h * 8 + u]));
                  }
-               }
              }
              int* ex = etmp + (tl & 1) * kSubThreads;  // two tiles in flight between the halves
              ex[tid] = e;
@@ -544,21 +546,22 @@ __device__ __forceinline__ void sub_flush(const SubTC& tcs, unsigned& gt, unsign
              const double* gsv = stage + (tl & 1) * 16 * kSubThreads + tid;
              const int er = (r < N) ? eG[r] : 0;
              const unsigned ta = tacc + ((unsigned)(wq * 32) << 16);
+             uint32_t v[2][OZS][8];  // both halves' loads in flight before one wait
 #pragma unroll
-             for (int h = 0; h < 2; ++h) {
-               uint32_t v[OZS][8];
+             for (int h = 0; h < 2; ++h)
 #pragma unroll
-               for (int g = 0; g < OZS; ++g) tc::ld8(v[g], ta + (unsigned)(g * TN + half * 16 + h * 8));
-               tc::wait_ld();
+               for (int g = 0; g < OZS; ++g) tc::ld8(v[h][g], ta + (unsigned)(g * TN + half * 16 + h * 8));
+             tc::wait_ld();
+#pragma unroll
+             for (int h = 0; h < 2; ++h)
 #pragma unroll
                for (int u = 0; u < 8; ++u) {
                  const int c = c0 + h * 8 + u;
-                 const long long sv = group_sum(v, u);
+                 const long long sv = group_sum(v[h], u);
                  if (sv != 0 && r < N && c < N)
                    Gs[(long long)c * N + r] =
                        gsv[(h * 8 + u) * kSubThreads] - ozaki::ldexp_i64(sv, er + eT[c] + kEOff);
                }
-             }
            },
            cb0, cbs);
 }
