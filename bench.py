@@ -93,7 +93,7 @@ METRIC = "HS-field updates/s (walkers*N*Lt / half-sweep time)"
 # flushed, and each walker's G, chain and slices are its own, so this cold-cache traffic
 # grows in proportion to the walkers a launch covers.
 NCU_TRAFFIC_8_WALKERS = {
-    "metropolis": ("metropolis_sub_kernel", 4436480 + 256),
+    "metropolis": ("metropolis_sub_kernel", 4379392 + 0),
     "product": ("oz_prod_tc_kernel<3,7>", 8307200 + 0),
 }
 
