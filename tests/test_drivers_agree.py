@@ -25,8 +25,7 @@ CONFIG = """
 [Model]
     type = "RepulsiveHubbard"
 [Lattice]
-    cell = [ 4, 4 ]
-    momentum = "MPoint"
+    %s
     momentum_list = "%s"
 [MonteCarlo]
     beta = 1.0
@@ -60,18 +59,25 @@ def _numbers(path):
     return np.array([float(x) for x in open(path).read().split()])
 
 
-@pytest.mark.parametrize("observables,klist,walkers", [
-    ('"filling_number", "kinetic_energy", "s_wave_pairing_corr"', "KstarsAll", 2),  # device binning path
-    ('"all"', "DeltaLine", 3),                                                       # dynamic path
-    ('"density_of_states", "greens_functions"', "KstarsAll", 1),                   # dynamic only
+SQUARE = 'cell = [ 4, 4 ]\n    momentum = "MPoint"'
+CUBIC = 'type = "Cubic"\n    cell = [ 3, 3, 3 ]\n    momentum = "XPoint"'
+
+
+@pytest.mark.parametrize("lattice,observables,klist,walkers", [
+    (SQUARE, '"filling_number", "kinetic_energy", "s_wave_pairing_corr"', "KstarsAll", 2),  # device binning path
+    (SQUARE, '"all"', "DeltaLine", 3),                                                       # dynamic path
+    (SQUARE, '"density_of_states", "greens_functions"', "KstarsAll", 1),                   # dynamic only
+    (CUBIC, '"all"', "LambdaLine", 2),  # cubic: 3-D momenta, no superfluid stiffness
 ])
-def test_python_and_native_drivers_write_the_same_results(fake, tmp_path, monkeypatch, observables, klist, walkers):
+def test_python_and_native_drivers_write_the_same_results(fake, tmp_path, monkeypatch, lattice, observables, klist,
+                                                          walkers):
     lib, exe = fake
-    cfg_text = CONFIG % (klist, observables)
+    cfg_text = CONFIG % (lattice, klist, observables)
+    nsite = 27 if lattice == CUBIC else 16
     cfg_path = tmp_path / "config.toml"
     cfg_path.write_text(cfg_text)
     for who in ("py", "cpp"):  # each starts from the same fields file, which each writes back
-        (tmp_path / f"fields_{who}.in").write_text(dio.format_fields([[(-1) ** (i + t) for i in range(16)]
+        (tmp_path / f"fields_{who}.in").write_text(dio.format_fields([[(-1) ** (i + t) for i in range(nsite)]
                                                                        for t in range(6)]))
     # Python driver over the stand-in library
     monkeypatch.setattr(dq, "LIB_PATH", lib)
