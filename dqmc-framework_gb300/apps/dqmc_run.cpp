@@ -4,8 +4,8 @@
 // walkers, thermalize, measure in bins, analyse, print mean +/- error per
 // observable, one JSON object per line.
 //
-// usage: dqmc_run key=value ...   keys: model (repulsive|attractive), L, t, U, mu,
-//        beta, Lt, pace, checkerboard (0|1), walkers, seed, warmup, bins, binsize,
+// usage: dqmc_run key=value ...   keys: model (repulsive|attractive), lattice (square|cubic),
+//        L, t, U, mu, beta, Lt, pace, checkerboard (0|1), walkers, seed, warmup, bins, binsize,
 //        between, fields (path of a "t i s" text file, reference fields.out format)
 #include <cstdio>
 #include <cstdlib>
@@ -19,7 +19,7 @@
 
 int main(int argc, char** argv) {
   std::map<std::string, std::string> kv = {
-      {"model", "repulsive"}, {"L", "4"}, {"t", "1"}, {"U", "4"}, {"mu", "0"}, {"beta", "4"}, {"Lt", "80"},
+      {"model", "repulsive"}, {"lattice", "square"}, {"L", "4"}, {"t", "1"}, {"U", "4"}, {"mu", "0"}, {"beta", "4"}, {"Lt", "80"},
       {"pace", "10"}, {"checkerboard", "0"}, {"walkers", "1"}, {"seed", "12345"}, {"warmup", "100"},
       {"bins", "10"}, {"binsize", "20"}, {"between", "0"}, {"fields", ""}, {"rng", "minstd"}};
   for (int i = 1; i < argc; ++i) {
@@ -36,9 +36,13 @@ int main(int argc, char** argv) {
     Model model = (kv["model"] == "attractive") ? (Model)AttractiveHubbard() : (Model)RepulsiveHubbard();
     model.set_model_params(std::stod(kv["t"]), std::fabs(std::stod(kv["U"])), std::stod(kv["mu"]));
     if (std::stoi(kv["checkerboard"])) model.link_checkerboard(); else model.link();
-    Square lattice;
     const int L = std::stoi(kv["L"]);
-    lattice.set_lattice_params({L, L});
+    if (kv["lattice"] != "square" && kv["lattice"] != "cubic")
+      throw Error(DQMC_ERR_ARG, "lattice must be square or cubic");
+    Square square;
+    Cubic cubic;
+    if (kv["lattice"] == "cubic") cubic.set_lattice_params({L, L, L}); else square.set_lattice_params({L, L});
+    const LatticeBase& lattice = (kv["lattice"] == "cubic") ? (const LatticeBase&)cubic : (const LatticeBase&)square;
     DqmcWalker walker;
     walker.set_physical_params(std::stod(kv["beta"]), std::stoi(kv["Lt"]));
     walker.set_stabilization_pace(std::stoi(kv["pace"]));

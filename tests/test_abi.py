@@ -140,6 +140,13 @@ def test_cpp_driver_fails_loudly_without_a_device(dq):
     assert r.returncode != 0 and "no CUDA device" in (r.stdout + r.stderr)
     r = subprocess.run([exe, "bogus=1"], capture_output=True, text=True, env=env, timeout=120)
     assert r.returncode != 0 and "unknown argument" in (r.stdout + r.stderr)
+    # the cubic lattice reaches the library (which then needs the device); bad lattices stop earlier
+    r = subprocess.run([exe, "lattice=cubic", "L=4"], capture_output=True, text=True, env=env, timeout=120)
+    assert r.returncode != 0 and "no CUDA device" in (r.stdout + r.stderr)
+    r = subprocess.run([exe, "lattice=honeycomb"], capture_output=True, text=True, env=env, timeout=120)
+    assert r.returncode != 0 and "square or cubic" in (r.stdout + r.stderr)
+    r = subprocess.run([exe, "lattice=cubic", "L=1"], capture_output=True, text=True, env=env, timeout=120)
+    assert r.returncode != 0 and "Cubic" in (r.stdout + r.stderr)
 
 
 def test_cpp_mirror_analysis_matches_python(tmp_path):
