@@ -10,7 +10,9 @@ functions run on the host) checks:
   * the tensor-core image layout: tc_index maps (line, k) of a slice padded to
     tc_lines(N) lines and ldk columns one-to-one onto [0, tc_slice_elems), and the
     16-deep chunk of any 128 consecutive lines starting at a multiple of 128 is one
-    contiguous range of 2048 elements (what one bulk copy moves).
+    contiguous range of 2048 elements (what one bulk copy moves);
+  * the submatrix Metropolis kernels' dynamic shared memory fits one CTA for every N and
+    spin count the library takes (a program linked against kernels_submatrix.cu).
 """
 import os
 import shutil
@@ -101,3 +103,44 @@ def test_stabilization_and_flush_slice_widths():
     S, B = map(int, re.search(r"constexpr int OZS = (\d+), OZB = (\d+);", sub).groups())
     KB = int(re.search(r"constexpr int KB = (\d+);", sub).group(1))
     assert S * (2 ** B - 1) ** 2 * KB < 2 ** 22
+
+
+SMEM_PROGRAM = r"""
+#include <cstdio>
+namespace dqmc {
+size_t submatrix_smem_bytes(int N, int S);
+size_t submatrix_block_smem_bytes(int S);
+size_t submatrix_flush_smem_bytes(int N);
+}
+int main() {
+  // the opt-in dynamic shared memory of one CTA on sm_100-class GPUs (227 KB), less 2 KB for
+  // the kernels' static shared memory
+  const size_t limit = 232448 - 2048;
+  int bad = 0;
+  for (int S = 1; S <= 2; ++S) {
+    for (int N = 1; N <= 1024; ++N) {
+      if (dqmc::submatrix_smem_bytes(N, S) > limit) { std::printf("fused N=%d S=%d\n", N, S); ++bad; break; }
+      if (dqmc::submatrix_flush_smem_bytes(N) > limit) { std::printf("flush N=%d\n", N); ++bad; break; }
+    }
+    if (dqmc::submatrix_block_smem_bytes(S) > limit) { std::printf("block S=%d\n", S); ++bad; }
+  }
+  std::printf("%s\n", bad ? "FAIL" : "OK");
+  return bad ? 1 : 0;
+}
+"""
+
+
+def test_submatrix_kernels_fit_in_shared_memory(tmp_path):
+    """The submatrix Metropolis kernels' dynamic shared memory (operand buffers, block state,
+    G staging, exponents), as the launches size it, fits one CTA for every N <= 1024 and both
+    spin counts; the functions are the library's own, linked from kernels_submatrix.cu."""
+    nvcc = shutil.which("nvcc") or ("/usr/local/cuda/bin/nvcc" if os.path.exists("/usr/local/cuda/bin/nvcc") else None)
+    if nvcc is None:
+        pytest.skip("nvcc not available")
+    src = tmp_path / "smem.cu"
+    src.write_text(SMEM_PROGRAM)
+    exe = tmp_path / "smem"
+    subprocess.run([nvcc, "-std=c++17", "-O1", "-gencode", "arch=compute_103a,code=sm_103a", "-I", CSRC, str(src),
+                    os.path.join(CSRC, "kernels_submatrix.cu"), "-o", str(exe)], check=True, timeout=600)
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0 and r.stdout.strip().endswith("OK"), r.stdout
